@@ -1,0 +1,271 @@
+"""ctypes mirror of include/cassandra_gb300.h and a thin context wrapper.
+
+The same wrapper drives any shared library that implements the header's entry
+points under a symbol prefix (``cass_`` for the CUDA library).  Arguments keep
+the reference's 1-based (im, is, ibox) indices.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import numpy as np
+
+CASS_OK = 0
+CASS_EINVAL = -1
+CASS_ECAPACITY = -2
+CASS_ECUDA = -3
+CASS_ETIMEDOUT = -4
+CASS_ESTATE = -5
+CASS_ENOMEM = -6
+CASS_EUNSUPPORTED = -7
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+VDW_NONE, VDW_LJ, VDW_MIE = 0, 1, 2
+VDW_SUM_CUT, VDW_SUM_CUT_TAIL, VDW_SUM_CUT_SHIFT, VDW_SUM_MINIMUM = 0, 1, 2, 3
+VDW_SUM_CUT_SWITCH, VDW_SUM_CHARMM, VDW_SUM_CUT_SHIFT_FORCE = 4, 5, 6
+CHARGE_NONE, CHARGE_COUL = 0, 1
+QQ_EWALD, QQ_CUT, QQ_MINIMUM, QQ_DSF = 0, 1, 2, 3
+MOVE_INSERTION, MOVE_DELETION, MOVE_TRANSLATION, MOVE_ROTATION, MOVE_INTRA = 0, 1, 2, 3, 4
+BONDED_FIXED, BONDED_HARMONIC = 0, 1
+
+_i32p = C.POINTER(C.c_int32)
+_f64p = C.POINTER(C.c_double)
+
+
+class CassConfig(C.Structure):
+    _fields_ = [("nspecies", C.c_int32), ("ntypes", C.c_int32), ("nboxes", C.c_int32),
+                ("precision", C.c_int32), ("device", C.c_int32), ("max_kvectors", C.c_int32),
+                ("max_molecules", _i32p)]
+
+
+class CassSpeciesDesc(C.Structure):
+    _fields_ = [("natoms", C.c_int32), ("atom_type", _i32p), ("charge", _f64p), ("mass", _f64p),
+                ("vdw_intra_scale", _f64p), ("charge_intra_scale", _f64p), ("bonded", _i32p),
+                ("nbonds", C.c_int32), ("bond_atoms", _i32p), ("bond_kind", _i32p), ("bond_param", _f64p),
+                ("nangles", C.c_int32), ("angle_atoms", _i32p), ("angle_kind", _i32p), ("angle_param", _f64p),
+                ("ndihedrals", C.c_int32), ("dihedral_atoms", _i32p), ("dihedral_rb", _f64p),
+                ("nimpropers", C.c_int32), ("improper_atoms", _i32p), ("improper_param", _f64p),
+                ("nfragments", C.c_int32), ("frag_natoms", _i32p), ("frag_atoms", _i32p),
+                ("frag_nconnect", _i32p), ("frag_connect", _i32p), ("frag_nconfig", _i32p),
+                ("frag_library", _f64p), ("l_coul_cbmc", C.c_int32)]
+
+
+class CassBoxDesc(C.Structure):
+    _fields_ = [("length", C.c_double * 3), ("vdw_style", C.c_int32), ("vdw_sum_style", C.c_int32),
+                ("rcut_vdw", C.c_double), ("rcut_coul", C.c_double), ("rcut_cbmc", C.c_double),
+                ("rcut_low", C.c_double), ("ron_switch", C.c_double), ("roff_switch", C.c_double),
+                ("charge_style", C.c_int32), ("charge_sum_style", C.c_int32), ("ewald_tol", C.c_double),
+                ("alpha_dsf", C.c_double), ("temperature", C.c_double)]
+
+
+class CassEnergy(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("total", "intra", "bond", "angle", "dihedral", "improper",
+                                          "intra_vdw", "intra_q", "inter", "inter_vdw", "inter_q",
+                                          "lrc", "reciprocal", "self")]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class CassWidomResult(C.Structure):
+    _fields_ = [("widom_sum", C.c_double), ("prefactor", C.c_double), ("n_insertions", C.c_int64),
+                ("n_overlaps", C.c_int64), ("n_trials", C.c_int64)]
+
+
+class CassWidomTrace(C.Structure):
+    _fields_ = [("widom_var", C.c_double), ("ln_pbias", C.c_double), ("e_inter", C.c_double),
+                ("e_first_trial_sum", C.c_double), ("selected_trial", C.c_int32), ("overlap", C.c_int32)]
+
+
+TRACE_DTYPE = np.dtype([("widom_var", "f8"), ("ln_pbias", "f8"), ("e_inter", "f8"),
+                        ("e_first_trial_sum", "f8"), ("selected_trial", "i4"), ("overlap", "i4")])
+assert TRACE_DTYPE.itemsize == C.sizeof(CassWidomTrace)
+
+# entry points of the header: name -> (restype, argtypes)
+SIGNATURES = {
+    "abi_version": (C.c_int, []),
+    "last_error": (C.c_char_p, []),
+    "ctx_create": (C.c_int, [C.POINTER(CassConfig), C.POINTER(C.c_void_p)]),
+    "ctx_destroy": (C.c_int, [C.c_void_p]),
+    "set_nonbond_table": (C.c_int, [C.c_void_p, C.c_int32, _f64p, _f64p, _f64p, _f64p]),
+    "set_species": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(CassSpeciesDesc)]),
+    "set_box": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(CassBoxDesc)]),
+    "set_molecules": (C.c_int, [C.c_void_p, C.c_int32, _i32p, _i32p, _i32p, _f64p]),
+    "remove_molecule": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "get_molecule": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _f64p]),
+    "mol_inter_energy": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _f64p, _f64p, _i32p]),
+    "mol_intra_energy": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _f64p, _f64p, _f64p, _i32p]),
+    "system_total_energy": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(CassEnergy), _i32p]),
+    "ewald_update": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _f64p]),
+    "ewald_restore": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "ewald_widom": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _f64p, _f64p]),
+    "widom_insert": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _i32p, C.c_int64, C.c_int32, C.c_int32,
+                               C.c_uint64, C.POINTER(CassWidomResult), C.c_void_p]),
+}
+
+
+class CassError(RuntimeError):
+    def __init__(self, fn: str, code: int, msg: str):
+        super().__init__(f"{fn} failed with status {code}: {msg}")
+        self.code = code
+
+
+def bind(lib: C.CDLL, prefix: str) -> dict:
+    """Bind every entry point of the header under `prefix`; returns name -> function."""
+    out = {}
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, prefix + name)
+        f.restype = res
+        f.argtypes = args
+        out[name] = f
+    return out
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int32).ravel())
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64).ravel())
+
+
+def _p(a: np.ndarray | None):
+    if a is None or a.size == 0:
+        return None
+    ct = _i32p if a.dtype == np.int32 else _f64p
+    return a.ctypes.data_as(ct)
+
+
+class Context:
+    """An opened context of a library implementing the header (GPU or oracle)."""
+
+    def __init__(self, fns: dict, nspecies: int, ntypes: int, nboxes: int,
+                 max_molecules: Sequence[int], precision: int = PREC_FP64,
+                 device: int = 0, max_kvectors: int = 100000):
+        self._f = fns
+        self._keep: list = []
+        mm = _i32(max_molecules)
+        cfg = CassConfig(nspecies, ntypes, nboxes, precision, device, max_kvectors, _p(mm))
+        h = C.c_void_p()
+        self._check("ctx_create", fns["ctx_create"](C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.nspecies, self.ntypes, self.nboxes = nspecies, ntypes, nboxes
+        self.max_molecules = list(max_molecules)
+        self.precision = precision
+        self.natoms: dict[int, int] = {}
+
+    # -- plumbing --------------------------------------------------------
+    def _check(self, fn: str, rc: int) -> None:
+        if rc != CASS_OK:
+            msg = self._f["last_error"]()
+            raise CassError(fn, rc, msg.decode() if msg else "")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._f["ctx_destroy"](self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- set-up ----------------------------------------------------------
+    def set_nonbond_table(self, eps, sig, mie_n=None, mie_m=None) -> None:
+        nt = self.ntypes
+        e, s = _f64(eps), _f64(sig)
+        n = _f64(mie_n if mie_n is not None else np.zeros(nt * nt))
+        m = _f64(mie_m if mie_m is not None else np.zeros(nt * nt))
+        self._check("set_nonbond_table", self._f["set_nonbond_table"](self._h, nt, _p(e), _p(s), _p(n), _p(m)))
+
+    def set_species(self, is_: int, sp) -> None:
+        """`sp` is a cassandra_gb300.system.Species."""
+        arrs = sp.desc_arrays()
+        d = CassSpeciesDesc()
+        for k, v in arrs.items():
+            if isinstance(v, np.ndarray):
+                setattr(d, k, _p(v))
+            else:
+                setattr(d, k, v)
+        self._check("set_species", self._f["set_species"](self._h, is_, C.byref(d)))
+        self.natoms[is_] = sp.natoms
+
+    def set_box(self, ibox: int, bx) -> None:
+        d = CassBoxDesc()
+        d.length[0], d.length[1], d.length[2] = bx.length
+        d.vdw_style, d.vdw_sum_style = bx.vdw_style, bx.vdw_sum_style
+        d.rcut_vdw, d.rcut_coul, d.rcut_cbmc, d.rcut_low = bx.rcut_vdw, bx.rcut_coul, bx.rcut_cbmc, bx.rcut_low
+        d.ron_switch, d.roff_switch = bx.ron_switch, bx.roff_switch
+        d.charge_style, d.charge_sum_style = bx.charge_style, bx.charge_sum_style
+        d.ewald_tol, d.alpha_dsf, d.temperature = bx.ewald_tol, bx.alpha_dsf, bx.temperature
+        self._check("set_box", self._f["set_box"](self._h, ibox, C.byref(d)))
+
+    def set_molecules(self, im, is_, ibox, xyz) -> None:
+        im, is_, ib, x = _i32(im), _i32(is_), _i32(ibox), _f64(xyz)
+        self._check("set_molecules", self._f["set_molecules"](self._h, len(im), _p(im), _p(is_), _p(ib), _p(x)))
+
+    def remove_molecule(self, im: int, is_: int) -> None:
+        self._check("remove_molecule", self._f["remove_molecule"](self._h, im, is_))
+
+    def get_molecule(self, im: int, is_: int) -> np.ndarray:
+        out = np.zeros(3 * self.natoms[is_])
+        self._check("get_molecule", self._f["get_molecule"](self._h, im, is_, _p(out)))
+        return out.reshape(-1, 3)
+
+    # -- energies ------------------------------------------------------
+    def mol_inter_energy(self, im: int, is_: int, cbmc: bool = False):
+        ev, eq, ov = C.c_double(), C.c_double(), C.c_int32()
+        self._check("mol_inter_energy", self._f["mol_inter_energy"](
+            self._h, im, is_, int(cbmc), C.byref(ev), C.byref(eq), C.byref(ov)))
+        return ev.value, eq.value, bool(ov.value)
+
+    def mol_intra_energy(self, im: int, is_: int, cbmc: bool = False):
+        a, b, c, ov = C.c_double(), C.c_double(), C.c_double(), C.c_int32()
+        self._check("mol_intra_energy", self._f["mol_intra_energy"](
+            self._h, im, is_, int(cbmc), C.byref(a), C.byref(b), C.byref(c), C.byref(ov)))
+        return a.value, b.value, c.value, bool(ov.value)
+
+    def system_total_energy(self, ibox: int, intra: bool = True):
+        e, ov = CassEnergy(), C.c_int32()
+        self._check("system_total_energy", self._f["system_total_energy"](
+            self._h, ibox, int(intra), C.byref(e), C.byref(ov)))
+        return e.as_dict(), bool(ov.value)
+
+    def ewald_update(self, im: int, is_: int, ibox: int, move_flag: int) -> float:
+        e = C.c_double()
+        self._check("ewald_update", self._f["ewald_update"](self._h, im, is_, ibox, move_flag, C.byref(e)))
+        return e.value
+
+    def ewald_restore(self, im: int, is_: int, ibox: int) -> None:
+        self._check("ewald_restore", self._f["ewald_restore"](self._h, im, is_, ibox))
+
+    def ewald_widom(self, is_: int, ibox: int, xyz) -> np.ndarray:
+        x = _f64(xyz)
+        n = x.size // (3 * self.natoms[is_])
+        out = np.zeros(n)
+        self._check("ewald_widom", self._f["ewald_widom"](self._h, is_, ibox, n, _p(x), _p(out)))
+        return out
+
+    def widom_insert(self, is_: int, boxes: Sequence[int], n_insertions: int, kappa_ins: int,
+                     kappa_dih: int, seed: int, trace: bool = False):
+        b = _i32(boxes)
+        res = (CassWidomResult * len(b))()
+        tr = np.zeros(len(b) * n_insertions, dtype=TRACE_DTYPE) if trace else None
+        self._check("widom_insert", self._f["widom_insert"](
+            self._h, is_, len(b), _p(b), n_insertions, kappa_ins, kappa_dih, C.c_uint64(seed & (2**64 - 1)),
+            res, tr.ctypes.data_as(C.c_void_p) if tr is not None else None))
+        out = [{"widom_sum": r.widom_sum, "prefactor": r.prefactor, "n_insertions": r.n_insertions,
+                "n_overlaps": r.n_overlaps, "n_trials": r.n_trials} for r in res]
+        if trace:
+            return out, tr.reshape(len(b), n_insertions)
+        return out

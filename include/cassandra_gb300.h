@@ -1,0 +1,233 @@
+/*
+ * cassandra_gb300.h -- C-ABI of the GB300 molecular-energy hot path.
+ *
+ * The entry points below replace Cassandra's Fortran energy / CBMC / Widom
+ * routines (module procedures that read module-global state) with calls on an
+ * opaque context that owns the device state.  Each declaration names the
+ * reference routine it stands in for (path:line inside the Cassandra source
+ * tree).  Conventions kept from the reference so that an ISO_C_BINDING shim can
+ * forward its arguments unchanged:
+ *   - molecule "locate" (im), species (is), box (ibox) and atom indices are
+ *     1-based;
+ *   - lengths in Angstrom, energies in Cassandra atomic units
+ *     (amu A^2 / ps^2 = 10 J/mol), epsilon already multiplied by kboltz,
+ *     charges in e;
+ *   - "overlap" is a data flag (core overlap found), not an error.
+ * Every function returns an int status: CASS_OK (0) or a negative CASS_E*
+ * code.  No exception or process exit crosses this boundary.  Caller-owned
+ * pointers are read or written only during the call.
+ */
+#ifndef CASSANDRA_GB300_H
+#define CASSANDRA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CASS_ABI_VERSION 1
+
+/* status codes */
+#define CASS_OK 0
+#define CASS_EINVAL (-1)     /* bad argument (index out of range, NULL, ...) */
+#define CASS_ECAPACITY (-2)  /* a size exceeds what the context was created for */
+#define CASS_ECUDA (-3)      /* CUDA runtime error */
+#define CASS_ETIMEDOUT (-4)  /* a bounded device-side wait gave up */
+#define CASS_ESTATE (-5)     /* call order violated (e.g. Widom before totals) */
+#define CASS_ENOMEM (-6)     /* device allocation failed */
+#define CASS_EUNSUPPORTED (-7) /* option not implemented on this path */
+
+/* arithmetic of the pair / trial energies */
+#define CASS_PREC_FP64 0   /* every operation in FP64 (reference arithmetic) */
+#define CASS_PREC_MIXED 1  /* FP32 pair math, FP64 accumulation and structure factors */
+
+/* VDW_Style / vdw sum styles (global_variables.f90: vdw_* parameters) */
+#define CASS_VDW_NONE 0
+#define CASS_VDW_LJ 1
+#define CASS_VDW_MIE 2
+#define CASS_VDW_SUM_CUT 0
+#define CASS_VDW_SUM_CUT_TAIL 1
+#define CASS_VDW_SUM_CUT_SHIFT 2
+#define CASS_VDW_SUM_MINIMUM 3
+#define CASS_VDW_SUM_CUT_SWITCH 4
+#define CASS_VDW_SUM_CHARMM 5
+#define CASS_VDW_SUM_CUT_SHIFT_FORCE 6
+
+/* Charge_Style */
+#define CASS_CHARGE_NONE 0
+#define CASS_CHARGE_COUL 1
+#define CASS_QQ_EWALD 0
+#define CASS_QQ_CUT 1
+#define CASS_QQ_MINIMUM 2
+#define CASS_QQ_DSF 3
+
+/* move_flag of Update_System_Ewald_Reciprocal_Energy (global_variables.f90:240-244) */
+#define CASS_MOVE_INSERTION 0
+#define CASS_MOVE_DELETION 1
+#define CASS_MOVE_TRANSLATION 2
+#define CASS_MOVE_ROTATION 3
+#define CASS_MOVE_INTRA 4
+
+/* bond / angle kinds */
+#define CASS_BONDED_FIXED 0
+#define CASS_BONDED_HARMONIC 1
+
+typedef struct cass_ctx cass_ctx;
+
+/* Sizes the context is created for.  max_molecules[is-1] is the number of
+ * molecule slots ("locates") of species is, as max_molecules in
+ * global_variables.f90. */
+typedef struct CassConfig {
+  int32_t nspecies;
+  int32_t ntypes;      /* number of nonbond atom types */
+  int32_t nboxes;
+  int32_t precision;   /* CASS_PREC_FP64 or CASS_PREC_MIXED */
+  int32_t device;      /* CUDA device ordinal (ignored by the CPU oracle) */
+  int32_t max_kvectors; /* capacity per box for Ewald k-vectors (maxk) */
+  const int32_t* max_molecules; /* [nspecies] */
+} CassConfig;
+
+/* One species: the parts of Species_Class / Nonbond_Class / bonded lists /
+ * Frag_Class (type_definitions.f90) that the hot path reads.  Atom and
+ * fragment indices inside are 1-based as in the .mcf file. */
+typedef struct CassSpeciesDesc {
+  int32_t natoms;
+  const int32_t* atom_type;          /* [natoms] 1-based nonbond type, 0 = no vdW */
+  const double* charge;              /* [natoms] */
+  const double* mass;                /* [natoms] */
+  const double* vdw_intra_scale;     /* [natoms*natoms], (ia-1)*natoms+(ja-1) */
+  const double* charge_intra_scale;  /* [natoms*natoms] */
+  const int32_t* bonded;             /* [natoms*natoms] l_bonded: 1-2 bonded pair */
+  int32_t nbonds;
+  const int32_t* bond_atoms;         /* [2*nbonds] */
+  const int32_t* bond_kind;          /* [nbonds] CASS_BONDED_* */
+  const double* bond_param;          /* [2*nbonds] fixed:(l0,tol) harmonic:(k,l0) */
+  int32_t nangles;
+  const int32_t* angle_atoms;        /* [3*nangles] */
+  const int32_t* angle_kind;         /* [nangles] */
+  const double* angle_param;         /* [2*nangles] fixed:(theta0 deg,tol deg) harmonic:(k, theta0 rad) */
+  int32_t ndihedrals;                /* Ryckaert-Bellemans form (OPLS converted on input) */
+  const int32_t* dihedral_atoms;     /* [4*ndihedrals] */
+  const double* dihedral_rb;         /* [6*ndihedrals] c0..c5 */
+  int32_t nimpropers;                /* harmonic impropers */
+  const int32_t* improper_atoms;     /* [4*nimpropers] */
+  const double* improper_param;      /* [2*nimpropers] (k, phi0 rad) */
+  /* CBMC fragments (Fragment_Info / Fragment_Connectivity / fragment libraries) */
+  int32_t nfragments;
+  const int32_t* frag_natoms;        /* [nfragments] */
+  const int32_t* frag_atoms;         /* concatenated; the first atom of each fragment is its anchor */
+  const int32_t* frag_nconnect;      /* [nfragments] */
+  const int32_t* frag_connect;       /* concatenated connected fragment ids */
+  const int32_t* frag_nconfig;       /* [nfragments] library size */
+  const double* frag_library;        /* concatenated [nconfig][frag_natoms][3] */
+  int32_t l_coul_cbmc;               /* species_list%L_Coul_CBMC */
+} CassSpeciesDesc;
+
+/* One simulation box (Box_Class + the per-box cutoffs and styles). */
+typedef struct CassBoxDesc {
+  double length[3];       /* orthorhombic edges (cubic when all equal), A */
+  int32_t vdw_style;      /* CASS_VDW_* */
+  int32_t vdw_sum_style;  /* CASS_VDW_SUM_* */
+  double rcut_vdw, rcut_coul, rcut_cbmc, rcut_low;
+  double ron_switch, roff_switch;  /* cut_switch only */
+  int32_t charge_style;      /* CASS_CHARGE_* */
+  int32_t charge_sum_style;  /* CASS_QQ_* */
+  double ewald_tol;          /* alpha, h_cut derived as input_routines.f90:711-716 */
+  double alpha_dsf;          /* <= 0: default of input_routines.f90:742-747 */
+  double temperature;        /* K */
+} CassBoxDesc;
+
+/* energy(ibox) components (Energy_Class, type_definitions.f90) */
+typedef struct CassEnergy {
+  double total, intra, bond, angle, dihedral, improper;
+  double intra_vdw, intra_q, inter, inter_vdw, inter_q;
+  double lrc, reciprocal, self;
+} CassEnergy;
+
+/* Result of one Widom_Insert call (widom_insert.f90:22) for one box. */
+typedef struct CassWidomResult {
+  double widom_sum;      /* sum of widom_var times the prefactor (widom_insert.f90:538) */
+  double prefactor;      /* V / ((N+1) Lambda^3), Lambda = 1 here (de Broglie applied by the host) */
+  int64_t n_insertions;
+  int64_t n_overlaps;
+  int64_t n_trials;      /* CBMC trial energies evaluated (kappa_ins + (nfrag-1)*kappa_dih per insertion) */
+} CassWidomResult;
+
+/* Per-insertion record, optional output for parity checks. */
+typedef struct CassWidomTrace {
+  double widom_var;      /* exp(-beta(dE - dE_frag) - ln_pbias), 0 on overlap */
+  double ln_pbias;
+  double e_inter;        /* full-cutoff inter energy incl. periodic qq and reciprocal */
+  double e_first_trial_sum; /* sum of the kappa_ins first-fragment trial energies (non-overlap) */
+  int32_t selected_trial;   /* first fragment trial chosen, 1-based, 0 if none */
+  int32_t overlap;          /* 1 cbmc, 2 inter, 3 intra overlap */
+} CassWidomTrace;
+
+/* ---- context ---------------------------------------------------------- */
+int cass_abi_version(void);
+const char* cass_last_error(void);      /* thread-local text of the last failure */
+int cass_ctx_create(const CassConfig* cfg, cass_ctx** out);
+int cass_ctx_destroy(cass_ctx* ctx);
+
+/* vdw_param1..4_table(ntypes,ntypes) after mixing (create_nonbond_table.f90:207-210);
+ * row-major [(itype-1)*ntypes+(jtype-1)] */
+int cass_set_nonbond_table(cass_ctx* ctx, int32_t ntypes, const double* eps,
+                           const double* sig, const double* mie_n, const double* mie_m);
+int cass_set_species(cass_ctx* ctx, int32_t is, const CassSpeciesDesc* desc);
+/* Box set-up; for Ewald boxes also Ewald_Reciprocal_Lattice_Vector_Setup
+ * (energy_routines.f90:2170-2323). */
+int cass_set_box(cass_ctx* ctx, int32_t ibox, const CassBoxDesc* desc);
+/* Writes atom_list coordinates of n molecules and marks them live in ibox[k]
+ * (all atoms exist).  xyz holds natoms(is[k])*3 doubles per molecule. */
+int cass_set_molecules(cass_ctx* ctx, int32_t n, const int32_t* im, const int32_t* is,
+                       const int32_t* ibox, const double* xyz);
+/* Marks molecule (im,is) not live (molecule_list%live = .FALSE.). */
+int cass_remove_molecule(cass_ctx* ctx, int32_t im, int32_t is);
+/* Reads back the coordinates of molecule (im,is). */
+int cass_get_molecule(cass_ctx* ctx, int32_t im, int32_t is, double* xyz);
+
+/* ---- energy routines -------------------------------------------------- */
+/* Compute_Molecule_Nonbond_Inter_Energy (energy_routines.f90:1088-1206);
+ * cbmc_flag selects the rcut_cbmc cutoffs of Check_AtomPair_Cutoff. */
+int cass_mol_inter_energy(cass_ctx* ctx, int32_t im, int32_t is, int32_t cbmc_flag,
+                          double* e_inter_vdw, double* e_inter_qq, int32_t* overlap);
+/* Compute_Molecule_Nonbond_Intra_Energy (energy_routines.f90:980-1085) */
+int cass_mol_intra_energy(cass_ctx* ctx, int32_t im, int32_t is, int32_t cbmc_flag,
+                          double* e_intra_vdw, double* e_intra_qq, double* e_inter_qq,
+                          int32_t* overlap);
+/* Compute_System_Total_Energy (energy_routines.f90:2648-2953), including
+ * Compute_System_Ewald_Reciprocal_Energy (:4111-4231), the self energy
+ * (:2553-2601) and Compute_LR_Correction (:2956-3023).  Rebuilds the
+ * structure factors cos_sum/sin_sum and cos_mol/sin_mol of the box. */
+int cass_system_total_energy(cass_ctx* ctx, int32_t ibox, int32_t intra_flag,
+                             CassEnergy* out, int32_t* overlap);
+/* Update_System_Ewald_Reciprocal_Energy (energy_routines.f90:2326-2497).
+ * Saves cos_sum/sin_sum (and the molecule's cos_mol/sin_mol) so that
+ * cass_ewald_restore can revert a rejected move (move_translate.f90:296-305). */
+int cass_ewald_update(cass_ctx* ctx, int32_t im, int32_t is, int32_t ibox,
+                      int32_t move_flag, double* e_reciprocal);
+int cass_ewald_restore(cass_ctx* ctx, int32_t im, int32_t is, int32_t ibox);
+/* Update_System_Ewald_Reciprocal_Energy_Widom (energy_routines.f90:2500-2550),
+ * batched: n test molecules of species is, coordinates [n][natoms][3];
+ * writes n absolute reciprocal energies. */
+int cass_ewald_widom(cass_ctx* ctx, int32_t is, int32_t ibox, int32_t n,
+                     const double* xyz, double* e_reciprocal);
+
+/* ---- CBMC / Widom ----------------------------------------------------- */
+/* Widom_Insert (widom_insert.f90:22-594) with Build_Molecule /
+ * Fragment_Placement (fragment_growth.f90:72-707,1449-2132) for every
+ * insertion, batched over nboxes boxes in one launch.  Insertion k of box b
+ * draws its random numbers from an lfsr258 stream seeded by (seed, b, k)
+ * (the same stream in the CPU oracle).  Requires a prior
+ * cass_system_total_energy of each listed box.  trace may be NULL; else it
+ * receives nboxes*n_insertions records, box-major. */
+int cass_widom_insert(cass_ctx* ctx, int32_t is, int32_t nboxes, const int32_t* ibox,
+                      int64_t n_insertions, int32_t kappa_ins, int32_t kappa_dih,
+                      uint64_t seed, CassWidomResult* out, CassWidomTrace* trace);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CASSANDRA_GB300_H */
