@@ -1,0 +1,364 @@
+"""Benchmark: batched CBMC Widom insertion (trial energies/s) on GB300.
+
+Workload: n-butane (4-site united atom, 2 CBMC fragments) inserted into 64
+frozen LJ boxes of uneven size (N uniform in 200..4000, rho* = 0.6, sigma 3.73 A,
+eps/k 148 K, 14 A cut_tail, rcut_cbmc 6.5 A, T 150 K) with kappa_ins = 12 and
+kappa_dih = 12, i.e. 24 trial energies per insertion; one step = 10^6
+insertions (15,625 per box) in one batched call.  Synthetic, seeded inputs.
+
+value : trial energies/s of the mixed-precision path, device time (CUDA events
+        around each step on the library's stream), inputs resident in HBM,
+        L2 flushed between steps.
+e2e   : the same metric through the public API with host buffers: upload the
+        frame, system energies of every box, Widom batch, results back.
+Also reported: the plain-FP64 GPU path on the same workload, the roofline of
+the Widom kernel, and the CPU FP64 oracle (OpenMP, all host cores) on a
+bounded sample.  `--impl reference` times the CPU restatement of the
+reference's algorithm (the reference itself is Fortran and cannot be built
+here) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "CBMC/Widom trial energies/s and MC sweeps/s vs plain FP64 GPU at stated error"
+UNIT = "trial energies/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--boxes", type=int, default=64)
+    p.add_argument("--insertions", type=int, default=1_000_000, help="insertions per step, all boxes")
+    p.add_argument("--kappa", type=int, default=12)
+    p.add_argument("--seed", type=int, default=2024)
+    p.add_argument("--fp64-steps", type=int, default=2)
+    p.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU-baseline sample length")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(args, rank):
+    from cassandra_gb300 import workloads
+    return workloads.widom_batch_system(nboxes=args.boxes, seed=args.seed, nconfig=1000)
+
+
+def cpu_baseline(system, args, per_box_cap=None):
+    """CPU FP64 oracle (restatement of the reference's Widom loop), OpenMP over insertions."""
+    from oracle import oracle
+    boxes = list(range(1, len(system.boxes) + 1))
+    with oracle.open_system(system) as o:
+        for b in boxes:
+            o.system_total_energy(b)
+        # calibrate on a small sample, then size the run to ~cpu_seconds
+        t0 = time.perf_counter()
+        o.widom_insert(2, boxes, 8, args.kappa, args.kappa, seed=1)
+        dt = max(time.perf_counter() - t0, 1e-3)
+        per = dt / (8 * len(boxes))
+        n = max(8, int(args.cpu_seconds / (per * len(boxes))))
+        if per_box_cap:
+            n = min(n, per_box_cap)
+        t0 = time.perf_counter()
+        res = o.widom_insert(2, boxes, n, args.kappa, args.kappa, seed=99)
+        dt = time.perf_counter() - t0
+    trials = sum(r["n_trials"] for r in res)
+    return {"value": trials / dt, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"{len(boxes)} boxes x {n} insertions ({trials} trial energies) in {dt:.2f} s, "
+                      f"FP64 C++ oracle, OpenMP over insertions"}
+
+
+def flush_l2(torch, buf):
+    buf.zero_()
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    system = build_workload(args, rank)
+    from oracle import oracle
+    boxes = list(range(1, len(system.boxes) + 1))
+    vals, times = [], []
+    with oracle.open_system(system) as o:
+        for b in boxes:
+            o.system_total_energy(b)
+        t0 = time.perf_counter()
+        o.widom_insert(2, boxes, 4, args.kappa, args.kappa, seed=1)
+        per = max(time.perf_counter() - t0, 1e-3) / (4 * len(boxes))
+        n = max(4, int(args.cpu_seconds / 3.0 / (per * len(boxes))))
+        for s in range(args.warmup):
+            o.widom_insert(2, boxes, 2, args.kappa, args.kappa, seed=1000 + s)
+        for s in range(args.steps):
+            t0 = time.perf_counter()
+            res = o.widom_insert(2, boxes, n, args.kappa, args.kappa, seed=s + 1)
+            dt = time.perf_counter() - t0
+            trials = sum(r["n_trials"] for r in res)
+            vals.append(trials / dt)
+            times.append(dt)
+    value = float(np.sum([v * t for v, t in zip(vals, times)]) / np.sum(times))
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * float(np.mean(times)),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "butane CBMC Widom into 64 frozen LJ boxes (N 200-4000, rho*=0.6), "
+                                  "kappa_ins=12, kappa_dih=12", "boxes": len(boxes),
+                      "insertions_per_step": n * len(boxes), "sample_per_box": n},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+                            "sample": f"{len(boxes)} boxes x {n} insertions per step; the reference is Fortran and "
+                                      f"no Fortran compiler exists here, so its C++ FP64 restatement is timed"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+    import cassandra_gb300 as cg
+    from cassandra_gb300 import abi, build
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    build.build()
+    dev = local
+    torch.cuda.set_device(dev)
+    system = build_workload(args, rank)
+    boxes = list(range(1, len(system.boxes) + 1))
+    n_per_box = max(1, args.insertions // len(boxes))
+    trials_per_ins = args.kappa + args.kappa  # kappa_ins + (nfrag - 1) kappa_dih, butane has 2 fragments
+    stream = torch.cuda.Stream(device=dev)
+    l2 = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def timed_steps(ctx, steps, warmup, seed0):
+        ctx.set_stream(stream.cuda_stream)
+        for s in range(warmup):
+            ctx.widom_insert(2, boxes, n_per_box, args.kappa, args.kappa, seed=seed0 + 1000 + s)
+        st0 = ctx.stats()
+        per_step, kern = [], []
+        barrier()
+        torch.cuda.synchronize()
+        for s in range(steps):
+            with torch.cuda.stream(stream):
+                flush_l2(torch, l2)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            res = ctx.widom_insert(2, boxes, n_per_box, args.kappa, args.kappa, seed=seed0 + s + rank * 7919)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            per_step.append(e0.elapsed_time(e1))
+            kern.append(ctx.stats()["widom_kernel_ms"])
+        barrier()
+        st1 = ctx.stats()
+        return per_step, kern, res, st1["kernel_launches"] - st0["kernel_launches"]
+
+    # headline: mixed precision
+    gctx = cg.open_system(system, precision=abi.PREC_MIXED, device=dev)
+    for b in boxes:
+        gctx.system_total_energy(b)
+    clocks = ClockSampler(dev)
+    clocks.start()
+    t_wall0 = time.perf_counter()
+    ms, kms, res, launches = timed_steps(gctx, args.steps, args.warmup, args.seed)
+    t_wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    total_ms = float(np.sum(ms))
+    if dist is not None:
+        t = torch.tensor([total_ms], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    trials_step = n_per_box * len(boxes) * trials_per_ins
+    value = trials_step * args.steps * world / (total_ms / 1000.0)
+    # work counts for the roofline (one extra, untimed pass)
+    gctx.set_count_pairs(True)
+    gctx.widom_insert(2, boxes, n_per_box, args.kappa, args.kappa, seed=args.seed + 555)
+    st = gctx.stats()
+    gctx.set_count_pairs(False)
+    # plain FP64 GPU path on the same workload
+    fctx = cg.open_system(system, precision=abi.PREC_FP64, device=dev)
+    for b in boxes:
+        fctx.system_total_energy(b)
+    fms, fkms, _, _ = timed_steps(fctx, args.fp64_steps, 1, args.seed)
+    fp64_value = trials_step * len(fms) / (float(np.sum(fms)) / 1000.0)
+    # accuracy of the mixed path against FP64 on this workload (per-insertion trace of a sub-batch)
+    sub = boxes[:8]
+    ra, ta = fctx.widom_insert(2, sub, 2000, args.kappa, args.kappa, seed=4242, trace=True)
+    rb, tb = gctx.widom_insert(2, sub, 2000, args.kappa, args.kappa, seed=4242, trace=True)
+    same = (ta["overlap"] == tb["overlap"]) & (ta["selected_trial"] == tb["selected_trial"])
+    ok = same & (ta["overlap"] == 0)
+    rel = np.abs(tb["e_inter"][ok] - ta["e_inter"][ok]) / np.maximum(np.abs(ta["e_inter"][ok]), 100.0)
+    accuracy = {"same_trial_selection": float(same.mean()),
+                "e_inter_max_rel_err": float(rel.max()) if rel.size else None,
+                "e_inter_mean_rel_err": float(rel.mean()) if rel.size else None,
+                "insertions_compared": int(same.size)}
+    fctx.close()
+
+    # roofline of the Widom kernel
+    from cassandra_gb300 import system as sysmod
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    kern_ms = float(np.mean(kms))
+    natoms = [sum(1 for bi in system.molecules.ibox if bi == b) for b in boxes]
+    box_bytes = 0
+    for b, na in zip(boxes, natoms):
+        L = system.boxes[b - 1].length[0]
+        nc = max(1, int(L // system.boxes[b - 1].rcut_cbmc)) ** 3
+        box_bytes += st["widom_grid_x"] * (na * 16 + (nc + 1) * 4)
+    alg_bytes = n_per_box * len(boxes) * 33 + box_bytes
+    achieved_gbs = alg_bytes / (kern_ms / 1000.0) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "k_widom_traffic.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            pj = json.load(f)
+        traffic = pj.get("dram_bytes_per_insertion", 0.0) * n_per_box * len(boxes) or None
+    flops = st["widom_pairs_visited"] * 15 + st["widom_pairs_in_cutoff"] * 8
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak = sm_count * 128 * 2 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+    achieved_tf = flops / (kern_ms / 1000.0) / 1e12
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "fp32 pair math / fp64 accumulation", "data": "synthetic",
+           "config": {"workload": "butane CBMC Widom into 64 frozen LJ boxes (N 200-4000, rho*=0.6), "
+                                  "kappa_ins=12, kappa_dih=12, 24 trial energies per insertion",
+                      "boxes": len(boxes), "insertions_per_step": n_per_box * len(boxes),
+                      "trial_energies_per_step": trials_step, "atoms_total": int(sum(natoms)),
+                      "l2": "flushed (256 MB write) between timed steps", "precision": "mixed",
+                      "parallelism": f"replicas x{world}"},
+           "gpu_launches": int(launches),
+           "wall_s": t_wall,
+           "fp64_gpu": {"value": fp64_value, "unit": UNIT, "ms_per_step": float(np.mean(fms)),
+                        "kernel_ms": float(np.mean(fkms)), "mixed_over_fp64": value / world / fp64_value},
+           "accuracy_vs_fp64": accuracy,
+           "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                        "frac": achieved_gbs / hbm_peak, "traffic": traffic,
+                        "note": "k_widom; algorithmic bytes = 33 B record per insertion + box staged once per CTA "
+                                "(peak of measured)"},
+           "compute_roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
+                                "frac": achieved_tf / fp32_peak, "pairs_visited": st["widom_pairs_visited"],
+                                "pairs_in_cutoff": st["widom_pairs_in_cutoff"],
+                                "note": "15 FP32 ops per visited pair + 8 per in-cutoff LJ pair; peak is nominal "
+                                        "(SMs x 128 lanes x 2 x max SM clock), not measured"},
+           "kernel_ms": kern_ms, "clocks": clk}
+
+    # end to end through the public API with host buffers (frame upload, energies, Widom, results back)
+    if not args.no_e2e:
+        xyz_frames = system.molecules.flat_xyz()
+        ims, iss, ibs = system.molecules.im, system.molecules.is_, system.molecules.ibox
+        e2e_steps = max(1, min(args.steps, 3))
+        s0 = gctx.stats()
+        gctx.set_stream(stream.cuda_stream)
+        t0 = time.perf_counter()
+        for s in range(e2e_steps):
+            gctx.set_molecules(ims, iss, ibs, xyz_frames)
+            for b in boxes:
+                gctx.system_total_energy(b)
+            gctx.widom_insert(2, boxes, n_per_box, args.kappa, args.kappa, seed=args.seed + 77 + s)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        s1 = gctx.stats()
+        out["e2e"] = {"value": trials_step * e2e_steps / dt, "unit": UNIT,
+                      "h2d_bytes_per_step": int((s1["h2d_bytes"] - s0["h2d_bytes"]) / e2e_steps),
+                      "d2h_bytes_per_step": int((s1["d2h_bytes"] - s0["d2h_bytes"]) / e2e_steps),
+                      "steps": e2e_steps,
+                      "note": "per step: set_molecules of all boxes, system_total_energy of each box, widom_insert; "
+                              "host wall clock"}
+    gctx.close()
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(system, args)
+    if rank == 0:
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

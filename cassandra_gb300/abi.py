@@ -80,6 +80,16 @@ class CassWidomTrace(C.Structure):
                 ("e_first_trial_sum", C.c_double), ("selected_trial", C.c_int32), ("overlap", C.c_int32)]
 
 
+class CassStats(C.Structure):
+    _fields_ = [("widom_ms", C.c_double), ("widom_kernel_ms", C.c_double), ("kernel_launches", C.c_int64),
+                ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("widom_pairs_visited", C.c_int64),
+                ("widom_pairs_in_cutoff", C.c_int64), ("widom_grid_x", C.c_int32), ("widom_grid_y", C.c_int32),
+                ("widom_block", C.c_int32), ("widom_smem_bytes", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 TRACE_DTYPE = np.dtype([("widom_var", "f8"), ("ln_pbias", "f8"), ("e_inter", "f8"),
                         ("e_first_trial_sum", "f8"), ("selected_trial", "i4"), ("overlap", "i4")])
 assert TRACE_DTYPE.itemsize == C.sizeof(CassWidomTrace)
@@ -104,7 +114,12 @@ SIGNATURES = {
     "ewald_widom": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _f64p, _f64p]),
     "widom_insert": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _i32p, C.c_int64, C.c_int32, C.c_int32,
                                C.c_uint64, C.POINTER(CassWidomResult), C.c_void_p]),
+    # run-time extensions of the GPU library (no counterpart in the reference)
+    "get_stats": (C.c_int, [C.c_void_p, C.POINTER(CassStats)]),
+    "set_count_pairs": (C.c_int, [C.c_void_p, C.c_int32]),
+    "set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
+OPTIONAL = {"get_stats", "set_count_pairs", "set_stream"}
 
 
 class CassError(RuntimeError):
@@ -117,6 +132,8 @@ def bind(lib: C.CDLL, prefix: str) -> dict:
     """Bind every entry point of the header under `prefix`; returns name -> function."""
     out = {}
     for name, (res, args) in SIGNATURES.items():
+        if name in OPTIONAL and not hasattr(lib, prefix + name):
+            continue
         f = getattr(lib, prefix + name)
         f.restype = res
         f.argtypes = args
@@ -255,6 +272,17 @@ class Context:
         out = np.zeros(n)
         self._check("ewald_widom", self._f["ewald_widom"](self._h, is_, ibox, n, _p(x), _p(out)))
         return out
+
+    def stats(self) -> dict:
+        st = CassStats()
+        self._check("get_stats", self._f["get_stats"](self._h, C.byref(st)))
+        return st.as_dict()
+
+    def set_count_pairs(self, on: bool) -> None:
+        self._check("set_count_pairs", self._f["set_count_pairs"](self._h, int(on)))
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        self._check("set_stream", self._f["set_stream"](self._h, C.c_void_p(stream_ptr) if stream_ptr else None))
 
     def widom_insert(self, is_: int, boxes: Sequence[int], n_insertions: int, kappa_ins: int,
                      kappa_dih: int, seed: int, trace: bool = False):

@@ -1,0 +1,1268 @@
+// cass_abi.cu -- C-ABI entry points of libcassgpu.so and the energy kernels
+// that back them:
+//   k_mol_inter      Compute_Molecule_Nonbond_Inter_Energy   (energy_routines.f90:1088-1206)
+//   k_pair_total     inter-molecular part of Compute_System_Total_Energy (:2775-2917)
+//   k_intra_total    intra + bonded part of Compute_System_Total_Energy  (:2697-2769)
+//   k_sfac / k_sfac_reduce  Compute_System_Ewald_Reciprocal_Energy     (:4111-4231)
+//   k_ewald_update   Update_System_Ewald_Reciprocal_Energy   (:2326-2497)
+//   k_ewald_widom    Update_System_Ewald_Reciprocal_Energy_Widom (:2500-2550)
+// Reductions are deterministic: each block writes a partial, the last block to
+// finish sums the partials in a fixed order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cass_ctx.h"
+
+namespace cassgpu {
+
+static thread_local std::string g_err;
+
+int set_error(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+int cuda_error(cudaError_t e, const char* where) {
+  g_err = std::string(where) + ": " + cudaGetErrorString(e);
+  return CASS_ECUDA;
+}
+
+cudaError_t h2d(cass_ctx_impl* c, void* dst, const void* src, size_t n) {
+  c->stats.h2d_bytes += (int64_t)n;
+  return cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, c->stream);
+}
+
+cudaError_t d2h(cass_ctx_impl* c, void* dst, const void* src, size_t n) {
+  c->stats.d2h_bytes += (int64_t)n;
+  return cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, c->stream);
+}
+
+// packed molecule record: mol slot, species (0-based), first packed atom, natoms
+using MolInfo = int4;
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  int nw = (blockDim.x + 31) >> 5;
+  v = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+  if (w == 0)
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;  // valid in thread 0
+}
+
+// Writes NV partial sums of this block, then the last block to finish sums
+// all partials (fixed order) into out[0..NV).  counter must start at 0 and is
+// reset by the last block.
+template <int NV>
+__device__ void reduce_partials(double (&v)[NV], double* partial, unsigned* counter, double* out, int* flag_in,
+                                int flag_val) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  int nb = gridDim.x * gridDim.y;
+  int bid = blockIdx.y * gridDim.x + blockIdx.x;
+  for (int k = 0; k < NV; ++k) {
+    double s = block_sum(v[k], sh);
+    if (threadIdx.x == 0) partial[(size_t)bid * NV + k] = s;
+  }
+  (void)flag_in;
+  (void)flag_val;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == (unsigned)(nb - 1));
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int k = 0; k < NV; ++k) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) s += __ldcg(&partial[(size_t)b * NV + k]);
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) out[k] = s;
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+// ---------------------------------------------------------------------------
+// K1: one molecule against every other live molecule of its box.
+template <bool MIXED>
+__global__ void __launch_bounds__(kBlock) k_mol_inter(BoxDev b, PairTable t, const double4_32a* __restrict__ p64,
+                                                      const float4* __restrict__ p32, const int4* __restrict__ meta,
+                                                      int n, int qslot, int qoff, int qn, int cbmc, int want_qq,
+                                                      double* partial, unsigned* counter, double* out, int* ovflag) {
+  __shared__ double4_32a qa[kMaxAtoms * 4];
+  __shared__ int qt[kMaxAtoms * 4];
+  for (int a = threadIdx.x; a < qn; a += blockDim.x) {
+    qa[a] = p64[qoff + a];
+    qt[a] = meta[qoff + a].y;
+  }
+  __syncthreads();
+  double ev = 0.0, eq = 0.0;
+  KahanF fv, fq;
+  bool ov = false;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    int4 mj = meta[j];
+    if (mj.x == qslot) continue;
+    double4_32a pj = p64[j];
+    for (int a = 0; a < qn; ++a) {
+      double dx = fold(qa[a].x - pj.x, b.hL[0], b.L[0]);
+      double dy = fold(qa[a].y - pj.y, b.hL[1], b.L[1]);
+      double dz = fold(qa[a].z - pj.z, b.hL[2], b.L[2]);
+      double r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 < b.rcut_lowsq) {
+        ov = true;
+        continue;
+      }
+      int m = cutoff_mask(b, r2, cbmc != 0);
+      if (!want_qq) m &= 1;
+      if (MIXED && b.vdw_style == CASS_VDW_LJ &&
+          (b.vdw_sum_style == CASS_VDW_SUM_CUT || b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL ||
+           b.vdw_sum_style == CASS_VDW_SUM_MINIMUM || cbmc)) {
+        if ((m & 1) && qt[a] >= 0 && mj.y >= 0) {
+          int k = pidx(qt[a], mj.y, t.ntypes);
+          fv.add(lj_pair_f(t.epsf[k], t.sig2f[k], (float)r2));
+        }
+      } else if (m & 1) {
+        ev += vdw_pair(t, b, qt[a], mj.y, r2, 1.0);
+      }
+      if (m & 2) {
+        if (MIXED && b.charge_sum_style == CASS_QQ_EWALD)
+          fq.add(qq_ewald_inter_f((float)b.alpha, (float)(qa[a].w * pj.w), (float)r2));
+        else
+          eq += qq_pair_inter(b, qa[a].w * pj.w, r2);
+      }
+    }
+  }
+  if (ov) atomicOr(ovflag, 1);
+  double v[2] = {ev + fv.value(), eq + fq.value()};
+  reduce_partials<2>(v, partial, counter, out, nullptr, 0);
+}
+
+// ---------------------------------------------------------------------------
+// K6a: all inter-molecular pairs of a box (pairs (i,j), j > i, different molecules).
+constexpr int kTileJ = 2048;
+
+template <bool MIXED>
+__global__ void __launch_bounds__(kBlock) k_pair_total(BoxDev b, PairTable t, const double4_32a* __restrict__ p64,
+                                                       const int4* __restrict__ meta, int n, double* partial,
+                                                       unsigned* counter, double* out, int* ovflag) {
+  __shared__ double4_32a sj[kBlock];
+  __shared__ int4 sm[kBlock];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double4_32a pi = i < n ? p64[i] : make_double4_32a(0, 0, 0, 0);
+  int4 mi = i < n ? meta[i] : make_int4(-1, -1, -1, -1);
+  double ev = 0.0, eq = 0.0;
+  KahanF fv, fq;
+  bool ov = false;
+  int j0 = blockIdx.y * kTileJ;
+  int j1 = min(n, j0 + kTileJ);
+  int ilo = blockIdx.x * blockDim.x;
+  if (j1 > ilo + 1) {
+    for (int jt = max(j0, ilo); jt < j1; jt += kBlock) {
+      __syncthreads();
+      int jj = jt + threadIdx.x;
+      if (jj < j1) {
+        sj[threadIdx.x] = p64[jj];
+        sm[threadIdx.x] = meta[jj];
+      }
+      __syncthreads();
+      int cnt = min(kBlock, j1 - jt);
+      if (i < n) {
+        for (int k = 0; k < cnt; ++k) {
+          int j = jt + k;
+          if (j <= i) continue;
+          int4 mj = sm[k];
+          if (mj.x == mi.x) continue;
+          double4_32a pj = sj[k];
+          double dx = fold(pi.x - pj.x, b.hL[0], b.L[0]);
+          double dy = fold(pi.y - pj.y, b.hL[1], b.L[1]);
+          double dz = fold(pi.z - pj.z, b.hL[2], b.L[2]);
+          double r2 = dx * dx + dy * dy + dz * dz;
+          if (r2 < b.rcut_lowsq) {
+            ov = true;
+            continue;
+          }
+          int m = cutoff_mask(b, r2, false);
+          if (m & 1) {
+            if (MIXED && b.vdw_style == CASS_VDW_LJ &&
+                (b.vdw_sum_style == CASS_VDW_SUM_CUT || b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL ||
+                 b.vdw_sum_style == CASS_VDW_SUM_MINIMUM)) {
+              if (mi.y >= 0 && mj.y >= 0) {
+                int kk = pidx(mi.y, mj.y, t.ntypes);
+                fv.add(lj_pair_f(t.epsf[kk], t.sig2f[kk], (float)r2));
+              }
+            } else {
+              ev += vdw_pair(t, b, mi.y, mj.y, r2, 1.0);
+            }
+          }
+          if (m & 2) {
+            if (MIXED && b.charge_sum_style == CASS_QQ_EWALD)
+              fq.add(qq_ewald_inter_f((float)b.alpha, (float)(pi.w * pj.w), (float)r2));
+            else
+              eq += qq_pair_inter(b, pi.w * pj.w, r2);
+          }
+        }
+      }
+    }
+  }
+  if (ov) atomicOr(ovflag, 1);
+  double v[2] = {ev + fv.value(), eq + fq.value()};
+  reduce_partials<2>(v, partial, counter, out, nullptr, 0);
+}
+
+__global__ void __launch_bounds__(kBlock) k_intra_total(BoxDev b, PairTable t, SpeciesPools P,
+                                                        const double4_32a* __restrict__ p64,
+                                                        const MolInfo* __restrict__ mols, int nm, double* partial,
+                                                        unsigned* counter, double* out, int* ovflag) {
+  double v[7] = {0, 0, 0, 0, 0, 0, 0};
+  double r[3 * 64];
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nm; m += gridDim.x * blockDim.x) {
+    MolInfo mi = mols[m];
+    int na = min(mi.w, 64);
+    for (int a = 0; a < na; ++a) {
+      double4_32a p = p64[mi.z + a];
+      r[3 * a] = p.x;
+      r[3 * a + 1] = p.y;
+      r[3 * a + 2] = p.z;
+    }
+    IntraOut o = molecule_intra(P, mi.y, b, t, r);
+    if (o.overlap) {
+      atomicOr(ovflag, 1);
+      continue;
+    }
+    v[0] += o.bond;
+    v[1] += o.angle;
+    v[2] += o.dih;
+    v[3] += o.imp;
+    v[4] += o.ivdw;
+    v[5] += o.iqq;
+    v[6] += o.pqq;
+  }
+  reduce_partials<7>(v, partial, counter, out, nullptr, 0);
+}
+
+// ---------------------------------------------------------------------------
+// Ewald structure factors.  kvec[k] = (hx, hy, hz, Cn).
+constexpr int kSfacMolChunk = 64;
+
+__global__ void __launch_bounds__(128) k_sfac(const double4_32a* __restrict__ kvec, int nv, const double4_32a* __restrict__ p64,
+                                              const MolInfo* __restrict__ mols, int nm, const int* __restrict__ charged,
+                                              double* cos_mol, double* sin_mol, int stride, double2* part) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  int m0 = blockIdx.y * kSfacMolChunk, m1 = min(nm, m0 + kSfacMolChunk);
+  if (k >= nv) return;
+  double4_32a h = kvec[k];
+  double cs = 0.0, sn = 0.0;
+  for (int m = m0; m < m1; ++m) {
+    MolInfo mi = mols[m];
+    if (!charged[mi.y]) continue;
+    double c = 0.0, s = 0.0;
+    for (int a = 0; a < mi.w; ++a) {
+      double4_32a p = p64[mi.z + a];
+      double hdotr = h.x * p.x + h.y * p.y + h.z * p.z;
+      double sv, cv;
+      sincos(hdotr, &sv, &cv);
+      c = c + p.w * cv;
+      s = s + p.w * sv;
+    }
+    cos_mol[(size_t)mi.x * stride + k] = c;
+    sin_mol[(size_t)mi.x * stride + k] = s;
+    cs += c;
+    sn += s;
+  }
+  part[(size_t)blockIdx.y * nv + k] = make_double2(cs, sn);
+}
+
+__global__ void __launch_bounds__(kBlock) k_sfac_reduce(const double4_32a* __restrict__ kvec, int nv, const double2* part,
+                                                        int nchunks, double* cos_sum, double* sin_sum, double* partial,
+                                                        unsigned* counter, double* out) {
+  double e = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nv; k += gridDim.x * blockDim.x) {
+    double c = 0.0, s = 0.0;
+    for (int ch = 0; ch < nchunks; ++ch) {
+      double2 p = part[(size_t)ch * nv + k];
+      c += p.x;
+      s += p.y;
+    }
+    cos_sum[k] = c;
+    sin_sum[k] = s;
+    e += kvec[k].w * (c * c + s * s);
+  }
+  double v[1] = {e};
+  reduce_partials<1>(v, partial, counter, out, nullptr, 0);
+}
+
+// Update_System_Ewald_Reciprocal_Energy: thread per k-vector.
+__global__ void __launch_bounds__(kBlock) k_ewald_update(const double4_32a* __restrict__ kvec, int nv,
+                                                         const double4_32a* __restrict__ q_atoms, int qn, int move_flag,
+                                                         double* cos_sum, double* sin_sum, double* cos_mol,
+                                                         double* sin_mol, double* partial, unsigned* counter,
+                                                         double* out) {
+  double e = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nv; k += gridDim.x * blockDim.x) {
+    double4_32a h = kvec[k];
+    double c = cos_sum[k], s = sin_sum[k];
+    if (move_flag == CASS_MOVE_DELETION) {
+      c = c - cos_mol[k];
+      s = s - sin_mol[k];
+    } else {
+      double cn = 0.0, sn = 0.0;
+      for (int a = 0; a < qn; ++a) {
+        double4_32a p = q_atoms[a];
+        double hdotr = h.x * p.x + h.y * p.y + h.z * p.z;
+        double sv, cv;
+        sincos(hdotr, &sv, &cv);
+        cn = cn + p.w * cv;
+        sn = sn + p.w * sv;
+      }
+      if (move_flag == CASS_MOVE_INSERTION) {
+        c = c + cn;
+        s = s + sn;
+      } else {
+        c = c + (cn - cos_mol[k]);
+        s = s + (sn - sin_mol[k]);
+      }
+      cos_mol[k] = cn;
+      sin_mol[k] = sn;
+    }
+    cos_sum[k] = c;
+    sin_sum[k] = s;
+    e = e + h.w * (c * c + s * s);
+  }
+  double v[1] = {e};
+  reduce_partials<1>(v, partial, counter, out, nullptr, 0);
+}
+
+// Update_System_Ewald_Reciprocal_Energy_Widom: block per test molecule.
+__global__ void __launch_bounds__(kBlock) k_ewald_widom(const double4_32a* __restrict__ kvec, int nv,
+                                                        const double* __restrict__ cos_sum,
+                                                        const double* __restrict__ sin_sum, const double* __restrict__ xyz,
+                                                        const double* __restrict__ q, int na, double* out) {
+  __shared__ double sh[32];
+  const double* r = xyz + (size_t)blockIdx.x * 3 * na;
+  double e = 0.0;
+  for (int k = threadIdx.x; k < nv; k += blockDim.x) {
+    double4_32a h = kvec[k];
+    double dc = 0.0, ds = 0.0;
+    for (int a = 0; a < na; ++a) {
+      double hdotr = h.x * r[3 * a] + h.y * r[3 * a + 1] + h.z * r[3 * a + 2];
+      double sv, cv;
+      sincos(hdotr, &sv, &cv);
+      dc += q[a] * cv;
+      ds += q[a] * sv;
+    }
+    double c = cos_sum[k] + dc, s = sin_sum[k] + ds;
+    e = e + h.w * (c * c + s * s);
+  }
+  e = block_sum(e, sh);
+  if (threadIdx.x == 0) out[blockIdx.x] = e * kCHARGE_FACTOR;
+}
+
+// ---------------------------------------------------------------------------
+// host helpers
+
+static int ensure_scratch(cass_ctx* c, int nblocks, int nv) {
+  int rc = c->d_partial.reserve((size_t)nblocks * nv * sizeof(double));
+  if (rc) return rc;
+  if (!c->d_counter.p) {
+    rc = c->d_counter.reserve(64);
+    if (rc) return rc;
+    CASS_CUDA(cudaMemsetAsync(c->d_counter.p, 0, 64, c->stream));
+  }
+  rc = c->d_result.reserve(64 * sizeof(double));
+  return rc;
+}
+
+static int species_pool_upload(cass_ctx* c, DevBuf& d_hdr, DevBuf& d_ip, DevBuf& d_dp, SpeciesPools& P) {
+  std::vector<SpeciesDevHdr> hdr(c->nspecies);
+  std::vector<int> ip;
+  std::vector<double> dp;
+  for (int is = 0; is < c->nspecies; ++is) {
+    const SpeciesH& s = c->sp[is];
+    SpeciesDevHdr& h = hdr[is];
+    memset(&h, 0, sizeof(h));
+    h.natoms = s.natoms;
+    h.has_charge = s.has_charge;
+    h.l_coul_cbmc = s.l_coul_cbmc;
+    h.type_off = (int)ip.size();
+    ip.insert(ip.end(), s.type.begin(), s.type.end());
+    h.bonded_off = (int)ip.size();
+    ip.insert(ip.end(), s.bonded.begin(), s.bonded.end());
+    h.q_off = (int)dp.size();
+    dp.insert(dp.end(), s.q.begin(), s.q.end());
+    h.mass_off = (int)dp.size();
+    dp.insert(dp.end(), s.mass.begin(), s.mass.end());
+    h.vs_off = (int)dp.size();
+    dp.insert(dp.end(), s.vscale.begin(), s.vscale.end());
+    h.qs_off = (int)dp.size();
+    dp.insert(dp.end(), s.qscale.begin(), s.qscale.end());
+    h.nbonds = (int)s.bond_kind.size();
+    h.bond_atoms_off = (int)ip.size();
+    ip.insert(ip.end(), s.bond_atoms.begin(), s.bond_atoms.end());
+    h.bond_kind_off = (int)ip.size();
+    ip.insert(ip.end(), s.bond_kind.begin(), s.bond_kind.end());
+    h.bond_param_off = (int)dp.size();
+    dp.insert(dp.end(), s.bond_param.begin(), s.bond_param.end());
+    h.nangles = (int)s.angle_kind.size();
+    h.angle_atoms_off = (int)ip.size();
+    ip.insert(ip.end(), s.angle_atoms.begin(), s.angle_atoms.end());
+    h.angle_kind_off = (int)ip.size();
+    ip.insert(ip.end(), s.angle_kind.begin(), s.angle_kind.end());
+    h.angle_param_off = (int)dp.size();
+    dp.insert(dp.end(), s.angle_param.begin(), s.angle_param.end());
+    h.ndih = (int)s.dih_atoms.size() / 4;
+    h.dih_atoms_off = (int)ip.size();
+    ip.insert(ip.end(), s.dih_atoms.begin(), s.dih_atoms.end());
+    h.dih_rb_off = (int)dp.size();
+    dp.insert(dp.end(), s.dih_rb.begin(), s.dih_rb.end());
+    h.nimp = (int)s.imp_atoms.size() / 4;
+    h.imp_atoms_off = (int)ip.size();
+    ip.insert(ip.end(), s.imp_atoms.begin(), s.imp_atoms.end());
+    h.imp_param_off = (int)dp.size();
+    dp.insert(dp.end(), s.imp_param.begin(), s.imp_param.end());
+  }
+  ip.push_back(0);
+  dp.push_back(0.0);
+  int rc = d_hdr.reserve(hdr.size() * sizeof(SpeciesDevHdr));
+  if (!rc) rc = d_ip.reserve(ip.size() * sizeof(int));
+  if (!rc) rc = d_dp.reserve(dp.size() * sizeof(double));
+  if (rc) return rc;
+  CASS_CUDA(h2d(c, d_hdr.p, hdr.data(), hdr.size() * sizeof(SpeciesDevHdr)));
+  CASS_CUDA(h2d(c, d_ip.p, ip.data(), ip.size() * sizeof(int)));
+  CASS_CUDA(h2d(c, d_dp.p, dp.data(), dp.size() * sizeof(double)));
+  P.hdr = d_hdr.as<SpeciesDevHdr>();
+  P.ip = d_ip.as<int>();
+  P.dp = d_dp.as<double>();
+  return CASS_OK;
+}
+
+int ensure_pools(cass_ctx* c) {
+  if (!c->pools_dirty) return CASS_OK;
+  int rc = species_pool_upload(c, c->d_sp_hdr, c->d_sp_ip, c->d_sp_dp, c->pools);
+  if (!rc) c->pools_dirty = false;
+  return rc;
+}
+
+}  // namespace cassgpu
+
+using namespace cassgpu;
+
+namespace {
+
+int set_device(cass_ctx* c) {
+  CASS_CUDA(cudaSetDevice(c->device));
+  return CASS_OK;
+}
+
+int check_mol(cass_ctx* c, int im, int is) {
+  if (is < 1 || is > c->nspecies) return set_error(CASS_EINVAL, "species index out of range");
+  if (im < 1 || im > c->max_mol[is - 1]) return set_error(CASS_EINVAL, "molecule locate out of range");
+  if (!c->sp[is - 1].defined) return set_error(CASS_ESTATE, "species not defined");
+  return CASS_OK;
+}
+
+int mol_slot(cass_ctx* c, int im, int is) { return c->mol_base[is - 1] + im - 1; }
+
+void invalidate(cass_ctx* c, int ibox) {
+  if (ibox < 0 || ibox >= c->nboxes) return;
+  c->box[ibox].energy_valid = false;
+  c->box[ibox].pack_dirty = true;
+  c->box[ibox].cell_dirty = true;
+}
+
+// Packs the live molecules of a box (species-major, locate order) and uploads.
+int pack_box(cass_ctx* c, int ibox) {
+  BoxH& B = c->box[ibox];
+  if (!B.pack_dirty) return CASS_OK;
+  std::vector<double4_32a> p64;
+  std::vector<float4> p32;
+  std::vector<int4> meta;
+  std::vector<int4> molinfo;
+  B.pk_mol.clear();
+  B.pk_mol_off.clear();
+  for (int is = 0; is < c->nspecies; ++is) {
+    const SpeciesH& s = c->sp[is];
+    if (!s.defined) continue;
+    for (int im = 0; im < c->max_mol[is]; ++im) {
+      int slot = c->mol_base[is] + im;
+      if (c->mol_box[slot] != ibox) continue;
+      B.pk_mol.push_back(slot);
+      B.pk_mol_off.push_back((int)p64.size());
+      molinfo.push_back(make_int4(slot, is, (int)p64.size(), s.natoms));
+      const double* r = &s.pos[(size_t)im * 3 * s.natoms];
+      for (int a = 0; a < s.natoms; ++a) {
+        p64.push_back(make_double4_32a(r[3 * a], r[3 * a + 1], r[3 * a + 2], s.q[a]));
+        float tf;
+        int ty = s.type[a];
+        memcpy(&tf, &ty, sizeof(float));
+        p32.push_back(make_float4((float)r[3 * a], (float)r[3 * a + 1], (float)r[3 * a + 2], tf));
+        meta.push_back(make_int4(slot, s.type[a], is, a));
+      }
+    }
+  }
+  B.npacked = (int)p64.size();
+  B.npacked_mols = (int)molinfo.size();
+  size_t n = std::max<size_t>(1, p64.size());
+  int rc = B.d_p64.reserve(n * sizeof(double4_32a));
+  if (!rc) rc = B.d_p32.reserve(n * sizeof(float4));
+  if (!rc) rc = B.d_meta.reserve(n * sizeof(int4));
+  if (!rc) rc = B.d_molinfo.reserve(std::max<size_t>(1, molinfo.size()) * sizeof(int4));
+  if (rc) return rc;
+  if (!p64.empty()) {
+    CASS_CUDA(h2d(c, B.d_p64.p, p64.data(), p64.size() * sizeof(double4_32a)));
+    CASS_CUDA(h2d(c, B.d_p32.p, p32.data(), p32.size() * sizeof(float4)));
+    CASS_CUDA(h2d(c, B.d_meta.p, meta.data(), meta.size() * sizeof(int4)));
+    CASS_CUDA(h2d(c, B.d_molinfo.p, molinfo.data(), molinfo.size() * sizeof(int4)));
+  }
+  // pageable host vectors go out of scope below: wait for the copies
+  CASS_CUDA(cudaStreamSynchronize(c->stream));
+  B.pack_dirty = false;
+  return CASS_OK;
+}
+
+int sync_result(cass_ctx* c, int n) {
+  c->h_result.resize(n);
+  CASS_CUDA(d2h(c, c->h_result.data(), c->d_result.p, n * sizeof(double)));
+  CASS_CUDA(cudaStreamSynchronize(c->stream));
+  return CASS_OK;
+}
+
+int ensure_cos_mol(cass_ctx* c, int nv) {
+  if (nv <= c->cos_mol_stride && c->d_cos_mol.p) return CASS_OK;
+  int stride = std::max(nv, c->cos_mol_stride);
+  size_t bytes = (size_t)std::max(1, c->nmol_slots) * stride * sizeof(double);
+  int rc = c->d_cos_mol.reserve(bytes);
+  if (!rc) rc = c->d_sin_mol.reserve(bytes);
+  if (!rc) rc = c->d_cos_mol_old.reserve((size_t)stride * sizeof(double));
+  if (!rc) rc = c->d_sin_mol_old.reserve((size_t)stride * sizeof(double));
+  if (rc) return rc;
+  CASS_CUDA(cudaMemsetAsync(c->d_cos_mol.p, 0, bytes, c->stream));
+  CASS_CUDA(cudaMemsetAsync(c->d_sin_mol.p, 0, bytes, c->stream));
+  c->cos_mol_stride = stride;
+  return CASS_OK;
+}
+
+bool box_has_ewald(const BoxH& b) {
+  return b.desc.charge_style == CASS_CHARGE_COUL && b.desc.charge_sum_style == CASS_QQ_EWALD;
+}
+
+// Compute_LR_Correction (energy_routines.f90:2956-3023), host FP64 (O(ntypes^2)).
+double lr_correction(cass_ctx* c, const BoxH& B, const std::vector<double>& nb) {
+  int nt = c->ntypes;
+  double e = 0.0;
+  if (B.desc.vdw_style == CASS_VDW_LJ) {
+    for (int ia = 0; ia < nt; ++ia) {
+      double eij = 0.0;
+      for (int ja = 0; ja < nt; ++ja) {
+        double eps = c->pt.eps[pidx(ia, ja, nt)], s2 = c->pt.sig2[pidx(ia, ja, nt)];
+        double s6 = s2 * s2 * s2, s12 = s6 * s6;
+        eij = eij + nb[ja] * 4.0 * eps * (s12 / (9.0 * B.rcut9) - (s6 / (3.0 * B.rcut3)));
+      }
+      e = e + nb[ia] * eij;
+    }
+    e = 2.0 * kPI * e / B.dev.volume;
+  } else if (B.desc.vdw_style == CASS_VDW_MIE) {
+    for (int ia = 0; ia < nt; ++ia) {
+      double eij = 0.0;
+      for (int ja = 0; ja < nt; ++ja) {
+        int k = pidx(ia, ja, nt);
+        double eps = c->pt.eps[k], sig = std::sqrt(c->pt.sig2[k]), n = c->pt.mie_n[k], m = c->pt.mie_m[k];
+        double sor = sig / B.desc.rcut_vdw;
+        eij = eij + nb[ja] * c->pt.mie_c[k] * eps * std::pow(B.desc.rcut_vdw, 3.0) *
+                        ((std::pow(sor, n) / (3.0 - n)) + (std::pow(sor, m) / (m - 3.0)));
+      }
+      e = e + nb[ia] * eij;
+    }
+    e = -2.0 * kPI * e / B.dev.volume;
+  }
+  return e;
+}
+
+std::vector<double> count_beads(cass_ctx* c, int ibox) {
+  std::vector<double> nb(c->ntypes, 0.0);
+  for (int is = 0; is < c->nspecies; ++is) {
+    const SpeciesH& s = c->sp[is];
+    if (!s.defined) continue;
+    for (int im = 0; im < c->max_mol[is]; ++im)
+      if (c->mol_box[c->mol_base[is] + im] == ibox)
+        for (int a = 0; a < s.natoms; ++a)
+          if (s.type[a] >= 0) nb[s.type[a]] += 1.0;
+  }
+  return nb;
+}
+
+}  // namespace
+
+namespace cassgpu {
+int pack_box_ext(cass_ctx* c, int ibox) { return pack_box(c, ibox); }
+}  // namespace cassgpu
+
+// ===========================================================================
+// exported entry points
+extern "C" {
+
+int cass_abi_version(void) { return CASS_ABI_VERSION; }
+const char* cass_last_error(void) { return g_err.c_str(); }
+
+int cass_ctx_create(const CassConfig* cfg, cass_ctx** out) {
+  if (!cfg || !out || cfg->nspecies < 1 || cfg->ntypes < 1 || cfg->ntypes > kMaxTypes || cfg->nboxes < 1 ||
+      !cfg->max_molecules)
+    return set_error(CASS_EINVAL, "bad config (ntypes must be 1..8)");
+  if (cfg->precision != CASS_PREC_FP64 && cfg->precision != CASS_PREC_MIXED)
+    return set_error(CASS_EINVAL, "bad precision");
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev < 1) return set_error(CASS_ECUDA, "no CUDA device available");
+  if (cfg->device < 0 || cfg->device >= ndev) return set_error(CASS_EINVAL, "device ordinal out of range");
+  cass_ctx* c = new cass_ctx();
+  c->device = cfg->device;
+  c->precision = cfg->precision;
+  c->nspecies = cfg->nspecies;
+  c->ntypes = cfg->ntypes;
+  c->nboxes = cfg->nboxes;
+  if (cfg->max_kvectors > 0) c->max_kvec = cfg->max_kvectors;
+  c->max_mol.assign(cfg->max_molecules, cfg->max_molecules + cfg->nspecies);
+  c->mol_base.resize(c->nspecies);
+  int tot = 0;
+  for (int i = 0; i < c->nspecies; ++i) {
+    if (c->max_mol[i] < 0) {
+      delete c;
+      return set_error(CASS_EINVAL, "negative max_molecules");
+    }
+    c->mol_base[i] = tot;
+    tot += c->max_mol[i];
+  }
+  c->nmol_slots = tot;
+  c->mol_box.assign(tot, -1);
+  c->sp.resize(c->nspecies);
+  c->box.resize(c->nboxes);
+  if (cudaSetDevice(c->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return set_error(CASS_ECUDA, "stream creation failed");
+  }
+  c->stream = c->own_stream;
+  for (int k = 0; k < 4; ++k)
+    if (cudaEventCreate(&c->ev[k]) != cudaSuccess) {
+      delete c;
+      return set_error(CASS_ECUDA, "event creation failed");
+    }
+  *out = c;
+  return CASS_OK;
+}
+
+int cass_ctx_destroy(cass_ctx* c) {
+  if (!c) return CASS_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto& s : c->sp) s.d_library.release();
+  c->box.clear();
+  for (int k = 0; k < 4; ++k)
+    if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+  cudaStreamDestroy(c->own_stream);
+  delete c;
+  return CASS_OK;
+}
+
+int cass_get_stats(cass_ctx* c, CassStats* out) {
+  if (!c || !out) return set_error(CASS_EINVAL, "NULL argument");
+  *out = c->stats;
+  return CASS_OK;
+}
+
+int cass_set_count_pairs(cass_ctx* c, int32_t on) {
+  if (!c) return set_error(CASS_EINVAL, "NULL context");
+  c->count_pairs = on ? 1 : 0;
+  return CASS_OK;
+}
+
+int cass_set_stream(cass_ctx* c, void* stream) {
+  if (!c) return set_error(CASS_EINVAL, "NULL context");
+  CASS_CUDA(cudaStreamSynchronize(c->stream));
+  c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+  return CASS_OK;
+}
+
+int cass_set_nonbond_table(cass_ctx* c, int32_t nt, const double* eps, const double* sig, const double* mn,
+                           const double* mm) {
+  if (!c || nt != c->ntypes || !eps || !sig) return set_error(CASS_EINVAL, "bad nonbond table");
+  PairTable& t = c->pt;
+  memset(&t, 0, sizeof(t));
+  t.ntypes = nt;
+  for (int i = 0; i < nt * nt; ++i) {
+    t.eps[i] = eps[i];
+    t.sig2[i] = sig[i] * sig[i];
+    t.mie_n[i] = mn ? mn[i] : 0.0;
+    t.mie_m[i] = mm ? mm[i] : 0.0;
+    double n = t.mie_n[i], m = t.mie_m[i];
+    t.mie_c[i] = (n > m && m > 0) ? n / (n - m) * std::pow(n / m, m / (n - m)) : 0.0;
+    t.epsf[i] = (float)t.eps[i];
+    t.sig2f[i] = (float)t.sig2[i];
+  }
+  c->pt_set = true;
+  for (int b = 0; b < c->nboxes; ++b) c->box[b].energy_valid = false;
+  return CASS_OK;
+}
+
+int cass_set_species(cass_ctx* c, int32_t is, const CassSpeciesDesc* d) {
+  if (!c || is < 1 || is > c->nspecies || !d || d->natoms < 1) return set_error(CASS_EINVAL, "bad species");
+  if (!d->atom_type || !d->charge || !d->mass || !d->vdw_intra_scale || !d->charge_intra_scale || !d->bonded)
+    return set_error(CASS_EINVAL, "species arrays missing");
+  if (d->natoms > 64) return set_error(CASS_ECAPACITY, "species with more than 64 atoms");
+  if (d->nfragments > 0 && (!d->frag_natoms || !d->frag_atoms || !d->frag_nconnect || !d->frag_nconfig))
+    return set_error(CASS_EINVAL, "fragment arrays missing");
+  {  // every 1-based index of the descriptor must name an atom / fragment of this species
+    const int n = d->natoms;
+    auto bad = [&](const int32_t* a, long cnt, int hi) {
+      for (long k = 0; k < cnt; ++k)
+        if (a[k] < 1 || a[k] > hi) return true;
+      return false;
+    };
+    if ((d->nbonds > 0 && (!d->bond_atoms || bad(d->bond_atoms, 2L * d->nbonds, n))) ||
+        (d->nangles > 0 && (!d->angle_atoms || bad(d->angle_atoms, 3L * d->nangles, n))) ||
+        (d->ndihedrals > 0 && (!d->dihedral_atoms || bad(d->dihedral_atoms, 4L * d->ndihedrals, n))) ||
+        (d->nimpropers > 0 && (!d->improper_atoms || bad(d->improper_atoms, 4L * d->nimpropers, n))))
+      return set_error(CASS_EINVAL, "bonded atom index out of range");
+    long nfa = 0, nfc = 0;
+    for (int f = 0; f < d->nfragments; ++f) {
+      if (d->frag_natoms[f] < 1 || d->frag_natoms[f] > n || d->frag_nconnect[f] < 0 || d->frag_nconfig[f] < 0)
+        return set_error(CASS_EINVAL, "bad fragment sizes");
+      nfa += d->frag_natoms[f];
+      nfc += d->frag_nconnect[f];
+    }
+    if (bad(d->frag_atoms, nfa, n) || (nfc > 0 && (!d->frag_connect || bad(d->frag_connect, nfc, d->nfragments))))
+      return set_error(CASS_EINVAL, "fragment atom / connection index out of range");
+  }
+  SpeciesH& s = c->sp[is - 1];
+  int n = d->natoms;
+  s.natoms = n;
+  s.type.resize(n);
+  for (int i = 0; i < n; ++i) {
+    s.type[i] = d->atom_type[i] - 1;
+    if (s.type[i] >= c->ntypes) return set_error(CASS_EINVAL, "atom type out of range");
+  }
+  s.q.assign(d->charge, d->charge + n);
+  s.mass.assign(d->mass, d->mass + n);
+  s.vscale.assign(d->vdw_intra_scale, d->vdw_intra_scale + n * n);
+  s.qscale.assign(d->charge_intra_scale, d->charge_intra_scale + n * n);
+  s.bonded.assign(d->bonded, d->bonded + n * n);
+  s.bond_atoms.clear(); s.bond_kind.clear(); s.bond_param.clear();
+  for (int k = 0; k < d->nbonds; ++k) {
+    s.bond_atoms.push_back(d->bond_atoms[2 * k] - 1);
+    s.bond_atoms.push_back(d->bond_atoms[2 * k + 1] - 1);
+    s.bond_kind.push_back(d->bond_kind[k]);
+    s.bond_param.push_back(d->bond_param[2 * k]);
+    s.bond_param.push_back(d->bond_param[2 * k + 1]);
+  }
+  s.angle_atoms.clear(); s.angle_kind.clear(); s.angle_param.clear();
+  for (int k = 0; k < d->nangles; ++k) {
+    for (int j = 0; j < 3; ++j) s.angle_atoms.push_back(d->angle_atoms[3 * k + j] - 1);
+    s.angle_kind.push_back(d->angle_kind[k]);
+    s.angle_param.push_back(d->angle_param[2 * k]);
+    s.angle_param.push_back(d->angle_param[2 * k + 1]);
+  }
+  s.dih_atoms.clear(); s.dih_rb.clear();
+  for (int k = 0; k < d->ndihedrals; ++k) {
+    for (int j = 0; j < 4; ++j) s.dih_atoms.push_back(d->dihedral_atoms[4 * k + j] - 1);
+    for (int j = 0; j < 6; ++j) s.dih_rb.push_back(d->dihedral_rb[6 * k + j]);
+  }
+  s.imp_atoms.clear(); s.imp_param.clear();
+  for (int k = 0; k < d->nimpropers; ++k) {
+    for (int j = 0; j < 4; ++j) s.imp_atoms.push_back(d->improper_atoms[4 * k + j] - 1);
+    s.imp_param.push_back(d->improper_param[2 * k]);
+    s.imp_param.push_back(d->improper_param[2 * k + 1]);
+  }
+  s.nfrag = d->nfragments;
+  s.frag_atoms.clear(); s.frag_connect.clear(); s.frag_nconfig.clear(); s.library.clear(); s.lib_off.clear();
+  s.prob_ins.clear(); s.cum_prob_ins.clear();
+  int off = 0, coff = 0, tot = 0;
+  size_t loff = 0;
+  for (int f = 0; f < s.nfrag; ++f) {
+    std::vector<int> at;
+    for (int j = 0; j < d->frag_natoms[f]; ++j) at.push_back(d->frag_atoms[off + j] - 1);
+    off += d->frag_natoms[f];
+    s.frag_atoms.push_back(at);
+    std::vector<int> cn;
+    for (int j = 0; j < d->frag_nconnect[f]; ++j) cn.push_back(d->frag_connect[coff + j] - 1);
+    coff += d->frag_nconnect[f];
+    s.frag_connect.push_back(cn);
+    s.frag_nconfig.push_back(d->frag_nconfig[f]);
+    size_t len = (size_t)d->frag_nconfig[f] * d->frag_natoms[f] * 3;
+    s.lib_off.push_back((int)s.library.size());
+    if (len && d->frag_library) s.library.insert(s.library.end(), d->frag_library + loff, d->frag_library + loff + len);
+    loff += len;
+    tot += d->frag_natoms[f];
+  }
+  int acc = 0;
+  for (int f = 0; f < s.nfrag; ++f) {  // input_routines.f90:2844-2848
+    s.prob_ins.push_back((double)d->frag_natoms[f] / (double)tot);
+    acc += d->frag_natoms[f];
+    s.cum_prob_ins.push_back(f == 0 ? s.prob_ins[0] : (double)acc / (double)tot);
+  }
+  s.l_coul_cbmc = d->l_coul_cbmc != 0;
+  s.has_charge = false;
+  for (int i = 0; i < n; ++i)
+    if (s.q[i] != 0.0) s.has_charge = true;
+  s.pos.assign((size_t)c->max_mol[is - 1] * 3 * n, 0.0);
+  s.d_library.release();
+  if (!s.library.empty()) {
+    int rc = s.d_library.reserve(s.library.size() * sizeof(double));
+    if (rc) return rc;
+    CASS_CUDA(h2d(c, s.d_library.p, s.library.data(), s.library.size() * sizeof(double)));
+  }
+  s.defined = true;
+  c->pools_dirty = true;
+  for (int b = 0; b < c->nboxes; ++b) invalidate(c, b);
+  return CASS_OK;
+}
+
+int cass_set_box(cass_ctx* c, int32_t ibox, const CassBoxDesc* d) {
+  if (!c || ibox < 1 || ibox > c->nboxes || !d) return set_error(CASS_EINVAL, "bad box");
+  for (int k = 0; k < 3; ++k)
+    if (!(d->length[k] > 0.0)) return set_error(CASS_EINVAL, "box length must be positive");
+  BoxH& B = c->box[ibox - 1];
+  B.desc = *d;
+  BoxDev& v = B.dev;
+  memset(&v, 0, sizeof(v));
+  for (int k = 0; k < 3; ++k) {
+    v.L[k] = d->length[k];
+    v.hL[k] = 0.5 * d->length[k];
+    v.Lf[k] = (float)v.L[k];
+    v.hLf[k] = (float)v.hL[k];
+  }
+  v.volume = v.L[0] * v.L[1] * v.L[2];
+  v.vdw_style = d->vdw_style;
+  v.vdw_sum_style = d->vdw_sum_style;
+  v.charge_style = d->charge_style;
+  v.charge_sum_style = d->charge_sum_style;
+  double rcoul = d->charge_style == CASS_CHARGE_COUL ? d->rcut_coul : 0.0;
+  v.rcut_vdw = d->rcut_vdw;
+  v.rcut_coul = rcoul;
+  v.rcut_vdwsq = d->rcut_vdw * d->rcut_vdw;
+  v.rcut_coulsq = rcoul * rcoul;
+  v.rcut_cbmcsq = d->rcut_cbmc * d->rcut_cbmc;
+  v.rcut_lowsq = d->rcut_low * d->rcut_low;
+  v.ron_switch_sq = d->ron_switch * d->ron_switch;
+  v.roff_switch_sq = d->roff_switch * d->roff_switch;
+  if (d->vdw_sum_style == CASS_VDW_SUM_CUT_SWITCH) {
+    double d2 = v.roff_switch_sq - v.ron_switch_sq;
+    v.switch_factor1 = 1.0 / (d2 * d2 * d2);
+    v.switch_factor2 = v.roff_switch_sq - 3.0 * v.ron_switch_sq;
+  }
+  v.beta = 1.0 / (kKBOLTZ * d->temperature);
+  B.rcut_max = std::max(d->rcut_vdw, rcoul);  // precalculate.f90:79-83
+  B.rcut3 = d->rcut_vdw * d->rcut_vdw * d->rcut_vdw;
+  B.rcut9 = B.rcut3 * B.rcut3 * B.rcut3;
+  B.kvec.clear();
+  B.nvecs = 0;
+  if (d->charge_style == CASS_CHARGE_COUL && d->charge_sum_style == CASS_QQ_EWALD) {
+    if (!(d->ewald_tol > 0.0 && d->ewald_tol < 1.0)) return set_error(CASS_EINVAL, "ewald_tol must be in (0,1)");
+    double p = -std::log(d->ewald_tol);  // input_routines.f90:711-716
+    v.alpha = std::sqrt(p) / rcoul;
+    double hcut = 2.0 * p / rcoul;
+    // Ewald_Reciprocal_Lattice_Vector_Setup, orthorhombic branch (energy_routines.f90:2260-2311)
+    double const_val = 1.0 / (4.0 * v.alpha * v.alpha), hcutsq = hcut * hcut;
+    int kz = (int)((hcut * v.L[2]) / kTWOPI) + 1, ky = (int)((hcut * v.L[1]) / kTWOPI) + 1,
+        kx = (int)((hcut * v.L[0]) / kTWOPI) + 1;
+    for (int nz = -kz; nz <= kz; ++nz)
+      for (int ny = -ky; ny <= ky; ++ny)
+        for (int nx = 0; nx <= kx; ++nx) {
+          if (nx == 0 && ny == 0 && nz == 0) continue;
+          double hx = kTWOPI * (double)nx / v.L[0], hy = kTWOPI * (double)ny / v.L[1], hz = kTWOPI * (double)nz / v.L[2];
+          double h2 = hx * hx + hy * hy + hz * hz;
+          if (h2 < hcutsq) {
+            if (B.nvecs >= c->max_kvec) return set_error(CASS_ECAPACITY, "Total number of k vectors exceeded");
+            double cn = kTWOPI / v.volume * std::exp(-h2 * const_val) / h2;
+            if (nx != 0) cn = 2.0 * kTWOPI / v.volume * std::exp(-h2 * const_val) / h2;
+            B.kvec.insert(B.kvec.end(), {hx, hy, hz, cn});
+            ++B.nvecs;
+          }
+        }
+    v.nvecs = B.nvecs;
+    size_t nb = std::max(1, B.nvecs) * sizeof(double);
+    int rc = B.d_kvec.reserve(std::max(1, B.nvecs) * sizeof(double4_32a));
+    if (!rc) rc = B.d_cos_sum.reserve(nb);
+    if (!rc) rc = B.d_sin_sum.reserve(nb);
+    if (!rc) rc = B.d_cos_old.reserve(nb);
+    if (!rc) rc = B.d_sin_old.reserve(nb);
+    if (rc) return rc;
+    CASS_CUDA(h2d(c, B.d_kvec.p, B.kvec.data(), B.kvec.size() * sizeof(double)));
+    CASS_CUDA(cudaMemsetAsync(B.d_cos_sum.p, 0, nb, c->stream));
+    CASS_CUDA(cudaMemsetAsync(B.d_sin_sum.p, 0, nb, c->stream));
+    CASS_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  if (d->charge_style == CASS_CHARGE_COUL && d->charge_sum_style == CASS_QQ_DSF) {
+    double a = d->alpha_dsf;
+    if (a <= 0.0) {  // input_routines.f90:742-747
+      a = 0.425 - rcoul * 0.02;
+      if (a < 0.0) a = 3.3930702 / rcoul;
+    }
+    v.alpha_dsf = a;
+    v.dsf_factor1 = std::erfc(a * rcoul) / rcoul;
+    v.dsf_factor2 = v.dsf_factor1 / rcoul + 2.0 * a * std::exp(-a * a * rcoul * rcoul) / (kROOTPI * rcoul);
+  }
+  B.defined = true;
+  invalidate(c, ibox - 1);
+  return CASS_OK;
+}
+
+int cass_set_molecules(cass_ctx* c, int32_t n, const int32_t* im, const int32_t* is, const int32_t* ibox,
+                       const double* xyz) {
+  if (!c || n < 0 || (n > 0 && (!im || !is || !ibox || !xyz))) return set_error(CASS_EINVAL, "bad molecule list");
+  size_t off = 0;
+  for (int k = 0; k < n; ++k) {
+    int rc = check_mol(c, im[k], is[k]);
+    if (rc) return rc;
+    if (ibox[k] < 1 || ibox[k] > c->nboxes) return set_error(CASS_EINVAL, "box index out of range");
+    SpeciesH& s = c->sp[is[k] - 1];
+    int slot = mol_slot(c, im[k], is[k]);
+    int old = c->mol_box[slot];
+    memcpy(&s.pos[(size_t)(im[k] - 1) * 3 * s.natoms], xyz + off, 3 * s.natoms * sizeof(double));
+    off += 3 * s.natoms;
+    int nb = ibox[k] - 1;
+    c->mol_box[slot] = nb;
+    if (old >= 0 && old != nb) invalidate(c, old);
+    BoxH& B = c->box[nb];
+    if (old == nb && !B.pack_dirty) {
+      // molecule stays in its box: patch its packed atoms in place
+      int p = -1;
+      for (size_t q = 0; q < B.pk_mol.size(); ++q)
+        if (B.pk_mol[q] == slot) { p = B.pk_mol_off[q]; break; }
+      if (p >= 0) {
+        std::vector<double4_32a> p64(s.natoms);
+        std::vector<float4> p32(s.natoms);
+        const double* r = &s.pos[(size_t)(im[k] - 1) * 3 * s.natoms];
+        for (int a = 0; a < s.natoms; ++a) {
+          p64[a] = make_double4_32a(r[3 * a], r[3 * a + 1], r[3 * a + 2], s.q[a]);
+          float tf;
+          int ty = s.type[a];
+          memcpy(&tf, &ty, sizeof(float));
+          p32[a] = make_float4((float)r[3 * a], (float)r[3 * a + 1], (float)r[3 * a + 2], tf);
+        }
+        CASS_CUDA(h2d(c, B.d_p64.as<double4_32a>() + p, p64.data(), s.natoms * sizeof(double4_32a)));
+        CASS_CUDA(h2d(c, B.d_p32.as<float4>() + p, p32.data(), s.natoms * sizeof(float4)));
+        CASS_CUDA(cudaStreamSynchronize(c->stream));
+        B.energy_valid = false;
+        B.cell_dirty = true;
+        continue;
+      }
+    }
+    invalidate(c, nb);
+  }
+  return CASS_OK;
+}
+
+int cass_remove_molecule(cass_ctx* c, int32_t im, int32_t is) {
+  if (!c) return set_error(CASS_EINVAL, "NULL context");
+  int rc = check_mol(c, im, is);
+  if (rc) return rc;
+  int slot = mol_slot(c, im, is);
+  if (c->mol_box[slot] >= 0) invalidate(c, c->mol_box[slot]);
+  c->mol_box[slot] = -1;
+  return CASS_OK;
+}
+
+int cass_get_molecule(cass_ctx* c, int32_t im, int32_t is, double* xyz) {
+  if (!c || !xyz) return set_error(CASS_EINVAL, "NULL argument");
+  int rc = check_mol(c, im, is);
+  if (rc) return rc;
+  const SpeciesH& s = c->sp[is - 1];
+  memcpy(xyz, &s.pos[(size_t)(im - 1) * 3 * s.natoms], 3 * s.natoms * sizeof(double));
+  return CASS_OK;
+}
+
+int cass_mol_inter_energy(cass_ctx* c, int32_t im, int32_t is, int32_t cbmc, double* ev, double* eq, int32_t* ov) {
+  if (!c || !ev || !eq || !ov) return set_error(CASS_EINVAL, "NULL argument");
+  int rc = check_mol(c, im, is);
+  if (rc) return rc;
+  if (!c->pt_set) return set_error(CASS_ESTATE, "nonbond table not set");
+  int slot = mol_slot(c, im, is);
+  int ibox = c->mol_box[slot];
+  if (ibox < 0) return set_error(CASS_ESTATE, "molecule not live");
+  if ((rc = set_device(c)) || (rc = pack_box(c, ibox))) return rc;
+  BoxH& B = c->box[ibox];
+  int qoff = -1;
+  for (size_t q = 0; q < B.pk_mol.size(); ++q)
+    if (B.pk_mol[q] == slot) { qoff = B.pk_mol_off[q]; break; }
+  const SpeciesH& s = c->sp[is - 1];
+  if (s.natoms > kMaxAtoms * 4) return set_error(CASS_ECAPACITY, "query molecule too large");
+  int nblk = std::max(1, std::min(148, (B.npacked + kBlock - 1) / kBlock));
+  if ((rc = ensure_scratch(c, nblk, 2))) return rc;
+  int rc2 = c->d_query.reserve(16);
+  if (rc2) return rc2;
+  CASS_CUDA(cudaMemsetAsync(c->d_query.p, 0, sizeof(int), c->stream));
+  int want_qq = (cbmc && !s.l_coul_cbmc) ? 0 : 1;
+  if (c->precision == CASS_PREC_MIXED)
+    k_mol_inter<true><<<nblk, kBlock, 0, c->stream>>>(B.dev, c->pt, B.d_p64.as<double4_32a>(), B.d_p32.as<float4>(),
+                                                      B.d_meta.as<int4>(), B.npacked, slot, qoff, s.natoms, cbmc,
+                                                      want_qq, c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
+                                                      c->d_result.as<double>(), c->d_query.as<int>());
+  else
+    k_mol_inter<false><<<nblk, kBlock, 0, c->stream>>>(B.dev, c->pt, B.d_p64.as<double4_32a>(), B.d_p32.as<float4>(),
+                                                       B.d_meta.as<int4>(), B.npacked, slot, qoff, s.natoms, cbmc,
+                                                       want_qq, c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
+                                                       c->d_result.as<double>(), c->d_query.as<int>());
+  CASS_CUDA(cudaGetLastError());
+  count_launch(c);
+  int hov = 0;
+  CASS_CUDA(d2h(c, &hov, c->d_query.p, sizeof(int)));
+  if ((rc = sync_result(c, 2))) return rc;
+  *ov = hov ? 1 : 0;
+  *ev = hov ? 0.0 : c->h_result[0];
+  *eq = hov ? 0.0 : c->h_result[1];
+  return CASS_OK;
+}
+
+int cass_mol_intra_energy(cass_ctx* c, int32_t im, int32_t is, int32_t cbmc, double* eiv, double* eiq, double* eoq,
+                          int32_t* ov) {
+  if (!c || !eiv || !eiq || !eoq || !ov) return set_error(CASS_EINVAL, "NULL argument");
+  int rc = check_mol(c, im, is);
+  if (rc) return rc;
+  int slot = mol_slot(c, im, is);
+  int ibox = c->mol_box[slot];
+  if (ibox < 0) return set_error(CASS_ESTATE, "molecule not live");
+  if (cbmc) return set_error(CASS_EUNSUPPORTED, "intra energy with the CBMC cutoff is computed inside the Widom kernel");
+  if ((rc = set_device(c)) || (rc = pack_box(c, ibox))) return rc;
+  if ((rc = ensure_pools(c))) return rc;
+  BoxH& B = c->box[ibox];
+  int q = -1;
+  for (size_t k = 0; k < B.pk_mol.size(); ++k)
+    if (B.pk_mol[k] == slot) { q = (int)k; break; }
+  if ((rc = ensure_scratch(c, 1, 7))) return rc;
+  if ((rc = c->d_query.reserve(16))) return rc;
+  CASS_CUDA(cudaMemsetAsync(c->d_query.p, 0, sizeof(int), c->stream));
+  k_intra_total<<<1, kBlock, 0, c->stream>>>(B.dev, c->pt, c->pools, B.d_p64.as<double4_32a>(), B.d_molinfo.as<int4>() + q, 1,
+                                             c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
+                                             c->d_result.as<double>(), c->d_query.as<int>());
+  CASS_CUDA(cudaGetLastError());
+  count_launch(c);
+  int hov = 0;
+  CASS_CUDA(d2h(c, &hov, c->d_query.p, sizeof(int)));
+  if ((rc = sync_result(c, 7))) return rc;
+  *ov = hov ? 1 : 0;
+  *eiv = c->h_result[4];
+  *eiq = c->h_result[5];
+  *eoq = c->h_result[6];
+  return CASS_OK;
+}
+
+int cass_system_total_energy(cass_ctx* c, int32_t ibox1, int32_t intra_flag, CassEnergy* out, int32_t* overlap) {
+  if (!c || ibox1 < 1 || ibox1 > c->nboxes || !out || !overlap) return set_error(CASS_EINVAL, "bad arguments");
+  if (!c->pt_set) return set_error(CASS_ESTATE, "nonbond table not set");
+  int ibox = ibox1 - 1;
+  BoxH& B = c->box[ibox];
+  if (!B.defined) return set_error(CASS_ESTATE, "box not defined");
+  int rc;
+  if ((rc = set_device(c)) || (rc = pack_box(c, ibox))) return rc;
+  if ((rc = ensure_pools(c))) return rc;
+  CassEnergy E = B.energy;
+  CassEnergy keep = E;
+  E = CassEnergy{};
+  *overlap = 0;
+  if ((rc = c->d_query.reserve(16))) return rc;
+  CASS_CUDA(cudaMemsetAsync(c->d_query.p, 0, sizeof(int), c->stream));
+  int n = B.npacked;
+  std::vector<double> res;
+  if (intra_flag && B.npacked_mols > 0) {
+    int nblk = std::max(1, std::min(296, (B.npacked_mols + kBlock - 1) / kBlock));
+    if ((rc = ensure_scratch(c, nblk, 7))) return rc;
+    k_intra_total<<<nblk, kBlock, 0, c->stream>>>(B.dev, c->pt, c->pools, B.d_p64.as<double4_32a>(), B.d_molinfo.as<int4>(),
+                                                   B.npacked_mols, c->d_partial.as<double>(),
+                                                   c->d_counter.as<unsigned>(), c->d_result.as<double>(),
+                                                   c->d_query.as<int>());
+    CASS_CUDA(cudaGetLastError());
+  count_launch(c);
+    if ((rc = sync_result(c, 7))) return rc;
+    E.bond = c->h_result[0];
+    E.angle = c->h_result[1];
+    E.dihedral = c->h_result[2];
+    E.improper = c->h_result[3];
+    E.intra_vdw = c->h_result[4];
+    E.intra_q = c->h_result[5];
+    E.inter_q = c->h_result[6];
+    E.intra = E.bond + E.angle + E.dihedral + E.improper + E.intra_q + E.intra_vdw;
+  } else if (!intra_flag) {
+    E.intra = keep.intra; E.bond = keep.bond; E.angle = keep.angle; E.dihedral = keep.dihedral;
+    E.improper = keep.improper; E.intra_vdw = keep.intra_vdw; E.intra_q = keep.intra_q;
+  }
+  if (n > 1) {
+    dim3 grid((n + kBlock - 1) / kBlock, (n + kTileJ - 1) / kTileJ);
+    if ((rc = ensure_scratch(c, grid.x * grid.y, 2))) return rc;
+    if (c->precision == CASS_PREC_MIXED)
+      k_pair_total<true><<<grid, kBlock, 0, c->stream>>>(B.dev, c->pt, B.d_p64.as<double4_32a>(), B.d_meta.as<int4>(), n,
+                                                        c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
+                                                        c->d_result.as<double>(), c->d_query.as<int>());
+    else
+      k_pair_total<false><<<grid, kBlock, 0, c->stream>>>(B.dev, c->pt, B.d_p64.as<double4_32a>(), B.d_meta.as<int4>(), n,
+                                                         c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
+                                                         c->d_result.as<double>(), c->d_query.as<int>());
+    CASS_CUDA(cudaGetLastError());
+  count_launch(c);
+    if ((rc = sync_result(c, 2))) return rc;
+    E.inter_vdw += c->h_result[0];
+    E.inter_q += c->h_result[1];
+  }
+  int hov = 0;
+  CASS_CUDA(d2h(c, &hov, c->d_query.p, sizeof(int)));
+  CASS_CUDA(cudaStreamSynchronize(c->stream));
+  if (hov) {
+    *overlap = 1;
+    B.energy_valid = false;
+    return CASS_OK;
+  }
+  E.inter = E.inter_q + E.inter_vdw;
+  if (B.desc.charge_style == CASS_CHARGE_COUL) {
+    if (box_has_ewald(B) && B.nvecs > 0) {
+      int nv = B.nvecs;
+      if ((rc = ensure_cos_mol(c, nv))) return rc;
+      DevBuf& part = c->d_box_sums;
+      int nchunks = std::max(1, (B.npacked_mols + kSfacMolChunk - 1) / kSfacMolChunk);
+      if ((rc = part.reserve((size_t)nchunks * nv * sizeof(double2)))) return rc;
+      std::vector<int> charged(c->nspecies);
+      for (int is = 0; is < c->nspecies; ++is) charged[is] = c->sp[is].has_charge ? 1 : 0;
+      DevBuf& dch = c->d_cell_count;  // small reuse: species charged flags
+      if ((rc = dch.reserve(std::max(c->nspecies, 1) * sizeof(int) + 256))) return rc;
+      CASS_CUDA(h2d(c, dch.p, charged.data(), c->nspecies * sizeof(int)));
+      if (B.npacked_mols > 0) {
+        dim3 g((nv + 127) / 128, nchunks);
+        k_sfac<<<g, 128, 0, c->stream>>>(B.d_kvec.as<double4_32a>(), nv, B.d_p64.as<double4_32a>(), B.d_molinfo.as<int4>(),
+                                         B.npacked_mols, dch.as<int>(), c->d_cos_mol.as<double>(),
+                                         c->d_sin_mol.as<double>(), c->cos_mol_stride, part.as<double2>());
+        CASS_CUDA(cudaGetLastError());
+  count_launch(c);
+      } else {
+        CASS_CUDA(cudaMemsetAsync(part.p, 0, (size_t)nv * sizeof(double2), c->stream));
+      }
+      int nblk = std::max(1, std::min(148, (nv + kBlock - 1) / kBlock));
+      if ((rc = ensure_scratch(c, nblk, 1))) return rc;
+      k_sfac_reduce<<<nblk, kBlock, 0, c->stream>>>(B.d_kvec.as<double4_32a>(), nv, part.as<double2>(), nchunks,
+                                                    B.d_cos_sum.as<double>(), B.d_sin_sum.as<double>(),
+                                                    c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
+                                                    c->d_result.as<double>());
+      CASS_CUDA(cudaGetLastError());
+  count_launch(c);
+      if ((rc = sync_result(c, 1))) return rc;
+      E.reciprocal = c->h_result[0] * kCHARGE_FACTOR;
+      E.inter = E.inter + E.reciprocal;
+    }
+    // Compute_System_Self_Energy (energy_routines.f90:2553-2601), O(nmol) host sum of charges squared
+    double es = 0.0;
+    for (int is = 0; is < c->nspecies; ++is) {
+      const SpeciesH& s = c->sp[is];
+      if (!s.defined) continue;
+      double qq = 0.0;
+      for (int a = 0; a < s.natoms; ++a) qq += s.q[a] * s.q[a];
+      for (int im = 0; im < c->max_mol[is]; ++im)
+        if (c->mol_box[c->mol_base[is] + im] == ibox)
+          for (int a = 0; a < s.natoms; ++a) es = es + s.q[a] * s.q[a];
+    }
+    if (B.desc.charge_sum_style == CASS_QQ_EWALD) E.self = -es * kCHARGE_FACTOR * B.dev.alpha / kROOTPI;
+    else if (B.desc.charge_sum_style == CASS_QQ_DSF)
+      E.self = -(es * (B.dev.alpha_dsf / kROOTPI + B.dev.dsf_factor1 / 2.0)) * kCHARGE_FACTOR;
+    E.inter = E.inter + E.self;
+  }
+  if (B.desc.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) {
+    E.lrc = lr_correction(c, B, count_beads(c, ibox));
+    E.inter = E.inter + E.lrc;
+  }
+  E.total = E.intra + E.inter;
+  B.energy = E;
+  B.energy_valid = true;
+  *out = E;
+  return CASS_OK;
+}
+
+int cass_ewald_update(cass_ctx* c, int32_t im, int32_t is, int32_t ibox1, int32_t move_flag, double* e_recip) {
+  if (!c || !e_recip) return set_error(CASS_EINVAL, "NULL argument");
+  int rc = check_mol(c, im, is);
+  if (rc) return rc;
+  if (ibox1 < 1 || ibox1 > c->nboxes) return set_error(CASS_EINVAL, "box index");
+  if (move_flag < 0 || move_flag > 4) return set_error(CASS_EINVAL, "bad move_flag");
+  BoxH& B = c->box[ibox1 - 1];
+  if (!box_has_ewald(B)) return set_error(CASS_ESTATE, "box has no Ewald sum");
+  if ((rc = set_device(c))) return rc;
+  int nv = B.nvecs;
+  if ((rc = ensure_cos_mol(c, nv))) return rc;
+  int slot = mol_slot(c, im, is);
+  const SpeciesH& s = c->sp[is - 1];
+  size_t nb = (size_t)nv * sizeof(double);
+  double* cm = c->d_cos_mol.as<double>() + (size_t)slot * c->cos_mol_stride;
+  double* sm = c->d_sin_mol.as<double>() + (size_t)slot * c->cos_mol_stride;
+  CASS_CUDA(cudaMemcpyAsync(B.d_cos_old.p, B.d_cos_sum.p, nb, cudaMemcpyDeviceToDevice, c->stream));
+  CASS_CUDA(cudaMemcpyAsync(B.d_sin_old.p, B.d_sin_sum.p, nb, cudaMemcpyDeviceToDevice, c->stream));
+  CASS_CUDA(cudaMemcpyAsync(c->d_cos_mol_old.p, cm, nb, cudaMemcpyDeviceToDevice, c->stream));
+  CASS_CUDA(cudaMemcpyAsync(c->d_sin_mol_old.p, sm, nb, cudaMemcpyDeviceToDevice, c->stream));
+  std::vector<double4_32a> qa(s.natoms);
+  const double* r = &s.pos[(size_t)(im - 1) * 3 * s.natoms];
+  for (int a = 0; a < s.natoms; ++a) qa[a] = make_double4_32a(r[3 * a], r[3 * a + 1], r[3 * a + 2], s.q[a]);
+  if ((rc = c->d_query.reserve(std::max<size_t>(16, qa.size() * sizeof(double4_32a))))) return rc;
+  CASS_CUDA(h2d(c, c->d_query.p, qa.data(), qa.size() * sizeof(double4_32a)));
+  int nblk = std::max(1, std::min(148, (nv + kBlock - 1) / kBlock));
+  if ((rc = ensure_scratch(c, nblk, 1))) return rc;
+  k_ewald_update<<<nblk, kBlock, 0, c->stream>>>(B.d_kvec.as<double4_32a>(), nv, c->d_query.as<double4_32a>(), s.natoms,
+                                                 move_flag, B.d_cos_sum.as<double>(), B.d_sin_sum.as<double>(), cm, sm,
+                                                 c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
+                                                 c->d_result.as<double>());
+  CASS_CUDA(cudaGetLastError());
+  count_launch(c);
+  if ((rc = sync_result(c, 1))) return rc;
+  *e_recip = c->h_result[0] * kCHARGE_FACTOR;
+  B.energy_valid = false;
+  return CASS_OK;
+}
+
+int cass_ewald_restore(cass_ctx* c, int32_t im, int32_t is, int32_t ibox1) {
+  if (!c) return set_error(CASS_EINVAL, "NULL context");
+  int rc = check_mol(c, im, is);
+  if (rc) return rc;
+  if (ibox1 < 1 || ibox1 > c->nboxes) return set_error(CASS_EINVAL, "box index");
+  BoxH& B = c->box[ibox1 - 1];
+  if (!box_has_ewald(B) || !c->d_cos_mol.p) return set_error(CASS_ESTATE, "nothing to restore");
+  if ((rc = set_device(c))) return rc;
+  int slot = mol_slot(c, im, is);
+  size_t nb = (size_t)B.nvecs * sizeof(double);
+  double* cm = c->d_cos_mol.as<double>() + (size_t)slot * c->cos_mol_stride;
+  double* sm = c->d_sin_mol.as<double>() + (size_t)slot * c->cos_mol_stride;
+  CASS_CUDA(cudaMemcpyAsync(B.d_cos_sum.p, B.d_cos_old.p, nb, cudaMemcpyDeviceToDevice, c->stream));
+  CASS_CUDA(cudaMemcpyAsync(B.d_sin_sum.p, B.d_sin_old.p, nb, cudaMemcpyDeviceToDevice, c->stream));
+  CASS_CUDA(cudaMemcpyAsync(cm, c->d_cos_mol_old.p, nb, cudaMemcpyDeviceToDevice, c->stream));
+  CASS_CUDA(cudaMemcpyAsync(sm, c->d_sin_mol_old.p, nb, cudaMemcpyDeviceToDevice, c->stream));
+  CASS_CUDA(cudaStreamSynchronize(c->stream));
+  return CASS_OK;
+}
+
+int cass_ewald_widom(cass_ctx* c, int32_t is, int32_t ibox1, int32_t n, const double* xyz, double* e) {
+  if (!c || is < 1 || is > c->nspecies || ibox1 < 1 || ibox1 > c->nboxes || n < 0 || (n > 0 && (!xyz || !e)))
+    return set_error(CASS_EINVAL, "bad arguments");
+  BoxH& B = c->box[ibox1 - 1];
+  if (!box_has_ewald(B)) return set_error(CASS_ESTATE, "box has no Ewald sum");
+  if (n == 0) return CASS_OK;
+  int rc;
+  if ((rc = set_device(c))) return rc;
+  const SpeciesH& s = c->sp[is - 1];
+  size_t nx = (size_t)n * 3 * s.natoms;
+  DevBuf& dx = c->d_widom_xyz;
+  DevBuf& dout = c->d_widom_out;
+  if ((rc = dx.reserve(nx * sizeof(double) + s.natoms * sizeof(double)))) return rc;
+  if ((rc = dout.reserve((size_t)n * sizeof(double)))) return rc;
+  CASS_CUDA(h2d(c, dx.p, xyz, nx * sizeof(double)));
+  double* dq = dx.as<double>() + nx;
+  CASS_CUDA(h2d(c, dq, s.q.data(), s.natoms * sizeof(double)));
+  k_ewald_widom<<<n, kBlock, 0, c->stream>>>(B.d_kvec.as<double4_32a>(), B.nvecs, B.d_cos_sum.as<double>(),
+                                             B.d_sin_sum.as<double>(), dx.as<double>(), dq, s.natoms, dout.as<double>());
+  CASS_CUDA(cudaGetLastError());
+  count_launch(c);
+  CASS_CUDA(d2h(c, e, dout.p, n * sizeof(double)));
+  CASS_CUDA(cudaStreamSynchronize(c->stream));
+  return CASS_OK;
+}
+
+}  // extern "C"

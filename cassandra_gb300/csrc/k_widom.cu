@@ -1,0 +1,1305 @@
+// k_widom.cu -- batched CBMC Widom insertion on the GPU.
+//
+//   k_cell_count / k_cell_scan / k_cell_scatter / k_cell_sort
+//       per-box cell lists (counting sort, deterministic order inside a cell);
+//       the GPU counterpart of Sector_Setup / CBMC_Cell_List_Setup
+//       (sector_routines.f90:39-374).  Cells only accelerate the search:
+//       every pair with r <= cutoff is visited exactly once, whatever the cell
+//       count, so the energies are those of the molecule loop of
+//       Compute_Molecule_Nonbond_Inter_Energy_Widom (energy_routines.f90:1266-1297).
+//   k_widom
+//       one thread per Widom insertion: Build_Molecule with kappa_ins first-
+//       fragment trials and Fragment_Placement with kappa_dih dihedral trials
+//       (fragment_growth.f90:72-707, 1449-2132), then the full-cutoff energy,
+//       intramolecular and bonded energies of the grown molecule
+//       (widom_insert.f90:320-447).  The CTA's box (cell-sorted atoms and cell
+//       offsets) is staged in shared memory when it fits.
+//   k_widom_recip
+//       Update_System_Ewald_Reciprocal_Energy_Widom (energy_routines.f90:2500-2550)
+//       for the insertions that survived, when the box carries an Ewald sum.
+//   k_widom_finalize
+//       widom_var = exp(-beta (dE - dE_frag) - ln_pbias) and the per-box sums
+//       (widom_insert.f90:445-447, 538), in a fixed order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "cass_ctx.h"
+
+namespace cassgpu {
+
+struct WidomSpecies {
+  int natoms, nfrag, is0;
+  int kappa_ins, kappa_dih;
+  int want_qq_cbmc;  // Coulomb in CBMC trials (L_Coul_CBMC)
+  double ln_kappa_ins, ln_kappa_dih_term;
+  double mass[kMaxAtoms];
+  double q[kMaxAtoms];
+  int type[kMaxAtoms];
+  int frag_natoms[kMaxFrags];
+  signed char frag_atoms[kMaxFrags][kMaxAtoms];
+  int frag_nconnect[kMaxFrags];
+  signed char frag_connect[kMaxFrags][kMaxFrags];
+  int nconfig[kMaxFrags];
+  long long lib_off[kMaxFrags];
+  double prob_ins[kMaxFrags], cum_prob_ins[kMaxFrags], ln_prob_ins[kMaxFrags];
+};
+
+struct BoxSrc {
+  const double4_32a* p64;
+  const float4* p32;
+  const int4* meta;
+};
+
+// Per-insertion record: dE_intra, dE_inter (without reciprocal), dE_frag, ln_pbias.
+using WRec = double4_32a;
+
+__device__ __forceinline__ int wrapc(int c, int n) {
+  c %= n;
+  return c < 0 ? c + n : c;
+}
+
+// ---------------------------------------------------------------------------
+// K7: cell lists of the batch boxes
+__device__ __forceinline__ int cell_index(const BoxDev& b, double x, double y, double z) {
+  int c[3];
+  double p[3] = {x, y, z};
+  for (int d = 0; d < 3; ++d) {
+    double w = p[d] - b.L[d] * floor((p[d] + b.hL[d]) / b.L[d]);  // wrapped into [-L/2, L/2)
+    int k = (int)floor((w + b.hL[d]) * b.cell_inv[d]);
+    c[d] = min(max(k, 0), b.nc[d] - 1);
+  }
+  return (c[2] * b.nc[1] + c[1]) * b.nc[0] + c[0];
+}
+
+__global__ void k_cell_count(const BoxSrc* src, const BoxDev* boxes, int* cell_of, int* count) {
+  int k = blockIdx.y;
+  const BoxDev& b = boxes[k];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b.natoms) return;
+  double4_32a p = src[k].p64[i];
+  int c = cell_index(b, p.x, p.y, p.z);
+  cell_of[b.atom_off + i] = c;
+  atomicAdd(&count[b.cell_off + c], 1);
+}
+
+// exclusive scan of the box's cell counts; cstart holds local atom indices
+__global__ void k_cell_scan(const BoxDev* boxes, const int* count, int* cstart, int* fill) {
+  int k = blockIdx.x;
+  const BoxDev& b = boxes[k];
+  int nc = b.nc[0] * b.nc[1] * b.nc[2];
+  __shared__ int carry;
+  __shared__ int warp_tot[32];
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  int* cs = cstart + b.cell_off + k;
+  for (int base = 0; base < nc; base += blockDim.x) {
+    int c = base + threadIdx.x;
+    int v = c < nc ? count[b.cell_off + c] : 0;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if ((threadIdx.x & 31) >= o) x += y;
+    }
+    if ((threadIdx.x & 31) == 31) warp_tot[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      int nw = blockDim.x >> 5;
+      int t = threadIdx.x < nw ? warp_tot[threadIdx.x] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, t, o);
+        if (threadIdx.x >= o) t += y;
+      }
+      if (threadIdx.x < nw) warp_tot[threadIdx.x] = t;
+    }
+    __syncthreads();
+    int w = threadIdx.x >> 5;
+    int excl = x - v + (w > 0 ? warp_tot[w - 1] : 0) + carry;
+    if (c < nc) {
+      cs[c] = excl;
+      fill[b.cell_off + c] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) cs[nc] = carry;
+}
+
+__global__ void k_cell_scatter(const BoxSrc* src, const BoxDev* boxes, const int* cell_of, const int* cstart,
+                               int* fill, double4_32a* c64, float4* c32, int* ctype, float* cq32, int* corig) {
+  int k = blockIdx.y;
+  const BoxDev& b = boxes[k];
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b.natoms) return;
+  int c = cell_of[b.atom_off + i];
+  int pos = cstart[b.cell_off + k + c] + atomicAdd(&fill[b.cell_off + c], 1);
+  int g = b.atom_off + pos;
+  c64[g] = src[k].p64[i];
+  c32[g] = src[k].p32[i];
+  ctype[g] = src[k].meta[i].y;
+  cq32[g] = (float)src[k].p64[i].w;
+  corig[g] = i;
+}
+
+// insertion sort of each cell by packed index: a deterministic order
+__global__ void k_cell_sort(const BoxDev* boxes, int nb, const int* cstart, double4_32a* c64, float4* c32, int* ctype,
+                            float* cq32, int* corig) {
+  int k = blockIdx.y;
+  if (k >= nb) return;
+  const BoxDev& b = boxes[k];
+  int nc = b.nc[0] * b.nc[1] * b.nc[2];
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const int* cs = cstart + b.cell_off + k;
+  int s = b.atom_off + cs[c], e = b.atom_off + cs[c + 1];
+  for (int i = s + 1; i < e; ++i) {
+    int key = corig[i];
+    double4_32a a64 = c64[i];
+    float4 a32 = c32[i];
+    int at = ctype[i];
+    float aq = cq32[i];
+    int j = i - 1;
+    while (j >= s && corig[j] > key) {
+      corig[j + 1] = corig[j];
+      c64[j + 1] = c64[j];
+      c32[j + 1] = c32[j];
+      ctype[j + 1] = ctype[j];
+      cq32[j + 1] = cq32[j];
+      --j;
+    }
+    corig[j + 1] = key;
+    c64[j + 1] = a64;
+    c32[j + 1] = a32;
+    ctype[j + 1] = at;
+    cq32[j + 1] = aq;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// box queries
+
+struct BoxView {
+  const BoxDev* b;          // shared-memory copy
+  const double4_32a* p64;   // cell-sorted FP64 atoms (x, y, z, q) of this box (smem or global)
+  const int* ptype;         // their types (smem or global)
+  const float4* p32;        // cell-sorted FP32 atoms (x, y, z, type bits) (smem or global)
+  const float* q32;         // FP32 charges (global)
+  const int* cstart;        // cell starts, local atom indices (smem or global)
+  const double4_32a* g64;   // global FP64 atoms, for exact threshold decisions
+  double rc_cbmc, rc_full;
+  bool fast_mixed;          // LJ cut/cut_tail(/Ewald) styles run in FP32
+};
+
+constexpr float kBand = 2e-5f;  // relative band around r^2 thresholds re-evaluated in FP64
+
+// Energy of one test atom at p against every box atom within the cutoff.
+// Returns true on core overlap (r^2 < rcut_low^2), as Compute_MoleculePair_Energy
+// (energy_routines.f90:1676-1679) does.
+struct PairCount {
+  unsigned long long visited = 0, in_cut = 0;
+};
+
+template <bool MIXED>
+__device__ bool query_box(const BoxView& V, const PairTable& T, const double p[3], int qt, double qch, bool cbmc,
+                          bool want_qq, double& eout, PairCount& pc) {
+  const BoxDev& b = *V.b;
+  double rc = cbmc ? V.rc_cbmc : V.rc_full;
+  int lo[3], hi[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    double u = (p[d] + b.hL[d]) * b.cell_inv[d];
+    double w = rc * b.cell_inv[d];
+    int l = (int)floor(u - w - 1e-6), h = (int)floor(u + w + 1e-6);
+    if (h - l + 1 >= b.nc[d]) {
+      l = 0;
+      h = b.nc[d] - 1;
+    }
+    lo[d] = l;
+    hi[d] = h;
+  }
+  const bool qq_on = want_qq && b.charge_style == CASS_CHARGE_COUL;
+  if (MIXED && V.fast_mixed) {
+    const float px = (float)p[0], py = (float)p[1], pz = (float)p[2];
+    const double rv2 = cbmc ? b.rcut_cbmcsq : b.rcut_vdwsq;
+    const double rq2 = cbmc ? b.rcut_cbmcsq : b.rcut_coulsq;
+    const float rv2lo = (float)rv2 * (1.0f - kBand), rv2hi = (float)rv2 * (1.0f + kBand);
+    const float rq2lo = (float)rq2 * (1.0f - kBand), rq2hi = (float)rq2 * (1.0f + kBand);
+    const float low2 = (float)b.rcut_lowsq;
+    const float low2lo = low2 * (1.0f - kBand), low2hi = low2 * (1.0f + kBand);
+    const float alpha = (float)b.alpha;
+    const float qf = (float)qch;
+    const bool vdw_on = qt >= 0 && b.vdw_style == CASS_VDW_LJ;
+    float eps_row[kMaxTypes], sig_row[kMaxTypes];
+#pragma unroll
+    for (int t = 0; t < kMaxTypes; ++t) {
+      eps_row[t] = vdw_on && t < T.ntypes ? T.epsf[qt * T.ntypes + t] : 0.0f;
+      sig_row[t] = vdw_on && t < T.ntypes ? T.sig2f[qt * T.ntypes + t] : 0.0f;
+    }
+    KahanF acc;
+    for (int cz = lo[2]; cz <= hi[2]; ++cz) {
+      int wz = wrapc(cz, b.nc[2]);
+      for (int cy = lo[1]; cy <= hi[1]; ++cy) {
+        int row = (wz * b.nc[1] + wrapc(cy, b.nc[1])) * b.nc[0];
+        int cx = lo[0];
+        while (cx <= hi[0]) {
+          int wx = wrapc(cx, b.nc[0]);
+          int run = min(hi[0] - cx, b.nc[0] - 1 - wx) + 1;
+          int j1 = V.cstart[row + wx + run];
+          pc.visited += (unsigned long long)(j1 - V.cstart[row + wx]);
+          for (int j = V.cstart[row + wx]; j < j1; ++j) {
+            float4 a = V.p32[j];
+            float dx = fold(px - a.x, b.hLf[0], b.Lf[0]);
+            float dy = fold(py - a.y, b.hLf[1], b.Lf[1]);
+            float dz = fold(pz - a.z, b.hLf[2], b.Lf[2]);
+            float r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 > rv2hi && (!qq_on || r2 > rq2hi)) continue;
+            double r2x = -1.0;  // exact FP64 r^2, computed only near a threshold
+            if (r2 < low2hi) {
+              if (r2 < low2lo) return true;
+              double4_32a g = V.g64[j];
+              double ex = fold(p[0] - g.x, b.hL[0], b.L[0]), ey = fold(p[1] - g.y, b.hL[1], b.L[1]),
+                     ez = fold(p[2] - g.z, b.hL[2], b.L[2]);
+              r2x = ex * ex + ey * ey + ez * ez;
+              if (r2x < b.rcut_lowsq) return true;
+            }
+            bool vin, qin;
+            if (r2 <= rv2lo) vin = true;
+            else if (r2 > rv2hi) vin = false;
+            else {
+              if (r2x < 0.0) {
+                double4_32a g = V.g64[j];
+                double ex = fold(p[0] - g.x, b.hL[0], b.L[0]), ey = fold(p[1] - g.y, b.hL[1], b.L[1]),
+                       ez = fold(p[2] - g.z, b.hL[2], b.L[2]);
+                r2x = ex * ex + ey * ey + ez * ez;
+              }
+              vin = r2x <= rv2;
+            }
+            if (vin) {
+              ++pc.in_cut;
+              int tj = __float_as_int(a.w);
+              float e = 0.0f, s2 = 0.0f;
+#pragma unroll
+              for (int t = 0; t < kMaxTypes; ++t)
+                if (t == tj) {
+                  e = eps_row[t];
+                  s2 = sig_row[t];
+                }
+              if (tj >= 0) acc.add(lj_pair_f(e, s2, r2));
+            }
+            if (qq_on) {
+              if (r2 <= rq2lo) qin = true;
+              else if (r2 > rq2hi) qin = false;
+              else {
+                if (r2x < 0.0) {
+                  double4_32a g = V.g64[j];
+                  double ex = fold(p[0] - g.x, b.hL[0], b.L[0]), ey = fold(p[1] - g.y, b.hL[1], b.L[1]),
+                         ez = fold(p[2] - g.z, b.hL[2], b.L[2]);
+                  r2x = ex * ex + ey * ey + ez * ez;
+                }
+                qin = r2x <= rq2;
+              }
+              if (qin) acc.add(qq_ewald_inter_f(alpha, qf * V.q32[j], r2));
+            }
+          }
+          cx += run;
+        }
+      }
+    }
+    eout = acc.value();
+    return false;
+  }
+  // FP64 path (and mixed fallback for styles without an FP32 kernel)
+  const double4_32a* P = MIXED ? V.g64 : V.p64;
+  double acc = 0.0;
+  for (int cz = lo[2]; cz <= hi[2]; ++cz) {
+    int wz = wrapc(cz, b.nc[2]);
+    for (int cy = lo[1]; cy <= hi[1]; ++cy) {
+      int row = (wz * b.nc[1] + wrapc(cy, b.nc[1])) * b.nc[0];
+      int cx = lo[0];
+      while (cx <= hi[0]) {
+        int wx = wrapc(cx, b.nc[0]);
+        int run = min(hi[0] - cx, b.nc[0] - 1 - wx) + 1;
+        int j1 = V.cstart[row + wx + run];
+        pc.visited += (unsigned long long)(j1 - V.cstart[row + wx]);
+        for (int j = V.cstart[row + wx]; j < j1; ++j) {
+          double4_32a a = P[j];
+          double dx = fold(p[0] - a.x, b.hL[0], b.L[0]);
+          double dy = fold(p[1] - a.y, b.hL[1], b.L[1]);
+          double dz = fold(p[2] - a.z, b.hL[2], b.L[2]);
+          double r2 = dx * dx + dy * dy + dz * dz;
+          if (r2 < b.rcut_lowsq) return true;
+          int m = cutoff_mask(b, r2, cbmc);
+          if (!qq_on) m &= 1;
+          if (m) ++pc.in_cut;
+          if (m & 1) acc += vdw_pair(T, b, qt, V.ptype[j], r2, 1.0);
+          if (m & 2) acc += qq_pair_inter(b, qch * a.w, r2);
+        }
+        cx += run;
+      }
+    }
+  }
+  eout = acc;
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// test-molecule helpers (FP64)
+
+__device__ __forceinline__ void get_com(const WidomSpecies& S, const double* r, unsigned exist, double com[3]) {
+  double tm = 0, x = 0, y = 0, z = 0;
+  for (int k = 0; k < S.natoms; ++k) {
+    if (!((exist >> k) & 1u)) continue;
+    double m = S.mass[k];
+    tm += m;
+    x += m * r[3 * k];
+    y += m * r[3 * k + 1];
+    z += m * r[3 * k + 2];
+  }
+  com[0] = x / tm;
+  com[1] = y / tm;
+  com[2] = z / tm;
+}
+
+// Get_Aligner_Hanger (fragment_growth.f90:2135-2185), row-major
+__device__ void aligner_hanger(double v1[3], double v2[3], double al[9], double hg[9]) {
+  double n1 = sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+  for (int i = 0; i < 3; ++i) v1[i] = v1[i] / n1;
+  double n2 = sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
+  for (int i = 0; i < 3; ++i) v2[i] = v2[i] / n2;
+  double p1[3] = {v1[1] * v2[2] - v1[2] * v2[1], -v1[0] * v2[2] + v1[2] * v2[0], v1[0] * v2[1] - v1[1] * v2[0]};
+  double np1 = sqrt(p1[0] * p1[0] + p1[1] * p1[1] + p1[2] * p1[2]);
+  for (int i = 0; i < 3; ++i) p1[i] = p1[i] / np1;
+  double p2[3] = {v1[1] * p1[2] - v1[2] * p1[1], -v1[0] * p1[2] + v1[2] * p1[0], v1[0] * p1[1] - v1[1] * p1[0]};
+  double np2 = sqrt(p2[0] * p2[0] + p2[1] * p2[1] + p2[2] * p2[2]);
+  for (int i = 0; i < 3; ++i) p2[i] = p2[i] / np2;
+  for (int i = 0; i < 3; ++i) {
+    al[i] = v1[i];
+    al[3 + i] = p2[i];
+    al[6 + i] = p1[i];
+    hg[i * 3 + 0] = v1[i];
+    hg[i * 3 + 1] = p2[i];
+    hg[i * 3 + 2] = p1[i];
+  }
+}
+
+// Compute_Molecule_Dihedral_Energy over dihedrals whose atoms all exist (RB form)
+__device__ double dihedral_masked(const SpeciesDevHdr& H, const SpeciesPools& P, const double* r, unsigned exist) {
+  double e = 0.0;
+  for (int k = 0; k < H.ndih; ++k) {
+    const int* a = P.ip + H.dih_atoms_off + 4 * k;
+    unsigned m = (1u << a[0]) | (1u << a[1]) | (1u << a[2]) | (1u << a[3]);
+    if ((exist & m) != m) continue;
+    double c1 = dihedral_cos_d(r, a[0], a[1], a[2], a[3]);
+    double cv[6] = {1.0, c1, c1 * c1, 0, 0, 0};
+    cv[3] = cv[1] * cv[2];
+    cv[4] = cv[2] * cv[2];
+    cv[5] = cv[2] * cv[3];
+    double d = 0;
+    for (int j = 0; j < 6; ++j) d += cv[j] * P.dp[H.dih_rb_off + 6 * k + j];
+    e += d;
+  }
+  return e;
+}
+
+// Compute_Atom_Nonbond_Intra_Energy (energy_routines.f90:691-737), CBMC cutoffs
+__device__ bool atom_intra(const SpeciesDevHdr& H, const SpeciesPools& P, const BoxDev& b, const PairTable& T, int ia,
+                           const double* r, unsigned exist, double& eiv, double& eiq, double& eoq) {
+  eiv = eiq = eoq = 0.0;
+  int n = H.natoms;
+  for (int ja = 0; ja < n; ++ja) {
+    if (ja == ia || !((exist >> ja) & 1u)) continue;
+    double vs = P.dp[H.vs_off + ia * n + ja], qs = P.dp[H.qs_off + ia * n + ja];
+    bool nzv = vs > 0.0, nzq = qs > 0.0;
+    if (!(nzv || nzq)) continue;
+    double dx = r[3 * ja] - r[3 * ia], dy = r[3 * ja + 1] - r[3 * ia + 1], dz = r[3 * ja + 2] - r[3 * ia + 2];
+    double r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 < b.rcut_lowsq && nzv) return true;
+    int m = cutoff_mask(b, r2, true);
+    if (!nzv) m &= ~1;
+    if (!nzq) m &= ~2;
+    if (m & 1) eiv += vdw_pair(T, b, P.ip[H.type_off + ja], P.ip[H.type_off + ia], r2, P.dp[H.vs_off + ja * n + ia]);
+    if (m & 2) {
+      double per = 0.0;
+      eiq += qq_pair_intra(b, P.dp[H.q_off + ja] * P.dp[H.q_off + ia], r2, P.dp[H.qs_off + ja * n + ia], &per);
+      eoq += per;
+    }
+  }
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// K8: one Widom insertion per thread
+
+template <bool MIXED>
+__device__ void run_insertion(const WidomSpecies& S, const SpeciesPools& P, const PairTable& T, const BoxView& V,
+                              const double* __restrict__ lib, Lfsr rng, WRec& rec, int& status, double* xyz_out,
+                              CassWidomTrace* tr, PairCount& pc) {
+  const BoxDev& b = *V.b;
+  const SpeciesDevHdr& H = P.hdr[S.is0];
+  const int n = S.natoms;
+  const double beta = b.beta;
+  double r[3 * kMaxAtoms];
+  unsigned exist = 0u;
+  double ln_pbias = 0.0, ln_pseq;
+  double first_sum = 0.0;
+  int selected = 0;
+  bool cbmc_overlap = false;
+
+  // Step 1: first fragment and growth order (fragment_growth.f90:218-253, 1317-1446)
+  double u = rng.next();
+  int fstart = 0;
+  while (fstart < S.nfrag && !(u < S.cum_prob_ins[fstart])) ++fstart;
+  if (fstart >= S.nfrag) fstart = S.nfrag - 1;
+  ln_pseq = S.ln_prob_ins[fstart];
+  int order[kMaxFrags];
+  int norder = 1;
+  order[0] = fstart;
+  unsigned live = 1u << fstart;
+  if (S.nfrag > 1) {
+    int hang[kMaxFrags];
+    int nh = 0;
+    for (int k = 0; k < S.frag_nconnect[fstart]; ++k) {
+      int f = S.frag_connect[fstart][k];
+      if (!((live >> f) & 1u)) hang[nh++] = f;
+    }
+    while (nh > 0) {
+      double prob[kMaxFrags], cum[kMaxFrags];
+      for (int k = 0; k < nh; ++k) {
+        prob[k] = (double)(S.frag_natoms[hang[k]] - 2);
+        cum[k] = (k == 0 ? 0.0 : cum[k - 1]) + prob[k];
+      }
+      double tot = cum[nh - 1];
+      for (int k = 0; k < nh; ++k) {
+        prob[k] = prob[k] / tot;
+        cum[k] = cum[k] / tot;
+      }
+      double uu = rng.next();
+      int k = 0;
+      while (k < nh && !(uu < cum[k])) ++k;
+      if (k >= nh) k = nh - 1;
+      int f = hang[k];
+      ln_pseq = ln_pseq + log(prob[k]);
+      order[norder++] = f;
+      live |= 1u << f;
+      for (int q = k; q + 1 < nh; ++q) hang[q] = hang[q + 1];
+      --nh;
+      for (int q = 0; q < S.frag_nconnect[f]; ++q) {
+        int g = S.frag_connect[f][q];
+        if (!((live >> g) & 1u) && nh < kMaxFrags) hang[nh++] = g;
+      }
+    }
+  }
+
+  // Step 2: library conformation of the first fragment (:274-304)
+  const int nfa = S.frag_natoms[fstart];
+  {
+    int nconf = S.nconfig[fstart];
+    int conf = (int)(rng.next() * nconf);
+    if (conf >= nconf) conf = nconf - 1;
+    const double* L0 = lib + S.lib_off[fstart] + (size_t)conf * nfa * 3;
+    for (int i = 0; i < nfa; ++i) {
+      int a = S.frag_atoms[fstart][i];
+      r[3 * a] = L0[3 * i];
+      r[3 * a + 1] = L0[3 * i + 1];
+      r[3 * a + 2] = L0[3 * i + 2];
+      exist |= 1u << a;
+    }
+  }
+
+  // Step 3: Get_COM + Rotate_Molecule_Eulerian (rotation_routines.f90:41-137)
+  double com[3];
+  get_com(S, r, exist, com);
+  {
+    double theta = acos(1.0 - 2.0 * rng.next());
+    double phi = (1.0 - 2.0 * rng.next()) * kPI;
+    double psi = (1.0 - 2.0 * rng.next()) * kPI;
+    double st, ct, sp, cp, ss, cs;
+    sincos(theta, &st, &ct);
+    sincos(phi, &sp, &cp);
+    sincos(psi, &ss, &cs);
+    double r11 = cs * cp - ct * sp * ss, r12 = cs * sp + ct * cp * ss, r13 = ss * st;
+    double r21 = -ss * cp - ct * sp * cs, r22 = -ss * sp + ct * cp * cs, r23 = cs * st;
+    double r31 = st * sp, r32 = -st * cp, r33 = ct;
+    for (int i = 0; i < nfa; ++i) {
+      int a = S.frag_atoms[fstart][i];
+      double x = r[3 * a] - com[0], y = r[3 * a + 1] - com[1], z = r[3 * a + 2] - com[2];
+      r[3 * a] = (r11 * x + r12 * y + r13 * z) + com[0];
+      r[3 * a + 1] = (r21 * x + r22 * y + r23 * z) + com[1];
+      r[3 * a + 2] = (r31 * x + r32 * y + r33 * z) + com[2];
+    }
+  }
+
+  // Step 4: kappa_ins trial positions of the first fragment (:383-620)
+  const int ki = S.kappa_ins;
+  double nrg[kMaxKappa], w[kMaxKappa];
+  unsigned ovm = 0u;
+  double r0[3 * kMaxAtoms];
+  for (int i = 0; i < 3 * n; ++i) r0[i] = r[i];
+  const double com_old[3] = {com[0], com[1], com[2]};
+  Lfsr replay = rng;
+  for (int it = 0; it < ki; ++it) {
+    double ax = (0.5 - rng.next()) * b.L[0];
+    double ay = (0.5 - rng.next()) * b.L[1];
+    double az = (0.5 - rng.next()) * b.L[2];
+    double e = 0.0;
+    bool ov = false;
+    for (int i = 0; i < nfa && !ov; ++i) {
+      int a = S.frag_atoms[fstart][i];
+      double p[3] = {r0[3 * a] - com_old[0] + ax, r0[3 * a + 1] - com_old[1] + ay, r0[3 * a + 2] - com_old[2] + az};
+      double ea;
+      ov = query_box<MIXED>(V, T, p, S.type[a], S.q[a], true, S.want_qq_cbmc != 0, ea, pc);
+      e += ea;
+    }
+    nrg[it] = e;
+    w[it] = 0.0;
+    if (ov) {
+      ovm |= 1u << it;
+    } else {
+      double nk = beta * nrg[it];
+      if (nk >= kMAX_KBT) {
+        ovm |= 1u << it;
+      } else {
+        w[it] = exp(-nk);
+        first_sum += nrg[it];
+      }
+    }
+    if (it > 0) w[it] = w[it - 1] + w[it];
+  }
+  int sel = -1;
+  if (ovm == ((ki >= 32) ? 0xffffffffu : ((1u << ki) - 1u))) {
+    cbmc_overlap = true;
+  } else {
+    double rn = rng.next() * w[ki - 1];
+    int i = 0;
+    while (i < ki && !(rn < w[i])) ++i;
+    if (i == ki) cbmc_overlap = true;
+    else sel = i;
+  }
+  if (!cbmc_overlap) {
+    ln_pbias = ln_pbias - beta * nrg[sel] - log(w[ki - 1]);
+    double ax = 0, ay = 0, az = 0;
+    for (int k = 0; k <= sel; ++k) {
+      ax = (0.5 - replay.next()) * b.L[0];
+      ay = (0.5 - replay.next()) * b.L[1];
+      az = (0.5 - replay.next()) * b.L[2];
+    }
+    for (int i = 0; i < nfa; ++i) {
+      int a = S.frag_atoms[fstart][i];
+      r[3 * a] = r0[3 * a] - com_old[0] + ax;
+      r[3 * a + 1] = r0[3 * a + 1] - com_old[1] + ay;
+      r[3 * a + 2] = r0[3 * a + 2] - com_old[2] + az;
+    }
+    selected = sel + 1;
+  }
+
+  // Step 5: Fragment_Placement (:1449-2132)
+  if (!cbmc_overlap && norder > 1) {
+    double e_prev = dihedral_masked(H, P, r, exist);
+    unsigned placed = 1u << fstart;
+    const int kd = S.kappa_dih;
+    double dn[kMaxKappa], dd[kMaxKappa];
+    for (int oi = 1; oi < norder && !cbmc_overlap; ++oi) {
+      const int f = order[oi];
+      const int nf = S.frag_natoms[f];
+      unsigned grown = exist;
+      int nconf = S.nconfig[f];
+      int cf = (int)(rng.next() * nconf);
+      cf = (int)(rng.next() * nconf);  // the duplicated draw of fragment_growth.f90:1578,1584
+      if (cf >= nconf) cf = nconf - 1;
+      double cfg[3 * kMaxAtoms];
+      const double* Lf = lib + S.lib_off[f] + (size_t)cf * nf * 3;
+      for (int j = 0; j < nf; ++j) {
+        int a = S.frag_atoms[f][j];
+        exist |= 1u << a;
+        cfg[3 * a] = Lf[3 * j];
+        cfg[3 * a + 1] = Lf[3 * j + 1];
+        cfg[3 * a + 2] = Lf[3 * j + 2];
+      }
+      const unsigned combined = exist, newex = combined & ~grown;
+      int fc = -1;
+      for (int q = 0; q < S.frag_nconnect[f]; ++q) {
+        int g = S.frag_connect[f][q];
+        if ((placed >> g) & 1u) {
+          fc = g;
+          break;
+        }
+      }
+      if (fc < 0) {  // no placed neighbour: the fragment graph is not connected
+        cbmc_overlap = true;
+        break;
+      }
+      const int anc_i = S.frag_atoms[f][0], anc_c = S.frag_atoms[fc][0];
+      int ids[kMaxAtoms], nid = 0;
+      for (int j = 0; j < nf; ++j) {
+        int a = S.frag_atoms[f][j];
+        if (a != anc_i && a != anc_c) ids[nid++] = a;
+      }
+      unsigned idmask = 0u;
+      for (int j = 0; j < nid; ++j) idmask |= 1u << ids[j];
+      int atom_ifrag = nid > 0 ? ids[0] : S.frag_atoms[f][nf - 1];
+      int atom_fc = S.frag_atoms[fc][S.frag_natoms[fc] - 1];
+      for (int j = 0; j < S.frag_natoms[fc]; ++j) {
+        int a = S.frag_atoms[fc][j];
+        if (a != anc_i && a != anc_c) {
+          atom_fc = a;
+          break;
+        }
+      }
+      double v1[3], v2[3], al_i[9], hg_i[9], al_c[9], hg_c[9];
+      for (int d = 0; d < 3; ++d) {
+        v1[d] = cfg[3 * anc_i + d] - cfg[3 * anc_c + d];
+        v2[d] = cfg[3 * atom_ifrag + d] - cfg[3 * anc_c + d];
+      }
+      aligner_hanger(v1, v2, al_i, hg_i);
+      for (int d = 0; d < 3; ++d) {
+        v1[d] = r[3 * anc_i + d] - r[3 * anc_c + d];
+        v2[d] = r[3 * atom_fc + d] - r[3 * anc_c + d];
+      }
+      aligner_hanger(v1, v2, al_c, hg_c);
+      const double tx = cfg[3 * anc_c], ty = cfg[3 * anc_c + 1], tz = cfg[3 * anc_c + 2];
+      for (int j = 0; j < nf; ++j) {
+        int a = S.frag_atoms[f][j];
+        double x = cfg[3 * a] - tx, y = cfg[3 * a + 1] - ty, z = cfg[3 * a + 2] - tz;
+        cfg[3 * a] = x * al_i[0] + y * al_i[1] + z * al_i[2];
+        cfg[3 * a + 1] = x * al_i[3] + y * al_i[4] + z * al_i[5];
+        cfg[3 * a + 2] = x * al_i[6] + y * al_i[7] + z * al_i[8];
+      }
+      const double theta0 = kTWOPI * rng.next();
+      const double dtheta = kTWOPI / (double)kd;
+      unsigned dov = 0u;
+      double dw[kMaxKappa];
+      double theta = theta0;
+      for (int ii = 0; ii < kd; ++ii) {
+        if (ii > 0) theta = theta + dtheta;
+        double sth, cth;
+        sincos(theta, &sth, &cth);
+        for (int j = 0; j < nid; ++j) {
+          int a = ids[j];
+          double x = cfg[3 * a], y = cfg[3 * a + 1], z = cfg[3 * a + 2];
+          double yr = cth * y + sth * z, zr = -sth * y + cth * z;
+          r[3 * a] = (x * hg_c[0] + yr * hg_c[1] + zr * hg_c[2]) + r[3 * anc_c];
+          r[3 * a + 1] = (x * hg_c[3] + yr * hg_c[4] + zr * hg_c[5]) + r[3 * anc_c + 1];
+          r[3 * a + 2] = (x * hg_c[6] + yr * hg_c[7] + zr * hg_c[8]) + r[3 * anc_c + 2];
+        }
+        dn[ii] = 0.0;
+        dd[ii] = 0.0;
+        exist &= ~idmask;
+        double niv = 0.0, niq = 0.0, noq = 0.0;
+        bool ov = false;
+        for (int j = 0; j < nid; ++j) {
+          exist |= 1u << ids[j];
+          double eiv, eiq, eoq;
+          if (atom_intra(H, P, b, T, ids[j], r, exist, eiv, eiq, eoq)) {
+            ov = true;
+            break;
+          }
+          niv += eiv;
+          niq += eiq;
+          noq += eoq;
+        }
+        if (ov) {
+          dw[ii] = ii > 0 ? dw[ii - 1] : 0.0;
+          dov |= 1u << ii;
+          exist |= idmask;
+          continue;
+        }
+        double einter = 0.0;
+        for (int a = 0; a < n && !ov; ++a) {
+          if (!((newex >> a) & 1u)) continue;
+          double p[3] = {r[3 * a], r[3 * a + 1], r[3 * a + 2]};
+          double ea;
+          ov = query_box<MIXED>(V, T, p, S.type[a], S.q[a], true, S.want_qq_cbmc != 0, ea, pc);
+          einter += ea;
+        }
+        exist = combined;
+        if (ov) {
+          dw[ii] = 0.0;
+          dov |= 1u << ii;
+        } else {
+          double ed = dihedral_masked(H, P, r, exist);
+          dd[ii] = ed;
+          dn[ii] = ed + niv + niq + einter + noq - e_prev;
+          double nk = beta * dn[ii];
+          if (nk >= kMAX_KBT) {
+            dw[ii] = 0.0;
+            dov |= 1u << ii;
+          } else {
+            dw[ii] = exp(-nk);
+          }
+        }
+        if (ii > 0) dw[ii] = dw[ii - 1] + dw[ii];
+      }
+      if (dov == ((kd >= 32) ? 0xffffffffu : ((1u << kd) - 1u))) {
+        cbmc_overlap = true;
+        break;
+      }
+      double pp = rng.next() * dw[kd - 1];
+      int trl = 0;
+      while (trl < kd && !(pp < dw[trl])) ++trl;
+      if (trl == kd) {
+        cbmc_overlap = true;
+        break;
+      }
+      ln_pbias = ln_pbias - beta * dn[trl] - log(dw[kd - 1]);
+      theta = theta0;
+      for (int ii = 1; ii <= trl; ++ii) theta = theta + dtheta;
+      double sth, cth;
+      sincos(theta, &sth, &cth);
+      for (int j = 0; j < nid; ++j) {
+        int a = ids[j];
+        double x = cfg[3 * a], y = cfg[3 * a + 1], z = cfg[3 * a + 2];
+        double yr = cth * y + sth * z, zr = -sth * y + cth * z;
+        r[3 * a] = (x * hg_c[0] + yr * hg_c[1] + zr * hg_c[2]) + r[3 * anc_c];
+        r[3 * a + 1] = (x * hg_c[3] + yr * hg_c[4] + zr * hg_c[5]) + r[3 * anc_c + 1];
+        r[3 * a + 2] = (x * hg_c[6] + yr * hg_c[7] + zr * hg_c[8]) + r[3 * anc_c + 2];
+      }
+      e_prev = dd[trl];
+      placed |= 1u << f;
+    }
+    if (!cbmc_overlap) get_com(S, r, exist, com);
+  }
+
+  // widom_insert.f90:350-447
+  ln_pbias = ln_pbias + ln_pseq;
+  ln_pbias = ln_pbias + S.ln_kappa_ins;
+  ln_pbias = ln_pbias + S.ln_kappa_dih_term;
+  if (tr) {
+    tr->ln_pbias = ln_pbias;
+    tr->e_first_trial_sum = first_sum;
+    tr->selected_trial = selected;
+    tr->e_inter = 0.0;
+  }
+  rec = make_double4_32a(0.0, 0.0, 0.0, ln_pbias);
+  if (cbmc_overlap) {
+    status = 1;
+    return;
+  }
+  const unsigned all = (n >= 32) ? 0xffffffffu : ((1u << n) - 1u);
+  exist = all;
+  if (S.nfrag > 1) {  // Fold_Molecule, orthorhombic branch
+    for (int d = 0; d < 3; ++d) {
+      if (com[d] > b.hL[d]) {
+        com[d] = com[d] - b.L[d];
+        for (int a = 0; a < n; ++a) r[3 * a + d] -= b.L[d];
+      } else if (com[d] < -b.hL[d]) {
+        com[d] = com[d] + b.L[d];
+        for (int a = 0; a < n; ++a) r[3 * a + d] += b.L[d];
+      }
+    }
+  }
+  double e_inter = 0.0;
+  for (int a = 0; a < n; ++a) {
+    double p[3] = {r[3 * a], r[3 * a + 1], r[3 * a + 2]};
+    double ea;
+    if (query_box<MIXED>(V, T, p, S.type[a], S.q[a], false, true, ea, pc)) {
+      status = 2;
+      return;
+    }
+    e_inter += ea;
+  }
+  IntraOut io = molecule_intra(P, S.is0, b, T, r);
+  if (io.overlap) {
+    status = 3;
+    return;
+  }
+  e_inter = e_inter + io.pqq;
+  double dE_inter = e_inter + b.e_inter_constant;
+  double dE_intra = io.ivdw + io.iqq;
+  dE_intra = dE_intra + io.bond + io.angle + io.dih + io.imp;
+  rec = make_double4_32a(dE_intra, dE_inter, io.angle, ln_pbias);
+  status = 0;
+  if (tr) tr->e_inter = e_inter;
+  if (xyz_out)
+    for (int i = 0; i < 3 * n; ++i) xyz_out[i] = r[i];
+}
+
+template <bool MIXED, bool SMEM>
+__global__ void __launch_bounds__(128) k_widom(WidomSpecies S, PairTable T, SpeciesPools P, const BoxDev* boxes,
+                                               const int* box_ids, const double4_32a* c64, const float4* c32,
+                                               const int* ctype, const float* cq32, const int* cstart,
+                                               const double* __restrict__ lib, long long n_ins, uint64_t seed,
+                                               WRec* rec, signed char* status, double* xyz, int want_xyz,
+                                               CassWidomTrace* trace, unsigned long long* pair_counts) {
+  extern __shared__ __align__(32) unsigned char smem[];
+  __shared__ BoxDev sb;
+  const int k = blockIdx.y;
+  if (threadIdx.x == 0) sb = boxes[k];
+  __syncthreads();
+  const int na = sb.natoms;
+  const int ncell = sb.nc[0] * sb.nc[1] * sb.nc[2];
+  BoxView V;
+  V.b = &sb;
+  V.g64 = c64 + sb.atom_off;
+  V.q32 = cq32 + sb.atom_off;
+  V.rc_cbmc = sqrt(sb.rcut_cbmcsq);
+  double rfull = sqrt(fmax(sb.rcut_vdwsq, sb.rcut_coulsq));
+  if (sb.vdw_sum_style == CASS_VDW_SUM_MINIMUM || sb.vdw_sum_style == CASS_VDW_SUM_CHARMM ||
+      (sb.charge_style == CASS_CHARGE_COUL && sb.charge_sum_style == CASS_QQ_MINIMUM))
+    rfull = 1e30;
+  if (sb.vdw_sum_style == CASS_VDW_SUM_CUT_SWITCH) rfull = fmax(rfull, sqrt(sb.roff_switch_sq));
+  V.rc_full = rfull;
+  V.fast_mixed = sb.vdw_style == CASS_VDW_LJ &&
+                 (sb.vdw_sum_style == CASS_VDW_SUM_CUT || sb.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) &&
+                 (sb.charge_style == CASS_CHARGE_NONE || sb.charge_sum_style == CASS_QQ_EWALD);
+  if (SMEM) {
+    int* cs = reinterpret_cast<int*>(smem);
+    for (int c = threadIdx.x; c <= ncell; c += blockDim.x) cs[c] = cstart[sb.cell_off + k + c];
+    size_t off = ((size_t)(ncell + 1) * sizeof(int) + 31) & ~(size_t)31;
+    if (MIXED) {
+      float4* s32 = reinterpret_cast<float4*>(smem + off);
+      for (int j = threadIdx.x; j < na; j += blockDim.x) s32[j] = c32[sb.atom_off + j];
+      V.p32 = s32;
+      V.p64 = V.g64;
+      V.ptype = ctype + sb.atom_off;
+    } else {
+      double4_32a* s64 = reinterpret_cast<double4_32a*>(smem + off);
+      int* st = reinterpret_cast<int*>(smem + off + (size_t)na * sizeof(double4_32a));
+      for (int j = threadIdx.x; j < na; j += blockDim.x) {
+        s64[j] = c64[sb.atom_off + j];
+        st[j] = ctype[sb.atom_off + j];
+      }
+      V.p64 = s64;
+      V.ptype = st;
+      V.p32 = c32 + sb.atom_off;
+    }
+    V.cstart = cs;
+    __syncthreads();
+  } else {
+    V.cstart = cstart + sb.cell_off + k;
+    V.p64 = c64 + sb.atom_off;
+    V.p32 = c32 + sb.atom_off;
+    V.ptype = ctype + sb.atom_off;
+  }
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  PairCount pc;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n_ins; i += stride) {
+    size_t g = (size_t)k * n_ins + i;
+    Lfsr rng = seed_stream(seed, box_ids[k], i);
+    WRec rr;
+    int st = 0;
+    run_insertion<MIXED>(S, P, T, V, lib, rng, rr, st, want_xyz ? xyz + g * 3 * S.natoms : nullptr,
+                         trace ? trace + g : nullptr, pc);
+    rec[g] = rr;
+    status[g] = (signed char)st;
+    if (trace) trace[g].overlap = st;
+  }
+  if (pair_counts) {
+    atomicAdd(&pair_counts[0], pc.visited);
+    atomicAdd(&pair_counts[1], pc.in_cut);
+  }
+}
+
+// E_recip of each surviving insertion (absolute, as the reference computes it)
+__global__ void __launch_bounds__(256) k_widom_recip(const BoxDev* boxes, const double4_32a* kvec_all,
+                                                     const double* cos_all, const double* sin_all,
+                                                     const int* kvec_box_off, const int* ewald_box, long long n_ins,
+                                                     int na, const double* q, const signed char* status,
+                                                     const double* xyz, WRec* rec, CassWidomTrace* trace) {
+  __shared__ double sh[32];
+  long long gi = blockIdx.x;
+  int k = (int)(gi / n_ins);
+  if (!ewald_box[k] || status[gi] != 0) return;
+  const double4_32a* kv = kvec_all + kvec_box_off[k];
+  const double* cs = cos_all + kvec_box_off[k];
+  const double* sn = sin_all + kvec_box_off[k];
+  int nv = boxes[k].nvecs;
+  const double* r = xyz + (size_t)gi * 3 * na;
+  double e = 0.0;
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+    double4_32a h = kv[i];
+    double dc = 0.0, ds = 0.0;
+    for (int a = 0; a < na; ++a) {
+      double hdotr = h.x * r[3 * a] + h.y * r[3 * a + 1] + h.z * r[3 * a + 2];
+      double s, c;
+      sincos(hdotr, &s, &c);
+      dc += q[a] * c;
+      ds += q[a] * s;
+    }
+    double c = cs[i] + dc, s = sn[i] + ds;
+    e = e + h.w * (c * c + s * s);
+  }
+  for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = e;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+    double er = t * kCHARGE_FACTOR;
+    rec[gi].y = rec[gi].y + er;
+    if (trace) trace[gi].e_inter += er;
+  }
+}
+
+// widom_var and per-box sums; block per box, fixed-order reduction
+__global__ void __launch_bounds__(256) k_widom_finalize(const BoxDev* boxes, long long n_ins, const WRec* rec,
+                                                        const signed char* status, double* box_sum,
+                                                        long long* box_ov, CassWidomTrace* trace) {
+  __shared__ double shs[32];
+  __shared__ long long sho[32];
+  int k = blockIdx.x;
+  double beta = boxes[k].beta, ec = boxes[k].e_inter_constant;
+  double s = 0.0;
+  long long nov = 0;
+  for (long long i = threadIdx.x; i < n_ins; i += blockDim.x) {
+    size_t g = (size_t)k * n_ins + i;
+    double v = 0.0;
+    if (status[g] == 0) {
+      WRec r = rec[g];
+      double dE = r.x + r.y;
+      v = exp(-beta * (dE - r.z) - r.w);
+      s += v;
+    } else {
+      ++nov;
+    }
+    if (trace) {
+      trace[g].widom_var = v;
+      if (status[g] == 0) trace[g].e_inter = rec[g].y - ec;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_down_sync(0xffffffffu, s, o);
+    nov += __shfl_down_sync(0xffffffffu, nov, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    shs[threadIdx.x >> 5] = s;
+    sho[threadIdx.x >> 5] = nov;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    long long o = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      t += shs[w];
+      o += sho[w];
+    }
+    box_sum[k] = t;
+    box_ov[k] = o;
+  }
+}
+
+}  // namespace cassgpu
+
+using namespace cassgpu;
+
+namespace {
+
+double lrc_host(cass_ctx* c, const BoxH& B, const std::vector<double>& nb) {
+  int nt = c->ntypes;
+  double e = 0.0;
+  if (B.desc.vdw_style == CASS_VDW_LJ) {
+    for (int ia = 0; ia < nt; ++ia) {
+      double eij = 0.0;
+      for (int ja = 0; ja < nt; ++ja) {
+        double eps = c->pt.eps[pidx(ia, ja, nt)], s2 = c->pt.sig2[pidx(ia, ja, nt)];
+        double s6 = s2 * s2 * s2, s12 = s6 * s6;
+        eij = eij + nb[ja] * 4.0 * eps * (s12 / (9.0 * B.rcut9) - (s6 / (3.0 * B.rcut3)));
+      }
+      e = e + nb[ia] * eij;
+    }
+    e = 2.0 * kPI * e / B.dev.volume;
+  } else if (B.desc.vdw_style == CASS_VDW_MIE) {
+    for (int ia = 0; ia < nt; ++ia) {
+      double eij = 0.0;
+      for (int ja = 0; ja < nt; ++ja) {
+        int k = pidx(ia, ja, nt);
+        double sor = std::sqrt(c->pt.sig2[k]) / B.desc.rcut_vdw;
+        eij = eij + nb[ja] * c->pt.mie_c[k] * c->pt.eps[k] * std::pow(B.desc.rcut_vdw, 3.0) *
+                        ((std::pow(sor, c->pt.mie_n[k]) / (3.0 - c->pt.mie_n[k])) +
+                         (std::pow(sor, c->pt.mie_m[k]) / (c->pt.mie_m[k] - 3.0)));
+      }
+      e = e + nb[ia] * eij;
+    }
+    e = -2.0 * kPI * e / B.dev.volume;
+  }
+  return e;
+}
+
+}  // namespace
+
+namespace cassgpu {
+int ensure_pools(cass_ctx* c);
+int pack_box_ext(cass_ctx* c, int ibox);
+}  // namespace cassgpu
+
+extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const int32_t* iboxes, int64_t n_ins,
+                                 int32_t kappa_ins, int32_t kappa_dih, uint64_t seed, CassWidomResult* out,
+                                 CassWidomTrace* trace) {
+  if (!c || is1 < 1 || is1 > c->nspecies || nboxes < 1 || !iboxes || !out || n_ins < 0)
+    return set_error(CASS_EINVAL, "bad widom arguments");
+  if (kappa_ins < 1 || kappa_ins > kMaxKappa) return set_error(CASS_EINVAL, "kappa_ins must be in 1..32");
+  const SpeciesH& s = c->sp[is1 - 1];
+  if (!s.defined) return set_error(CASS_ESTATE, "species not defined");
+  if (s.nfrag < 1) return set_error(CASS_EINVAL, "species has no CBMC fragments");
+  if (s.nfrag > 1 && (kappa_dih < 1 || kappa_dih > kMaxKappa)) return set_error(CASS_EINVAL, "kappa_dih must be in 1..32");
+  if (s.natoms > kMaxAtoms) return set_error(CASS_ECAPACITY, "test species has more than 16 atoms");
+  if (s.nfrag > kMaxFrags) return set_error(CASS_ECAPACITY, "test species has more than 8 fragments");
+  for (int f = 0; f < s.nfrag; ++f) {
+    if (s.frag_nconfig[f] < 1) return set_error(CASS_EINVAL, "fragment library is empty");
+    if (s.frag_connect[f].size() > (size_t)kMaxFrags) return set_error(CASS_ECAPACITY, "too many fragment connections");
+  }
+  if (!c->pt_set) return set_error(CASS_ESTATE, "nonbond table not set");
+  for (int k = 0; k < nboxes; ++k) {
+    int ib = iboxes[k] - 1;
+    if (ib < 0 || ib >= c->nboxes) return set_error(CASS_EINVAL, "box index out of range");
+    if (!c->box[ib].energy_valid) return set_error(CASS_ESTATE, "system energy of box not computed");
+  }
+  int rc;
+  CASS_CUDA(cudaSetDevice(c->device));
+  if ((rc = ensure_pools(c))) return rc;
+  const int is0 = is1 - 1;
+
+  // test species tables
+  WidomSpecies S;
+  memset(&S, 0, sizeof(S));
+  S.natoms = s.natoms;
+  S.nfrag = s.nfrag;
+  S.is0 = is0;
+  S.kappa_ins = kappa_ins;
+  S.kappa_dih = s.nfrag > 1 ? kappa_dih : 0;
+  S.want_qq_cbmc = s.l_coul_cbmc ? 1 : 0;
+  S.ln_kappa_ins = std::log((double)kappa_ins);
+  S.ln_kappa_dih_term = kappa_dih != 0 ? (double)(s.nfrag - 1) * std::log((double)kappa_dih) : 0.0;
+  for (int a = 0; a < s.natoms; ++a) {
+    S.mass[a] = s.mass[a];
+    S.q[a] = s.q[a];
+    S.type[a] = s.type[a];
+  }
+  for (int f = 0; f < s.nfrag; ++f) {
+    S.frag_natoms[f] = (int)s.frag_atoms[f].size();
+    for (size_t j = 0; j < s.frag_atoms[f].size(); ++j) S.frag_atoms[f][j] = (signed char)s.frag_atoms[f][j];
+    S.frag_nconnect[f] = (int)s.frag_connect[f].size();
+    for (size_t j = 0; j < s.frag_connect[f].size(); ++j) S.frag_connect[f][j] = (signed char)s.frag_connect[f][j];
+    S.nconfig[f] = s.frag_nconfig[f];
+    S.lib_off[f] = s.lib_off[f];
+    S.prob_ins[f] = s.prob_ins[f];
+    S.cum_prob_ins[f] = s.cum_prob_ins[f];
+    S.ln_prob_ins[f] = std::log(s.prob_ins[f]);
+  }
+
+  // per-box constants and cell grids
+  std::vector<BoxDev> bd(nboxes);
+  std::vector<BoxSrc> src(nboxes);
+  std::vector<int> kvoff(nboxes, 0), has_ew(nboxes, 0);
+  int atom_off = 0, cell_off = 0, kv_total = 0, max_na = 0;
+  size_t max_smem = 0;
+  const bool mixed = c->precision == CASS_PREC_MIXED;
+  bool any_recip = false;
+  for (int k = 0; k < nboxes; ++k) {
+    int ib = iboxes[k] - 1;
+    if ((rc = pack_box_ext(c, ib))) return rc;
+    BoxH& B = c->box[ib];
+    BoxDev v = B.dev;
+    double rcell = B.desc.rcut_cbmc > 0.0 ? B.desc.rcut_cbmc : B.rcut_max;
+    int ncell = 1;
+    for (int d = 0; d < 3; ++d) {
+      v.nc[d] = std::max(1, (int)std::floor(v.L[d] / rcell));
+      v.nc[d] = std::min(v.nc[d], 64);
+      v.cell_inv[d] = (double)v.nc[d] / v.L[d];
+      ncell *= v.nc[d];
+    }
+    v.atom_off = atom_off;
+    v.natoms = B.npacked;
+    v.cell_off = cell_off;
+    // Widom_Insert set-up (widom_insert.f90:201-245)
+    int nmols = 1;
+    for (int im = 0; im < c->max_mol[is0]; ++im)
+      if (c->mol_box[c->mol_base[is0] + im] == ib) ++nmols;
+    v.prefactor = v.volume / (double)nmols;
+    double lrc_diff = 0.0;
+    if (B.desc.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) {
+      std::vector<double> nb(c->ntypes, 0.0);
+      for (int js = 0; js < c->nspecies; ++js) {
+        const SpeciesH& t = c->sp[js];
+        if (!t.defined) continue;
+        for (int jm = 0; jm < c->max_mol[js]; ++jm)
+          if (c->mol_box[c->mol_base[js] + jm] == ib)
+            for (int a = 0; a < t.natoms; ++a)
+              if (t.type[a] >= 0) nb[t.type[a]] += 1.0;
+      }
+      for (int a = 0; a < s.natoms; ++a)
+        if (s.type[a] >= 0) nb[s.type[a]] += 1.0;
+      lrc_diff = lrc_host(c, B, nb) - B.energy.lrc;
+    }
+    double e_self = 0.0, e_recip_in = 0.0;
+    if (B.desc.charge_style == CASS_CHARGE_COUL && s.has_charge) {
+      double qq = 0.0;
+      for (int a = 0; a < s.natoms; ++a) qq += s.q[a] * s.q[a];
+      if (B.desc.charge_sum_style == CASS_QQ_EWALD) e_self = -qq * kCHARGE_FACTOR * v.alpha / kROOTPI;
+      else if (B.desc.charge_sum_style == CASS_QQ_DSF)
+        e_self = -qq * (v.alpha_dsf / kROOTPI + v.dsf_factor1 / 2.0) * kCHARGE_FACTOR;
+      e_recip_in = B.energy.reciprocal;
+    }
+    v.e_inter_constant = lrc_diff + e_self - e_recip_in;
+    if (B.desc.charge_style == CASS_CHARGE_COUL && B.desc.charge_sum_style == CASS_QQ_EWALD && s.has_charge &&
+        B.nvecs > 0) {
+      has_ew[k] = 1;
+      any_recip = true;
+    }
+    kvoff[k] = kv_total;
+    kv_total += B.nvecs;
+    bd[k] = v;
+    src[k].p64 = B.d_p64.as<double4_32a>();
+    src[k].p32 = B.d_p32.as<float4>();
+    src[k].meta = B.d_meta.as<int4>();
+    size_t sm = (((size_t)(ncell + 1) * sizeof(int) + 31) & ~(size_t)31) +
+                (size_t)B.npacked * (mixed ? sizeof(float4) : (sizeof(double4_32a) + sizeof(int)));
+    max_smem = std::max(max_smem, sm);
+    max_na = std::max(max_na, B.npacked);
+    atom_off += B.npacked;
+    cell_off += ncell;
+  }
+  const int total_atoms = std::max(1, atom_off), total_cells = cell_off;
+  // device buffers
+  DevBuf& dbox = c->d_boxdev;
+  if ((rc = dbox.reserve(nboxes * sizeof(BoxDev) + nboxes * sizeof(BoxSrc) + 3 * nboxes * sizeof(int) + 64))) return rc;
+  BoxDev* d_bd = dbox.as<BoxDev>();
+  BoxSrc* d_src = reinterpret_cast<BoxSrc*>(d_bd + nboxes);
+  int* d_ids = reinterpret_cast<int*>(d_src + nboxes);
+  int* d_kvoff = d_ids + nboxes;
+  int* d_hasew = d_kvoff + nboxes;
+  if ((rc = c->d_c64.reserve((size_t)total_atoms * sizeof(double4_32a)))) return rc;
+  if ((rc = c->d_c32.reserve((size_t)total_atoms * sizeof(float4) + (size_t)total_atoms * 2 * sizeof(int)))) return rc;
+  if ((rc = c->d_cq32.reserve((size_t)total_atoms * sizeof(float)))) return rc;
+  if ((rc = c->d_cell_start.reserve(((size_t)total_cells + nboxes) * sizeof(int)))) return rc;
+  if ((rc = c->d_cell_count.reserve(((size_t)total_cells * 2 + 64) * sizeof(int)))) return rc;
+  if ((rc = c->d_cell_of.reserve((size_t)total_atoms * sizeof(int)))) return rc;
+  float4* d_c32 = c->d_c32.as<float4>();
+  int* d_ctype = reinterpret_cast<int*>(d_c32 + total_atoms);
+  int* d_corig = d_ctype + total_atoms;
+  int* d_count = c->d_cell_count.as<int>();
+  int* d_fill = d_count + total_cells;
+  CASS_CUDA(h2d(c, d_bd, bd.data(), nboxes * sizeof(BoxDev)));
+  CASS_CUDA(h2d(c, d_src, src.data(), nboxes * sizeof(BoxSrc)));
+  CASS_CUDA(h2d(c, d_ids, iboxes, nboxes * sizeof(int)));
+  CASS_CUDA(h2d(c, d_kvoff, kvoff.data(), nboxes * sizeof(int)));
+  CASS_CUDA(h2d(c, d_hasew, has_ew.data(), nboxes * sizeof(int)));
+  CASS_CUDA(cudaEventRecord(c->ev[0], c->stream));
+  CASS_CUDA(cudaMemsetAsync(d_count, 0, (size_t)std::max(1, total_cells) * sizeof(int), c->stream));
+  // K7
+  if (max_na > 0) {
+    dim3 g((max_na + 255) / 256, nboxes);
+    k_cell_count<<<g, 256, 0, c->stream>>>(d_src, d_bd, c->d_cell_of.as<int>(), d_count);
+    k_cell_scan<<<nboxes, 1024, 0, c->stream>>>(d_bd, d_count, c->d_cell_start.as<int>(), d_fill);
+    k_cell_scatter<<<g, 256, 0, c->stream>>>(d_src, d_bd, c->d_cell_of.as<int>(), c->d_cell_start.as<int>(), d_fill,
+                                             c->d_c64.as<double4_32a>(), d_c32, d_ctype, c->d_cq32.as<float>(), d_corig);
+    int maxc = 1;
+    for (int k = 0; k < nboxes; ++k) maxc = std::max(maxc, bd[k].nc[0] * bd[k].nc[1] * bd[k].nc[2]);
+    dim3 gs((maxc + 127) / 128, nboxes);
+    k_cell_sort<<<gs, 128, 0, c->stream>>>(d_bd, nboxes, c->d_cell_start.as<int>(), c->d_c64.as<double4_32a>(), d_c32,
+                                           d_ctype, c->d_cq32.as<float>(), d_corig);
+  } else {
+    k_cell_scan<<<nboxes, 1024, 0, c->stream>>>(d_bd, d_count, c->d_cell_start.as<int>(), d_fill);
+  }
+  CASS_CUDA(cudaGetLastError());
+  count_launch(c, max_na > 0 ? 4 : 1);
+  // per-insertion records
+  size_t nrec = (size_t)nboxes * (size_t)std::max<int64_t>(1, n_ins);
+  DevBuf& drec = c->d_widom_out;
+  if ((rc = drec.reserve(nrec * (sizeof(WRec) + 1) + 64))) return rc;
+  WRec* d_rec = drec.as<WRec>();
+  signed char* d_status = reinterpret_cast<signed char*>(d_rec + nrec);
+  double* d_xyz = nullptr;
+  if (any_recip) {
+    if ((rc = c->d_widom_xyz.reserve(nrec * 3 * s.natoms * sizeof(double) + s.natoms * sizeof(double)))) return rc;
+    d_xyz = c->d_widom_xyz.as<double>();
+  }
+  CassWidomTrace* d_trace = nullptr;
+  if (trace) {
+    if ((rc = c->d_trace.reserve(nrec * sizeof(CassWidomTrace)))) return rc;
+    d_trace = c->d_trace.as<CassWidomTrace>();
+  }
+  if ((rc = c->d_box_sums.reserve((size_t)nboxes * (sizeof(double) + sizeof(long long)) + 2 * sizeof(long long))))
+    return rc;
+  double* d_bsum = c->d_box_sums.as<double>();
+  long long* d_bov = reinterpret_cast<long long*>(d_bsum + nboxes);
+  unsigned long long* d_pairs = c->count_pairs ? reinterpret_cast<unsigned long long*>(d_bov + nboxes) : nullptr;
+  if (d_pairs) CASS_CUDA(cudaMemsetAsync(d_pairs, 0, 2 * sizeof(unsigned long long), c->stream));
+  // K8 launch shape: 128-thread CTAs, enough CTAs per box to fill every SM
+  bool use_smem = max_smem <= (size_t)200 * 1024;
+  int dev_sms = 0;
+  CASS_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
+  const int threads = 128;
+  auto launch = [&](auto kern) -> int {
+    if (use_smem) CASS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem));
+    int per_sm = 1;
+    CASS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, use_smem ? max_smem : 0));
+    per_sm = std::max(per_sm, 1);
+    long long want = ((long long)dev_sms * per_sm * 2 + nboxes - 1) / nboxes;
+    long long need = (n_ins + threads - 1) / threads;
+    int chunks = (int)std::max<long long>(1, std::min(want, need));
+    dim3 g(chunks, nboxes);
+    c->stats.widom_grid_x = chunks;
+    c->stats.widom_grid_y = nboxes;
+    c->stats.widom_block = threads;
+    c->stats.widom_smem_bytes = use_smem ? (int)max_smem : 0;
+    CASS_CUDA(cudaEventRecord(c->ev[1], c->stream));
+    kern<<<g, threads, use_smem ? max_smem : 0, c->stream>>>(
+        S, c->pt, c->pools, d_bd, d_ids, c->d_c64.as<double4_32a>(), d_c32, d_ctype, c->d_cq32.as<float>(),
+        c->d_cell_start.as<int>(), s.d_library.as<double>(), (long long)n_ins, seed, d_rec, d_status, d_xyz,
+        any_recip ? 1 : 0, d_trace, d_pairs);
+    CASS_CUDA(cudaGetLastError());
+    CASS_CUDA(cudaEventRecord(c->ev[2], c->stream));
+    count_launch(c);
+    return CASS_OK;
+  };
+  if (n_ins > 0) {
+    if (mixed) rc = use_smem ? launch(k_widom<true, true>) : launch(k_widom<true, false>);
+    else rc = use_smem ? launch(k_widom<false, true>) : launch(k_widom<false, false>);
+    if (rc) return rc;
+    if (any_recip) {
+      // k-vectors and structure factors of the batch boxes, concatenated
+      if ((rc = c->d_partial.reserve((size_t)std::max(1, kv_total) * sizeof(double) * 6))) return rc;
+      double4_32a* d_kv = reinterpret_cast<double4_32a*>(c->d_partial.p);
+      double* d_cs = reinterpret_cast<double*>(d_kv + kv_total);
+      double* d_sn = d_cs + kv_total;
+      for (int k = 0; k < nboxes; ++k) {
+        BoxH& B = c->box[iboxes[k] - 1];
+        if (!B.nvecs) continue;
+        CASS_CUDA(cudaMemcpyAsync(d_kv + kvoff[k], B.d_kvec.p, B.nvecs * sizeof(double4_32a), cudaMemcpyDeviceToDevice,
+                                  c->stream));
+        CASS_CUDA(cudaMemcpyAsync(d_cs + kvoff[k], B.d_cos_sum.p, B.nvecs * sizeof(double), cudaMemcpyDeviceToDevice,
+                                  c->stream));
+        CASS_CUDA(cudaMemcpyAsync(d_sn + kvoff[k], B.d_sin_sum.p, B.nvecs * sizeof(double), cudaMemcpyDeviceToDevice,
+                                  c->stream));
+      }
+      double* d_q = d_xyz + nrec * 3 * s.natoms;
+      CASS_CUDA(h2d(c, d_q, s.q.data(), s.natoms * sizeof(double)));
+      k_widom_recip<<<(unsigned)nrec, 256, 0, c->stream>>>(d_bd, d_kv, d_cs, d_sn, d_kvoff, d_hasew, (long long)n_ins,
+                                                          s.natoms, d_q, d_status, d_xyz, d_rec, d_trace);
+      CASS_CUDA(cudaGetLastError());
+  count_launch(c);
+    }
+  }
+  k_widom_finalize<<<nboxes, 256, 0, c->stream>>>(d_bd, (long long)n_ins, d_rec, d_status, d_bsum, d_bov, d_trace);
+  CASS_CUDA(cudaGetLastError());
+  count_launch(c);
+  CASS_CUDA(cudaEventRecord(c->ev[3], c->stream));
+  unsigned long long hpairs[2] = {0, 0};
+  if (d_pairs) CASS_CUDA(d2h(c, hpairs, d_pairs, sizeof(hpairs)));
+  std::vector<double> hs(nboxes);
+  std::vector<long long> ho(nboxes);
+  CASS_CUDA(d2h(c, hs.data(), d_bsum, nboxes * sizeof(double)));
+  CASS_CUDA(d2h(c, ho.data(), d_bov, nboxes * sizeof(long long)));
+  if (trace)
+    CASS_CUDA(d2h(c, trace, d_trace, nrec * sizeof(CassWidomTrace)));
+  CASS_CUDA(cudaStreamSynchronize(c->stream));
+  float ms_all = 0.0f, ms_k = 0.0f;
+  CASS_CUDA(cudaEventElapsedTime(&ms_all, c->ev[0], c->ev[3]));
+  if (n_ins > 0) CASS_CUDA(cudaEventElapsedTime(&ms_k, c->ev[1], c->ev[2]));
+  c->stats.widom_ms = ms_all;
+  c->stats.widom_kernel_ms = ms_k;
+  c->stats.widom_pairs_visited = (int64_t)hpairs[0];
+  c->stats.widom_pairs_in_cutoff = (int64_t)hpairs[1];
+  for (int k = 0; k < nboxes; ++k) {
+    out[k].widom_sum = hs[k] * bd[k].prefactor;
+    out[k].prefactor = bd[k].prefactor;
+    out[k].n_insertions = n_ins;
+    out[k].n_overlaps = ho[k];
+    out[k].n_trials = n_ins * (int64_t)(kappa_ins + (s.nfrag - 1) * (s.nfrag > 1 ? kappa_dih : 0));
+  }
+  return CASS_OK;
+}

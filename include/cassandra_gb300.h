@@ -226,6 +226,25 @@ int cass_widom_insert(cass_ctx* ctx, int32_t is, int32_t nboxes, const int32_t* 
                       int64_t n_insertions, int32_t kappa_ins, int32_t kappa_dih,
                       uint64_t seed, CassWidomResult* out, CassWidomTrace* trace);
 
+/* ---- run-time extensions (no counterpart in the reference) ------------- */
+/* Counters of a context, for measurement.  Times are CUDA-event durations on
+ * the context's stream of the most recent cass_widom_insert call. */
+typedef struct CassStats {
+  double widom_ms;          /* whole call: cell lists + CBMC kernel + reciprocal + reduction */
+  double widom_kernel_ms;   /* the CBMC Widom kernel alone */
+  int64_t kernel_launches;  /* kernels launched by this context since creation */
+  int64_t h2d_bytes, d2h_bytes;  /* host<->device bytes copied since creation */
+  int64_t widom_pairs_visited;   /* box atoms visited by the last Widom call (count_pairs mode) */
+  int64_t widom_pairs_in_cutoff; /* of which inside a cutoff */
+  int32_t widom_grid_x, widom_grid_y, widom_block;
+  int32_t widom_smem_bytes;
+} CassStats;
+int cass_get_stats(cass_ctx* ctx, CassStats* out);
+/* count_pairs != 0 makes the Widom kernel count visited / in-cutoff pairs. */
+int cass_set_count_pairs(cass_ctx* ctx, int32_t count_pairs);
+/* Runs the context's work on a caller-owned cudaStream_t (NULL: its own). */
+int cass_set_stream(cass_ctx* ctx, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

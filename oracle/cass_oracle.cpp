@@ -1216,6 +1216,8 @@ int orc_set_species(orc_ctx* c, int32_t is, const CassSpeciesDesc* d) {
     return fail(CASS_EINVAL, "species arrays missing");
   if (d->nfragments > 0 && (!d->frag_natoms || !d->frag_atoms || !d->frag_nconnect || !d->frag_nconfig))
     return fail(CASS_EINVAL, "fragment arrays missing");
+  for (int f = 0; f < d->nfragments; ++f)
+    if (d->frag_natoms[f] < 1 || d->frag_natoms[f] > d->natoms) return fail(CASS_EINVAL, "bad fragment sizes");
   Species& s = c->sp[is - 1];
   int n = d->natoms;
   s = Species();

@@ -1,0 +1,251 @@
+"""GPU parity: libcassgpu.so through its C-ABI against the FP64 oracle and the
+reference's golden values.
+
+FP64 path : same arithmetic as the reference; energies agree with the oracle to
+            1e-10 relative (summation order is the only difference) and
+            per-insertion Widom records (status, selected trial, ln_pbias,
+            widom_var) agree insertion by insertion.
+mixed path: FP32 pair math with FP64 accumulation; trial and total energies
+            within 1e-5 of the FP64 oracle relative to the sum of |pair
+            terms| (MIXED_TOL below), Widom statistics within their error.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import cassandra_gb300 as cg
+import helpers
+from cassandra_gb300 import abi, workloads
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+KJ = 0.01
+FP64_TOL = 1e-10
+MIXED_TOL = 1e-5
+
+
+def close(a, b, rel, scale=1.0):
+    return abs(a - b) <= rel * max(abs(b), scale)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from cassandra_gb300 import build
+    build.build()
+    oracle.build()
+
+
+@pytest.mark.parametrize("prec", [abi.PREC_FP64, abi.PREC_MIXED])
+@pytest.mark.parametrize("name", ["water_spce", "pentane"])
+def test_pregen_frame_totals(name, prec):
+    d = helpers.golden(f"pregen_{name}.npz")
+    for f, want in enumerate(d["energy_total_kjmol"]):
+        s = helpers.pregen_system(name, f)
+        with oracle.open_system(s) as o, cg.open_system(s, precision=prec) as g:
+            eo, ovo = o.system_total_energy(1)
+            eg, ovg = g.system_total_energy(1)
+        assert ovo == ovg == False
+        if prec == abi.PREC_FP64:
+            for k in eo:
+                assert close(eg[k], eo[k], FP64_TOL, 1e-6), (f, k, eg[k], eo[k])
+            assert abs(eg["total"] * KJ - want) <= 5e-8 * abs(want) + 1e-4
+        else:
+            scale = abs(eo["inter_vdw"]) + abs(eo["inter_q"]) + abs(eo["intra"])
+            assert abs(eg["total"] - eo["total"]) <= MIXED_TOL * scale, (f, eg["total"], eo["total"])
+
+
+@pytest.mark.parametrize("k", range(4))
+def test_nist_spce_fp64(k):
+    s = helpers.nist_spce_system(k)
+    with oracle.open_system(s) as o, cg.open_system(s, precision=abi.PREC_FP64) as g:
+        eo, _ = o.system_total_energy(1)
+        eg, _ = g.system_total_energy(1)
+    for key in eo:
+        assert close(eg[key], eo[key], FP64_TOL, 1e-6), (key, eg[key], eo[key])
+
+
+@pytest.mark.parametrize("k", range(8))
+def test_nist_lj_fp64(k):
+    d = helpers.golden("nist_lj.npz")
+    f, L, rc, tot, vdw, lrc = d["checks"][k]
+    s = helpers.single_atom_system(d[f"xyz{int(f)}"], L, rcut=rc)
+    with cg.open_system(s, precision=abi.PREC_FP64) as g:
+        eg, ov = g.system_total_energy(1)
+    assert not ov
+    for got, want in ((eg["total"], tot), (eg["inter_vdw"], vdw), (eg["lrc"], lrc)):
+        assert abs(got * KJ - want) <= 1e-2 * abs(want)
+
+
+@pytest.mark.parametrize("prec", [abi.PREC_FP64, abi.PREC_MIXED])
+def test_molecule_energies(prec):
+    s = helpers.pregen_system("water_spce", 3)
+    rng = np.random.default_rng(3)
+    with oracle.open_system(s) as o, cg.open_system(s, precision=prec) as g:
+        for im in rng.choice(90, 12, replace=False) + 1:
+            for cbmc in (False, True):
+                a = o.mol_inter_energy(int(im), 1, cbmc)
+                b = g.mol_inter_energy(int(im), 1, cbmc)
+                assert a[2] == b[2]
+                tol = FP64_TOL if prec == abi.PREC_FP64 else MIXED_TOL
+                scale = abs(a[0]) + abs(a[1]) + 1.0
+                assert abs(a[0] - b[0]) <= tol * scale and abs(a[1] - b[1]) <= tol * scale, (im, cbmc, a, b)
+            ia = o.mol_intra_energy(int(im), 1)
+            ib = g.mol_intra_energy(int(im), 1)
+            assert ia[3] == ib[3]
+            for x, y in zip(ia[:3], ib[:3]):
+                assert close(y, x, FP64_TOL, 1e-6)
+
+
+def test_molecule_overlap_flag():
+    s = helpers.pregen_system("water_spce", 0)
+    xyz = s.molecules.xyz[1].copy()
+    xyz += s.molecules.xyz[0][0] - xyz[0] + np.array([0.3, 0.0, 0.0])  # O atoms 0.3 A apart
+    with oracle.open_system(s) as o, cg.open_system(s, precision=abi.PREC_FP64) as g:
+        for c in (o, g):
+            c.set_molecules([2], [1], [1], xyz)
+        assert o.mol_inter_energy(2, 1)[2] is True
+        assert g.mol_inter_energy(2, 1)[2] is True
+        assert g.system_total_energy(1)[1] is True
+
+
+@pytest.mark.parametrize("move", [abi.MOVE_TRANSLATION, abi.MOVE_ROTATION, abi.MOVE_DELETION])
+def test_ewald_update_and_restore(move):
+    s = helpers.pregen_system("water_spce", 2)
+    with oracle.open_system(s) as o, cg.open_system(s, precision=abi.PREC_FP64) as g:
+        e0o = o.system_total_energy(1)[0]["reciprocal"]
+        e0g = g.system_total_energy(1)[0]["reciprocal"]
+        assert close(e0g, e0o, FP64_TOL)
+        xyz = s.molecules.xyz[6] + np.array([0.41, -0.27, 0.13])
+        if move != abi.MOVE_DELETION:
+            for c in (o, g):
+                c.set_molecules([7], [1], [1], xyz)
+        eo = o.ewald_update(7, 1, 1, move)
+        eg = g.ewald_update(7, 1, 1, move)
+        assert close(eg, eo, FP64_TOL), (eg, eo)
+        g.ewald_restore(7, 1, 1)
+        o.ewald_restore(7, 1, 1)
+        # after a restore the next update from the restored state matches again
+        eo2 = o.ewald_update(7, 1, 1, abi.MOVE_INTRA)
+        eg2 = g.ewald_update(7, 1, 1, abi.MOVE_INTRA)
+        assert close(eg2, eo2, FP64_TOL)
+
+
+def test_ewald_widom_batch():
+    s = helpers.pregen_system("water_spce", 5)
+    rng = np.random.default_rng(5)
+    base = s.molecules.xyz[0]
+    L = s.boxes[0].length[0]
+    xyz = np.concatenate([(base - base.mean(0)) @ workloads.random_rotation(rng).T + (rng.random(3) - 0.5) * L
+                          for _ in range(24)])
+    with oracle.open_system(s) as o, cg.open_system(s, precision=abi.PREC_FP64) as g:
+        o.system_total_energy(1)
+        g.system_total_energy(1)
+        a = o.ewald_widom(1, 1, xyz)
+        b = g.ewald_widom(1, 1, xyz)
+    assert np.allclose(b, a, rtol=FP64_TOL, atol=0)
+
+
+def _butane_batch(sizes, seed=9):
+    return workloads.widom_batch_system(nboxes=len(sizes), sizes=sizes, seed=seed, nconfig=200)
+
+
+def _totals(ctx, nb):
+    for b in range(1, nb + 1):
+        ctx.system_total_energy(b)
+
+
+def test_widom_fp64_matches_oracle_per_insertion():
+    sizes = [200, 450, 900]
+    s = _butane_batch(sizes)
+    n = 384
+    with oracle.open_system(s) as o, cg.open_system(s, precision=abi.PREC_FP64) as g:
+        _totals(o, 3)
+        _totals(g, 3)
+        ro, to = o.widom_insert(2, [1, 2, 3], n, 12, 12, seed=77, trace=True)
+        rg, tg = g.widom_insert(2, [1, 2, 3], n, 12, 12, seed=77, trace=True)
+    assert np.array_equal(to["overlap"], tg["overlap"])
+    assert np.array_equal(to["selected_trial"], tg["selected_trial"])
+    assert np.allclose(tg["ln_pbias"], to["ln_pbias"], rtol=1e-10, atol=1e-10)
+    ok = to["overlap"] == 0
+    assert ok.sum() > 0.5 * ok.size
+    assert np.allclose(tg["widom_var"][ok], to["widom_var"][ok], rtol=1e-8, atol=0)
+    assert np.allclose(tg["e_inter"][ok], to["e_inter"][ok], rtol=1e-9, atol=1e-8)
+    for a, b in zip(ro, rg):
+        assert a["n_overlaps"] == b["n_overlaps"] and a["n_trials"] == b["n_trials"]
+        assert close(b["widom_sum"], a["widom_sum"], 1e-8)
+
+
+def test_widom_mixed_matches_fp64():
+    sizes = [300, 700]
+    s = _butane_batch(sizes, seed=21)
+    n = 2048
+    with cg.open_system(s, precision=abi.PREC_FP64) as d, cg.open_system(s, precision=abi.PREC_MIXED) as m:
+        _totals(d, 2)
+        _totals(m, 2)
+        rd, td = d.widom_insert(2, [1, 2], n, 12, 12, seed=5, trace=True)
+        rm, tm = m.widom_insert(2, [1, 2], n, 12, 12, seed=5, trace=True)
+    same = (td["overlap"] == tm["overlap"]) & (td["selected_trial"] == tm["selected_trial"])
+    assert same.mean() > 0.98
+    ok = same & (td["overlap"] == 0)
+    # full-cutoff inter energies of the grown molecule: FP32 pairs, FP64 sums
+    ed, em = td["e_inter"][ok], tm["e_inter"][ok]
+    assert np.all(np.abs(em - ed) <= MIXED_TOL * np.maximum(np.abs(ed), 100.0))
+    # mu' per box agrees within the FP64 run's statistical error
+    for b in range(2):
+        w_d = td["widom_var"][b]
+        w_m = tm["widom_var"][b]
+        err = w_d.std() / math.sqrt(n) + 1e-300
+        assert abs(w_m.mean() - w_d.mean()) <= 3 * err + 1e-3 * abs(w_d.mean())
+
+
+def test_widom_deterministic():
+    s = _butane_batch([400])
+    with cg.open_system(s, precision=abi.PREC_MIXED) as g:
+        g.system_total_energy(1)
+        a = g.widom_insert(2, [1], 1000, 12, 12, seed=3)
+        b = g.widom_insert(2, [1], 1000, 12, 12, seed=3)
+    assert a == b
+
+
+def test_widom_charged_spce_fp64():
+    s = helpers.pregen_system("water_spce", 0)
+    sp = s.species[0]
+    sp.libraries = [workloads.water_species().libraries[0] * 1.0]
+    n = 96
+    with oracle.open_system(s) as o, cg.open_system(s, precision=abi.PREC_FP64) as g:
+        o.system_total_energy(1)
+        g.system_total_energy(1)
+        ro, to = o.widom_insert(1, [1], n, 12, 0, seed=11, trace=True)
+        rg, tg = g.widom_insert(1, [1], n, 12, 0, seed=11, trace=True)
+    assert np.array_equal(to["overlap"], tg["overlap"])
+    assert np.array_equal(to["selected_trial"], tg["selected_trial"])
+    ok = to["overlap"] == 0
+    assert np.allclose(tg["e_inter"][ok], to["e_inter"][ok], rtol=1e-9, atol=1e-7)
+    assert np.allclose(tg["widom_var"][ok], to["widom_var"][ok], rtol=1e-8, atol=0)
+
+
+def test_widom_edge_cases():
+    s = _butane_batch([200, 250])
+    with cg.open_system(s, precision=abi.PREC_MIXED) as g:
+        with pytest.raises(abi.CassError) as e:
+            g.widom_insert(2, [1], 10, 12, 12, seed=1)
+        assert e.value.code == abi.CASS_ESTATE
+        g.system_total_energy(1)
+        g.system_total_energy(2)
+        with pytest.raises(abi.CassError):
+            g.widom_insert(2, [1], 10, 33, 12, seed=1)
+        with pytest.raises(abi.CassError):
+            g.widom_insert(2, [3], 10, 12, 12, seed=1)
+        r = g.widom_insert(2, [1, 2], 0, 12, 12, seed=1)
+        assert r[0]["widom_sum"] == 0.0 and r[0]["n_insertions"] == 0
+    # an empty box: every insertion is an ideal-gas insertion (no neighbours)
+    s2 = _butane_batch([200])
+    s2.molecules = type(s2.molecules)()
+    with oracle.open_system(s2) as o, cg.open_system(s2, precision=abi.PREC_FP64) as g:
+        o.system_total_energy(1)
+        g.system_total_energy(1)
+        ro, to = o.widom_insert(2, [1], 64, 12, 12, seed=4, trace=True)
+        rg, tg = g.widom_insert(2, [1], 64, 12, 12, seed=4, trace=True)
+    assert np.allclose(tg["widom_var"], to["widom_var"], rtol=1e-9)
