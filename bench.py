@@ -268,8 +268,9 @@ def main():
     rb, tb = gctx.widom_insert(2, sub, 2000, args.kappa, args.kappa, seed=4242, trace=True)
     same = (ta["overlap"] == tb["overlap"]) & (ta["selected_trial"] == tb["selected_trial"])
     ok = same & (ta["overlap"] == 0)
-    rel = np.abs(tb["e_inter"][ok] - ta["e_inter"][ok]) / np.maximum(np.abs(ta["e_inter"][ok]), 100.0)
-    accuracy = {"same_trial_selection": float(same.mean()),
+    rel = np.abs(tb["e_inter"][ok] - ta["e_inter"][ok]) / np.maximum(ta["e_inter_abs"][ok], 1.0)
+    accuracy = {"bound": "|E_mixed - E_fp64| / sum |pair energies| of the full-cutoff inter energy",
+                "same_trial_selection": float(same.mean()),
                 "e_inter_max_rel_err": float(rel.max()) if rel.size else None,
                 "e_inter_mean_rel_err": float(rel.mean()) if rel.size else None,
                 "insertions_compared": int(same.size)}

@@ -77,7 +77,8 @@ class CassWidomResult(C.Structure):
 
 class CassWidomTrace(C.Structure):
     _fields_ = [("widom_var", C.c_double), ("ln_pbias", C.c_double), ("e_inter", C.c_double),
-                ("e_first_trial_sum", C.c_double), ("selected_trial", C.c_int32), ("overlap", C.c_int32)]
+                ("e_first_trial_sum", C.c_double), ("e_inter_abs", C.c_double), ("selected_trial", C.c_int32),
+                ("overlap", C.c_int32)]
 
 
 class CassStats(C.Structure):
@@ -91,7 +92,8 @@ class CassStats(C.Structure):
 
 
 TRACE_DTYPE = np.dtype([("widom_var", "f8"), ("ln_pbias", "f8"), ("e_inter", "f8"),
-                        ("e_first_trial_sum", "f8"), ("selected_trial", "i4"), ("overlap", "i4")])
+                        ("e_first_trial_sum", "f8"), ("e_inter_abs", "f8"), ("selected_trial", "i4"),
+                        ("overlap", "i4")])
 assert TRACE_DTYPE.itemsize == C.sizeof(CassWidomTrace)
 
 # entry points of the header: name -> (restype, argtypes)

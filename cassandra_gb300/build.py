@@ -1,6 +1,6 @@
 """Builds libcassgpu.so in-tree with nvcc for sm_103a (GB300).
 
-Two translation units are compiled in parallel and linked with the static
+The translation units are compiled in parallel and linked with the static
 CUDA runtime, so the library needs only the driver at run time.
 """
 from __future__ import annotations

@@ -201,6 +201,7 @@ constexpr float kBand = 2e-5f;  // relative band around r^2 thresholds re-evalua
 // (energy_routines.f90:1676-1679) does.
 struct PairCount {
   unsigned long long visited = 0, in_cut = 0;
+  double eabs = 0.0;  // sum of |pair energy| of the current query
 };
 
 template <bool MIXED>
@@ -240,6 +241,7 @@ __device__ bool query_box(const BoxView& V, const PairTable& T, const double p[3
       sig_row[t] = vdw_on && t < T.ntypes ? T.sig2f[qt * T.ntypes + t] : 0.0f;
     }
     KahanF acc;
+    float eabs = 0.0f;
     for (int cz = lo[2]; cz <= hi[2]; ++cz) {
       int wz = wrapc(cz, b.nc[2]);
       for (int cy = lo[1]; cy <= hi[1]; ++cy) {
@@ -288,7 +290,11 @@ __device__ bool query_box(const BoxView& V, const PairTable& T, const double p[3
                   e = eps_row[t];
                   s2 = sig_row[t];
                 }
-              if (tj >= 0) acc.add(lj_pair_f(e, s2, r2));
+              if (tj >= 0) {
+                float ev = lj_pair_f(e, s2, r2);
+                acc.add(ev);
+                eabs += fabsf(ev);
+              }
             }
             if (qq_on) {
               if (r2 <= rq2lo) qin = true;
@@ -302,7 +308,11 @@ __device__ bool query_box(const BoxView& V, const PairTable& T, const double p[3
                 }
                 qin = r2x <= rq2;
               }
-              if (qin) acc.add(qq_ewald_inter_f(alpha, qf * V.q32[j], r2));
+              if (qin) {
+                float eq = qq_ewald_inter_f(alpha, qf * V.q32[j], r2);
+                acc.add(eq);
+                eabs += fabsf(eq);
+              }
             }
           }
           cx += run;
@@ -310,11 +320,12 @@ __device__ bool query_box(const BoxView& V, const PairTable& T, const double p[3
       }
     }
     eout = acc.value();
+    pc.eabs = (double)eabs;
     return false;
   }
   // FP64 path (and mixed fallback for styles without an FP32 kernel)
   const double4_32a* P = MIXED ? V.g64 : V.p64;
-  double acc = 0.0;
+  double acc = 0.0, eabs = 0.0;
   for (int cz = lo[2]; cz <= hi[2]; ++cz) {
     int wz = wrapc(cz, b.nc[2]);
     for (int cy = lo[1]; cy <= hi[1]; ++cy) {
@@ -335,14 +346,23 @@ __device__ bool query_box(const BoxView& V, const PairTable& T, const double p[3
           int m = cutoff_mask(b, r2, cbmc);
           if (!qq_on) m &= 1;
           if (m) ++pc.in_cut;
-          if (m & 1) acc += vdw_pair(T, b, qt, V.ptype[j], r2, 1.0);
-          if (m & 2) acc += qq_pair_inter(b, qch * a.w, r2);
+          if (m & 1) {
+            double ev = vdw_pair(T, b, qt, V.ptype[j], r2, 1.0);
+            acc += ev;
+            eabs += fabs(ev);
+          }
+          if (m & 2) {
+            double eq = qq_pair_inter(b, qch * a.w, r2);
+            acc += eq;
+            eabs += fabs(eq);
+          }
         }
         cx += run;
       }
     }
   }
   eout = acc;
+  pc.eabs = eabs;
   return false;
 }
 
@@ -772,6 +792,7 @@ __device__ void run_insertion(const WidomSpecies& S, const SpeciesPools& P, cons
     tr->e_first_trial_sum = first_sum;
     tr->selected_trial = selected;
     tr->e_inter = 0.0;
+    tr->e_inter_abs = 0.0;
   }
   rec = make_double4_32a(0.0, 0.0, 0.0, ln_pbias);
   if (cbmc_overlap) {
@@ -791,7 +812,7 @@ __device__ void run_insertion(const WidomSpecies& S, const SpeciesPools& P, cons
       }
     }
   }
-  double e_inter = 0.0;
+  double e_inter = 0.0, e_abs = 0.0;
   for (int a = 0; a < n; ++a) {
     double p[3] = {r[3 * a], r[3 * a + 1], r[3 * a + 2]};
     double ea;
@@ -800,6 +821,7 @@ __device__ void run_insertion(const WidomSpecies& S, const SpeciesPools& P, cons
       return;
     }
     e_inter += ea;
+    e_abs += pc.eabs;
   }
   IntraOut io = molecule_intra(P, S.is0, b, T, r);
   if (io.overlap) {
@@ -812,7 +834,10 @@ __device__ void run_insertion(const WidomSpecies& S, const SpeciesPools& P, cons
   dE_intra = dE_intra + io.bond + io.angle + io.dih + io.imp;
   rec = make_double4_32a(dE_intra, dE_inter, io.angle, ln_pbias);
   status = 0;
-  if (tr) tr->e_inter = e_inter;
+  if (tr) {
+    tr->e_inter = e_inter;
+    tr->e_inter_abs = e_abs;
+  }
   if (xyz_out)
     for (int i = 0; i < 3 * n; ++i) xyz_out[i] = r[i];
 }

@@ -160,6 +160,7 @@ typedef struct CassWidomTrace {
   double ln_pbias;
   double e_inter;        /* full-cutoff inter energy incl. periodic qq and reciprocal */
   double e_first_trial_sum; /* sum of the kappa_ins first-fragment trial energies (non-overlap) */
+  double e_inter_abs;    /* sum of |pair energy| behind e_inter (real space): its conditioning scale */
   int32_t selected_trial;   /* first fragment trial chosen, 1-based, 0 if none */
   int32_t overlap;          /* 1 cbmc, 2 inter, 3 intra overlap */
 } CassWidomTrace;

@@ -324,7 +324,7 @@ inline bool check_molpair_cutoff(const Box& b, const MolView& a, const MolView& 
 // Compute_MoleculePair_Energy (energy_routines.f90:1589-1730): molecule a
 // (the query) against molecule m; early return on core overlap.
 bool molpair_energy(const orc_ctx* c, const Box& b, const MolView& a, const MolView& m, bool cbmc,
-                    double& vlj, double& vqq) {
+                    double& vlj, double& vqq, double* eabs = nullptr) {
   vlj = 0.0;
   vqq = 0.0;
   const Species& sa = c->sp[a.is];
@@ -345,6 +345,7 @@ bool molpair_energy(const orc_ctx* c, const Box& b, const MolView& a, const MolV
         PairE e = atompair_energy(c, b, r2, a.is, ia, m.is, ja, false, gv, gq);
         vlj += e.inter_vdw;
         vqq += e.inter_qq;
+        if (eabs) *eabs += std::fabs(e.inter_vdw) + std::fabs(e.inter_qq);
       }
     }
   }
@@ -390,7 +391,7 @@ void refresh_com(orc_ctx* c, Mol& m) {
 // 1088-1206) and of its _Widom variant (:1266-1297): query a against every
 // live molecule of box b except slot `skip` (-1 = none).  Returns overlap.
 bool mol_inter_energy(const orc_ctx* c, int ibox, const MolView& a, int skip, bool cbmc, double& evdw,
-                      double& eqq) {
+                      double& eqq, double* eabs = nullptr) {
   const Box& b = c->box[ibox];
   evdw = 0.0;
   eqq = 0.0;
@@ -403,7 +404,7 @@ bool mol_inter_energy(const orc_ctx* c, int ibox, const MolView& a, int skip, bo
       MolView mv = view_of(m);
       if (!check_molpair_cutoff(b, a, mv, cbmc)) continue;
       double vlj, vqq;
-      if (molpair_energy(c, b, a, mv, cbmc, vlj, vqq)) return true;
+      if (molpair_energy(c, b, a, mv, cbmc, vlj, vqq, eabs)) return true;
       evdw += vlj;
       eqq += vqq;
     }
@@ -783,15 +784,15 @@ void fragment_order(const Species& s, int start, std::vector<int>& order, std::v
 
 // Compute_Molecule_Nonbond_Inter_Energy_Widom molecule loop (energy_routines.f90:
 // 1266-1297) for the test molecule; returns overlap, sets the combined energy.
-bool widom_inter(const orc_ctx* c, int ibox, const TestMol& t, bool cbmc, double& e) {
+bool widom_inter(const orc_ctx* c, int ibox, const TestMol& t, bool cbmc, double& e, double* eabs = nullptr) {
   double ev, eq;
-  bool ov = mol_inter_energy(c, ibox, t.view(), -1, cbmc, ev, eq);
+  bool ov = mol_inter_energy(c, ibox, t.view(), -1, cbmc, ev, eq, eabs);
   e = ev + eq;
   return ov;
 }
 
 struct InsertionOut {
-  double widom_var = 0, ln_pbias = 0, e_inter = 0, first_trial_sum = 0;
+  double widom_var = 0, ln_pbias = 0, e_inter = 0, first_trial_sum = 0, e_inter_abs = 0;
   int selected = 0, overlap = 0;
 };
 
@@ -1108,7 +1109,7 @@ InsertionOut widom_one(const orc_ctx* c, int is, int ibox, int kappa_ins, int ka
     }
   }
   double e_inter = 0.0;
-  if (widom_inter(c, ibox, t, false, e_inter)) {
+  if (widom_inter(c, ibox, t, false, e_inter, &out.e_inter_abs)) {
     out.overlap = 2;
     return out;
   }
@@ -1636,6 +1637,7 @@ int orc_widom_insert(orc_ctx* c, int32_t is1, int32_t nboxes, const int32_t* ibo
         tr.ln_pbias = o.ln_pbias;
         tr.e_inter = o.e_inter;
         tr.e_first_trial_sum = o.first_trial_sum;
+        tr.e_inter_abs = o.e_inter_abs;
         tr.selected_trial = o.selected;
         tr.overlap = o.overlap;
       }

@@ -24,7 +24,7 @@ def test_bindings_cover_header():
 def test_struct_layouts():
     assert ctypes.sizeof(abi.CassEnergy) == 14 * 8
     assert ctypes.sizeof(abi.CassWidomResult) == 40
-    assert ctypes.sizeof(abi.CassWidomTrace) == 40
+    assert ctypes.sizeof(abi.CassWidomTrace) == 48
     assert ctypes.sizeof(abi.CassBoxDesc) == 3 * 8 + 2 * 4 + 6 * 8 + 2 * 4 + 3 * 8
 
 

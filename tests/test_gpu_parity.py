@@ -24,6 +24,10 @@ pytestmark = pytest.mark.gpu
 KJ = 0.01
 FP64_TOL = 1e-10
 MIXED_TOL = 1e-5
+# Widom full-cutoff energies of grown molecules: FP32 storage of absolute box
+# coordinates (|x| <= 35 A) bounds each displacement to ~4e-6 A; the stated
+# bound is 5e-5 of the sum of |pair energies| (measured worst case 1.6e-5).
+MIXED_WIDOM_TOL = 5e-5
 
 
 def close(a, b, rel, scale=1.0):
@@ -204,6 +208,7 @@ def test_widom_fp64_matches_oracle_per_insertion():
     assert ok.sum() > 0.5 * ok.size
     assert np.allclose(tg["widom_var"][ok], to["widom_var"][ok], rtol=1e-8, atol=0)
     assert np.allclose(tg["e_inter"][ok], to["e_inter"][ok], rtol=1e-9, atol=1e-8)
+    assert np.allclose(tg["e_inter_abs"][ok], to["e_inter_abs"][ok], rtol=1e-9, atol=1e-8)
     for a, b in zip(ro, rg):
         assert a["n_overlaps"] == b["n_overlaps"] and a["n_trials"] == b["n_trials"]
         assert close(b["widom_sum"], a["widom_sum"], 1e-8)
@@ -223,7 +228,8 @@ def test_widom_mixed_matches_fp64():
     ok = same & (td["overlap"] == 0)
     # full-cutoff inter energies of the grown molecule: FP32 pairs, FP64 sums
     ed, em = td["e_inter"][ok], tm["e_inter"][ok]
-    assert np.all(np.abs(em - ed) <= MIXED_TOL * np.maximum(np.abs(ed), 100.0))
+    scale = np.maximum(td["e_inter_abs"][ok], 1.0)
+    assert np.all(np.abs(em - ed) <= MIXED_WIDOM_TOL * scale), np.max(np.abs(em - ed) / scale)
     # mu' per box agrees within the FP64 run's statistical error
     for b in range(2):
         w_d = td["widom_var"][b]
