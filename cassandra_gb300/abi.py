@@ -116,12 +116,16 @@ SIGNATURES = {
     "ewald_widom": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _f64p, _f64p]),
     "widom_insert": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _i32p, C.c_int64, C.c_int32, C.c_int32,
                                C.c_uint64, C.POINTER(CassWidomResult), C.c_void_p]),
-    # run-time extensions of the GPU library (no counterpart in the reference)
+    # allocation-free energy entry point and run-time extensions of the GPU
+    # library (no counterpart in the reference)
+    "mol_box_energy_noalloc": (C.c_int, [C.POINTER(CassBoxDesc), C.c_int32, _f64p, _f64p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
+                                         C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "get_stats": (C.c_int, [C.c_void_p, C.POINTER(CassStats)]),
     "set_count_pairs": (C.c_int, [C.c_void_p, C.c_int32]),
     "set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
-OPTIONAL = {"get_stats", "set_count_pairs", "set_stream"}
+OPTIONAL = {"get_stats", "set_count_pairs", "set_stream", "mol_box_energy_noalloc"}
 
 
 class CassError(RuntimeError):

@@ -227,6 +227,29 @@ int cass_widom_insert(cass_ctx* ctx, int32_t is, int32_t nboxes, const int32_t* 
                       int64_t n_insertions, int32_t kappa_ins, int32_t kappa_dih,
                       uint64_t seed, CassWidomResult* out, CassWidomTrace* trace);
 
+/* ---- allocation-free energy entry point -------------------------------- */
+/* No counterpart in the reference.  For hosts that cannot call cudaMalloc in
+ * their Monte Carlo move loop (device memory owned by another allocator, or an
+ * allocation that would synchronize the device mid-loop): the energy of one
+ * molecule against the atoms of a box, as cass_mol_inter_energy computes it,
+ * with caller-provided DEVICE arrays and no allocation of any kind.  Its
+ * scratch (16 KB: per-block partial sums, a block counter, an overlap flag) is
+ * a static device array that every GPU loading this library keeps until exit.
+ *   box_xyzq [n][4] x, y, z, charge; box_type [n] 1-based type (0: no vdW);
+ *   box_mol [n] molecule ids, atoms with box_mol == skip_mol are skipped;
+ *   query_xyzq [nq][4], query_type [nq]; eps/sig: host [ntypes*ntypes] tables.
+ *   out: device [3] = E_vdw, E_qq, overlap (1.0/0.0; energies 0 on overlap).
+ * Limits: n <= 262144, 1 <= nq <= 64, LJ or no vdW.  Larger sizes return
+ * CASS_ECAPACITY.  Runs on the current device, asynchronously on `stream`.
+ * All calls on a device share the scratch: calls that overlap on the GPU race.
+ * The first call on a device resolves the scratch address; make it before any
+ * stream capture. */
+int cass_mol_box_energy_noalloc(const CassBoxDesc* box, int32_t ntypes, const double* eps, const double* sig,
+                                const double* box_xyzq, const int32_t* box_type, const int32_t* box_mol,
+                                int32_t n, const double* query_xyzq, const int32_t* query_type, int32_t nq,
+                                int32_t skip_mol, int32_t cbmc_flag, int32_t l_coul_cbmc, int32_t precision,
+                                double* out, void* stream);
+
 /* ---- run-time extensions (no counterpart in the reference) ------------- */
 /* Counters of a context, for measurement.  Times are CUDA-event durations on
  * the context's stream of the most recent cass_widom_insert call. */
