@@ -45,6 +45,28 @@ cudaError_t d2h(cass_ctx_impl* c, void* dst, const void* src, size_t n) {
 // packed molecule record: mol slot, species (0-based), first packed atom, natoms
 using MolInfo = int4;
 
+struct BoxPtrs {
+  double4_32a* p64;
+  float4* p32;
+};
+
+__global__ void k_patch_atoms(const PatchRec* rec, int n, const BoxPtrs* bp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const PatchRec r = rec[i];
+  const BoxPtrs b = bp[r.box];
+  double4_32a p = b.p64[r.atom];
+  p.x = r.x;
+  p.y = r.y;
+  p.z = r.z;
+  b.p64[r.atom] = p;
+  float4 f = b.p32[r.atom];
+  f.x = (float)r.x;
+  f.y = (float)r.y;
+  f.z = (float)r.z;
+  b.p32[r.atom] = f;
+}
+
 constexpr int kBlock = 256;
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
@@ -478,6 +500,25 @@ void invalidate(cass_ctx* c, int ibox) {
   c->box[ibox].cell_dirty = true;
 }
 
+// live molecule slots of a box, species-major and in locate order
+const std::vector<int>& members(cass_ctx* c, int ibox) {
+  if (c->members_dirty) {
+    for (auto& m : c->box_members) m.clear();
+    c->box_members.resize(c->nboxes);
+    for (int slot = 0; slot < c->nmol_slots; ++slot) {
+      int b = c->mol_box[slot];
+      if (b >= 0 && c->sp[c->slot_sp[slot]].defined) c->box_members[b].push_back(slot);
+    }
+    c->members_dirty = false;
+  }
+  return c->box_members[ibox];
+}
+
+void set_mol_box(cass_ctx* c, int slot, int ibox) {
+  if (c->mol_box[slot] != ibox) c->members_dirty = true;
+  c->mol_box[slot] = ibox;
+}
+
 // Packs the live molecules of a box (species-major, locate order) and uploads.
 int pack_box(cass_ctx* c, int ibox) {
   BoxH& B = c->box[ibox];
@@ -488,12 +529,11 @@ int pack_box(cass_ctx* c, int ibox) {
   std::vector<int4> molinfo;
   B.pk_mol.clear();
   B.pk_mol_off.clear();
-  for (int is = 0; is < c->nspecies; ++is) {
-    const SpeciesH& s = c->sp[is];
-    if (!s.defined) continue;
-    for (int im = 0; im < c->max_mol[is]; ++im) {
-      int slot = c->mol_base[is] + im;
-      if (c->mol_box[slot] != ibox) continue;
+  for (int slot : members(c, ibox)) {
+    {
+      const int is = c->slot_sp[slot], im = slot - c->mol_base[is];
+      const SpeciesH& s = c->sp[is];
+      c->pk_index[slot] = (int)B.pk_mol.size();
       B.pk_mol.push_back(slot);
       B.pk_mol_off.push_back((int)p64.size());
       molinfo.push_back(make_int4(slot, is, (int)p64.size(), s.natoms));
@@ -588,13 +628,10 @@ double lr_correction(cass_ctx* c, const BoxH& B, const std::vector<double>& nb) 
 
 std::vector<double> count_beads(cass_ctx* c, int ibox) {
   std::vector<double> nb(c->ntypes, 0.0);
-  for (int is = 0; is < c->nspecies; ++is) {
-    const SpeciesH& s = c->sp[is];
-    if (!s.defined) continue;
-    for (int im = 0; im < c->max_mol[is]; ++im)
-      if (c->mol_box[c->mol_base[is] + im] == ibox)
-        for (int a = 0; a < s.natoms; ++a)
-          if (s.type[a] >= 0) nb[s.type[a]] += 1.0;
+  for (int slot : members(c, ibox)) {
+    const SpeciesH& s = c->sp[c->slot_sp[slot]];
+    for (int a = 0; a < s.natoms; ++a)
+      if (s.type[a] >= 0) nb[s.type[a]] += 1.0;
   }
   return nb;
 }
@@ -603,6 +640,7 @@ std::vector<double> count_beads(cass_ctx* c, int ibox) {
 
 namespace cassgpu {
 int pack_box_ext(cass_ctx* c, int ibox) { return pack_box(c, ibox); }
+const std::vector<int>& members_ext(cass_ctx* c, int ibox) { return members(c, ibox); }
 }  // namespace cassgpu
 
 // ===========================================================================
@@ -642,6 +680,10 @@ int cass_ctx_create(const CassConfig* cfg, cass_ctx** out) {
   }
   c->nmol_slots = tot;
   c->mol_box.assign(tot, -1);
+  c->pk_index.assign(tot, -1);
+  c->slot_sp.resize(tot);
+  for (int i = 0; i < c->nspecies; ++i)
+    for (int m = 0; m < c->max_mol[i]; ++m) c->slot_sp[c->mol_base[i] + m] = i;
   c->sp.resize(c->nspecies);
   c->box.resize(c->nboxes);
   if (cudaSetDevice(c->device) != cudaSuccess ||
@@ -663,7 +705,10 @@ int cass_ctx_destroy(cass_ctx* c) {
   if (!c) return CASS_OK;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
-  for (auto& s : c->sp) s.d_library.release();
+  for (auto& s : c->sp) {
+    s.d_library.release();
+    s.d_library_f.release();
+  }
   c->box.clear();
   for (int k = 0; k < 4; ++k)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
@@ -813,12 +858,18 @@ int cass_set_species(cass_ctx* c, int32_t is, const CassSpeciesDesc* d) {
     if (s.q[i] != 0.0) s.has_charge = true;
   s.pos.assign((size_t)c->max_mol[is - 1] * 3 * n, 0.0);
   s.d_library.release();
+  s.d_library_f.release();
   if (!s.library.empty()) {
     int rc = s.d_library.reserve(s.library.size() * sizeof(double));
     if (rc) return rc;
     CASS_CUDA(h2d(c, s.d_library.p, s.library.data(), s.library.size() * sizeof(double)));
+    // FP32 copy read by the mixed-precision Widom kernel
+    std::vector<float> lf(s.library.begin(), s.library.end());
+    if ((rc = s.d_library_f.reserve(lf.size() * sizeof(float)))) return rc;
+    CASS_CUDA(h2d(c, s.d_library_f.p, lf.data(), lf.size() * sizeof(float)));
   }
   s.defined = true;
+  c->members_dirty = true;
   c->pools_dirty = true;
   for (int b = 0; b < c->nboxes; ++b) invalidate(c, b);
   return CASS_OK;
@@ -917,45 +968,67 @@ int cass_set_box(cass_ctx* c, int32_t ibox, const CassBoxDesc* d) {
 int cass_set_molecules(cass_ctx* c, int32_t n, const int32_t* im, const int32_t* is, const int32_t* ibox,
                        const double* xyz) {
   if (!c || n < 0 || (n > 0 && (!im || !is || !ibox || !xyz))) return set_error(CASS_EINVAL, "bad molecule list");
-  size_t off = 0;
   for (int k = 0; k < n; ++k) {
     int rc = check_mol(c, im[k], is[k]);
     if (rc) return rc;
     if (ibox[k] < 1 || ibox[k] > c->nboxes) return set_error(CASS_EINVAL, "box index out of range");
+  }
+  // molecules that stay in a packed box are patched in place by one scatter
+  // launch; any other change repacks the boxes involved on their next use
+  std::vector<int> patch_slots;
+  size_t off = 0;
+  for (int k = 0; k < n; ++k) {
     SpeciesH& s = c->sp[is[k] - 1];
-    int slot = mol_slot(c, im[k], is[k]);
-    int old = c->mol_box[slot];
+    const int slot = mol_slot(c, im[k], is[k]);
+    const int old = c->mol_box[slot], nb = ibox[k] - 1;
     memcpy(&s.pos[(size_t)(im[k] - 1) * 3 * s.natoms], xyz + off, 3 * s.natoms * sizeof(double));
     off += 3 * s.natoms;
-    int nb = ibox[k] - 1;
-    c->mol_box[slot] = nb;
+    set_mol_box(c, slot, nb);
     if (old >= 0 && old != nb) invalidate(c, old);
-    BoxH& B = c->box[nb];
-    if (old == nb && !B.pack_dirty) {
-      // molecule stays in its box: patch its packed atoms in place
-      int p = -1;
-      for (size_t q = 0; q < B.pk_mol.size(); ++q)
-        if (B.pk_mol[q] == slot) { p = B.pk_mol_off[q]; break; }
-      if (p >= 0) {
-        std::vector<double4_32a> p64(s.natoms);
-        std::vector<float4> p32(s.natoms);
-        const double* r = &s.pos[(size_t)(im[k] - 1) * 3 * s.natoms];
-        for (int a = 0; a < s.natoms; ++a) {
-          p64[a] = make_double4_32a(r[3 * a], r[3 * a + 1], r[3 * a + 2], s.q[a]);
-          float tf;
-          int ty = s.type[a];
-          memcpy(&tf, &ty, sizeof(float));
-          p32[a] = make_float4((float)r[3 * a], (float)r[3 * a + 1], (float)r[3 * a + 2], tf);
-        }
-        CASS_CUDA(h2d(c, B.d_p64.as<double4_32a>() + p, p64.data(), s.natoms * sizeof(double4_32a)));
-        CASS_CUDA(h2d(c, B.d_p32.as<float4>() + p, p32.data(), s.natoms * sizeof(float4)));
-        CASS_CUDA(cudaStreamSynchronize(c->stream));
-        B.energy_valid = false;
-        B.cell_dirty = true;
-        continue;
-      }
+    if (old == nb && !c->box[nb].pack_dirty) patch_slots.push_back(slot);
+    else invalidate(c, nb);
+  }
+  c->h_patch.clear();
+  for (int slot : patch_slots) {
+    const int b = c->mol_box[slot];
+    BoxH& B = c->box[b];
+    if (B.pack_dirty) continue;  // repacked from the host copy instead
+    const int sp = c->slot_sp[slot];
+    const SpeciesH& s = c->sp[sp];
+    const int first = B.pk_mol_off[c->pk_index[slot]];
+    const double* r = &s.pos[(size_t)(slot - c->mol_base[sp]) * 3 * s.natoms];
+    for (int a = 0; a < s.natoms; ++a) {
+      PatchRec q;
+      q.x = r[3 * a];
+      q.y = r[3 * a + 1];
+      q.z = r[3 * a + 2];
+      q.box = b;
+      q.atom = first + a;
+      c->h_patch.push_back(q);
     }
-    invalidate(c, nb);
+    B.energy_valid = false;
+    B.cell_dirty = true;
+  }
+  const int np = (int)c->h_patch.size();
+  if (np > 0) {
+    int rc = set_device(c);
+    if (rc) return rc;
+    std::vector<BoxPtrs> bp(c->nboxes);
+    for (int b = 0; b < c->nboxes; ++b) {
+      bp[b].p64 = c->box[b].d_p64.as<double4_32a>();
+      bp[b].p32 = c->box[b].d_p32.as<float4>();
+    }
+    const size_t rec_bytes = (size_t)np * sizeof(PatchRec);
+    if ((rc = c->d_patch.reserve(rec_bytes + bp.size() * sizeof(BoxPtrs)))) return rc;
+    PatchRec* d_rec = c->d_patch.as<PatchRec>();
+    BoxPtrs* d_bp = reinterpret_cast<BoxPtrs*>(d_rec + np);
+    CASS_CUDA(h2d(c, d_rec, c->h_patch.data(), rec_bytes));
+    CASS_CUDA(h2d(c, d_bp, bp.data(), bp.size() * sizeof(BoxPtrs)));
+    k_patch_atoms<<<(np + kBlock - 1) / kBlock, kBlock, 0, c->stream>>>(d_rec, np, d_bp);
+    CASS_CUDA(cudaGetLastError());
+    count_launch(c);
+    // the staging vectors are reused by the next call: wait for the copies
+    CASS_CUDA(cudaStreamSynchronize(c->stream));
   }
   return CASS_OK;
 }
@@ -966,7 +1039,7 @@ int cass_remove_molecule(cass_ctx* c, int32_t im, int32_t is) {
   if (rc) return rc;
   int slot = mol_slot(c, im, is);
   if (c->mol_box[slot] >= 0) invalidate(c, c->mol_box[slot]);
-  c->mol_box[slot] = -1;
+  set_mol_box(c, slot, -1);
   return CASS_OK;
 }
 
@@ -989,9 +1062,7 @@ int cass_mol_inter_energy(cass_ctx* c, int32_t im, int32_t is, int32_t cbmc, dou
   if (ibox < 0) return set_error(CASS_ESTATE, "molecule not live");
   if ((rc = set_device(c)) || (rc = pack_box(c, ibox))) return rc;
   BoxH& B = c->box[ibox];
-  int qoff = -1;
-  for (size_t q = 0; q < B.pk_mol.size(); ++q)
-    if (B.pk_mol[q] == slot) { qoff = B.pk_mol_off[q]; break; }
+  const int qoff = B.pk_mol_off[c->pk_index[slot]];
   const SpeciesH& s = c->sp[is - 1];
   if (s.natoms > kMaxAtoms * 4) return set_error(CASS_ECAPACITY, "query molecule too large");
   int nblk = std::max(1, std::min(148, (B.npacked + kBlock - 1) / kBlock));
@@ -1033,9 +1104,7 @@ int cass_mol_intra_energy(cass_ctx* c, int32_t im, int32_t is, int32_t cbmc, dou
   if ((rc = set_device(c)) || (rc = pack_box(c, ibox))) return rc;
   if ((rc = ensure_pools(c))) return rc;
   BoxH& B = c->box[ibox];
-  int q = -1;
-  for (size_t k = 0; k < B.pk_mol.size(); ++k)
-    if (B.pk_mol[k] == slot) { q = (int)k; break; }
+  const int q = c->pk_index[slot];
   if ((rc = ensure_scratch(c, 1, 7))) return rc;
   if ((rc = c->d_query.reserve(16))) return rc;
   CASS_CUDA(cudaMemsetAsync(c->d_query.p, 0, sizeof(int), c->stream));
@@ -1155,14 +1224,9 @@ int cass_system_total_energy(cass_ctx* c, int32_t ibox1, int32_t intra_flag, Cas
     }
     // Compute_System_Self_Energy (energy_routines.f90:2553-2601), O(nmol) host sum of charges squared
     double es = 0.0;
-    for (int is = 0; is < c->nspecies; ++is) {
-      const SpeciesH& s = c->sp[is];
-      if (!s.defined) continue;
-      double qq = 0.0;
-      for (int a = 0; a < s.natoms; ++a) qq += s.q[a] * s.q[a];
-      for (int im = 0; im < c->max_mol[is]; ++im)
-        if (c->mol_box[c->mol_base[is] + im] == ibox)
-          for (int a = 0; a < s.natoms; ++a) es = es + s.q[a] * s.q[a];
+    for (int slot : members(c, ibox)) {
+      const SpeciesH& s = c->sp[c->slot_sp[slot]];
+      for (int a = 0; a < s.natoms; ++a) es = es + s.q[a] * s.q[a];
     }
     if (B.desc.charge_sum_style == CASS_QQ_EWALD) E.self = -es * kCHARGE_FACTOR * B.dev.alpha / kROOTPI;
     else if (B.desc.charge_sum_style == CASS_QQ_DSF)

@@ -91,6 +91,7 @@ struct SpeciesH {
   std::vector<int> lib_off;     // start (in doubles) of each fragment's library
   bool l_coul_cbmc = false, has_charge = false;
   DevBuf d_library;
+  DevBuf d_library_f;  // FP32 copy of `library`
   // host FP64 coordinates of every molecule slot [max_mol][natoms][3]
   std::vector<double> pos;
 };
@@ -114,6 +115,12 @@ struct BoxH {
   bool cell_dirty = true;
 };
 
+// in-place coordinate update of one packed atom (charge and type stay)
+struct PatchRec {
+  double x, y, z;
+  int box, atom;
+};
+
 struct cass_ctx_impl {
   int device = 0, precision = CASS_PREC_FP64;
   cudaStream_t stream = nullptr, own_stream = nullptr;
@@ -128,6 +135,15 @@ struct cass_ctx_impl {
   PairTable pt{};
   bool pt_set = false;
   std::vector<int> mol_box;  // -1 = not live
+  std::vector<int> slot_sp;  // species (0-based) of each molecule slot
+  // live molecule slots of each box in slot order (species-major, locate
+  // order), rebuilt from mol_box when membership changed
+  std::vector<std::vector<int>> box_members;
+  bool members_dirty = true;
+  std::vector<int> pk_index;  // slot -> packed molecule index in its box (valid while the box is packed)
+  // staged in-place coordinate updates of set_molecules
+  std::vector<PatchRec> h_patch;
+  DevBuf d_patch;
   // structure factors of molecules: [nmol_slots][max nvecs] x2, allocated on first use
   DevBuf d_cos_mol, d_sin_mol, d_cos_mol_old, d_sin_mol_old;
   int cos_mol_stride = 0;

@@ -68,6 +68,20 @@ __host__ __device__ inline int pidx(int i, int j, int nt) { return i * nt + j; }
 // lfsr258 (random_generators.f90:95-122) and the per-insertion stream seeding.
 struct Lfsr {
   uint64_t s1, s2, s3, s4, s5;
+  // advances the five components (the state update of rranf)
+  __host__ __device__ inline void next_bits() {
+    uint64_t b;
+    b = ((s1 << 1) ^ s1) >> 53;
+    s1 = ((s1 & 0xFFFFFFFFFFFFFFFEull) << 10) ^ b;
+    b = ((s2 << 24) ^ s2) >> 50;
+    s2 = ((s2 & 0xFFFFFFFFFFFFFE00ull) << 5) ^ b;
+    b = ((s3 << 3) ^ s3) >> 23;
+    s3 = ((s3 & 0xFFFFFFFFFFFFF000ull) << 29) ^ b;
+    b = ((s4 << 5) ^ s4) >> 24;
+    s4 = ((s4 & 0xFFFFFFFFFFFE0000ull) << 23) ^ b;
+    b = ((s5 << 3) ^ s5) >> 33;
+    s5 = ((s5 & 0xFFFFFFFFFF800000ull) << 8) ^ b;
+  }
   __host__ __device__ inline double next() {
     uint64_t b;
     b = ((s1 << 1) ^ s1) >> 53;

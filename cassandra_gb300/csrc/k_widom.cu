@@ -186,15 +186,9 @@ struct BoxView {
   const BoxDev* b;          // shared-memory copy
   const double4_32a* p64;   // cell-sorted FP64 atoms (x, y, z, q) of this box (smem or global)
   const int* ptype;         // their types (smem or global)
-  const float4* p32;        // cell-sorted FP32 atoms (x, y, z, type bits) (smem or global)
-  const float* q32;         // FP32 charges (global)
   const int* cstart;        // cell starts, local atom indices (smem or global)
-  const double4_32a* g64;   // global FP64 atoms, for exact threshold decisions
   double rc_cbmc, rc_full;
-  bool fast_mixed;          // LJ cut/cut_tail(/Ewald) styles run in FP32
 };
-
-constexpr float kBand = 2e-5f;  // relative band around r^2 thresholds re-evaluated in FP64
 
 // Energy of one test atom at p against every box atom within the cutoff.
 // Returns true on core overlap (r^2 < rcut_low^2), as Compute_MoleculePair_Energy
@@ -204,7 +198,6 @@ struct PairCount {
   double eabs = 0.0;  // sum of |pair energy| of the current query
 };
 
-template <bool MIXED>
 __device__ bool query_box(const BoxView& V, const PairTable& T, const double p[3], int qt, double qch, bool cbmc,
                           bool want_qq, double& eout, PairCount& pc) {
   const BoxDev& b = *V.b;
@@ -213,7 +206,7 @@ __device__ bool query_box(const BoxView& V, const PairTable& T, const double p[3
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     double u = (p[d] + b.hL[d]) * b.cell_inv[d];
-    double w = rc * b.cell_inv[d];
+    double w = fmin(rc * b.cell_inv[d], 1.0e6);
     int l = (int)floor(u - w - 1e-6), h = (int)floor(u + w + 1e-6);
     if (h - l + 1 >= b.nc[d]) {
       l = 0;
@@ -223,108 +216,7 @@ __device__ bool query_box(const BoxView& V, const PairTable& T, const double p[3
     hi[d] = h;
   }
   const bool qq_on = want_qq && b.charge_style == CASS_CHARGE_COUL;
-  if (MIXED && V.fast_mixed) {
-    const float px = (float)p[0], py = (float)p[1], pz = (float)p[2];
-    const double rv2 = cbmc ? b.rcut_cbmcsq : b.rcut_vdwsq;
-    const double rq2 = cbmc ? b.rcut_cbmcsq : b.rcut_coulsq;
-    const float rv2lo = (float)rv2 * (1.0f - kBand), rv2hi = (float)rv2 * (1.0f + kBand);
-    const float rq2lo = (float)rq2 * (1.0f - kBand), rq2hi = (float)rq2 * (1.0f + kBand);
-    const float low2 = (float)b.rcut_lowsq;
-    const float low2lo = low2 * (1.0f - kBand), low2hi = low2 * (1.0f + kBand);
-    const float alpha = (float)b.alpha;
-    const float qf = (float)qch;
-    const bool vdw_on = qt >= 0 && b.vdw_style == CASS_VDW_LJ;
-    float eps_row[kMaxTypes], sig_row[kMaxTypes];
-#pragma unroll
-    for (int t = 0; t < kMaxTypes; ++t) {
-      eps_row[t] = vdw_on && t < T.ntypes ? T.epsf[qt * T.ntypes + t] : 0.0f;
-      sig_row[t] = vdw_on && t < T.ntypes ? T.sig2f[qt * T.ntypes + t] : 0.0f;
-    }
-    KahanF acc;
-    float eabs = 0.0f;
-    for (int cz = lo[2]; cz <= hi[2]; ++cz) {
-      int wz = wrapc(cz, b.nc[2]);
-      for (int cy = lo[1]; cy <= hi[1]; ++cy) {
-        int row = (wz * b.nc[1] + wrapc(cy, b.nc[1])) * b.nc[0];
-        int cx = lo[0];
-        while (cx <= hi[0]) {
-          int wx = wrapc(cx, b.nc[0]);
-          int run = min(hi[0] - cx, b.nc[0] - 1 - wx) + 1;
-          int j1 = V.cstart[row + wx + run];
-          pc.visited += (unsigned long long)(j1 - V.cstart[row + wx]);
-          for (int j = V.cstart[row + wx]; j < j1; ++j) {
-            float4 a = V.p32[j];
-            float dx = fold(px - a.x, b.hLf[0], b.Lf[0]);
-            float dy = fold(py - a.y, b.hLf[1], b.Lf[1]);
-            float dz = fold(pz - a.z, b.hLf[2], b.Lf[2]);
-            float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 > rv2hi && (!qq_on || r2 > rq2hi)) continue;
-            double r2x = -1.0;  // exact FP64 r^2, computed only near a threshold
-            if (r2 < low2hi) {
-              if (r2 < low2lo) return true;
-              double4_32a g = V.g64[j];
-              double ex = fold(p[0] - g.x, b.hL[0], b.L[0]), ey = fold(p[1] - g.y, b.hL[1], b.L[1]),
-                     ez = fold(p[2] - g.z, b.hL[2], b.L[2]);
-              r2x = ex * ex + ey * ey + ez * ez;
-              if (r2x < b.rcut_lowsq) return true;
-            }
-            bool vin, qin;
-            if (r2 <= rv2lo) vin = true;
-            else if (r2 > rv2hi) vin = false;
-            else {
-              if (r2x < 0.0) {
-                double4_32a g = V.g64[j];
-                double ex = fold(p[0] - g.x, b.hL[0], b.L[0]), ey = fold(p[1] - g.y, b.hL[1], b.L[1]),
-                       ez = fold(p[2] - g.z, b.hL[2], b.L[2]);
-                r2x = ex * ex + ey * ey + ez * ez;
-              }
-              vin = r2x <= rv2;
-            }
-            if (vin) {
-              ++pc.in_cut;
-              int tj = __float_as_int(a.w);
-              float e = 0.0f, s2 = 0.0f;
-#pragma unroll
-              for (int t = 0; t < kMaxTypes; ++t)
-                if (t == tj) {
-                  e = eps_row[t];
-                  s2 = sig_row[t];
-                }
-              if (tj >= 0) {
-                float ev = lj_pair_f(e, s2, r2);
-                acc.add(ev);
-                eabs += fabsf(ev);
-              }
-            }
-            if (qq_on) {
-              if (r2 <= rq2lo) qin = true;
-              else if (r2 > rq2hi) qin = false;
-              else {
-                if (r2x < 0.0) {
-                  double4_32a g = V.g64[j];
-                  double ex = fold(p[0] - g.x, b.hL[0], b.L[0]), ey = fold(p[1] - g.y, b.hL[1], b.L[1]),
-                         ez = fold(p[2] - g.z, b.hL[2], b.L[2]);
-                  r2x = ex * ex + ey * ey + ez * ez;
-                }
-                qin = r2x <= rq2;
-              }
-              if (qin) {
-                float eq = qq_ewald_inter_f(alpha, qf * V.q32[j], r2);
-                acc.add(eq);
-                eabs += fabsf(eq);
-              }
-            }
-          }
-          cx += run;
-        }
-      }
-    }
-    eout = acc.value();
-    pc.eabs = (double)eabs;
-    return false;
-  }
-  // FP64 path (and mixed fallback for styles without an FP32 kernel)
-  const double4_32a* P = MIXED ? V.g64 : V.p64;
+  const double4_32a* P = V.p64;
   double acc = 0.0, eabs = 0.0;
   for (int cz = lo[2]; cz <= hi[2]; ++cz) {
     int wz = wrapc(cz, b.nc[2]);
@@ -454,7 +346,6 @@ __device__ bool atom_intra(const SpeciesDevHdr& H, const SpeciesPools& P, const 
 // ---------------------------------------------------------------------------
 // K8: one Widom insertion per thread
 
-template <bool MIXED>
 __device__ void run_insertion(const WidomSpecies& S, const SpeciesPools& P, const PairTable& T, const BoxView& V,
                               const double* __restrict__ lib, Lfsr rng, WRec& rec, int& status, double* xyz_out,
                               CassWidomTrace* tr, PairCount& pc) {
@@ -571,7 +462,7 @@ __device__ void run_insertion(const WidomSpecies& S, const SpeciesPools& P, cons
       int a = S.frag_atoms[fstart][i];
       double p[3] = {r0[3 * a] - com_old[0] + ax, r0[3 * a + 1] - com_old[1] + ay, r0[3 * a + 2] - com_old[2] + az};
       double ea;
-      ov = query_box<MIXED>(V, T, p, S.type[a], S.q[a], true, S.want_qq_cbmc != 0, ea, pc);
+      ov = query_box(V, T, p, S.type[a], S.q[a], true, S.want_qq_cbmc != 0, ea, pc);
       e += ea;
     }
     nrg[it] = e;
@@ -732,7 +623,7 @@ __device__ void run_insertion(const WidomSpecies& S, const SpeciesPools& P, cons
           if (!((newex >> a) & 1u)) continue;
           double p[3] = {r[3 * a], r[3 * a + 1], r[3 * a + 2]};
           double ea;
-          ov = query_box<MIXED>(V, T, p, S.type[a], S.q[a], true, S.want_qq_cbmc != 0, ea, pc);
+          ov = query_box(V, T, p, S.type[a], S.q[a], true, S.want_qq_cbmc != 0, ea, pc);
           einter += ea;
         }
         exist = combined;
@@ -816,7 +707,7 @@ __device__ void run_insertion(const WidomSpecies& S, const SpeciesPools& P, cons
   for (int a = 0; a < n; ++a) {
     double p[3] = {r[3 * a], r[3 * a + 1], r[3 * a + 2]};
     double ea;
-    if (query_box<MIXED>(V, T, p, S.type[a], S.q[a], false, true, ea, pc)) {
+    if (query_box(V, T, p, S.type[a], S.q[a], false, true, ea, pc)) {
       status = 2;
       return;
     }
@@ -842,13 +733,737 @@ __device__ void run_insertion(const WidomSpecies& S, const SpeciesPools& P, cons
     for (int i = 0; i < 3 * n; ++i) xyz_out[i] = r[i];
 }
 
-template <bool MIXED, bool SMEM>
+// ---------------------------------------------------------------------------
+// Mixed-precision Widom kernel: one insertion per thread, FP32 throughout.
+//
+// GB300 issues FP64 at 1/64 of its FP32 rate, so this kernel reads only FP32
+// tables (species, box constants, fragment libraries, cell-sorted atoms) and
+// keeps the test molecule, the trial energies and the Boltzmann weights in
+// FP32; pair energies accumulate in compensated FP32 sums.  Only the
+// per-insertion record is widened to FP64 (adding the box's FP64 constant
+// E_lrc_diff + E_self - E_recip_old).  Cell stencils carry a per-row
+// periodic image shift, so the minimum-image fold per pair is needed only in
+// a dimension whose stencil spans the whole box.
+
+// FP32 copy of the test species' tables (kernel parameter)
+struct SpeciesF {
+  int natoms, nbonds, nangles, ndih, nimp;
+  float q[kMaxAtoms], mass[kMaxAtoms];
+  int type[kMaxAtoms];
+  float vs[kMaxAtoms * kMaxAtoms], qs[kMaxAtoms * kMaxAtoms];
+  unsigned bonded[kMaxAtoms];  // bit j of bonded[i]: i-j is a 1-2 pair
+  signed char bond_atoms[kMaxBonded][2], angle_atoms[kMaxBonded][3], dih_atoms[kMaxBonded][4],
+      imp_atoms[kMaxBonded][4];
+  unsigned char bond_harm[kMaxBonded], angle_harm[kMaxBonded];
+  float bond_k[kMaxBonded], bond_l0[kMaxBonded], angle_k[kMaxBonded], angle_t0[kMaxBonded];
+  float rb[kMaxBonded][6], imp_k[kMaxBonded], imp_p0[kMaxBonded];
+  float cum_prob_ins[kMaxFrags];
+};
+
+// FP32 constants of the CTA's box
+struct BoxF {
+  float L[3], hL[3], cinv[3];
+  int nc[3];
+  float rcb2, rv2, rq2, low2, rc_cbmc, rc_full, beta, kmaxE, alpha;
+  int charge_on;
+};
+
+// uniform in [0, 1) from an lfsr258 draw without the FP64 unit: the reference
+// value x*2^-64 + 0.5 (x signed) equals (x ^ 2^63) / 2^64; keep its top 23 bits
+__device__ __forceinline__ float draw_f(Lfsr& g) {
+  g.next_bits();
+  unsigned v = (unsigned)(((g.s1 ^ g.s2 ^ g.s3 ^ g.s4 ^ g.s5) ^ 0x8000000000000000ull) >> 41);
+  return (__int_as_float(0x4B000000 | v) - 8388608.0f) * 1.1920928955078125e-7f;
+}
+
+__device__ __forceinline__ void get_com_f(const SpeciesF& S, const float* r, unsigned exist, float com[3]) {
+  float tm = 0, x = 0, y = 0, z = 0;
+  for (int k = 0; k < S.natoms; ++k) {
+    if (!((exist >> k) & 1u)) continue;
+    float m = S.mass[k];
+    tm += m;
+    x += m * r[3 * k];
+    y += m * r[3 * k + 1];
+    z += m * r[3 * k + 2];
+  }
+  float inv = 1.0f / tm;
+  com[0] = x * inv;
+  com[1] = y * inv;
+  com[2] = z * inv;
+}
+
+__device__ void aligner_hanger_f(float v1[3], float v2[3], float al[9], float hg[9]) {
+  float n1 = rsqrtf(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+  for (int i = 0; i < 3; ++i) v1[i] *= n1;
+  float n2 = rsqrtf(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
+  for (int i = 0; i < 3; ++i) v2[i] *= n2;
+  float p1[3] = {v1[1] * v2[2] - v1[2] * v2[1], -v1[0] * v2[2] + v1[2] * v2[0], v1[0] * v2[1] - v1[1] * v2[0]};
+  float np1 = rsqrtf(p1[0] * p1[0] + p1[1] * p1[1] + p1[2] * p1[2]);
+  for (int i = 0; i < 3; ++i) p1[i] *= np1;
+  float p2[3] = {v1[1] * p1[2] - v1[2] * p1[1], -v1[0] * p1[2] + v1[2] * p1[0], v1[0] * p1[1] - v1[1] * p1[0]};
+  float np2 = rsqrtf(p2[0] * p2[0] + p2[1] * p2[1] + p2[2] * p2[2]);
+  for (int i = 0; i < 3; ++i) p2[i] *= np2;
+  for (int i = 0; i < 3; ++i) {
+    al[i] = v1[i];
+    al[3 + i] = p2[i];
+    al[6 + i] = p1[i];
+    hg[i * 3 + 0] = v1[i];
+    hg[i * 3 + 1] = p2[i];
+    hg[i * 3 + 2] = p1[i];
+  }
+}
+
+
+__device__ __forceinline__ float lj_or_zero(const float2* ljp, int ti, int tj, float scale, float r2) {
+  if (ti < 0 || tj < 0) return 0.0f;
+  float2 es = ljp[ti * kMaxTypes + tj];
+  return lj_pair_f(es.x * scale, es.y, r2);
+}
+
+// Compute_Molecule_Dihedral_Energy (RB form) over dihedrals whose atoms all exist
+__device__ float dihedral_f(const SpeciesF& S, const float* r, unsigned exist) {
+  float e = 0.0f;
+  for (int k = 0; k < S.ndih; ++k) {
+    const signed char* a = S.dih_atoms[k];
+    unsigned m = (1u << a[0]) | (1u << a[1]) | (1u << a[2]) | (1u << a[3]);
+    if ((exist & m) != m) continue;
+    float rx12 = r[3 * a[0]] - r[3 * a[1]], ry12 = r[3 * a[0] + 1] - r[3 * a[1] + 1], rz12 = r[3 * a[0] + 2] - r[3 * a[1] + 2];
+    float rx32 = r[3 * a[2]] - r[3 * a[1]], ry32 = r[3 * a[2] + 1] - r[3 * a[1] + 1], rz32 = r[3 * a[2] + 2] - r[3 * a[1] + 2];
+    float rx34 = r[3 * a[2]] - r[3 * a[3]], ry34 = r[3 * a[2] + 1] - r[3 * a[3] + 1], rz34 = r[3 * a[2] + 2] - r[3 * a[3] + 2];
+    float mx = ry12 * rz32 - ry32 * rz12, my = -rx12 * rz32 + rz12 * rx32, mz = rx12 * ry32 - ry12 * rx32;
+    float nx = ry32 * rz34 - rz32 * ry34, ny = -rx32 * rz34 + rz32 * rx34, nz = rx32 * ry34 - ry32 * rx34;
+    float c = (mx * nx + my * ny + mz * nz) * rsqrtf((mx * mx + my * my + mz * mz) * (nx * nx + ny * ny + nz * nz));
+    const float* cb = S.rb[k];
+    e += cb[0] + c * (cb[1] + c * (cb[2] + c * (cb[3] + c * (cb[4] + c * cb[5]))));
+  }
+  return e;
+}
+
+// intramolecular pair energy with the species scales (LJ + Ewald real space)
+__device__ __forceinline__ void intra_pair_f(const SpeciesF& S, const BoxF& f, const float2* ljp, int ia, int ja,
+                                             float r2, bool vdw, bool qq, float& eiv, float& eiq, float& eoq) {
+  const int n = S.natoms;
+  if (vdw) eiv += lj_or_zero(ljp, S.type[ia], S.type[ja], S.vs[ia * n + ja], r2);
+  if (qq) {
+    float rinv = rsqrtf(r2);
+    float eij = S.q[ia] * S.q[ja] * rinv * (float)kCHARGE_FACTOR;
+    float erf_val = 1.0f - erfc_asf(f.alpha * r2 * rinv);
+    eiq += S.qs[ia * n + ja] * eij;
+    eoq += -erf_val * eij;
+  }
+}
+
+// Compute_Atom_Nonbond_Intra_Energy (energy_routines.f90:691-737), CBMC cutoff
+__device__ bool atom_intra_f(const SpeciesF& S, const BoxF& f, const float2* ljp, int ia, const float* r,
+                             unsigned exist, float& eiv, float& eiq, float& eoq) {
+  eiv = eiq = eoq = 0.0f;
+  const int n = S.natoms;
+  for (int ja = 0; ja < n; ++ja) {
+    if (ja == ia || !((exist >> ja) & 1u)) continue;
+    const bool nzv = S.vs[ia * n + ja] > 0.0f, nzq = S.qs[ia * n + ja] > 0.0f;
+    if (!(nzv || nzq)) continue;
+    float dx = r[3 * ja] - r[3 * ia], dy = r[3 * ja + 1] - r[3 * ia + 1], dz = r[3 * ja + 2] - r[3 * ia + 2];
+    float r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 < f.low2 && nzv) return true;
+    const bool in = r2 <= f.rcb2;
+    intra_pair_f(S, f, ljp, ja, ia, r2, in && nzv, in && nzq && f.charge_on, eiv, eiq, eoq);
+  }
+  return false;
+}
+
+struct IntraF {
+  float bond, angle, dih, imp, ivdw, iqq, pqq;
+  bool overlap;
+};
+
+// bonded + Compute_Molecule_Nonbond_Intra_Energy (full cutoffs), FP32
+__device__ IntraF molecule_intra_f(const SpeciesF& S, const BoxF& f, const float2* ljp, const float* r) {
+  IntraF o{0, 0, 0, 0, 0, 0, 0, false};
+  for (int k = 0; k < S.nbonds; ++k) {
+    if (!S.bond_harm[k]) continue;
+    int a = S.bond_atoms[k][0], c = S.bond_atoms[k][1];
+    float dx = r[3 * a] - r[3 * c], dy = r[3 * a + 1] - r[3 * c + 1], dz = r[3 * a + 2] - r[3 * c + 2];
+    float l = sqrtf(dx * dx + dy * dy + dz * dz);
+    o.bond += S.bond_k[k] * (l - S.bond_l0[k]) * (l - S.bond_l0[k]);
+  }
+  for (int k = 0; k < S.nangles; ++k) {
+    if (!S.angle_harm[k]) continue;
+    int a1 = S.angle_atoms[k][0], a2 = S.angle_atoms[k][1], a3 = S.angle_atoms[k][2];
+    float rx21 = r[3 * a2] - r[3 * a1], ry21 = r[3 * a2 + 1] - r[3 * a1 + 1], rz21 = r[3 * a2 + 2] - r[3 * a1 + 2];
+    float rx32 = r[3 * a3] - r[3 * a2], ry32 = r[3 * a3 + 1] - r[3 * a2 + 1], rz32 = r[3 * a3 + 2] - r[3 * a2 + 2];
+    float C23 = rx21 * rx32 + ry21 * ry32 + rz21 * rz32, C22 = rx21 * rx21 + ry21 * ry21 + rz21 * rz21,
+          C33 = rx32 * rx32 + ry32 * ry32 + rz32 * rz32;
+    float ct = fmaxf(fminf(C23 * rsqrtf(C33 * C22), 0.999999f), -0.999999f);
+    float th = (float)kPI - acosf(ct);
+    o.angle += S.angle_k[k] * (th - S.angle_t0[k]) * (th - S.angle_t0[k]);
+  }
+  o.dih = dihedral_f(S, r, 0xffffffffu);
+  for (int k = 0; k < S.nimp; ++k) {
+    const signed char* a = S.imp_atoms[k];
+    float rx12 = r[3 * a[0]] - r[3 * a[1]], ry12 = r[3 * a[0] + 1] - r[3 * a[1] + 1], rz12 = r[3 * a[0] + 2] - r[3 * a[1] + 2];
+    float rx32 = r[3 * a[2]] - r[3 * a[1]], ry32 = r[3 * a[2] + 1] - r[3 * a[1] + 1], rz32 = r[3 * a[2] + 2] - r[3 * a[1] + 2];
+    float rx34 = r[3 * a[2]] - r[3 * a[3]], ry34 = r[3 * a[2] + 1] - r[3 * a[3] + 1], rz34 = r[3 * a[2] + 2] - r[3 * a[3] + 2];
+    float mx = ry12 * rz32 - ry32 * rz12, my = -rx12 * rz32 + rz12 * rx32, mz = rx12 * ry32 - ry12 * rx32;
+    float nx = ry32 * rz34 - rz32 * ry34, ny = -rx32 * rz34 + rz32 * rx34, nz = rx32 * ry34 - ry32 * rx34;
+    float cp = (mx * nx + my * ny + mz * nz) * rsqrtf((mx * mx + my * my + mz * mz) * (nx * nx + ny * ny + nz * nz));
+    cp = fminf(1.0f, fmaxf(-1.0f, cp));
+    float phi = copysignf(acosf(cp), rx12 * nx + ry12 * ny + rz12 * nz);
+    o.imp += S.imp_k[k] * (phi - S.imp_p0[k]) * (phi - S.imp_p0[k]);
+  }
+  const int n = S.natoms;
+  for (int ia = 0; ia < n; ++ia)
+    for (int ja = ia + 1; ja < n; ++ja) {
+      float dx = r[3 * ia] - r[3 * ja], dy = r[3 * ia + 1] - r[3 * ja + 1], dz = r[3 * ia + 2] - r[3 * ja + 2];
+      float r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 <= f.low2 && !((S.bonded[ia] >> ja) & 1u)) {
+        o.overlap = true;
+        return o;
+      }
+      intra_pair_f(S, f, ljp, ia, ja, r2, r2 <= f.rv2, f.charge_on && r2 <= f.rq2, o.ivdw, o.iqq, o.pqq);
+    }
+  return o;
+}
+
+// Cell-list view of the CTA's box
+struct BoxViewF {
+  const BoxF* f;
+  const float4* p32;   // cell-sorted atoms (x, y, z, type bits), smem or global
+  const float* q32;    // their charges (global)
+  const int* cstart;   // cell starts, local atom indices, smem or global
+  const float2* ljp;   // (eps, sigma^2) [kMaxTypes][kMaxTypes], smem
+};
+
+struct QueryAcc {
+  KahanF e;
+  float eabs = 0.0f;
+  unsigned long long visited = 0, in_cut = 0;
+};
+
+// FP32 energy of one test atom at p against the box atoms within the cutoff,
+// added to A.  Returns true on core overlap (r^2 < rcut_low^2), as
+// Compute_MoleculePair_Energy (energy_routines.f90:1676-1679) does.
+__device__ bool query_f(const BoxViewF& V, QueryAcc& A, float px, float py, float pz, int ta, float qa, bool cbmc,
+                        bool want_qq) {
+  const BoxF& f = *V.f;
+  const float rc = cbmc ? f.rc_cbmc : f.rc_full;
+  const float p[3] = {px, py, pz};
+  int lo[3], hi[3];
+  bool full[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float w = fminf(rc * f.cinv[d], 1.0e5f);
+    const float ul = fminf(fmaxf((p[d] + f.hL[d]) * f.cinv[d] - w - 1e-3f, -1.0e6f), 1.0e6f);
+    const float uh = fminf(fmaxf((p[d] + f.hL[d]) * f.cinv[d] + w + 1e-3f, -1.0e6f), 1.0e6f);
+    const int l = (int)floorf(ul), h = (int)floorf(uh);
+    full[d] = h - l + 1 >= f.nc[d];
+    lo[d] = full[d] ? 0 : l;
+    hi[d] = full[d] ? f.nc[d] - 1 : h;
+  }
+  const bool fold_any = full[0] || full[1] || full[2];
+  const float rv2 = cbmc ? f.rcb2 : f.rv2;
+  const float rq2 = cbmc ? f.rcb2 : f.rq2;
+  const float low2 = f.low2;
+  const bool vdw_on = ta >= 0;
+  const bool qq_on = want_qq && f.charge_on && qa != 0.0f;
+  const float rsel2 = fmaxf(vdw_on ? rv2 : -1.0f, qq_on ? rq2 : -1.0f);
+  const float2* lrow = V.ljp + (vdw_on ? ta : 0) * kMaxTypes;
+  const int nc0 = f.nc[0], nc1 = f.nc[1], nc2 = f.nc[2];
+  for (int cz = lo[2]; cz <= hi[2]; ++cz) {
+    const int wz = wrapc(cz, nc2);
+    const float qz = pz + (float)((wz - cz) / nc2) * f.L[2];
+    for (int cy = lo[1]; cy <= hi[1]; ++cy) {
+      const int wy = wrapc(cy, nc1);
+      const float qy = py + (float)((wy - cy) / nc1) * f.L[1];
+      const int row = (wz * nc1 + wy) * nc0;
+      int cx = lo[0];
+      while (cx <= hi[0]) {
+        const int wx = wrapc(cx, nc0);
+        const int run = min(hi[0] - cx, nc0 - 1 - wx) + 1;
+        const float qx = px + (float)((wx - cx) / nc0) * f.L[0];
+        const int j0 = V.cstart[row + wx], j1 = V.cstart[row + wx + run];
+        A.visited += (unsigned long long)(j1 - j0);
+        for (int j = j0; j < j1; ++j) {
+          const float4 a = V.p32[j];
+          float dx = qx - a.x, dy = qy - a.y, dz = qz - a.z;
+          if (fold_any) {
+            if (full[0]) dx = fold(dx, f.hL[0], f.L[0]);
+            if (full[1]) dy = fold(dy, f.hL[1], f.L[1]);
+            if (full[2]) dz = fold(dz, f.hL[2], f.L[2]);
+          }
+          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+          if (r2 < low2) return true;
+          if (r2 > rsel2) continue;
+          ++A.in_cut;
+          const int tj = __float_as_int(a.w);
+          if (vdw_on && tj >= 0 && r2 <= rv2) {
+            const float2 es = lrow[tj];
+            const float ev = lj_pair_f(es.x, es.y, r2);
+            A.e.add(ev);
+            A.eabs += fabsf(ev);
+          }
+          if (qq_on && r2 <= rq2) {
+            const float eq = qq_ewald_inter_f(f.alpha, qa * V.q32[j], r2);
+            A.e.add(eq);
+            A.eabs += fabsf(eq);
+          }
+        }
+        cx += run;
+      }
+    }
+  }
+  return false;
+}
+
+// Boltzmann choice among k trials (fragment_growth.f90:569-620, 1994-2046):
+// weights exp(-beta (U - U_min)) and the rule "rand * sum < cumulative sum";
+// returns the trial or -1 and sets *lnw = ln sum_t exp(-beta U_t)
+__device__ __forceinline__ int select_trial_f(int k, const float* u, unsigned ovm, float beta, float pick, float* lnw) {
+  float umin = 3.0e38f;
+  for (int t = 0; t < k; ++t)
+    if (!((ovm >> t) & 1u)) umin = fminf(umin, u[t]);
+  if (umin == 3.0e38f) return -1;
+  float w[kMaxKappa];
+  float cum = 0.0f;
+  for (int t = 0; t < k; ++t) {
+    cum += ((ovm >> t) & 1u) ? 0.0f : __expf(-beta * (u[t] - umin));
+    w[t] = cum;
+  }
+  const float x = pick * cum;
+  int sel = 0;
+  while (sel < k && !(x < w[sel])) ++sel;
+  if (sel == k) return -1;
+  *lnw = -beta * umin + logf(cum);
+  return sel;
+}
+
+// Record of one insertion (FP32 parts)
+struct RecF {
+  float dE_intra, e_inter, dE_frag, ln_pbias, e_abs, first_sum;
+  int status, selected;
+};
+
+// Energy of atoms `ids` against the box: sum into e, true on overlap
+__device__ __forceinline__ bool query_atoms_f(const BoxViewF& V, QueryAcc& A, const SpeciesF& S, const float* r,
+                                              const int* ids, int n, float sx, float sy, float sz, bool cbmc,
+                                              bool want_qq) {
+  for (int i = 0; i < n; ++i) {
+    const int a = ids[i];
+    if (query_f(V, A, r[3 * a] + sx, r[3 * a + 1] + sy, r[3 * a + 2] + sz, S.type[a], S.q[a], cbmc, want_qq))
+      return true;
+  }
+  return false;
+}
+
+// One Widom insertion: Widom_Insert (widom_insert.f90:250-447) with the CBMC
+// growth of Build_Molecule (fragment_growth.f90:120-900) and
+// Fragment_Placement (:1449-2132), in FP32
+__device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const BoxViewF& V,
+                                const float* __restrict__ lib, Lfsr rng, double* xyz_out, QueryAcc& cnt) {
+  const BoxF& f = *V.f;
+  const int n = S.natoms;
+  RecF out{0, 0, 0, 0, 0, 0, 0, 0};
+  float r[3 * kMaxAtoms];
+  unsigned exist = 0u;
+  float ln_pbias = 0.0f;
+  bool cbmc_overlap = false;
+
+  // Step 1: first fragment and growth order (fragment_growth.f90:218-253, 1317-1446)
+  const float u = draw_f(rng);
+  int fstart = 0;
+  while (fstart < S.nfrag && !(u < SF.cum_prob_ins[fstart])) ++fstart;
+  if (fstart >= S.nfrag) fstart = S.nfrag - 1;
+  float ln_pseq = (float)S.ln_prob_ins[fstart];
+  int order[kMaxFrags];
+  int norder = 1;
+  order[0] = fstart;
+  unsigned live = 1u << fstart;
+  if (S.nfrag > 1) {
+    int hang[kMaxFrags];
+    int nh = 0;
+    for (int k = 0; k < S.frag_nconnect[fstart]; ++k) {
+      const int g = S.frag_connect[fstart][k];
+      if (!((live >> g) & 1u)) hang[nh++] = g;
+    }
+    while (nh > 0) {
+      float tot = 0.0f;
+      for (int k = 0; k < nh; ++k) tot += (float)(S.frag_natoms[hang[k]] - 2);
+      const float uu = draw_f(rng);
+      int k = 0;
+      float cum = 0.0f;
+      for (; k < nh; ++k) {
+        cum += (float)(S.frag_natoms[hang[k]] - 2) / tot;
+        if (uu < cum) break;
+      }
+      if (k >= nh) k = nh - 1;
+      const int g = hang[k];
+      if (nh > 1) ln_pseq += logf((float)(S.frag_natoms[g] - 2) / tot);
+      order[norder++] = g;
+      live |= 1u << g;
+      for (int q = k; q + 1 < nh; ++q) hang[q] = hang[q + 1];
+      --nh;
+      for (int q = 0; q < S.frag_nconnect[g]; ++q) {
+        const int h = S.frag_connect[g][q];
+        if (!((live >> h) & 1u) && nh < kMaxFrags) hang[nh++] = h;
+      }
+    }
+  }
+  // Step 2: library conformation of the first fragment (:274-304)
+  const int nfa = S.frag_natoms[fstart];
+  int fa_ids[kMaxAtoms];
+  {
+    const int nconf = S.nconfig[fstart];
+    const int conf = min((int)(draw_f(rng) * (float)nconf), nconf - 1);
+    const float* L0 = lib + S.lib_off[fstart] + (size_t)conf * nfa * 3;
+    for (int i = 0; i < nfa; ++i) {
+      const int a = S.frag_atoms[fstart][i];
+      fa_ids[i] = a;
+      r[3 * a] = L0[3 * i];
+      r[3 * a + 1] = L0[3 * i + 1];
+      r[3 * a + 2] = L0[3 * i + 2];
+      exist |= 1u << a;
+    }
+  }
+  // Step 3: random orientation about the COM (rotation_routines.f90:41-137);
+  // the fragment is kept relative to its COM until a position is chosen
+  float com[3];
+  get_com_f(SF, r, exist, com);
+  {
+    const float theta = acosf(1.0f - 2.0f * draw_f(rng));
+    const float phi = (1.0f - 2.0f * draw_f(rng)) * (float)kPI;
+    const float psi = (1.0f - 2.0f * draw_f(rng)) * (float)kPI;
+    float st, ct, sp, cp, ss, cs;
+    sincosf(theta, &st, &ct);
+    sincosf(phi, &sp, &cp);
+    sincosf(psi, &ss, &cs);
+    const float r11 = cs * cp - ct * sp * ss, r12 = cs * sp + ct * cp * ss, r13 = ss * st;
+    const float r21 = -ss * cp - ct * sp * cs, r22 = -ss * sp + ct * cp * cs, r23 = cs * st;
+    const float r31 = st * sp, r32 = -st * cp, r33 = ct;
+    for (int i = 0; i < nfa; ++i) {
+      const int a = fa_ids[i];
+      const float x = r[3 * a] - com[0], y = r[3 * a + 1] - com[1], z = r[3 * a + 2] - com[2];
+      r[3 * a] = r11 * x + r12 * y + r13 * z;
+      r[3 * a + 1] = r21 * x + r22 * y + r23 * z;
+      r[3 * a + 2] = r31 * x + r32 * y + r33 * z;
+    }
+  }
+  // Step 4: kappa_ins trial positions of the first fragment (:383-620)
+  const int ki = S.kappa_ins;
+  const bool cbmc_qq = S.want_qq_cbmc != 0;
+  float nrg[kMaxKappa];
+  unsigned ovm = 0u;
+  const Lfsr replay = rng;
+  for (int it = 0; it < ki; ++it) {
+    const float ax = (0.5f - draw_f(rng)) * f.L[0];
+    const float ay = (0.5f - draw_f(rng)) * f.L[1];
+    const float az = (0.5f - draw_f(rng)) * f.L[2];
+    QueryAcc A;
+    bool ov = query_atoms_f(V, A, SF, r, fa_ids, nfa, ax, ay, az, true, cbmc_qq);
+    cnt.visited += A.visited;
+    cnt.in_cut += A.in_cut;
+    const float e = A.e.s + A.e.c;
+    ov = ov || e >= f.kmaxE;
+    nrg[it] = e;
+    if (ov) ovm |= 1u << it;
+    else out.first_sum += e;
+  }
+  {
+    float lnw = 0.0f;
+    const int sel = select_trial_f(ki, nrg, ovm, f.beta, draw_f(rng), &lnw);
+    if (sel < 0) {
+      cbmc_overlap = true;
+    } else {
+      ln_pbias = ln_pbias - f.beta * nrg[sel] - lnw;
+      Lfsr rp = replay;
+      float ax = 0, ay = 0, az = 0;
+      for (int k = 0; k <= sel; ++k) {
+        ax = (0.5f - draw_f(rp)) * f.L[0];
+        ay = (0.5f - draw_f(rp)) * f.L[1];
+        az = (0.5f - draw_f(rp)) * f.L[2];
+      }
+      for (int i = 0; i < nfa; ++i) {
+        const int a = fa_ids[i];
+        r[3 * a] += ax;
+        r[3 * a + 1] += ay;
+        r[3 * a + 2] += az;
+      }
+      com[0] = ax;
+      com[1] = ay;
+      com[2] = az;
+      out.selected = sel + 1;
+    }
+  }
+  // Step 5: Fragment_Placement, kappa_dih dihedral trials per fragment
+  if (!cbmc_overlap && norder > 1) {
+    float e_prev = dihedral_f(SF, r, exist);
+    unsigned placed = 1u << fstart;
+    const int kd = S.kappa_dih;
+    float dn[kMaxKappa], dd[kMaxKappa];
+    for (int oi = 1; oi < norder && !cbmc_overlap; ++oi) {
+      const int fr = order[oi];
+      const int nf = S.frag_natoms[fr];
+      const unsigned grown = exist;
+      const int nconf = S.nconfig[fr];
+      draw_f(rng);  // the duplicated draw of fragment_growth.f90:1578,1584
+      const int cf = min((int)(draw_f(rng) * (float)nconf), nconf - 1);
+      float cfg[3 * kMaxAtoms];
+      const float* Lf = lib + S.lib_off[fr] + (size_t)cf * nf * 3;
+      for (int j = 0; j < nf; ++j) {
+        const int a = S.frag_atoms[fr][j];
+        exist |= 1u << a;
+        cfg[3 * a] = Lf[3 * j];
+        cfg[3 * a + 1] = Lf[3 * j + 1];
+        cfg[3 * a + 2] = Lf[3 * j + 2];
+      }
+      const unsigned combined = exist;
+      int fc = -1;
+      for (int q = 0; q < S.frag_nconnect[fr]; ++q) {
+        const int g = S.frag_connect[fr][q];
+        if ((placed >> g) & 1u) {
+          fc = g;
+          break;
+        }
+      }
+      if (fc < 0) {  // no placed neighbour: the fragment graph is not connected
+        cbmc_overlap = true;
+        break;
+      }
+      const int anc_i = S.frag_atoms[fr][0], anc_c = S.frag_atoms[fc][0];
+      int ids[kMaxAtoms], nid = 0;
+      for (int j = 0; j < nf; ++j) {
+        const int a = S.frag_atoms[fr][j];
+        if (a != anc_i && a != anc_c) ids[nid++] = a;
+      }
+      int newids[kMaxAtoms], nnew = 0;
+      for (int a = 0; a < n; ++a)
+        if (((combined & ~grown) >> a) & 1u) newids[nnew++] = a;
+      unsigned idmask = 0u;
+      for (int j = 0; j < nid; ++j) idmask |= 1u << ids[j];
+      const int atom_ifrag = nid > 0 ? ids[0] : S.frag_atoms[fr][nf - 1];
+      int atom_fc = S.frag_atoms[fc][S.frag_natoms[fc] - 1];
+      for (int j = 0; j < S.frag_natoms[fc]; ++j) {
+        const int a = S.frag_atoms[fc][j];
+        if (a != anc_i && a != anc_c) {
+          atom_fc = a;
+          break;
+        }
+      }
+      float v1[3], v2[3], al_i[9], hg_i[9], al_c[9], hg_c[9];
+      for (int d = 0; d < 3; ++d) {
+        v1[d] = cfg[3 * anc_i + d] - cfg[3 * anc_c + d];
+        v2[d] = cfg[3 * atom_ifrag + d] - cfg[3 * anc_c + d];
+      }
+      aligner_hanger_f(v1, v2, al_i, hg_i);
+      for (int d = 0; d < 3; ++d) {
+        v1[d] = r[3 * anc_i + d] - r[3 * anc_c + d];
+        v2[d] = r[3 * atom_fc + d] - r[3 * anc_c + d];
+      }
+      aligner_hanger_f(v1, v2, al_c, hg_c);
+      const float tx = cfg[3 * anc_c], ty = cfg[3 * anc_c + 1], tz = cfg[3 * anc_c + 2];
+      for (int j = 0; j < nid; ++j) {
+        const int a = ids[j];
+        const float x = cfg[3 * a] - tx, y = cfg[3 * a + 1] - ty, z = cfg[3 * a + 2] - tz;
+        cfg[3 * a] = x * al_i[0] + y * al_i[1] + z * al_i[2];
+        cfg[3 * a + 1] = x * al_i[3] + y * al_i[4] + z * al_i[5];
+        cfg[3 * a + 2] = x * al_i[6] + y * al_i[7] + z * al_i[8];
+      }
+      const float theta0 = (float)kTWOPI * draw_f(rng);
+      const float dtheta = (float)kTWOPI / (float)kd;
+      unsigned dov = 0u;
+      for (int ii = 0; ii < kd; ++ii) {
+        float sth, cth;
+        sincosf(theta0 + (float)ii * dtheta, &sth, &cth);
+        for (int j = 0; j < nid; ++j) {
+          const int a = ids[j];
+          const float x = cfg[3 * a], y = cfg[3 * a + 1], z = cfg[3 * a + 2];
+          const float yr = cth * y + sth * z, zr = -sth * y + cth * z;
+          r[3 * a] = (x * hg_c[0] + yr * hg_c[1] + zr * hg_c[2]) + r[3 * anc_c];
+          r[3 * a + 1] = (x * hg_c[3] + yr * hg_c[4] + zr * hg_c[5]) + r[3 * anc_c + 1];
+          r[3 * a + 2] = (x * hg_c[6] + yr * hg_c[7] + zr * hg_c[8]) + r[3 * anc_c + 2];
+        }
+        dn[ii] = 0.0f;
+        dd[ii] = 0.0f;
+        exist &= ~idmask;
+        float niv = 0.0f, niq = 0.0f, noq = 0.0f;
+        bool ov = false;
+        for (int j = 0; j < nid && !ov; ++j) {
+          exist |= 1u << ids[j];
+          float eiv, eiq, eoq;
+          ov = atom_intra_f(SF, f, V.ljp, ids[j], r, exist, eiv, eiq, eoq);
+          niv += eiv;
+          niq += eiq;
+          noq += eoq;
+        }
+        if (ov) {
+          exist = combined;
+          dov |= 1u << ii;
+          continue;
+        }
+        QueryAcc A;
+        ov = query_atoms_f(V, A, SF, r, newids, nnew, 0.0f, 0.0f, 0.0f, true, cbmc_qq);
+        cnt.visited += A.visited;
+        cnt.in_cut += A.in_cut;
+        exist = combined;
+        if (!ov) {
+          const float ed = dihedral_f(SF, r, exist);
+          dd[ii] = ed;
+          dn[ii] = ed + niv + niq + (A.e.s + A.e.c) + noq - e_prev;
+          ov = dn[ii] >= f.kmaxE;
+        }
+        if (ov) dov |= 1u << ii;
+      }
+      float lnw = 0.0f;
+      const int trl = select_trial_f(kd, dn, dov, f.beta, draw_f(rng), &lnw);
+      if (trl < 0) {
+        cbmc_overlap = true;
+        break;
+      }
+      ln_pbias = ln_pbias - f.beta * dn[trl] - lnw;
+      float sth, cth;
+      sincosf(theta0 + (float)trl * dtheta, &sth, &cth);
+      for (int j = 0; j < nid; ++j) {
+        const int a = ids[j];
+        const float x = cfg[3 * a], y = cfg[3 * a + 1], z = cfg[3 * a + 2];
+        const float yr = cth * y + sth * z, zr = -sth * y + cth * z;
+        r[3 * a] = (x * hg_c[0] + yr * hg_c[1] + zr * hg_c[2]) + r[3 * anc_c];
+        r[3 * a + 1] = (x * hg_c[3] + yr * hg_c[4] + zr * hg_c[5]) + r[3 * anc_c + 1];
+        r[3 * a + 2] = (x * hg_c[6] + yr * hg_c[7] + zr * hg_c[8]) + r[3 * anc_c + 2];
+      }
+      e_prev = dd[trl];
+      placed |= 1u << fr;
+    }
+    if (!cbmc_overlap) get_com_f(SF, r, exist, com);
+  }
+  // widom_insert.f90:350-447
+  ln_pbias = ln_pbias + ln_pseq + (float)S.ln_kappa_ins + (float)S.ln_kappa_dih_term;
+  out.ln_pbias = ln_pbias;
+  if (cbmc_overlap) {
+    out.status = 1;
+    return out;
+  }
+  if (S.nfrag > 1) {  // Fold_Molecule, orthorhombic branch
+    for (int d = 0; d < 3; ++d) {
+      const float sh = com[d] > f.hL[d] ? -f.L[d] : (com[d] < -f.hL[d] ? f.L[d] : 0.0f);
+      if (sh != 0.0f)
+        for (int a = 0; a < n; ++a) r[3 * a + d] += sh;
+    }
+  }
+  QueryAcc A;
+  bool ov = false;
+  for (int a = 0; a < n && !ov; ++a)
+    ov = query_f(V, A, r[3 * a], r[3 * a + 1], r[3 * a + 2], SF.type[a], SF.q[a], false, true);
+  cnt.visited += A.visited;
+  cnt.in_cut += A.in_cut;
+  if (ov) {
+    out.status = 2;
+    return out;
+  }
+  const IntraF io = molecule_intra_f(SF, f, V.ljp, r);
+  if (io.overlap) {
+    out.status = 3;
+    return out;
+  }
+  out.e_inter = (A.e.s + A.e.c) + io.pqq;
+  out.e_abs = A.eabs;
+  out.dE_intra = (io.ivdw + io.iqq) + io.bond + io.angle + io.dih + io.imp;
+  out.dE_frag = io.angle;
+  out.status = 0;
+  if (xyz_out)
+    for (int i = 0; i < 3 * n; ++i) xyz_out[i] = (double)r[i];
+  return out;
+}
+
+template <bool SMEM>
+__global__ void __launch_bounds__(128) k_widom_f32(WidomSpecies S, SpeciesF SF, PairTable T, const BoxDev* boxes,
+                                                   const int* box_ids, const float4* c32, const float* cq32,
+                                                   const int* cstart, const float* __restrict__ libf, long long n_ins,
+                                                   uint64_t seed, WRec* rec, signed char* status, double* xyz,
+                                                   int want_xyz, CassWidomTrace* trace,
+                                                   unsigned long long* pair_counts) {
+  extern __shared__ __align__(32) unsigned char smem[];
+  __shared__ BoxF sf;
+  __shared__ float2 s_ljp[kMaxTypes * kMaxTypes];
+  __shared__ int s_atom_off, s_cell_off, s_natoms;
+  __shared__ double s_ec;
+  const int k = blockIdx.y;
+  if (threadIdx.x == 0) {
+    const BoxDev& b = boxes[k];
+    for (int d = 0; d < 3; ++d) {
+      sf.L[d] = (float)b.L[d];
+      sf.hL[d] = (float)b.hL[d];
+      sf.cinv[d] = (float)b.cell_inv[d];
+      sf.nc[d] = b.nc[d];
+    }
+    sf.rcb2 = (float)b.rcut_cbmcsq;
+    sf.rv2 = (float)b.rcut_vdwsq;
+    sf.rq2 = (float)b.rcut_coulsq;
+    sf.low2 = (float)b.rcut_lowsq;
+    sf.rc_cbmc = (float)sqrt(b.rcut_cbmcsq);
+    sf.rc_full = (float)sqrt(fmax(b.rcut_vdwsq, b.rcut_coulsq));
+    sf.beta = (float)b.beta;
+    sf.kmaxE = (float)(kMAX_KBT / b.beta);
+    sf.alpha = (float)b.alpha;
+    sf.charge_on = b.charge_style == CASS_CHARGE_COUL;
+    s_atom_off = b.atom_off;
+    s_cell_off = b.cell_off;
+    s_natoms = b.natoms;
+    s_ec = b.e_inter_constant;
+  }
+  for (int i = threadIdx.x; i < kMaxTypes * kMaxTypes; i += blockDim.x) {
+    const int a = i / kMaxTypes, c = i % kMaxTypes;
+    const bool ok = a < T.ntypes && c < T.ntypes;
+    s_ljp[i] = ok ? make_float2(T.epsf[a * T.ntypes + c], T.sig2f[a * T.ntypes + c]) : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const int ncell = sf.nc[0] * sf.nc[1] * sf.nc[2];
+  BoxViewF V;
+  V.f = &sf;
+  V.q32 = cq32 + s_atom_off;
+  V.ljp = s_ljp;
+  if (SMEM) {
+    int* cs = reinterpret_cast<int*>(smem);
+    for (int c = threadIdx.x; c <= ncell; c += blockDim.x) cs[c] = cstart[s_cell_off + k + c];
+    const size_t off = ((size_t)(ncell + 1) * sizeof(int) + 31) & ~(size_t)31;
+    float4* s32 = reinterpret_cast<float4*>(smem + off);
+    for (int j = threadIdx.x; j < s_natoms; j += blockDim.x) s32[j] = c32[s_atom_off + j];
+    V.p32 = s32;
+    V.cstart = cs;
+    __syncthreads();
+  } else {
+    V.p32 = c32 + s_atom_off;
+    V.cstart = cstart + s_cell_off + k;
+  }
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  QueryAcc cnt;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n_ins; i += stride) {
+    const size_t g = (size_t)k * n_ins + i;
+    const Lfsr rng = seed_stream(seed, box_ids[k], i);
+    const RecF o = run_insertion_f(S, SF, V, libf, rng, want_xyz ? xyz + g * 3 * S.natoms : nullptr, cnt);
+    const double e_int = (double)o.e_inter;
+    rec[g] = make_double4_32a((double)o.dE_intra, e_int + s_ec, (double)o.dE_frag, (double)o.ln_pbias);
+    status[g] = (signed char)o.status;
+    if (trace) {
+      CassWidomTrace& t = trace[g];
+      t.ln_pbias = (double)o.ln_pbias;
+      t.e_first_trial_sum = (double)o.first_sum;
+      t.selected_trial = o.selected;
+      t.e_inter = o.status == 0 ? e_int : 0.0;
+      t.e_inter_abs = o.status == 0 ? (double)o.e_abs : 0.0;
+      t.overlap = o.status;
+    }
+  }
+  if (pair_counts) {
+    atomicAdd(&pair_counts[0], cnt.visited);
+    atomicAdd(&pair_counts[1], cnt.in_cut);
+  }
+}
+
+// FP64 kernel: one insertion per thread (the reference's arithmetic)
+template <bool SMEM>
 __global__ void __launch_bounds__(128) k_widom(WidomSpecies S, PairTable T, SpeciesPools P, const BoxDev* boxes,
-                                               const int* box_ids, const double4_32a* c64, const float4* c32,
-                                               const int* ctype, const float* cq32, const int* cstart,
-                                               const double* __restrict__ lib, long long n_ins, uint64_t seed,
-                                               WRec* rec, signed char* status, double* xyz, int want_xyz,
-                                               CassWidomTrace* trace, unsigned long long* pair_counts) {
+                                               const int* box_ids, const double4_32a* c64, const int* ctype,
+                                               const int* cstart, const double* __restrict__ lib, long long n_ins,
+                                               uint64_t seed, WRec* rec, signed char* status, double* xyz,
+                                               int want_xyz, CassWidomTrace* trace, unsigned long long* pair_counts) {
   extern __shared__ __align__(32) unsigned char smem[];
   __shared__ BoxDev sb;
   const int k = blockIdx.y;
@@ -858,8 +1473,6 @@ __global__ void __launch_bounds__(128) k_widom(WidomSpecies S, PairTable T, Spec
   const int ncell = sb.nc[0] * sb.nc[1] * sb.nc[2];
   BoxView V;
   V.b = &sb;
-  V.g64 = c64 + sb.atom_off;
-  V.q32 = cq32 + sb.atom_off;
   V.rc_cbmc = sqrt(sb.rcut_cbmcsq);
   double rfull = sqrt(fmax(sb.rcut_vdwsq, sb.rcut_coulsq));
   if (sb.vdw_sum_style == CASS_VDW_SUM_MINIMUM || sb.vdw_sum_style == CASS_VDW_SUM_CHARMM ||
@@ -867,36 +1480,23 @@ __global__ void __launch_bounds__(128) k_widom(WidomSpecies S, PairTable T, Spec
     rfull = 1e30;
   if (sb.vdw_sum_style == CASS_VDW_SUM_CUT_SWITCH) rfull = fmax(rfull, sqrt(sb.roff_switch_sq));
   V.rc_full = rfull;
-  V.fast_mixed = sb.vdw_style == CASS_VDW_LJ &&
-                 (sb.vdw_sum_style == CASS_VDW_SUM_CUT || sb.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) &&
-                 (sb.charge_style == CASS_CHARGE_NONE || sb.charge_sum_style == CASS_QQ_EWALD);
   if (SMEM) {
     int* cs = reinterpret_cast<int*>(smem);
     for (int c = threadIdx.x; c <= ncell; c += blockDim.x) cs[c] = cstart[sb.cell_off + k + c];
     size_t off = ((size_t)(ncell + 1) * sizeof(int) + 31) & ~(size_t)31;
-    if (MIXED) {
-      float4* s32 = reinterpret_cast<float4*>(smem + off);
-      for (int j = threadIdx.x; j < na; j += blockDim.x) s32[j] = c32[sb.atom_off + j];
-      V.p32 = s32;
-      V.p64 = V.g64;
-      V.ptype = ctype + sb.atom_off;
-    } else {
-      double4_32a* s64 = reinterpret_cast<double4_32a*>(smem + off);
-      int* st = reinterpret_cast<int*>(smem + off + (size_t)na * sizeof(double4_32a));
-      for (int j = threadIdx.x; j < na; j += blockDim.x) {
-        s64[j] = c64[sb.atom_off + j];
-        st[j] = ctype[sb.atom_off + j];
-      }
-      V.p64 = s64;
-      V.ptype = st;
-      V.p32 = c32 + sb.atom_off;
+    double4_32a* s64 = reinterpret_cast<double4_32a*>(smem + off);
+    int* st = reinterpret_cast<int*>(smem + off + (size_t)na * sizeof(double4_32a));
+    for (int j = threadIdx.x; j < na; j += blockDim.x) {
+      s64[j] = c64[sb.atom_off + j];
+      st[j] = ctype[sb.atom_off + j];
     }
+    V.p64 = s64;
+    V.ptype = st;
     V.cstart = cs;
     __syncthreads();
   } else {
     V.cstart = cstart + sb.cell_off + k;
     V.p64 = c64 + sb.atom_off;
-    V.p32 = c32 + sb.atom_off;
     V.ptype = ctype + sb.atom_off;
   }
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -906,8 +1506,8 @@ __global__ void __launch_bounds__(128) k_widom(WidomSpecies S, PairTable T, Spec
     Lfsr rng = seed_stream(seed, box_ids[k], i);
     WRec rr;
     int st = 0;
-    run_insertion<MIXED>(S, P, T, V, lib, rng, rr, st, want_xyz ? xyz + g * 3 * S.natoms : nullptr,
-                         trace ? trace + g : nullptr, pc);
+    run_insertion(S, P, T, V, lib, rng, rr, st, want_xyz ? xyz + g * 3 * S.natoms : nullptr,
+                  trace ? trace + g : nullptr, pc);
     rec[g] = rr;
     status[g] = (signed char)st;
     if (trace) trace[g].overlap = st;
@@ -1043,11 +1643,61 @@ double lrc_host(cass_ctx* c, const BoxH& B, const std::vector<double>& nb) {
   return e;
 }
 
+// FP32 tables of the test species for k_widom_mixed; false when the species
+// does not fit them (the FP64-geometry kernel runs instead)
+bool species_f(const SpeciesH& s, SpeciesF& F) {
+  memset(&F, 0, sizeof(F));
+  const int n = s.natoms;
+  const int nb = (int)s.bond_kind.size(), na = (int)s.angle_kind.size();
+  const int nd = (int)(s.dih_atoms.size() / 4), ni = (int)(s.imp_atoms.size() / 4);
+  if (n > kMaxAtoms || nb > kMaxBonded || na > kMaxBonded || nd > kMaxBonded || ni > kMaxBonded) return false;
+  F.natoms = n;
+  F.nbonds = nb;
+  F.nangles = na;
+  F.ndih = nd;
+  F.nimp = ni;
+  for (int a = 0; a < n; ++a) {
+    F.q[a] = (float)s.q[a];
+    F.mass[a] = (float)s.mass[a];
+    F.type[a] = s.type[a];
+    for (int b = 0; b < n; ++b) {
+      F.vs[a * n + b] = (float)s.vscale[a * n + b];
+      F.qs[a * n + b] = (float)s.qscale[a * n + b];
+      if (s.bonded[a * n + b]) F.bonded[a] |= 1u << b;
+    }
+  }
+  for (int k = 0; k < nb; ++k) {
+    F.bond_atoms[k][0] = (signed char)s.bond_atoms[2 * k];
+    F.bond_atoms[k][1] = (signed char)s.bond_atoms[2 * k + 1];
+    F.bond_harm[k] = s.bond_kind[k] == CASS_BONDED_HARMONIC;
+    F.bond_k[k] = (float)s.bond_param[2 * k];
+    F.bond_l0[k] = (float)s.bond_param[2 * k + 1];
+  }
+  for (int k = 0; k < na; ++k) {
+    for (int j = 0; j < 3; ++j) F.angle_atoms[k][j] = (signed char)s.angle_atoms[3 * k + j];
+    F.angle_harm[k] = s.angle_kind[k] == CASS_BONDED_HARMONIC;
+    F.angle_k[k] = (float)s.angle_param[2 * k];
+    F.angle_t0[k] = (float)s.angle_param[2 * k + 1];
+  }
+  for (int k = 0; k < nd; ++k) {
+    for (int j = 0; j < 4; ++j) F.dih_atoms[k][j] = (signed char)s.dih_atoms[4 * k + j];
+    for (int j = 0; j < 6; ++j) F.rb[k][j] = (float)s.dih_rb[6 * k + j];
+  }
+  for (int k = 0; k < ni; ++k) {
+    for (int j = 0; j < 4; ++j) F.imp_atoms[k][j] = (signed char)s.imp_atoms[4 * k + j];
+    F.imp_k[k] = (float)s.imp_param[2 * k];
+    F.imp_p0[k] = (float)s.imp_param[2 * k + 1];
+  }
+  for (int f = 0; f < s.nfrag; ++f) F.cum_prob_ins[f] = (float)s.cum_prob_ins[f];
+  return true;
+}
+
 }  // namespace
 
 namespace cassgpu {
 int ensure_pools(cass_ctx* c);
 int pack_box_ext(cass_ctx* c, int ibox);
+const std::vector<int>& members_ext(cass_ctx* c, int ibox);
 }  // namespace cassgpu
 
 extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const int32_t* iboxes, int64_t n_ins,
@@ -1110,9 +1760,11 @@ extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const
   std::vector<BoxSrc> src(nboxes);
   std::vector<int> kvoff(nboxes, 0), has_ew(nboxes, 0);
   int atom_off = 0, cell_off = 0, kv_total = 0, max_na = 0;
-  size_t max_smem = 0;
+  size_t max_smem32 = 0, max_smem64 = 0;
   const bool mixed = c->precision == CASS_PREC_MIXED;
   bool any_recip = false;
+  // the FP32 warp kernel covers LJ cut / cut_tail with no charges or Ewald
+  bool fast_mixed = c->pt.ntypes <= kMaxTypes;
   for (int k = 0; k < nboxes; ++k) {
     int ib = iboxes[k] - 1;
     if ((rc = pack_box_ext(c, ib))) return rc;
@@ -1130,20 +1782,18 @@ extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const
     v.natoms = B.npacked;
     v.cell_off = cell_off;
     // Widom_Insert set-up (widom_insert.f90:201-245)
+    const std::vector<int>& mem = members_ext(c, ib);
     int nmols = 1;
-    for (int im = 0; im < c->max_mol[is0]; ++im)
-      if (c->mol_box[c->mol_base[is0] + im] == ib) ++nmols;
+    for (int slot : mem)
+      if (c->slot_sp[slot] == is0) ++nmols;
     v.prefactor = v.volume / (double)nmols;
     double lrc_diff = 0.0;
     if (B.desc.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) {
       std::vector<double> nb(c->ntypes, 0.0);
-      for (int js = 0; js < c->nspecies; ++js) {
-        const SpeciesH& t = c->sp[js];
-        if (!t.defined) continue;
-        for (int jm = 0; jm < c->max_mol[js]; ++jm)
-          if (c->mol_box[c->mol_base[js] + jm] == ib)
-            for (int a = 0; a < t.natoms; ++a)
-              if (t.type[a] >= 0) nb[t.type[a]] += 1.0;
+      for (int slot : mem) {
+        const SpeciesH& t = c->sp[c->slot_sp[slot]];
+        for (int a = 0; a < t.natoms; ++a)
+          if (t.type[a] >= 0) nb[t.type[a]] += 1.0;
       }
       for (int a = 0; a < s.natoms; ++a)
         if (s.type[a] >= 0) nb[s.type[a]] += 1.0;
@@ -1159,6 +1809,9 @@ extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const
       e_recip_in = B.energy.reciprocal;
     }
     v.e_inter_constant = lrc_diff + e_self - e_recip_in;
+    fast_mixed = fast_mixed && B.desc.vdw_style == CASS_VDW_LJ &&
+                 (B.desc.vdw_sum_style == CASS_VDW_SUM_CUT || B.desc.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) &&
+                 (B.desc.charge_style == CASS_CHARGE_NONE || B.desc.charge_sum_style == CASS_QQ_EWALD);
     if (B.desc.charge_style == CASS_CHARGE_COUL && B.desc.charge_sum_style == CASS_QQ_EWALD && s.has_charge &&
         B.nvecs > 0) {
       has_ew[k] = 1;
@@ -1170,9 +1823,9 @@ extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const
     src[k].p64 = B.d_p64.as<double4_32a>();
     src[k].p32 = B.d_p32.as<float4>();
     src[k].meta = B.d_meta.as<int4>();
-    size_t sm = (((size_t)(ncell + 1) * sizeof(int) + 31) & ~(size_t)31) +
-                (size_t)B.npacked * (mixed ? sizeof(float4) : (sizeof(double4_32a) + sizeof(int)));
-    max_smem = std::max(max_smem, sm);
+    const size_t sm_cells = ((size_t)(ncell + 1) * sizeof(int) + 31) & ~(size_t)31;
+    max_smem32 = std::max(max_smem32, sm_cells + (size_t)B.npacked * sizeof(float4));
+    max_smem64 = std::max(max_smem64, sm_cells + (size_t)B.npacked * (sizeof(double4_32a) + sizeof(int)));
     max_na = std::max(max_na, B.npacked);
     atom_off += B.npacked;
     cell_off += ncell;
@@ -1243,8 +1896,12 @@ extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const
   long long* d_bov = reinterpret_cast<long long*>(d_bsum + nboxes);
   unsigned long long* d_pairs = c->count_pairs ? reinterpret_cast<unsigned long long*>(d_bov + nboxes) : nullptr;
   if (d_pairs) CASS_CUDA(cudaMemsetAsync(d_pairs, 0, 2 * sizeof(unsigned long long), c->stream));
-  // K8 launch shape: 128-thread CTAs, enough CTAs per box to fill every SM
-  bool use_smem = max_smem <= (size_t)200 * 1024;
+  // K8 launch shape: 128-thread CTAs, enough CTAs per box to fill every SM;
+  // the box is staged in shared memory when it fits
+  SpeciesF SF;
+  const bool f32 = mixed && fast_mixed && species_f(s, SF);
+  const size_t max_smem = f32 ? max_smem32 : max_smem64;
+  const bool use_smem = max_smem <= (size_t)200 * 1024;
   int dev_sms = 0;
   CASS_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
   const int threads = 128;
@@ -1263,17 +1920,39 @@ extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const
     c->stats.widom_smem_bytes = use_smem ? (int)max_smem : 0;
     CASS_CUDA(cudaEventRecord(c->ev[1], c->stream));
     kern<<<g, threads, use_smem ? max_smem : 0, c->stream>>>(
-        S, c->pt, c->pools, d_bd, d_ids, c->d_c64.as<double4_32a>(), d_c32, d_ctype, c->d_cq32.as<float>(),
-        c->d_cell_start.as<int>(), s.d_library.as<double>(), (long long)n_ins, seed, d_rec, d_status, d_xyz,
-        any_recip ? 1 : 0, d_trace, d_pairs);
+        S, c->pt, c->pools, d_bd, d_ids, c->d_c64.as<double4_32a>(), d_ctype, c->d_cell_start.as<int>(),
+        s.d_library.as<double>(), (long long)n_ins, seed, d_rec, d_status, d_xyz, any_recip ? 1 : 0, d_trace, d_pairs);
+    CASS_CUDA(cudaGetLastError());
+    CASS_CUDA(cudaEventRecord(c->ev[2], c->stream));
+    count_launch(c);
+    return CASS_OK;
+  };
+  // FP32 kernel of the mixed path
+  auto launch_f32 = [&](auto kern, const SpeciesF& SF) -> int {
+    if (use_smem) CASS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem));
+    int per_sm = 1;
+    CASS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, use_smem ? max_smem : 0));
+    per_sm = std::max(per_sm, 1);
+    long long want = ((long long)dev_sms * per_sm * 2 + nboxes - 1) / nboxes;
+    long long need = (n_ins + threads - 1) / threads;
+    int chunks = (int)std::max<long long>(1, std::min(want, need));
+    dim3 g(chunks, nboxes);
+    c->stats.widom_grid_x = chunks;
+    c->stats.widom_grid_y = nboxes;
+    c->stats.widom_block = threads;
+    c->stats.widom_smem_bytes = use_smem ? (int)max_smem : 0;
+    CASS_CUDA(cudaEventRecord(c->ev[1], c->stream));
+    kern<<<g, threads, use_smem ? max_smem : 0, c->stream>>>(
+        S, SF, c->pt, d_bd, d_ids, d_c32, c->d_cq32.as<float>(), c->d_cell_start.as<int>(), s.d_library_f.as<float>(),
+        (long long)n_ins, seed, d_rec, d_status, d_xyz, any_recip ? 1 : 0, d_trace, d_pairs);
     CASS_CUDA(cudaGetLastError());
     CASS_CUDA(cudaEventRecord(c->ev[2], c->stream));
     count_launch(c);
     return CASS_OK;
   };
   if (n_ins > 0) {
-    if (mixed) rc = use_smem ? launch(k_widom<true, true>) : launch(k_widom<true, false>);
-    else rc = use_smem ? launch(k_widom<false, true>) : launch(k_widom<false, false>);
+    if (f32) rc = use_smem ? launch_f32(k_widom_f32<true>, SF) : launch_f32(k_widom_f32<false>, SF);
+    else rc = use_smem ? launch(k_widom<true>) : launch(k_widom<false>);
     if (rc) return rc;
     if (any_recip) {
       // k-vectors and structure factors of the batch boxes, concatenated

@@ -106,11 +106,36 @@ struct orc_ctx {
   std::vector<Species> sp;
   std::vector<Box> box;
   std::vector<Mol> mol;  // slot = mol_base[is] + im
+  // live slots of each box in slot order (species-major, locate order), the
+  // counterpart of the reference's locate(:, is, ibox) arrays; sp_off[ibox][is]
+  // is the first member of species is
+  std::vector<std::vector<int>> members, sp_off;
+  bool members_dirty = true;
 };
 
 namespace {
 
 inline Mol& mol_of(orc_ctx* c, int is, int im) { return c->mol[c->mol_base[is] + im]; }
+
+void refresh_members(orc_ctx* c) {
+  if (!c->members_dirty) return;
+  c->members.assign(c->nboxes, {});
+  c->sp_off.assign(c->nboxes, std::vector<int>(c->nspecies + 1, 0));
+  for (size_t slot = 0; slot < c->mol.size(); ++slot) {
+    const Mol& m = c->mol[slot];
+    if (m.live && m.ibox >= 0 && m.ibox < c->nboxes) c->members[m.ibox].push_back((int)slot);
+  }
+  for (int b = 0; b < c->nboxes; ++b) {
+    const std::vector<int>& mem = c->members[b];
+    size_t k = 0;
+    for (int is = 0; is <= c->nspecies; ++is) {
+      const int lim = is < c->nspecies ? c->mol_base[is] : INT32_MAX;
+      while (k < mem.size() && mem[k] < lim) ++k;
+      c->sp_off[b][is] = (int)k;
+    }
+  }
+  c->members_dirty = false;
+}
 
 // ---------------------------------------------------------------------------
 // lfsr258 generator, random_generators.f90:95-122 (rranf), plus the
@@ -395,19 +420,15 @@ bool mol_inter_energy(const orc_ctx* c, int ibox, const MolView& a, int skip, bo
   const Box& b = c->box[ibox];
   evdw = 0.0;
   eqq = 0.0;
-  for (int js = 0; js < c->nspecies; ++js) {
-    for (int jm = 0; jm < c->max_mol[js]; ++jm) {
-      int slot = c->mol_base[js] + jm;
-      if (slot == skip) continue;
-      const Mol& m = c->mol[slot];
-      if (!m.live || m.ibox != ibox) continue;
-      MolView mv = view_of(m);
-      if (!check_molpair_cutoff(b, a, mv, cbmc)) continue;
-      double vlj, vqq;
-      if (molpair_energy(c, b, a, mv, cbmc, vlj, vqq, eabs)) return true;
-      evdw += vlj;
-      eqq += vqq;
-    }
+  for (int slot : c->members[ibox]) {
+    if (slot == skip) continue;
+    const Mol& m = c->mol[slot];
+    MolView mv = view_of(m);
+    if (!check_molpair_cutoff(b, a, mv, cbmc)) continue;
+    double vlj, vqq;
+    if (molpair_energy(c, b, a, mv, cbmc, vlj, vqq, eabs)) return true;
+    evdw += vlj;
+    eqq += vqq;
   }
   return false;
 }
@@ -627,11 +648,11 @@ double system_recip(orc_ctx* c, int ibox) {
   size_t nv = b.hx.size();
   std::fill(b.cos_sum.begin(), b.cos_sum.end(), 0.0);
   std::fill(b.sin_sum.begin(), b.sin_sum.end(), 0.0);
-  for (int is = 0; is < c->nspecies; ++is) {
+  for (int slot : c->members[ibox]) {
+    Mol& m = c->mol[slot];
+    const int is = m.is;
     if (!c->sp[is].has_charge) continue;
-    for (int im = 0; im < c->max_mol[is]; ++im) {
-      Mol& m = mol_of(c, is, im);
-      if (!m.live || m.ibox != ibox) continue;
+    {
       m.cos_mol.assign(nv, 0.0);
       m.sin_mol.assign(nv, 0.0);
       mol_structure_factor(c, b, is, m.r.data(), m.cos_mol.data(), m.sin_mol.data());
@@ -650,12 +671,10 @@ double system_recip(orc_ctx* c, int ibox) {
 double system_self(const orc_ctx* c, int ibox) {
   const Box& b = c->box[ibox];
   double es = 0;
-  for (int is = 0; is < c->nspecies; ++is)
-    for (int im = 0; im < c->max_mol[is]; ++im) {
-      const Mol& m = c->mol[c->mol_base[is] + im];
-      if (!m.live || m.ibox != ibox) continue;
-      for (int ia = 0; ia < c->sp[is].natoms; ++ia) es = es + c->sp[is].q[ia] * c->sp[is].q[ia];
-    }
+  for (int slot : c->members[ibox]) {
+    const Species& s = c->sp[c->mol[slot].is];
+    for (int ia = 0; ia < s.natoms; ++ia) es = es + s.q[ia] * s.q[ia];
+  }
   if (b.charge_sum_style == CASS_QQ_EWALD) return -es * CHARGE_FACTOR * b.alpha_ewald / ROOTPI;
   if (b.charge_sum_style == CASS_QQ_DSF) return -(es * (b.alpha_dsf / ROOTPI + b.dsf_factor1 / 2.0)) * CHARGE_FACTOR;
   return 0.0;
@@ -706,13 +725,11 @@ double lr_correction(const orc_ctx* c, const Box& b, const std::vector<double>& 
 
 std::vector<double> count_beads(const orc_ctx* c, int ibox) {
   std::vector<double> nb(c->ntypes, 0.0);
-  for (int is = 0; is < c->nspecies; ++is)
-    for (int im = 0; im < c->max_mol[is]; ++im) {
-      const Mol& m = c->mol[c->mol_base[is] + im];
-      if (!m.live || m.ibox != ibox) continue;
-      for (int ia = 0; ia < c->sp[is].natoms; ++ia)
-        if (c->sp[is].type[ia] >= 0) nb[c->sp[is].type[ia]] += 1.0;
-    }
+  for (int slot : c->members[ibox]) {
+    const Species& s = c->sp[c->mol[slot].is];
+    for (int ia = 0; ia < s.natoms; ++ia)
+      if (s.type[ia] >= 0) nb[s.type[ia]] += 1.0;
+  }
   return nb;
 }
 
@@ -955,6 +972,10 @@ InsertionOut widom_one(const orc_ctx* c, int is, int ibox, int kappa_ins, int ka
       int fc = -1;
       for (int g : s.frag_connect[f])
         if (placed[g]) { fc = g; break; }
+      if (fc < 0) {  // no placed neighbour: the fragment graph is not connected
+        cbmc_overlap = true;
+        break;
+      }
       int anc_i = atoms[0];
       int anc_c = s.frag_atoms[fc][0];
       std::vector<int> atom_id;
@@ -1359,6 +1380,7 @@ int orc_set_molecules(orc_ctx* c, int32_t n, const int32_t* im, const int32_t* i
     Mol& m = mol_of(c, is[k] - 1, im[k] - 1);
     int na = c->sp[is[k] - 1].natoms;
     if (m.live) invalidate_box(c, m.ibox);
+    if (!m.live || m.ibox != ibox[k] - 1) c->members_dirty = true;
     m.ibox = ibox[k] - 1;
     m.live = true;
     m.r.assign(xyz + off, xyz + off + 3 * na);
@@ -1375,6 +1397,7 @@ int orc_remove_molecule(orc_ctx* c, int32_t im, int32_t is) {
   if (rc) return rc;
   Mol& m = mol_of(c, is - 1, im - 1);
   if (m.live) invalidate_box(c, m.ibox);
+  if (m.live) c->members_dirty = true;
   m.live = false;
   return CASS_OK;
 }
@@ -1388,6 +1411,7 @@ int orc_get_molecule(orc_ctx* c, int32_t im, int32_t is, double* xyz) {
 }
 
 int orc_mol_inter_energy(orc_ctx* c, int32_t im, int32_t is, int32_t cbmc, double* ev, double* eq, int32_t* ov) {
+  if (c) refresh_members(c);
   int rc = check_ctx(c) ? CASS_EINVAL : check_mol(c, im, is);
   if (rc) return rc;
   Mol& m = mol_of(c, is - 1, im - 1);
@@ -1403,6 +1427,7 @@ int orc_mol_inter_energy(orc_ctx* c, int32_t im, int32_t is, int32_t cbmc, doubl
 
 int orc_mol_intra_energy(orc_ctx* c, int32_t im, int32_t is, int32_t cbmc, double* eiv, double* eiq, double* eoq,
                          int32_t* ov) {
+  if (c) refresh_members(c);
   int rc = check_ctx(c) ? CASS_EINVAL : check_mol(c, im, is);
   if (rc) return rc;
   Mol& m = mol_of(c, is - 1, im - 1);
@@ -1414,6 +1439,7 @@ int orc_mol_intra_energy(orc_ctx* c, int32_t im, int32_t is, int32_t cbmc, doubl
 
 // Compute_System_Total_Energy (energy_routines.f90:2648-2953)
 int orc_system_total_energy(orc_ctx* c, int32_t ibox1, int32_t intra_flag, CassEnergy* out, int32_t* overlap) {
+  if (c) refresh_members(c);
   if (check_ctx(c) || ibox1 < 1 || ibox1 > c->nboxes || !out || !overlap) return fail(CASS_EINVAL, "bad args");
   int ibox = ibox1 - 1;
   Box& b = c->box[ibox];
@@ -1425,9 +1451,9 @@ int orc_system_total_energy(orc_ctx* c, int32_t ibox1, int32_t intra_flag, CassE
     for (int is = 0; is < c->nspecies; ++is) {
       const Species& s = c->sp[is];
       double vi = 0, vb = 0, va = 0, vd = 0, vim = 0, viv = 0, viq = 0, voq = 0;
-      for (int im = 0; im < c->max_mol[is]; ++im) {
-        Mol& m = mol_of(c, is, im);
-        if (!m.live || m.ibox != ibox) continue;
+      const std::vector<int>& mem = c->members[ibox];
+      for (int k = c->sp_off[ibox][is]; k < c->sp_off[ibox][is + 1]; ++k) {
+        Mol& m = c->mol[mem[k]];
         double mb = bond_energy(s, m.r.data());
         double ma = angle_energy(s, m.r.data(), m.exist.data());
         double md = dihedral_energy(s, m.r.data(), m.exist.data());
@@ -1460,15 +1486,15 @@ int orc_system_total_energy(orc_ctx* c, int32_t ibox1, int32_t intra_flag, CassE
     E.improper = keep_intra[4]; E.intra_vdw = keep_intra[5]; E.intra_q = keep_intra[6]; E.self = keep_intra[7];
   }
   // inter-molecular pairs, same species then cross species
+  const std::vector<int>& mem = c->members[ibox];
+  const std::vector<int>& so = c->sp_off[ibox];
   for (int is1 = 0; is1 < c->nspecies; ++is1) {
-    for (int im1 = 0; im1 < c->max_mol[is1]; ++im1) {
-      Mol& m1 = mol_of(c, is1, im1);
-      if (!m1.live || m1.ibox != ibox) continue;
+    for (int k1 = so[is1]; k1 < so[is1 + 1]; ++k1) {
+      Mol& m1 = c->mol[mem[k1]];
       for (int is2 = is1; is2 < c->nspecies; ++is2) {
         double ev = 0, eq = 0;
-        for (int im2 = (is2 == is1 ? im1 + 1 : 0); im2 < c->max_mol[is2]; ++im2) {
-          Mol& m2 = mol_of(c, is2, im2);
-          if (!m2.live || m2.ibox != ibox) continue;
+        for (int k2 = (is2 == is1 ? k1 + 1 : so[is2]); k2 < so[is2 + 1]; ++k2) {
+          Mol& m2 = c->mol[mem[k2]];
           MolView a = view_of(m1), v = view_of(m2);
           if (!check_molpair_cutoff(b, a, v, false)) continue;
           double vlj, vqq;
@@ -1505,6 +1531,7 @@ int orc_system_total_energy(orc_ctx* c, int32_t ibox1, int32_t intra_flag, CassE
 
 // Update_System_Ewald_Reciprocal_Energy (energy_routines.f90:2326-2497)
 int orc_ewald_update(orc_ctx* c, int32_t im, int32_t is, int32_t ibox1, int32_t move_flag, double* e_recip) {
+  if (c) refresh_members(c);
   int rc = check_ctx(c) ? CASS_EINVAL : check_mol(c, im, is);
   if (rc) return rc;
   if (ibox1 < 1 || ibox1 > c->nboxes) return fail(CASS_EINVAL, "box index");
@@ -1552,6 +1579,7 @@ int orc_ewald_update(orc_ctx* c, int32_t im, int32_t is, int32_t ibox1, int32_t 
 }
 
 int orc_ewald_restore(orc_ctx* c, int32_t im, int32_t is, int32_t ibox1) {
+  if (c) refresh_members(c);
   int rc = check_ctx(c) ? CASS_EINVAL : check_mol(c, im, is);
   if (rc) return rc;
   Box& b = c->box[ibox1 - 1];
@@ -1564,6 +1592,7 @@ int orc_ewald_restore(orc_ctx* c, int32_t im, int32_t is, int32_t ibox1) {
 }
 
 int orc_ewald_widom(orc_ctx* c, int32_t is, int32_t ibox1, int32_t n, const double* xyz, double* e) {
+  if (c) refresh_members(c);
   if (check_ctx(c) || is < 1 || is > c->nspecies || ibox1 < 1 || ibox1 > c->nboxes) return fail(CASS_EINVAL, "bad");
   Box& b = c->box[ibox1 - 1];
   const Species& s = c->sp[is - 1];
@@ -1590,6 +1619,7 @@ int orc_ewald_widom(orc_ctx* c, int32_t is, int32_t ibox1, int32_t n, const doub
 int orc_widom_insert(orc_ctx* c, int32_t is1, int32_t nboxes, const int32_t* iboxes, int64_t n_ins,
                      int32_t kappa_ins, int32_t kappa_dih, uint64_t seed, CassWidomResult* out,
                      CassWidomTrace* trace) {
+  if (c) refresh_members(c);
   if (check_ctx(c) || is1 < 1 || is1 > c->nspecies || nboxes < 1 || !iboxes || !out || n_ins < 0 || kappa_ins < 1)
     return fail(CASS_EINVAL, "bad widom args");
   int is = is1 - 1;
@@ -1601,15 +1631,13 @@ int orc_widom_insert(orc_ctx* c, int32_t is1, int32_t nboxes, const int32_t* ibo
     if (ib < 0 || ib >= c->nboxes) return fail(CASS_EINVAL, "box index");
     if (!c->box[ib].energy_valid) return fail(CASS_ESTATE, "system energy of box not computed");
   }
+  // Widom_Insert set-up per box (widom_insert.f90:201-245)
+  std::vector<double> Ec(nboxes), prefactor(nboxes);
   for (int k = 0; k < nboxes; ++k) {
     int ibox = iboxes[k] - 1;
     const Box& b = c->box[ibox];
-    int nmols = 1;
-    for (int im = 0; im < c->max_mol[is]; ++im) {
-      const Mol& m = c->mol[c->mol_base[is] + im];
-      if (m.live && m.ibox == ibox) ++nmols;
-    }
-    double prefactor = b.volume / (double)nmols;
+    const int nmols = 1 + c->sp_off[ibox][is + 1] - c->sp_off[ibox][is];
+    prefactor[k] = b.volume / (double)nmols;
     double lrc_diff = 0.0;
     if (b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) {
       std::vector<double> nb = count_beads(c, ibox);
@@ -1622,13 +1650,24 @@ int orc_widom_insert(orc_ctx* c, int32_t is1, int32_t nboxes, const int32_t* ibo
       E_self = molecule_self(c, b, is);
       E_recip_in = b.energy.reciprocal;
     }
-    double Ec = lrc_diff + E_self - E_recip_in;
+    Ec[k] = lrc_diff + E_self - E_recip_in;
+  }
+  // every (box, insertion) is independent: one parallel loop over all of them,
+  // then per-box sums in insertion order (independent of the thread count)
+  const int64_t total = (int64_t)nboxes * n_ins;
+  std::vector<InsertionOut> res((size_t)total);
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int64_t g = 0; g < total; ++g) {
+    const int k = (int)(g / n_ins);
+    const int64_t i = g % n_ins;
+    Rng rng = seed_stream(seed, iboxes[k], i);
+    res[(size_t)g] = widom_one(c, is, iboxes[k] - 1, kappa_ins, kappa_dih, Ec[k], rng);
+  }
+  for (int k = 0; k < nboxes; ++k) {
     double wsum = 0.0;
     int64_t nov = 0;
-#pragma omp parallel for schedule(dynamic, 64) reduction(+ : wsum, nov)
     for (int64_t i = 0; i < n_ins; ++i) {
-      Rng rng = seed_stream(seed, iboxes[k], i);
-      InsertionOut o = widom_one(c, is, ibox, kappa_ins, kappa_dih, Ec, rng);
+      const InsertionOut& o = res[(size_t)k * n_ins + i];
       if (o.overlap) ++nov;
       else wsum += o.widom_var;
       if (trace) {
@@ -1642,8 +1681,8 @@ int orc_widom_insert(orc_ctx* c, int32_t is1, int32_t nboxes, const int32_t* ibo
         tr.overlap = o.overlap;
       }
     }
-    out[k].widom_sum = wsum * prefactor;
-    out[k].prefactor = prefactor;
+    out[k].widom_sum = wsum * prefactor[k];
+    out[k].prefactor = prefactor[k];
     out[k].n_insertions = n_ins;
     out[k].n_overlaps = nov;
     out[k].n_trials = n_ins * (int64_t)(kappa_ins + (s.nfrag - 1) * kappa_dih);
