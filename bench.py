@@ -51,6 +51,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU-baseline sample length")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-mc", action="store_true", help="skip the MC-sweep leg")
     return p.parse_args()
 
 
@@ -140,6 +141,69 @@ def cpu_baseline(system, args, per_box_cap=None):
     return {"value": trials / dt, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
             "sample": f"{len(boxes)} boxes x {n} insertions ({trials} trial energies) in {dt:.2f} s, "
                       f"FP64 C++ oracle, OpenMP over insertions"}
+
+
+def mc_leg(cg, abi, dev, with_cpu: bool) -> dict:
+    """NVT MC sweeps/s: the 500-sphere LJ box (translation) and the 256-water
+    Ewald box (translate/rotate 50/50), one chain and many independent chains."""
+    from cassandra_gb300 import workloads
+
+    def chains(system, boxes, nsweeps, precision, prob_translate, recompute=False):
+        ns = len(system.species)
+        with cg.open_system(system, precision=precision, device=dev) as g:
+            for b in boxes:
+                g.system_total_energy(b)
+            md, mr = [[0.8] * ns] * len(boxes), [[0.4] * ns] * len(boxes)
+            g.mc_sweeps(boxes, 1, md, mr, seed=1, prob_translate=prob_translate)  # warm-up
+            res, _, _ = g.mc_sweeps(boxes, nsweeps, md, mr, seed=2, prob_translate=prob_translate)
+            st = g.stats()
+            out = {"chains": len(boxes), "sweeps": nsweeps, "kernel_ms": st["mc_ms"],
+                   "sweeps_per_s": nsweeps * len(boxes) / (st["mc_ms"] / 1e3),
+                   "moves_per_s": st["mc_moves"] / (st["mc_ms"] / 1e3),
+                   "acceptance": sum(r["n_translate_accepted"] + r["n_rotate_accepted"] for r in res) /
+                   max(1, sum(r["n_translate"] + r["n_rotate"] for r in res))}
+            if recompute:  # the running FP64 bookkeeping against an FP64 recomputation of the final frame
+                m = system.molecules
+                xyz = np.concatenate([g.get_molecule(im, is_).ravel() for im, is_ in zip(m.im, m.is_)])
+                with cg.open_system(system, precision=abi.PREC_FP64, device=dev) as f:
+                    f.set_molecules(m.im, m.is_, m.ibox, xyz)
+                    e, _ = f.system_total_energy(boxes[0])
+                scale = abs(e["inter_vdw"]) + abs(e["inter_q"]) + abs(e["reciprocal"])
+                out["bookkeeping_rel_err"] = abs(res[0]["energy"]["total"] - e["total"]) / scale
+            return out
+
+    def cpu(system, nsweeps, prob_translate):
+        from oracle import oracle
+        ns = len(system.species)
+        with oracle.open_system(system) as o:
+            o.system_total_energy(1)
+            t0 = time.perf_counter()
+            o.mc_sweeps([1], nsweeps, [[0.8] * ns], [[0.4] * ns], seed=2, prob_translate=prob_translate)
+            dt = time.perf_counter() - t0
+        return {"sweeps_per_s": nsweeps / dt, "cores": 1, "kind": "port",
+                "sample": f"{nsweeps} sweeps of one chain, FP64 C++ oracle, one thread"}
+
+    out = {}
+    c0 = workloads.lj_nvt_system(nboxes=1)
+    c0r = workloads.lj_nvt_system(nboxes=304, seed=7)
+    out["lj500_translate"] = {
+        "workload": "500 LJ spheres, sigma 3.73 A, eps/k 148 K, 35 A box, T 150 K, 14 A cut_tail, translation",
+        "mixed_1chain": chains(c0, [1], 100, abi.PREC_MIXED, 1.0, recompute=True),
+        "fp64_1chain": chains(c0, [1], 20, abi.PREC_FP64, 1.0),
+        "mixed_304chains": chains(c0r, list(range(1, 305)), 20, abi.PREC_MIXED, 1.0),
+        "fp64_304chains": chains(c0r, list(range(1, 305)), 2, abi.PREC_FP64, 1.0)}
+    c1 = workloads.water_nvt_system(nboxes=1)
+    c1r = workloads.water_nvt_system(nboxes=152, seed=5)
+    out["water256_translate_rotate"] = {
+        "workload": "256 rigid 3-site waters, 19.7 A box, T 298 K, 9.8 A LJ + Ewald real space, tol 1e-5 "
+                    "(959 k-vectors), translate/rotate 50/50",
+        "mixed_1chain": chains(c1, [1], 20, abi.PREC_MIXED, 0.5, recompute=True),
+        "fp64_1chain": chains(c1, [1], 2, abi.PREC_FP64, 0.5),
+        "mixed_152chains": chains(c1r, list(range(1, 153)), 4, abi.PREC_MIXED, 0.5)}
+    if with_cpu:
+        out["lj500_translate"]["cpu_baseline"] = cpu(c0, 20, 1.0)
+        out["water256_translate_rotate"]["cpu_baseline"] = cpu(c1, 4, 0.5)
+    return out
 
 
 def flush_l2(torch, buf):
@@ -256,25 +320,30 @@ def main():
     gctx.widom_insert(2, boxes, n_per_box, args.kappa, args.kappa, seed=args.seed + 555)
     st = gctx.stats()
     gctx.set_count_pairs(False)
-    # plain FP64 GPU path on the same workload
-    fctx = cg.open_system(system, precision=abi.PREC_FP64, device=dev)
-    for b in boxes:
-        fctx.system_total_energy(b)
-    fms, fkms, _, _ = timed_steps(fctx, args.fp64_steps, 1, args.seed)
-    fp64_value = trials_step * len(fms) / (float(np.sum(fms)) / 1000.0)
-    # accuracy of the mixed path against FP64 on this workload (per-insertion trace of a sub-batch)
-    sub = boxes[:8]
-    ra, ta = fctx.widom_insert(2, sub, 2000, args.kappa, args.kappa, seed=4242, trace=True)
-    rb, tb = gctx.widom_insert(2, sub, 2000, args.kappa, args.kappa, seed=4242, trace=True)
-    same = (ta["overlap"] == tb["overlap"]) & (ta["selected_trial"] == tb["selected_trial"])
-    ok = same & (ta["overlap"] == 0)
-    rel = np.abs(tb["e_inter"][ok] - ta["e_inter"][ok]) / np.maximum(ta["e_inter_abs"][ok], 1.0)
-    accuracy = {"bound": "|E_mixed - E_fp64| / sum |pair energies| of the full-cutoff inter energy",
-                "same_trial_selection": float(same.mean()),
-                "e_inter_max_rel_err": float(rel.max()) if rel.size else None,
-                "e_inter_mean_rel_err": float(rel.mean()) if rel.size else None,
-                "insertions_compared": int(same.size)}
-    fctx.close()
+    # plain FP64 GPU path on the same workload, and the accuracy of the mixed
+    # path against it (per-insertion traces of a sub-batch)
+    fp64 = None
+    accuracy = None
+    if args.fp64_steps > 0:
+        fctx = cg.open_system(system, precision=abi.PREC_FP64, device=dev)
+        for b in boxes:
+            fctx.system_total_energy(b)
+        fms, fkms, _, _ = timed_steps(fctx, args.fp64_steps, 1, args.seed)
+        fp64_value = trials_step * len(fms) / (float(np.sum(fms)) / 1000.0)
+        fp64 = {"value": fp64_value, "unit": UNIT, "ms_per_step": float(np.mean(fms)),
+                "kernel_ms": float(np.mean(fkms)), "mixed_over_fp64": value / world / fp64_value}
+        sub = boxes[:8]
+        ra, ta = fctx.widom_insert(2, sub, 2000, args.kappa, args.kappa, seed=4242, trace=True)
+        rb, tb = gctx.widom_insert(2, sub, 2000, args.kappa, args.kappa, seed=4242, trace=True)
+        same = (ta["overlap"] == tb["overlap"]) & (ta["selected_trial"] == tb["selected_trial"])
+        ok = same & (ta["overlap"] == 0)
+        rel = np.abs(tb["e_inter"][ok] - ta["e_inter"][ok]) / np.maximum(ta["e_inter_abs"][ok], 1.0)
+        accuracy = {"bound": "|E_mixed - E_fp64| / sum |pair energies| of the full-cutoff inter energy",
+                    "same_trial_selection": float(same.mean()),
+                    "e_inter_max_rel_err": float(rel.max()) if rel.size else None,
+                    "e_inter_mean_rel_err": float(rel.mean()) if rel.size else None,
+                    "insertions_compared": int(same.size)}
+        fctx.close()
 
     # roofline of the Widom kernel
     from cassandra_gb300 import system as sysmod
@@ -295,11 +364,13 @@ def main():
     alg_bytes = n_per_box * len(boxes) * 33 + box_bytes
     achieved_gbs = alg_bytes / (kern_ms / 1000.0) / 1e9
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "k_widom_traffic.json")
+    prof = os.path.join(ROOT, "profiles", "k_widom_f32_butane_16boxes.md")
     if os.path.exists(prof):
+        import re
         with open(prof) as f:
-            pj = json.load(f)
-        traffic = pj.get("dram_bytes_per_insertion", 0.0) * n_per_box * len(boxes) or None
+            m = re.search(r"dram_bytes_per_insertion:\s*([0-9.eE+-]+)", f.read())
+        if m:
+            traffic = float(m.group(1)) * n_per_box * len(boxes)
     flops = st["widom_pairs_visited"] * 15 + st["widom_pairs_in_cutoff"] * 8
     sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
     fp32_peak = sm_count * 128 * 2 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
@@ -316,13 +387,13 @@ def main():
                       "parallelism": f"replicas x{world}"},
            "gpu_launches": int(launches),
            "wall_s": t_wall,
-           "fp64_gpu": {"value": fp64_value, "unit": UNIT, "ms_per_step": float(np.mean(fms)),
-                        "kernel_ms": float(np.mean(fkms)), "mixed_over_fp64": value / world / fp64_value},
+           "fp64_gpu": fp64,
            "accuracy_vs_fp64": accuracy,
            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                         "frac": achieved_gbs / hbm_peak, "traffic": traffic,
-                        "note": "k_widom; algorithmic bytes = 33 B record per insertion + box staged once per CTA "
-                                "(peak of measured)"},
+                        "note": "k_widom_f32; algorithmic bytes = 33 B record per insertion + box staged once per "
+                                "CTA; peak of measured; traffic scaled from the ncu capture of 16 boxes x 4000 "
+                                "insertions"},
            "compute_roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
                                 "frac": achieved_tf / fp32_peak, "pairs_visited": st["widom_pairs_visited"],
                                 "pairs_in_cutoff": st["widom_pairs_in_cutoff"],
@@ -353,6 +424,8 @@ def main():
                       "note": "per step: set_molecules of all boxes, system_total_energy of each box, widom_insert; "
                               "host wall clock"}
     gctx.close()
+    if not args.no_mc:
+        out["mc_sweeps"] = mc_leg(cg, abi, dev, rank == 0 and world == 1 and not args.no_cpu_baseline)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(system, args)
     if rank == 0:

@@ -81,11 +81,27 @@ class CassWidomTrace(C.Structure):
                 ("overlap", C.c_int32)]
 
 
+class CassMCParams(C.Structure):
+    _fields_ = [("nsweeps", C.c_int64), ("steps_per_sweep", C.c_int32), ("nupdate", C.c_int32),
+                ("prob_translate", C.c_double), ("target_accept", C.c_double)]
+
+
+class CassMCResult(C.Structure):
+    _fields_ = [("energy", CassEnergy), ("n_translate", C.c_int64), ("n_translate_accepted", C.c_int64),
+                ("n_rotate", C.c_int64), ("n_rotate_accepted", C.c_int64), ("n_overlap", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        d = {n: getattr(self, n) for n, _ in self._fields_ if n != "energy"}
+        d["energy"] = self.energy.as_dict()
+        return d
+
+
 class CassStats(C.Structure):
     _fields_ = [("widom_ms", C.c_double), ("widom_kernel_ms", C.c_double), ("kernel_launches", C.c_int64),
                 ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("widom_pairs_visited", C.c_int64),
                 ("widom_pairs_in_cutoff", C.c_int64), ("widom_grid_x", C.c_int32), ("widom_grid_y", C.c_int32),
-                ("widom_block", C.c_int32), ("widom_smem_bytes", C.c_int32)]
+                ("widom_block", C.c_int32), ("widom_smem_bytes", C.c_int32), ("mc_ms", C.c_double),
+                ("mc_moves", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -116,6 +132,8 @@ SIGNATURES = {
     "ewald_widom": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _f64p, _f64p]),
     "widom_insert": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _i32p, C.c_int64, C.c_int32, C.c_int32,
                                C.c_uint64, C.POINTER(CassWidomResult), C.c_void_p]),
+    "mc_sweeps": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.POINTER(CassMCParams), _f64p, _f64p, C.c_uint64,
+                            C.POINTER(CassMCResult)]),
     # allocation-free energy entry point and run-time extensions of the GPU
     # library (no counterpart in the reference)
     "mol_box_energy_noalloc": (C.c_int, [C.POINTER(CassBoxDesc), C.c_int32, _f64p, _f64p, C.c_void_p, C.c_void_p,
@@ -289,6 +307,21 @@ class Context:
 
     def set_stream(self, stream_ptr: int | None) -> None:
         self._check("set_stream", self._f["set_stream"](self._h, C.c_void_p(stream_ptr) if stream_ptr else None))
+
+    def mc_sweeps(self, boxes: Sequence[int], nsweeps: int, max_disp, max_rot, seed: int,
+                  prob_translate: float = 1.0, steps_per_sweep: int = 0, nupdate: int = 0,
+                  target_accept: float = 0.5):
+        """NVT translate/rotate sweeps, one chain per box.  max_disp / max_rot:
+        [nboxes][nspecies] arrays (adapted copies are returned)."""
+        b = _i32(boxes)
+        md = np.ascontiguousarray(np.array(max_disp, dtype=np.float64).reshape(len(b), -1))
+        mr = np.ascontiguousarray(np.array(max_rot, dtype=np.float64).reshape(len(b), -1))
+        prm = CassMCParams(nsweeps, steps_per_sweep, nupdate, prob_translate, target_accept)
+        res = (CassMCResult * len(b))()
+        self._check("mc_sweeps", self._f["mc_sweeps"](
+            self._h, len(b), _p(b), C.byref(prm), md.ctypes.data_as(_f64p), mr.ctypes.data_as(_f64p),
+            C.c_uint64(seed & (2**64 - 1)), res))
+        return [r.as_dict() for r in res], md, mr
 
     def widom_insert(self, is_: int, boxes: Sequence[int], n_insertions: int, kappa_ins: int,
                      kappa_dih: int, seed: int, trace: bool = False):

@@ -169,68 +169,94 @@ __global__ void __launch_bounds__(kBlock) k_mol_inter(BoxDev b, PairTable t, con
 }
 
 // ---------------------------------------------------------------------------
-// K6a: all inter-molecular pairs of a box (pairs (i,j), j > i, different molecules).
-constexpr int kTileJ = 2048;
+// K6a: all inter-molecular pairs of a box (pairs (i,j), j > i, different
+// molecules).  Block (x, y) takes atoms i of row block x against the j tile y,
+// staged in shared memory.  FAST (mixed precision, LJ cut / cut_tail with no
+// charges or Ewald): FP32 minimum image, r^2 and pair energies with
+// compensated FP32 sums; otherwise the FP64 pair functions.
+constexpr int kTileJ = 512;
 
-template <bool MIXED>
+template <bool FAST>
 __global__ void __launch_bounds__(kBlock) k_pair_total(BoxDev b, PairTable t, const double4_32a* __restrict__ p64,
                                                        const int4* __restrict__ meta, int n, double* partial,
                                                        unsigned* counter, double* out, int* ovflag) {
-  __shared__ double4_32a sj[kBlock];
-  __shared__ int4 sm[kBlock];
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double4_32a pi = i < n ? p64[i] : make_double4_32a(0, 0, 0, 0);
-  int4 mi = i < n ? meta[i] : make_int4(-1, -1, -1, -1);
+  __shared__ double4_32a sj[FAST ? 1 : kBlock];
+  __shared__ float4 sf[FAST ? kBlock : 1];
+  __shared__ int2 sm[kBlock];  // molecule slot, type
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const double4_32a pi = i < n ? p64[i] : make_double4_32a(0, 0, 0, 0);
+  const int4 mi = i < n ? meta[i] : make_int4(-1, -1, -1, -1);
+  const float4 pif = make_float4((float)pi.x, (float)pi.y, (float)pi.z, (float)pi.w);
   double ev = 0.0, eq = 0.0;
   KahanF fv, fq;
   bool ov = false;
-  int j0 = blockIdx.y * kTileJ;
-  int j1 = min(n, j0 + kTileJ);
-  int ilo = blockIdx.x * blockDim.x;
+  const int j0 = blockIdx.y * kTileJ;
+  const int j1 = min(n, j0 + kTileJ);
+  const int ilo = blockIdx.x * blockDim.x;
+  const float rv2f = (float)b.rcut_vdwsq, rq2f = (float)b.rcut_coulsq, low2f = (float)b.rcut_lowsq;
+  const float alphaf = (float)b.alpha;
+  const bool qq_on = b.charge_style == CASS_CHARGE_COUL;
+  float eps_row[kMaxTypes], sig_row[kMaxTypes];
+  if (FAST)
+#pragma unroll
+    for (int q = 0; q < kMaxTypes; ++q) {
+      const bool ok = mi.y >= 0 && q < t.ntypes;
+      eps_row[q] = ok ? t.epsf[pidx(mi.y, q, t.ntypes)] : 0.0f;
+      sig_row[q] = ok ? t.sig2f[pidx(mi.y, q, t.ntypes)] : 0.0f;
+    }
   if (j1 > ilo + 1) {
     for (int jt = max(j0, ilo); jt < j1; jt += kBlock) {
       __syncthreads();
-      int jj = jt + threadIdx.x;
+      const int jj = jt + threadIdx.x;
       if (jj < j1) {
-        sj[threadIdx.x] = p64[jj];
-        sm[threadIdx.x] = meta[jj];
+        const double4_32a pj = p64[jj];
+        const int4 mj = meta[jj];
+        if (FAST) sf[threadIdx.x] = make_float4((float)pj.x, (float)pj.y, (float)pj.z, (float)pj.w);
+        else sj[threadIdx.x] = pj;
+        sm[threadIdx.x] = make_int2(mj.x, mj.y);
       }
       __syncthreads();
-      int cnt = min(kBlock, j1 - jt);
-      if (i < n) {
-        for (int k = 0; k < cnt; ++k) {
-          int j = jt + k;
-          if (j <= i) continue;
-          int4 mj = sm[k];
-          if (mj.x == mi.x) continue;
-          double4_32a pj = sj[k];
-          double dx = fold(pi.x - pj.x, b.hL[0], b.L[0]);
-          double dy = fold(pi.y - pj.y, b.hL[1], b.L[1]);
-          double dz = fold(pi.z - pj.z, b.hL[2], b.L[2]);
-          double r2 = dx * dx + dy * dy + dz * dz;
+      const int cnt = min(kBlock, j1 - jt);
+      if (i >= n) continue;
+      for (int k = 0; k < cnt; ++k) {
+        const int j = jt + k;
+        if (j <= i) continue;
+        const int2 mj = sm[k];
+        if (mj.x == mi.x) continue;
+        if (FAST) {
+          const float4 pj = sf[k];
+          const float dx = fold(pif.x - pj.x, b.hLf[0], b.Lf[0]);
+          const float dy = fold(pif.y - pj.y, b.hLf[1], b.Lf[1]);
+          const float dz = fold(pif.z - pj.z, b.hLf[2], b.Lf[2]);
+          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+          if (r2 < low2f) {
+            ov = true;
+            continue;
+          }
+          if (r2 <= rv2f && mj.y >= 0) {
+            float e = 0.0f, s2 = 0.0f;
+#pragma unroll
+            for (int q = 0; q < kMaxTypes; ++q)
+              if (q == mj.y) {
+                e = eps_row[q];
+                s2 = sig_row[q];
+              }
+            fv.add(lj_pair_f(e, s2, r2));
+          }
+          if (qq_on && r2 <= rq2f) fq.add(qq_ewald_inter_f(alphaf, pif.w * pj.w, r2));
+        } else {
+          const double4_32a pj = sj[k];
+          const double dx = fold(pi.x - pj.x, b.hL[0], b.L[0]);
+          const double dy = fold(pi.y - pj.y, b.hL[1], b.L[1]);
+          const double dz = fold(pi.z - pj.z, b.hL[2], b.L[2]);
+          const double r2 = dx * dx + dy * dy + dz * dz;
           if (r2 < b.rcut_lowsq) {
             ov = true;
             continue;
           }
-          int m = cutoff_mask(b, r2, false);
-          if (m & 1) {
-            if (MIXED && b.vdw_style == CASS_VDW_LJ &&
-                (b.vdw_sum_style == CASS_VDW_SUM_CUT || b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL ||
-                 b.vdw_sum_style == CASS_VDW_SUM_MINIMUM)) {
-              if (mi.y >= 0 && mj.y >= 0) {
-                int kk = pidx(mi.y, mj.y, t.ntypes);
-                fv.add(lj_pair_f(t.epsf[kk], t.sig2f[kk], (float)r2));
-              }
-            } else {
-              ev += vdw_pair(t, b, mi.y, mj.y, r2, 1.0);
-            }
-          }
-          if (m & 2) {
-            if (MIXED && b.charge_sum_style == CASS_QQ_EWALD)
-              fq.add(qq_ewald_inter_f((float)b.alpha, (float)(pi.w * pj.w), (float)r2));
-            else
-              eq += qq_pair_inter(b, pi.w * pj.w, r2);
-          }
+          const int m = cutoff_mask(b, r2, false);
+          if (m & 1) ev += vdw_pair(t, b, mi.y, mj.y, r2, 1.0);
+          if (m & 2) eq += qq_pair_inter(b, pi.w * pj.w, r2);
         }
       }
     }
@@ -1165,7 +1191,10 @@ int cass_system_total_energy(cass_ctx* c, int32_t ibox1, int32_t intra_flag, Cas
   if (n > 1) {
     dim3 grid((n + kBlock - 1) / kBlock, (n + kTileJ - 1) / kTileJ);
     if ((rc = ensure_scratch(c, grid.x * grid.y, 2))) return rc;
-    if (c->precision == CASS_PREC_MIXED)
+    const bool fast = c->precision == CASS_PREC_MIXED && B.desc.vdw_style == CASS_VDW_LJ &&
+                      (B.desc.vdw_sum_style == CASS_VDW_SUM_CUT || B.desc.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) &&
+                      (B.desc.charge_style == CASS_CHARGE_NONE || B.desc.charge_sum_style == CASS_QQ_EWALD);
+    if (fast)
       k_pair_total<true><<<grid, kBlock, 0, c->stream>>>(B.dev, c->pt, B.d_p64.as<double4_32a>(), B.d_meta.as<int4>(), n,
                                                         c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
                                                         c->d_result.as<double>(), c->d_query.as<int>());

@@ -4,11 +4,11 @@
 // __device__ restatements of the per-pair arithmetic of Cassandra's
 // energy_routines.f90 in two precisions:
 //   FP64  : every operation in double, the reference arithmetic;
-//   mixed : FP32 minimum image, r^2, LJ/Mie and A&S erfc, with per-query
-//           compensated FP32 sums promoted to double.  Cutoff and overlap
-//           decisions whose FP32 r^2 lies within a narrow band of the
-//           threshold are re-evaluated in FP64, so both paths select the same
-//           pairs.
+//   mixed : FP32 minimum image, r^2, LJ and A&S erfc, with compensated FP32
+//           sums promoted to double.  Cutoff and overlap decisions are taken on
+//           the FP32 r^2, so a pair within about 1e-5 A^2 of a cutoff can fall
+//           on the other side than in FP64 (changing the energy by that pair's
+//           energy at the cutoff).
 #pragma once
 
 #include <cstdint>

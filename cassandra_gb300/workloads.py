@@ -169,3 +169,51 @@ def water_box(nmol: int, length: float, temperature: float = 298.0, rcut: float 
     bx = BoxSpec(length=(length,) * 3, rcut_vdw=rcut, rcut_coul=rcut, rcut_cbmc=min(6.5, rcut), rcut_low=0.85,
                  charge_style=abi.CHARGE_COUL, charge_sum_style=abi.QQ_EWALD, ewald_tol=tol, temperature=temperature)
     return System([sp], [bx], ms, ff, [nmol])
+
+
+def lj_nvt_system(nboxes: int = 1, n: int = 500, length: float = 35.0, sigma: float = 3.73, eps_K: float = 148.0,
+                  temperature: float = 150.0, rcut: float = 14.0, rcut_low: float = 1.0, seed: int = 2024) -> System:
+    """Single-site LJ fluid for NVT translation MC: n spheres per cubic box, uniform random
+    start with overlaps below 0.8 sigma rejected; boxes are independent replicas."""
+    rng = np.random.default_rng(seed)
+    sp = lj_sphere_species(eps_K, sigma)
+    ff = ForceField([sp])
+    boxes, ms = [], MoleculeSet()
+    loc = 1
+    for b in range(nboxes):
+        for p in lj_fluid_box(n, length, 0.8 * sigma, rng):
+            ms.add(loc, 1, b + 1, p[None, :])
+            loc += 1
+        boxes.append(BoxSpec(length=(length,) * 3, rcut_vdw=rcut, rcut_cbmc=min(6.5, rcut), rcut_low=rcut_low,
+                             temperature=temperature))
+    return System([sp], boxes, ms, ff, [loc - 1])
+
+
+def water_nvt_system(nboxes: int = 1, nmol: int = 256, length: float = 19.7, temperature: float = 298.0,
+                     rcut: float = 9.8, tol: float = 1e-5, seed: int = 11) -> System:
+    """Rigid 3-site water on a lattice with random orientations, LJ + Ewald; boxes are
+    independent replicas (each its own orientations)."""
+    rng = np.random.default_rng(seed)
+    sp = water_species()
+    ff = ForceField([sp])
+    n_side = int(math.ceil(nmol ** (1.0 / 3.0)))
+    a = length / n_side
+    base = sp.libraries[0][0]
+    com = (base * np.array([15.999, 1.008, 1.008])[:, None]).sum(0) / (15.999 + 2 * 1.008)
+    ms, boxes = MoleculeSet(), []
+    loc = 1
+    for b in range(nboxes):
+        k = 0
+        for ix in range(n_side):
+            for iy in range(n_side):
+                for iz in range(n_side):
+                    if k >= nmol:
+                        break
+                    c = (np.array([ix, iy, iz]) + 0.5) * a - 0.5 * length
+                    ms.add(loc, 1, b + 1, (base - com) @ random_rotation(rng).T + c)
+                    loc += 1
+                    k += 1
+        boxes.append(BoxSpec(length=(length,) * 3, rcut_vdw=rcut, rcut_coul=rcut, rcut_cbmc=min(6.5, rcut),
+                             rcut_low=0.85, charge_style=abi.CHARGE_COUL, charge_sum_style=abi.QQ_EWALD,
+                             ewald_tol=tol, temperature=temperature))
+    return System([sp], boxes, ms, ff, [loc - 1])

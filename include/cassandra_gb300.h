@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define CASS_ABI_VERSION 1
+#define CASS_ABI_VERSION 2
 
 /* status codes */
 #define CASS_OK 0
@@ -227,6 +227,40 @@ int cass_widom_insert(cass_ctx* ctx, int32_t is, int32_t nboxes, const int32_t* 
                       int64_t n_insertions, int32_t kappa_ins, int32_t kappa_dih,
                       uint64_t seed, CassWidomResult* out, CassWidomTrace* trace);
 
+/* ---- Monte Carlo sweeps ------------------------------------------------ */
+/* NVT Monte Carlo with translation (move_translate.f90:22-355) and rotation
+ * (move_rotate.f90:22-536) moves, the kind chosen as nvtmc_driver.f90:107-134
+ * does, one independent chain per listed box, all boxes in one launch.  Each
+ * move evaluates Compute_Molecule_Nonbond_Inter_Energy before and after the
+ * trial position, Update_System_Ewald_Reciprocal_Energy for charged species in
+ * Ewald boxes, and accept_or_reject (accept_or_reject.f90:22-65); the
+ * energy(ibox) bookkeeping and the structure factors stay FP64.  Box b draws
+ * its random numbers from the lfsr258 stream seeded by (seed, b, 0).  Requires
+ * a prior cass_system_total_energy of each listed box; afterwards the
+ * molecules, the structure factors and the energy of each box are those after
+ * its last move.  Replaces one translate/rotate host call sequence per move. */
+typedef struct CassMCParams {
+  int64_t nsweeps;
+  int32_t steps_per_sweep;  /* moves per sweep; 0 = the number of molecules in the box */
+  int32_t nupdate;          /* adapt the step sizes every nupdate trials of a move kind and
+                               species, as in equilibration runs; 0 = never */
+  double prob_translate;    /* cut_trans: a translation if rranf() <= prob_translate, else a rotation */
+  double target_accept;     /* translation acceptance the adaptation aims at (max_disp scaled by
+                               success_ratio / target_accept); 0.5 is the reference's rule */
+} CassMCParams;
+
+typedef struct CassMCResult {
+  CassEnergy energy;        /* energy(ibox) after the last move */
+  int64_t n_translate, n_translate_accepted;
+  int64_t n_rotate, n_rotate_accepted;
+  int64_t n_overlap;        /* trial positions rejected by the core-overlap test */
+} CassMCResult;
+
+/* max_disp, max_rot: [nboxes][nspecies] step sizes (A, rad) on input; the
+ * adapted sizes on output. */
+int cass_mc_sweeps(cass_ctx* ctx, int32_t nboxes, const int32_t* ibox, const CassMCParams* params,
+                   double* max_disp, double* max_rot, uint64_t seed, CassMCResult* out);
+
 /* ---- allocation-free energy entry point -------------------------------- */
 /* No counterpart in the reference.  For hosts that cannot call cudaMalloc in
  * their Monte Carlo move loop (device memory owned by another allocator, or an
@@ -262,6 +296,8 @@ typedef struct CassStats {
   int64_t widom_pairs_in_cutoff; /* of which inside a cutoff */
   int32_t widom_grid_x, widom_grid_y, widom_block;
   int32_t widom_smem_bytes;
+  double mc_ms;             /* the most recent cass_mc_sweeps: its kernel */
+  int64_t mc_moves;         /* moves it ran, all boxes */
 } CassStats;
 int cass_get_stats(cass_ctx* ctx, CassStats* out);
 /* count_pairs != 0 makes the Widom kernel count visited / in-cutoff pairs. */

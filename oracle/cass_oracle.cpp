@@ -1184,6 +1184,264 @@ void invalidate_box(orc_ctx* c, int ibox) {
   if (ibox >= 0 && ibox < c->nboxes) c->box[ibox].energy_valid = false;
 }
 
+// ---------------------------------------------------------------------------
+// NVT Monte Carlo moves (move_translate.f90, move_rotate.f90,
+// accept_or_reject.f90), one chain per box.
+
+// accept_or_reject (accept_or_reject.f90:22-65)
+bool accept_or_reject(double ln_pacc, Rng& rng) {
+  if (ln_pacc <= 0.0) return true;
+  if (ln_pacc < MAX_KBT) return rng.next() <= std::exp(-ln_pacc);
+  return false;
+}
+
+// species_list%linear (input_routines.f90:1955-1967): every angle fixed at 180 degrees
+bool species_linear(const Species& s) {
+  for (size_t k = 0; k < s.angle_kind.size(); ++k)
+    if (s.angle_kind[k] != CASS_BONDED_FIXED || s.angle_param[2 * k] != 180.0) return false;
+  return true;
+}
+
+// Update_System_Ewald_Reciprocal_Energy for a translated / rotated molecule
+// (energy_routines.f90:2384-2431); keeps the old sums for ewald_revert
+double ewald_move(const orc_ctx* c, Box& b, Mol& m) {
+  const size_t nv = b.hx.size();
+  b.cos_sum_old = b.cos_sum;
+  b.sin_sum_old = b.sin_sum;
+  if (m.cos_mol.size() != nv) {
+    m.cos_mol.assign(nv, 0.0);
+    m.sin_mol.assign(nv, 0.0);
+  }
+  m.cos_mol_old = m.cos_mol;
+  m.sin_mol_old = m.sin_mol;
+  std::vector<double> cn(nv), sn(nv);
+  mol_structure_factor(c, b, m.is, m.r.data(), cn.data(), sn.data());
+  double E = 0.0;
+  for (size_t i = 0; i < nv; ++i) {
+    b.cos_sum[i] = b.cos_sum[i] + (cn[i] - m.cos_mol[i]);
+    b.sin_sum[i] = b.sin_sum[i] + (sn[i] - m.sin_mol[i]);
+    E = E + b.Cn[i] * (b.cos_sum[i] * b.cos_sum[i] + b.sin_sum[i] * b.sin_sum[i]);
+    m.cos_mol[i] = cn[i];
+    m.sin_mol[i] = sn[i];
+  }
+  return E * CHARGE_FACTOR;
+}
+
+void ewald_revert(Box& b, Mol& m) {
+  b.cos_sum = b.cos_sum_old;
+  b.sin_sum = b.sin_sum_old;
+  m.cos_mol = m.cos_mol_old;
+  m.sin_mol = m.sin_mol_old;
+}
+
+struct McChain {
+  orc_ctx* c;
+  int ibox;
+  const CassMCParams* p;
+  double* max_disp;  // [nspecies] of this box
+  double* max_rot;
+  Rng rng;
+  CassEnergy E;
+  CassMCResult res{};
+  std::vector<int64_t> nt_disp, ns_disp, nt_rot, ns_rot;  // trials, successes since the last update
+  int err = CASS_OK;
+
+  int nmols(int is) const { return c->sp_off[ibox][is + 1] - c->sp_off[ibox][is]; }
+
+  // species choice of Translate / Rotate (move_translate.f90:150-170): only
+  // species with a nonzero step take part; -1 when none does
+  int pick_species(const double* step) {
+    int ntot = 0;
+    for (int is = 0; is < c->nspecies; ++is)
+      if (step[is] > 0.0) ntot += nmols(is);
+    if (ntot == 0) return -1;
+    double x = 0.0;
+    std::vector<double> xs(c->nspecies);
+    for (int is = 0; is < c->nspecies; ++is) {
+      xs[is] = (step[is] > 0.0 ? (double)nmols(is) / (double)ntot : 0.0) + (is > 0 ? x : 0.0);
+      x = xs[is];
+    }
+    const double u = rng.next();
+    int is = 0;
+    while (is < c->nspecies && !(u <= xs[is])) ++is;
+    if (is == c->nspecies)  // rounding left u above the last sum
+      for (is = c->nspecies - 1; is > 0 && !(step[is] > 0.0 && nmols(is) > 0); --is) {
+      }
+    return is;
+  }
+
+  Mol& pick_molecule(int is) {
+    const int im = std::min((int)(rng.next() * nmols(is)) + 1, nmols(is));  // rranf() may round to 1.0
+    return c->mol[c->members[ibox][c->sp_off[ibox][is] + im - 1]];
+  }
+
+  // the energy of m against the rest of the box; false sets err on an
+  // overlapping starting configuration (Clean_Abort in the reference)
+  bool old_energy(const Mol& m, int slot, double& ev, double& eq) {
+    if (mol_inter_energy(c, ibox, view_of(m), slot, false, ev, eq)) {
+      err = fail(CASS_ESTATE, "molecule energy too high before the move");
+      return false;
+    }
+    return true;
+  }
+
+  // energies after the trial position, the Ewald difference and the
+  // Metropolis test; reverts on rejection.  Returns acceptance.
+  bool finish_move(Mol& m, int slot, double ev_old, double eq_old, const std::vector<double>& r_old,
+                   const double* com_old) {
+    Box& b = c->box[ibox];
+    double ev, eq;
+    if (mol_inter_energy(c, ibox, view_of(m), slot, false, ev, eq)) {
+      m.r = r_old;
+      std::copy(com_old, com_old + 3, m.com);
+      ++res.n_overlap;
+      return false;
+    }
+    const bool ew = box_has_ewald(b) && c->sp[m.is].has_charge;
+    double dE = 0.0, E_recip = 0.0;
+    if (ew) {
+      E_recip = ewald_move(c, b, m);
+      dE = E_recip - E.reciprocal;
+    }
+    dE = dE + (ev - ev_old) + (eq - eq_old);
+    const bool acc = accept_or_reject(b.beta * dE, rng);
+    if (acc) {
+      E.total = E.total + dE;
+      E.inter = E.inter + dE;
+      E.inter_vdw = E.inter_vdw + ev - ev_old;
+      E.inter_q = E.inter_q + eq - eq_old;
+      if (ew) E.reciprocal = E_recip;
+    } else {
+      m.r = r_old;
+      std::copy(com_old, com_old + 3, m.com);
+      if (ew) ewald_revert(b, m);
+    }
+    return acc;
+  }
+
+  // Translate (move_translate.f90:22-355)
+  void translate() {
+    const int is = pick_species(max_disp);
+    if (is < 0) return;
+    Mol& m = pick_molecule(is);
+    const int slot = (int)(&m - c->mol.data());
+    ++res.n_translate;
+    ++nt_disp[is];
+    double ev_old, eq_old;
+    if (!old_energy(m, slot, ev_old, eq_old)) return;
+    const std::vector<double> r_old = m.r;
+    const double com_old[3] = {m.com[0], m.com[1], m.com[2]};
+    const Species& s = c->sp[is];
+    double d[3];
+    for (int k = 0; k < 3; ++k) d[k] = (2.0 * rng.next() - 1.0) * max_disp[is];
+    for (int a = 0; a < s.natoms; ++a)
+      for (int k = 0; k < 3; ++k) m.r[3 * a + k] = m.r[3 * a + k] + d[k];
+    for (int k = 0; k < 3; ++k) m.com[k] = m.com[k] + d[k];
+    // Fold_Molecule, orthorhombic branch (minimum_image_separation.f90:162-235)
+    const Box& b = c->box[ibox];
+    for (int k = 0; k < 3; ++k) {
+      double sh = 0.0;
+      if (m.com[k] > b.hL[k]) sh = -b.L[k];
+      else if (m.com[k] < -b.hL[k]) sh = b.L[k];
+      if (sh != 0.0) {
+        m.com[k] = m.com[k] + sh;
+        for (int a = 0; a < s.natoms; ++a) m.r[3 * a + k] = m.r[3 * a + k] + sh;
+      }
+    }
+    if (finish_move(m, slot, ev_old, eq_old, r_old, com_old)) {
+      ++res.n_translate_accepted;
+      ++ns_disp[is];
+    }
+    if (p->nupdate > 0 && nt_disp[is] % p->nupdate == 0) {  // :330-352, equilibration rule
+      const double ratio = (double)ns_disp[is] / (double)p->nupdate;
+      ns_disp[is] = 0;
+      if (ratio < 0.00005) {
+        max_disp[is] = 0.1 * max_disp[is];
+      } else {
+        double rsmall = b.rcut_vdw;
+        if (s.has_charge && b.charge_style != CASS_CHARGE_NONE) rsmall = std::min(b.rcut_vdw, b.rcut_coul);
+        max_disp[is] = std::min(rsmall, ratio / p->target_accept * max_disp[is]);
+      }
+    }
+  }
+
+  // Rotate (move_rotate.f90:22-536)
+  void rotate() {
+    const int is = pick_species(max_rot);
+    if (is < 0) return;
+    Mol& m = pick_molecule(is);
+    const int slot = (int)(&m - c->mol.data());
+    ++res.n_rotate;
+    ++nt_rot[is];
+    double ev_old, eq_old;
+    if (!old_energy(m, slot, ev_old, eq_old)) return;
+    const std::vector<double> r_old = m.r;
+    const double com_old[3] = {m.com[0], m.com[1], m.com[2]};
+    const Species& s = c->sp[is];
+    double R[9];
+    if (species_linear(s)) {  // Rotate_Molecule_Eulerian (:466-536)
+      const double theta = std::acos(1.0 - 2.0 * rng.next());
+      const double phi = (1.0 - 2.0 * rng.next()) * PI;
+      const double psi = (1.0 - 2.0 * rng.next()) * PI;
+      R[0] = std::cos(psi) * std::cos(phi) - std::cos(theta) * std::sin(phi) * std::sin(psi);
+      R[1] = std::cos(psi) * std::sin(phi) + std::cos(theta) * std::cos(phi) * std::sin(psi);
+      R[2] = std::sin(psi) * std::sin(theta);
+      R[3] = -std::sin(psi) * std::cos(phi) - std::cos(theta) * std::sin(phi) * std::cos(psi);
+      R[4] = -std::sin(psi) * std::sin(phi) + std::cos(theta) * std::cos(phi) * std::cos(psi);
+      R[5] = std::cos(psi) * std::sin(theta);
+      R[6] = std::sin(theta) * std::sin(phi);
+      R[7] = -std::sin(theta) * std::cos(phi);
+      R[8] = std::cos(theta);
+    } else {  // Rotate_Molecule_Axis (:362-463)
+      double psi1 = 0.0, psi2 = 0.0, psi3 = 0.0;
+      const int axis = (int)(3.0 * rng.next()) + 1;
+      const double ang = (2.0 * rng.next() - 1.0) * max_rot[is];
+      if (axis == 1) psi1 = ang;
+      else if (axis == 2) psi2 = ang;
+      else psi3 = ang;
+      const double c1 = std::cos(psi1), c2 = std::cos(psi2), c3 = std::cos(psi3);
+      const double s1 = std::sin(psi1), s2 = std::sin(psi2), s3 = std::sin(psi3);
+      R[0] = c1 * c3 - s1 * c2 * s3;
+      R[1] = s1 * c3 + c1 * c2 * s3;
+      R[2] = s2 * s3;
+      R[3] = -c1 * s3 - s1 * c2 * c3;
+      R[4] = -s1 * s3 + c1 * c2 * c3;
+      R[5] = s2 * c3;
+      R[6] = s1 * s2;
+      R[7] = -c1 * s2;
+      R[8] = c2;
+    }
+    for (int a = 0; a < s.natoms; ++a) {
+      const double x = m.r[3 * a] - m.com[0], y = m.r[3 * a + 1] - m.com[1], z = m.r[3 * a + 2] - m.com[2];
+      m.r[3 * a] = (R[0] * x + R[1] * y + R[2] * z) + m.com[0];
+      m.r[3 * a + 1] = (R[3] * x + R[4] * y + R[5] * z) + m.com[1];
+      m.r[3 * a + 2] = (R[6] * x + R[7] * y + R[8] * z) + m.com[2];
+    }
+    if (finish_move(m, slot, ev_old, eq_old, r_old, com_old)) {
+      get_com(c, is, m.r.data(), m.exist.data(), m.com);  // Get_COM on acceptance
+      ++res.n_rotate_accepted;
+      ++ns_rot[is];
+    }
+    if (p->nupdate > 0 && nt_rot[is] % p->nupdate == 0) {  // :307-326, equilibration rule
+      const double ratio = (double)ns_rot[is] / (double)p->nupdate;
+      ns_rot[is] = 0;
+      if (ratio < 0.5) max_rot[is] = std::max(0.01, 0.95 * max_rot[is]);
+      else max_rot[is] = std::min(PI, 1.05 * max_rot[is]);
+    }
+  }
+
+  void run() {
+    int nmol = 0;
+    for (int is = 0; is < c->nspecies; ++is) nmol += nmols(is);
+    const int64_t steps = p->nsweeps * (int64_t)(p->steps_per_sweep > 0 ? p->steps_per_sweep : nmol);
+    for (int64_t k = 0; k < steps && err == CASS_OK; ++k) {
+      if (rng.next() <= p->prob_translate) translate();  // nvtmc_driver.f90:107-134
+      else rotate();
+    }
+    res.energy = E;
+  }
+};
+
 }  // namespace
 
 extern "C" {
@@ -1687,6 +1945,48 @@ int orc_widom_insert(orc_ctx* c, int32_t is1, int32_t nboxes, const int32_t* ibo
     out[k].n_overlaps = nov;
     out[k].n_trials = n_ins * (int64_t)(kappa_ins + (s.nfrag - 1) * kappa_dih);
   }
+  return CASS_OK;
+}
+
+// NVT translate / rotate Monte Carlo, one chain per box (boxes in parallel)
+int orc_mc_sweeps(orc_ctx* c, int32_t nboxes, const int32_t* iboxes, const CassMCParams* p, double* max_disp,
+                  double* max_rot, uint64_t seed, CassMCResult* out) {
+  if (c) refresh_members(c);
+  if (check_ctx(c) || nboxes < 1 || !iboxes || !p || !max_disp || !max_rot || !out || p->nsweeps < 0 ||
+      p->steps_per_sweep < 0 || p->nupdate < 0 || !(p->target_accept > 0.0))
+    return fail(CASS_EINVAL, "bad mc arguments");
+  for (int k = 0; k < nboxes; ++k) {
+    const int ib = iboxes[k] - 1;
+    if (ib < 0 || ib >= c->nboxes) return fail(CASS_EINVAL, "box index");
+    for (int j = 0; j < k; ++j)
+      if (iboxes[j] == iboxes[k]) return fail(CASS_EINVAL, "box listed twice");
+    if (!c->box[ib].energy_valid) return fail(CASS_ESTATE, "system energy of box not computed");
+  }
+  std::vector<int> errs(nboxes, CASS_OK);
+  std::vector<std::string> msgs(nboxes);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int k = 0; k < nboxes; ++k) {
+    const int ib = iboxes[k] - 1;
+    McChain ch;
+    ch.c = c;
+    ch.ibox = ib;
+    ch.p = p;
+    ch.max_disp = max_disp + (size_t)k * c->nspecies;
+    ch.max_rot = max_rot + (size_t)k * c->nspecies;
+    ch.rng = seed_stream(seed, iboxes[k], 0);
+    ch.E = c->box[ib].energy;
+    ch.nt_disp.assign(c->nspecies, 0);
+    ch.ns_disp.assign(c->nspecies, 0);
+    ch.nt_rot.assign(c->nspecies, 0);
+    ch.ns_rot.assign(c->nspecies, 0);
+    ch.run();
+    c->box[ib].energy = ch.E;
+    out[k] = ch.res;
+    errs[k] = ch.err;
+    if (ch.err) msgs[k] = g_err;
+  }
+  for (int k = 0; k < nboxes; ++k)
+    if (errs[k]) return fail(errs[k], msgs[k]);
   return CASS_OK;
 }
 

@@ -13,7 +13,7 @@ def test_library_exports_header():
     assert len(names) >= 17
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
-    assert lib.cass_abi_version() == 1
+    assert lib.cass_abi_version() == 2
 
 
 def test_bindings_cover_header():
@@ -25,6 +25,9 @@ def test_struct_layouts():
     assert ctypes.sizeof(abi.CassEnergy) == 14 * 8
     assert ctypes.sizeof(abi.CassWidomResult) == 40
     assert ctypes.sizeof(abi.CassWidomTrace) == 48
+    assert ctypes.sizeof(abi.CassMCParams) == 8 + 2 * 4 + 2 * 8
+    assert ctypes.sizeof(abi.CassMCResult) == 14 * 8 + 5 * 8
+    assert ctypes.sizeof(abi.CassStats) == 2 * 8 + 5 * 8 + 4 * 4 + 8 + 8
     assert ctypes.sizeof(abi.CassBoxDesc) == 3 * 8 + 2 * 4 + 6 * 8 + 2 * 4 + 3 * 8
 
 
