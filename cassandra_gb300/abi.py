@@ -134,6 +134,7 @@ SIGNATURES = {
                                C.c_uint64, C.POINTER(CassWidomResult), C.c_void_p]),
     "mc_sweeps": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.POINTER(CassMCParams), _f64p, _f64p, C.c_uint64,
                             C.POINTER(CassMCResult)]),
+    "system_gradient": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(CassEnergy), _f64p, _f64p, _f64p, _f64p]),
     # allocation-free energy entry point and run-time extensions of the GPU
     # library (no counterpart in the reference)
     "mol_box_energy_noalloc": (C.c_int, [C.POINTER(CassBoxDesc), C.c_int32, _f64p, _f64p, C.c_void_p, C.c_void_p,
@@ -143,7 +144,7 @@ SIGNATURES = {
     "set_count_pairs": (C.c_int, [C.c_void_p, C.c_int32]),
     "set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
-OPTIONAL = {"get_stats", "set_count_pairs", "set_stream", "mol_box_energy_noalloc"}
+OPTIONAL = {"get_stats", "set_count_pairs", "set_stream", "mol_box_energy_noalloc", "system_gradient"}
 
 
 class CassError(RuntimeError):
@@ -322,6 +323,18 @@ class Context:
             self._h, len(b), _p(b), C.byref(prm), md.ctypes.data_as(_f64p), mr.ctypes.data_as(_f64p),
             C.c_uint64(seed & (2**64 - 1)), res))
         return [r.as_dict() for r in res], md, mr
+
+    def system_gradient(self, ibox: int, n_atoms_box: int):
+        """(energy dict, dU/dr [n_atoms_box, 3], dU/deps [nt, nt], dU/dsig [nt, nt], dU/dq [sum natoms])."""
+        e = CassEnergy()
+        g = np.zeros((n_atoms_box, 3))
+        de = np.zeros((self.ntypes, self.ntypes))
+        ds = np.zeros((self.ntypes, self.ntypes))
+        dq = np.zeros(int(sum(self.natoms[k] for k in sorted(self.natoms))))
+        self._check("system_gradient", self._f["system_gradient"](
+            self._h, ibox, C.byref(e), g.ctypes.data_as(_f64p), de.ctypes.data_as(_f64p), ds.ctypes.data_as(_f64p),
+            dq.ctypes.data_as(_f64p)))
+        return e.as_dict(), g, de, ds, dq
 
     def widom_insert(self, is_: int, boxes: Sequence[int], n_insertions: int, kappa_ins: int,
                      kappa_dih: int, seed: int, trace: bool = False):

@@ -1,0 +1,326 @@
+// k_grad.cu -- adjoint of the box energy: dU/dr, dU/d(eps, sigma), dU/dq.
+//
+// The energy differentiated is the one cass_system_total_energy returns for
+// LJ cut / cut_tail boxes with no charges or an Ewald sum (energy_routines.f90
+// :2648-2953): intramolecular nonbond pairs with their scale factors and no
+// periodic image (:980-1085), intermolecular LJ and real-space Ewald pairs
+// under the minimum image (:1589-1730, :1831-2053, :2088-2166), the long-range
+// correction (:2956-3023), the reciprocal sum (:4111-4231) and the self
+// energy (:2553-2601).  The real-space term is differentiated through the
+// Abramowitz-Stegun 7.1.26 erfc the energy uses, so the gradient is the exact
+// derivative of the computed energy (away from cutoff crossings, where the
+// truncated energy is discontinuous).  FP64 throughout.
+//
+//   k_grad_pairs  thread per atom i, all atoms j in shared-memory tiles:
+//                 the force on i, sum_j q_j dE/d(q_i q_j), and, for j > i, the
+//                 per-type-pair parameter derivatives (each pair counted once)
+//   k_grad_recip  thread per atom i, k-vectors in shared-memory tiles:
+//                 2 CF q_i sum_k Cn k (S_s cos - S_c sin) and
+//                 2 CF sum_k Cn (S_c cos + S_s sin)
+//   k_grad_types  fixed-order reduction of the per-atom parameter derivatives
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "cass_ctx.h"
+#include "cass_molecule.cuh"
+
+namespace cassgpu {
+
+constexpr int kGradBlock = 128;
+
+// A&S 7.1.26: erfc(x) = t P(t) exp(-x^2), t = 1/(1+px); returns erfc and its
+// derivative with respect to x
+__device__ __forceinline__ void erfc_as_d(double x, double& f, double& df) {
+  const double A1 = 0.254829592, A2 = -0.284496736, A3 = 1.421413741, A4 = -1.453152027, A5 = 1.061405429,
+               P = 0.3275911;
+  const double t = 1.0 / (1.0 + P * x);
+  const double poly = A1 + t * (A2 + t * (A3 + t * (A4 + t * A5)));
+  const double dpoly = A2 + t * (2.0 * A3 + t * (3.0 * A4 + t * 4.0 * A5));
+  const double e = exp(-x * x);
+  const double tp = t * poly;
+  f = tp * e;
+  // d(t poly)/dx = (poly + t dpoly) dt/dx, dt/dx = -P t^2
+  df = e * ((poly + t * dpoly) * (-P * t * t) - 2.0 * x * tp);
+}
+
+struct GradAtom {
+  double4_32a p;  // x, y, z, q
+  int mol, type, species, atom;
+};
+
+__global__ void __launch_bounds__(kGradBlock) k_grad_pairs(BoxDev b, PairTable T, SpeciesPools P,
+                                                           const double4_32a* __restrict__ p64,
+                                                           const int4* __restrict__ meta, int n, double* grad,
+                                                           double* dq, double* deps_atom, double* dsig_atom,
+                                                           int* ovflag) {
+  __shared__ double4_32a sp[kGradBlock];
+  __shared__ int4 sm[kGradBlock];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = i < n;
+  const double4_32a pi = live ? p64[i] : make_double4_32a(0, 0, 0, 0);
+  const int4 mi = live ? meta[i] : make_int4(-1, -1, -1, -1);
+  const bool lj = b.vdw_style == CASS_VDW_LJ;
+  const bool coul = b.charge_style == CASS_CHARGE_COUL;
+  double gx = 0, gy = 0, gz = 0, dqi = 0;
+  double de[kMaxTypes], ds[kMaxTypes];
+#pragma unroll
+  for (int t = 0; t < kMaxTypes; ++t) de[t] = ds[t] = 0.0;
+  bool ov = false;
+  const SpeciesDevHdr* hi = live ? &P.hdr[mi.z] : nullptr;
+  for (int j0 = 0; j0 < n; j0 += kGradBlock) {
+    __syncthreads();
+    if (j0 + threadIdx.x < n) {
+      sp[threadIdx.x] = p64[j0 + threadIdx.x];
+      sm[threadIdx.x] = meta[j0 + threadIdx.x];
+    }
+    __syncthreads();
+    if (!live) continue;
+    const int cnt = min(kGradBlock, n - j0);
+    for (int k = 0; k < cnt; ++k) {
+      const int j = j0 + k;
+      if (j == i) continue;
+      const double4_32a pj = sp[k];
+      const int4 mj = sm[k];
+      const bool intra = mj.x == mi.x;
+      double dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+      double vs = 1.0, qs = 1.0;
+      if (intra) {  // Compute_Molecule_Nonbond_Intra_Energy: no periodic image
+        const int na = hi->natoms;
+        vs = P.dp[hi->vs_off + mi.w * na + mj.w];
+        qs = P.dp[hi->qs_off + mi.w * na + mj.w];
+      } else {
+        dx = fold(dx, b.hL[0], b.L[0]);
+        dy = fold(dy, b.hL[1], b.L[1]);
+        dz = fold(dz, b.hL[2], b.L[2]);
+      }
+      const double r2 = dx * dx + dy * dy + dz * dz;
+      if (intra) {
+        if (r2 <= b.rcut_lowsq && !P.ip[hi->bonded_off + mi.w * hi->natoms + mj.w]) ov = true;
+      } else if (r2 < b.rcut_lowsq) {
+        ov = true;
+      }
+      double dEdr2 = 0.0;  // dE/d(r^2) of this pair
+      // LJ: E = 4 eps s (s12 - s6), s6 = (sigma^2/r^2)^3
+      if (lj && r2 <= b.rcut_vdwsq && mi.y >= 0 && mj.y >= 0) {
+        const int kk = pidx(mi.y, mj.y, T.ntypes);
+        const double eps = T.eps[kk], sig2 = T.sig2[kk];
+        if (eps != 0.0 && vs != 0.0) {
+          const double s2 = sig2 / r2, s6 = s2 * s2 * s2, s12 = s6 * s6;
+          dEdr2 += 4.0 * eps * vs * (-6.0 * s12 + 3.0 * s6) / r2;
+          if (j > i) {
+            de[mj.y] += 4.0 * vs * (s12 - s6);
+            ds[mj.y] += 4.0 * eps * vs * (12.0 * s12 - 6.0 * s6) / sqrt(sig2);
+          }
+        }
+      }
+      // Ewald real space: inter q q CF erfc(ar)/r; intra q q CF (qscale - erf(ar))/r
+      if (coul && r2 <= b.rcut_coulsq) {
+        const double r = sqrt(r2);
+        double f, df;
+        erfc_as_d(b.alpha * r, f, df);
+        const double g = intra ? (qs - (1.0 - f)) : f;  // erf = 1 - erfc
+        const double phi = kCHARGE_FACTOR * g / r;      // dE/d(q_i q_j)
+        const double dphi_dr = kCHARGE_FACTOR * (b.alpha * df / r - g / r2);
+        dqi += pj.w * phi;
+        dEdr2 += pi.w * pj.w * dphi_dr / (2.0 * r);
+      }
+      gx += 2.0 * dEdr2 * dx;
+      gy += 2.0 * dEdr2 * dy;
+      gz += 2.0 * dEdr2 * dz;
+    }
+  }
+  if (!live) return;
+  if (ov) atomicOr(ovflag, 1);
+  grad[3 * i] = gx;
+  grad[3 * i + 1] = gy;
+  grad[3 * i + 2] = gz;
+  dq[i] = dqi;
+  for (int t = 0; t < kMaxTypes; ++t) {
+    deps_atom[(size_t)i * kMaxTypes + t] = de[t];
+    dsig_atom[(size_t)i * kMaxTypes + t] = ds[t];
+  }
+}
+
+__global__ void __launch_bounds__(kGradBlock) k_grad_recip(const double4_32a* __restrict__ kvec,
+                                                           const double* __restrict__ cos_sum,
+                                                           const double* __restrict__ sin_sum, int nv,
+                                                           const double4_32a* __restrict__ p64, int n, double* grad,
+                                                           double* dq) {
+  __shared__ double4_32a sk[kGradBlock];
+  __shared__ double2 ss[kGradBlock];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = i < n;
+  const double4_32a pi = live ? p64[i] : make_double4_32a(0, 0, 0, 0);
+  double gx = 0, gy = 0, gz = 0, dqi = 0;
+  for (int k0 = 0; k0 < nv; k0 += kGradBlock) {
+    __syncthreads();
+    if (k0 + threadIdx.x < nv) {
+      sk[threadIdx.x] = kvec[k0 + threadIdx.x];
+      ss[threadIdx.x] = make_double2(cos_sum[k0 + threadIdx.x], sin_sum[k0 + threadIdx.x]);
+    }
+    __syncthreads();
+    if (!live) continue;
+    const int cnt = min(kGradBlock, nv - k0);
+    for (int k = 0; k < cnt; ++k) {
+      const double4_32a h = sk[k];
+      double s, c;
+      sincos(h.x * pi.x + h.y * pi.y + h.z * pi.z, &s, &c);
+      const double w = h.w * (ss[k].y * c - ss[k].x * s);
+      gx += w * h.x;
+      gy += w * h.y;
+      gz += w * h.z;
+      dqi += h.w * (ss[k].x * c + ss[k].y * s);
+    }
+  }
+  if (!live) return;
+  const double f = 2.0 * kCHARGE_FACTOR;
+  grad[3 * i] += f * pi.w * gx;
+  grad[3 * i + 1] += f * pi.w * gy;
+  grad[3 * i + 2] += f * pi.w * gz;
+  dq[i] += f * dqi;
+}
+
+// out[ti*kMaxTypes+tj] = sum over atoms of type ti of the per-atom values, in atom order
+__global__ void k_grad_types(const int4* __restrict__ meta, int n, const double* __restrict__ deps_atom,
+                             const double* __restrict__ dsig_atom, double* out_eps, double* out_sig) {
+  const int ti = blockIdx.x, tj = threadIdx.x;
+  if (tj >= kMaxTypes) return;
+  double e = 0.0, s = 0.0;
+  for (int i = 0; i < n; ++i) {
+    if (meta[i].y != ti) continue;
+    e += deps_atom[(size_t)i * kMaxTypes + tj];
+    s += dsig_atom[(size_t)i * kMaxTypes + tj];
+  }
+  out_eps[ti * kMaxTypes + tj] = e;
+  out_sig[ti * kMaxTypes + tj] = s;
+}
+
+int pack_box_ext(cass_ctx* c, int ibox);
+const std::vector<int>& members_ext(cass_ctx* c, int ibox);
+int ensure_pools(cass_ctx* c);
+
+}  // namespace cassgpu
+
+using namespace cassgpu;
+
+extern "C" int cass_system_total_energy(cass_ctx* c, int32_t ibox, int32_t intra_flag, CassEnergy* out,
+                                        int32_t* overlap);
+
+extern "C" int cass_system_gradient(cass_ctx* c, int32_t ibox1, CassEnergy* energy, double* dU_dr, double* dU_deps,
+                                    double* dU_dsig, double* dU_dq) {
+  if (!c || ibox1 < 1 || ibox1 > c->nboxes) return set_error(CASS_EINVAL, "bad arguments");
+  const int ib = ibox1 - 1;
+  BoxH& B = c->box[ib];
+  if (!B.defined) return set_error(CASS_ESTATE, "box not defined");
+  const CassBoxDesc& d = B.desc;
+  if (d.vdw_style != CASS_VDW_LJ && d.vdw_style != CASS_VDW_NONE)
+    return set_error(CASS_EUNSUPPORTED, "gradient: LJ or no vdW only");
+  if (d.vdw_style == CASS_VDW_LJ && d.vdw_sum_style != CASS_VDW_SUM_CUT && d.vdw_sum_style != CASS_VDW_SUM_CUT_TAIL)
+    return set_error(CASS_EUNSUPPORTED, "gradient: vdw sum style cut or cut_tail only");
+  if (d.charge_style == CASS_CHARGE_COUL && d.charge_sum_style != CASS_QQ_EWALD)
+    return set_error(CASS_EUNSUPPORTED, "gradient: charges need the Ewald sum");
+  for (int is = 0; is < c->nspecies; ++is) {
+    const SpeciesH& s = c->sp[is];
+    if (!s.defined) continue;
+    bool flexible = !s.dih_atoms.empty() || !s.imp_atoms.empty();
+    for (int k : s.bond_kind) flexible = flexible || k == CASS_BONDED_HARMONIC;
+    for (int k : s.angle_kind) flexible = flexible || k == CASS_BONDED_HARMONIC;
+    if (flexible) return set_error(CASS_EUNSUPPORTED, "gradient: species with harmonic or torsional terms");
+  }
+  // energy, packed atoms and structure factors of the current configuration
+  CassEnergy E;
+  int32_t ov = 0;
+  int rc = cass_system_total_energy(c, ibox1, 1, &E, &ov);
+  if (rc) return rc;
+  if (ov) return set_error(CASS_ESTATE, "gradient: the configuration has a core overlap");
+  if (energy) *energy = E;
+  const int n = B.npacked;
+  const int nt = c->ntypes;
+  const size_t bytes = (size_t)n * (3 + 1 + 2 * kMaxTypes) * sizeof(double) + 2 * kMaxTypes * kMaxTypes * sizeof(double) + 64;
+  if ((rc = c->d_grad.reserve(bytes))) return rc;
+  double* d_g = c->d_grad.as<double>();
+  double* d_dq = d_g + 3 * (size_t)n;
+  double* d_de = d_dq + n;
+  double* d_ds = d_de + (size_t)n * kMaxTypes;
+  double* d_te = d_ds + (size_t)n * kMaxTypes;
+  double* d_ts = d_te + kMaxTypes * kMaxTypes;
+  if ((rc = c->d_query.reserve(16))) return rc;
+  CASS_CUDA(cudaMemsetAsync(c->d_query.p, 0, sizeof(int), c->stream));
+  if (n > 0) {
+    const int nb = (n + kGradBlock - 1) / kGradBlock;
+    k_grad_pairs<<<nb, kGradBlock, 0, c->stream>>>(B.dev, c->pt, c->pools, B.d_p64.as<double4_32a>(),
+                                                   B.d_meta.as<int4>(), n, d_g, d_dq, d_de, d_ds,
+                                                   c->d_query.as<int>());
+    CASS_CUDA(cudaGetLastError());
+    count_launch(c);
+    if (d.charge_style == CASS_CHARGE_COUL && B.nvecs > 0) {
+      k_grad_recip<<<nb, kGradBlock, 0, c->stream>>>(B.d_kvec.as<double4_32a>(), B.d_cos_sum.as<double>(),
+                                                     B.d_sin_sum.as<double>(), B.nvecs, B.d_p64.as<double4_32a>(), n,
+                                                     d_g, d_dq);
+      CASS_CUDA(cudaGetLastError());
+      count_launch(c);
+    }
+    k_grad_types<<<kMaxTypes, 32, 0, c->stream>>>(B.d_meta.as<int4>(), n, d_de, d_ds, d_te, d_ts);
+    CASS_CUDA(cudaGetLastError());
+    count_launch(c);
+  }
+  std::vector<double> g(3 * (size_t)n), q(n), te(kMaxTypes * kMaxTypes, 0.0), ts(kMaxTypes * kMaxTypes, 0.0);
+  int hov = 0;
+  if (n > 0) {
+    CASS_CUDA(d2h(c, g.data(), d_g, g.size() * sizeof(double)));
+    CASS_CUDA(d2h(c, q.data(), d_dq, q.size() * sizeof(double)));
+    CASS_CUDA(d2h(c, te.data(), d_te, te.size() * sizeof(double)));
+    CASS_CUDA(d2h(c, ts.data(), d_ts, ts.size() * sizeof(double)));
+  }
+  CASS_CUDA(d2h(c, &hov, c->d_query.p, sizeof(int)));
+  CASS_CUDA(cudaStreamSynchronize(c->stream));
+  if (hov) return set_error(CASS_ESTATE, "gradient: the configuration has a core overlap");
+  // the packed order is species-major, locate order: the order of dU_dr
+  if (dU_dr) memcpy(dU_dr, g.data(), g.size() * sizeof(double));
+  if (dU_dq) {
+    std::vector<int> off(c->nspecies + 1, 0);
+    for (int is = 0; is < c->nspecies; ++is) off[is + 1] = off[is] + (c->sp[is].defined ? c->sp[is].natoms : 0);
+    for (int k = 0; k < off[c->nspecies]; ++k) dU_dq[k] = 0.0;
+    // d/dq_i of the self energy -CF alpha/sqrt(pi) sum q^2 (energy_routines.f90:2594)
+    const bool ew = d.charge_style == CASS_CHARGE_COUL;
+    for (size_t m = 0; m < B.pk_mol.size(); ++m) {
+      const int slot = B.pk_mol[m], is = c->slot_sp[slot];
+      const SpeciesH& s = c->sp[is];
+      for (int a = 0; a < s.natoms; ++a) {
+        double v = q[B.pk_mol_off[m] + a];
+        if (ew) v += -2.0 * kCHARGE_FACTOR * B.dev.alpha / kROOTPI * s.q[a];
+        dU_dq[off[is] + a] += v;
+      }
+    }
+  }
+  // the symmetric pair parameters: a pair of types (t, u) enters once per pair
+  // of atoms; the long-range correction adds
+  // 2 pi / V sum_t sum_u N_t N_u 4 eps_tu (sigma^12/(9 rc^9) - sigma^6/(3 rc^3))
+  if (dU_deps || dU_dsig) {
+    std::vector<double> nb(nt, 0.0);
+    for (int slot : members_ext(c, ib)) {
+      const SpeciesH& s = c->sp[c->slot_sp[slot]];
+      for (int a = 0; a < s.natoms; ++a)
+        if (s.type[a] >= 0) nb[s.type[a]] += 1.0;
+    }
+    const bool tail = d.vdw_style == CASS_VDW_LJ && d.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL;
+    for (int t = 0; t < nt; ++t)
+      for (int u = 0; u < nt; ++u) {
+        double e = te[t * kMaxTypes + u] + (t != u ? te[u * kMaxTypes + t] : 0.0);
+        double s = ts[t * kMaxTypes + u] + (t != u ? ts[u * kMaxTypes + t] : 0.0);
+        if (tail) {
+          const double sig = std::sqrt(c->pt.sig2[pidx(t, u, nt)]), eps = c->pt.eps[pidx(t, u, nt)];
+          const double mult = (t != u ? 2.0 : 1.0) * 2.0 * kPI / B.dev.volume * nb[t] * nb[u];
+          const double s3 = sig * sig * sig, s6 = s3 * s3;
+          e += mult * 4.0 * (s6 * s6 / (9.0 * B.rcut9) - s6 / (3.0 * B.rcut3));
+          s += mult * 4.0 * eps * (12.0 * s6 * s6 / sig / (9.0 * B.rcut9) - 6.0 * s6 / sig / (3.0 * B.rcut3));
+        }
+        if (dU_deps) dU_deps[t * nt + u] = e;
+        if (dU_dsig) dU_dsig[t * nt + u] = s;
+      }
+  }
+  return CASS_OK;
+}

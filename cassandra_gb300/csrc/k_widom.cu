@@ -1372,8 +1372,10 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
   return out;
 }
 
+constexpr int kF32Threads = 256;  // two CTAs per SM share nothing but each stages its box once for 8 warps
+
 template <bool SMEM>
-__global__ void __launch_bounds__(128) k_widom_f32(WidomSpecies S, SpeciesF SF, PairTable T, const BoxDev* boxes,
+__global__ void __launch_bounds__(kF32Threads) k_widom_f32(WidomSpecies S, SpeciesF SF, PairTable T, const BoxDev* boxes,
                                                    const int* box_ids, const float4* c32, const float* cq32,
                                                    const int* cstart, const float* __restrict__ libf, long long n_ins,
                                                    uint64_t seed, WRec* rec, signed char* status, double* xyz,
@@ -1931,18 +1933,18 @@ extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const
   auto launch_f32 = [&](auto kern, const SpeciesF& SF) -> int {
     if (use_smem) CASS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem));
     int per_sm = 1;
-    CASS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, use_smem ? max_smem : 0));
+    CASS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kF32Threads, use_smem ? max_smem : 0));
     per_sm = std::max(per_sm, 1);
     long long want = ((long long)dev_sms * per_sm * 2 + nboxes - 1) / nboxes;
-    long long need = (n_ins + threads - 1) / threads;
+    long long need = (n_ins + kF32Threads - 1) / kF32Threads;
     int chunks = (int)std::max<long long>(1, std::min(want, need));
     dim3 g(chunks, nboxes);
     c->stats.widom_grid_x = chunks;
     c->stats.widom_grid_y = nboxes;
-    c->stats.widom_block = threads;
+    c->stats.widom_block = kF32Threads;
     c->stats.widom_smem_bytes = use_smem ? (int)max_smem : 0;
     CASS_CUDA(cudaEventRecord(c->ev[1], c->stream));
-    kern<<<g, threads, use_smem ? max_smem : 0, c->stream>>>(
+    kern<<<g, kF32Threads, use_smem ? max_smem : 0, c->stream>>>(
         S, SF, c->pt, d_bd, d_ids, d_c32, c->d_cq32.as<float>(), c->d_cell_start.as<int>(), s.d_library_f.as<float>(),
         (long long)n_ins, seed, d_rec, d_status, d_xyz, any_recip ? 1 : 0, d_trace, d_pairs);
     CASS_CUDA(cudaGetLastError());

@@ -217,3 +217,43 @@ def water_nvt_system(nboxes: int = 1, nmol: int = 256, length: float = 19.7, tem
                              rcut_low=0.85, charge_style=abi.CHARGE_COUL, charge_sum_style=abi.QQ_EWALD,
                              ewald_tol=tol, temperature=temperature))
     return System([sp], boxes, ms, ff, [loc - 1])
+
+
+def water_gradient_system(nmol: int = 4096, length: float = 49.7, temperature: float = 298.0, rcut: float = 12.0,
+                          tol: float = 1e-6, min_inter: float = 1.5, seed: int = 13) -> System:
+    """Rigid 3-site waters on a cubic lattice with random orientations, each
+    orientation redrawn until its atoms are at least min_inter from every atom
+    of the molecules already placed; one Ewald box (the gradient workload)."""
+    rng = np.random.default_rng(seed)
+    sp = water_species()
+    ff = ForceField([sp])
+    n_side = int(math.ceil(nmol ** (1.0 / 3.0)))
+    a = length / n_side
+    base = sp.libraries[0][0]
+    com = (base * np.array([15.999, 1.008, 1.008])[:, None]).sum(0) / (15.999 + 2 * 1.008)
+    ms = MoleculeSet()
+    placed = {}  # lattice site -> atoms
+    md2 = min_inter * min_inter
+    k = 0
+    for ix in range(n_side):
+        for iy in range(n_side):
+            for iz in range(n_side):
+                if k >= nmol:
+                    break
+                c = (np.array([ix, iy, iz]) + 0.5) * a - 0.5 * length
+                near = [placed[(ix + dx) % n_side, (iy + dy) % n_side, (iz + dz) % n_side]
+                        for dx in (-1, 0, 1) for dy in (-1, 0, 1) for dz in (-1, 0, 1)
+                        if ((ix + dx) % n_side, (iy + dy) % n_side, (iz + dz) % n_side) in placed]
+                others = np.concatenate(near) if near else np.zeros((0, 3))
+                for _ in range(1000):
+                    xyz = (base - com) @ random_rotation(rng).T + c
+                    d = xyz[:, None, :] - others[None, :, :]
+                    d -= length * np.round(d / length)
+                    if not others.size or (d ** 2).sum(-1).min() >= md2:
+                        break
+                placed[(ix, iy, iz)] = xyz
+                ms.add(k + 1, 1, 1, xyz)
+                k += 1
+    bx = BoxSpec(length=(length,) * 3, rcut_vdw=rcut, rcut_coul=rcut, rcut_cbmc=min(6.5, rcut), rcut_low=0.85,
+                 charge_style=abi.CHARGE_COUL, charge_sum_style=abi.QQ_EWALD, ewald_tol=tol, temperature=temperature)
+    return System([sp], [bx], ms, ff, [nmol])

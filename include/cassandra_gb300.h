@@ -261,6 +261,27 @@ typedef struct CassMCResult {
 int cass_mc_sweeps(cass_ctx* ctx, int32_t nboxes, const int32_t* ibox, const CassMCParams* params,
                    double* max_disp, double* max_rot, uint64_t seed, CassMCResult* out);
 
+/* ---- configuration gradient (adjoint) ---------------------------------- */
+/* The derivatives of the total energy of box ibox, as cass_system_total_energy
+ * computes it (and returns it in *energy), for LJ cut / cut_tail boxes with no
+ * charges or an Ewald sum and rigid species (fixed bonds and angles, no
+ * dihedrals or impropers): intramolecular nonbond pairs with their scale
+ * factors, intermolecular LJ and real-space Ewald pairs, the long-range
+ * correction, the reciprocal sum and the self energy.  The real-space term is
+ * differentiated through the same A&S erfc.  No counterpart in the reference,
+ * which has no derivatives; computed in FP64.
+ *   dU_dr    [n][natoms(is)][3]: the live molecules of the box in species-major,
+ *            locate order;
+ *   dU_deps, dU_dsig [ntypes*ntypes]: derivatives with respect to the symmetric
+ *            mixed pair parameters eps_tu = eps_ut and sigma_tu = sigma_ut
+ *            (both entries hold the same value);
+ *   dU_dq    [sum over species of natoms]: derivative with respect to the charge
+ *            of each species atom, shared by all molecules of the species.
+ * Any output may be NULL.  A configuration with a core overlap returns
+ * CASS_ESTATE; other styles return CASS_EUNSUPPORTED. */
+int cass_system_gradient(cass_ctx* ctx, int32_t ibox, CassEnergy* energy, double* dU_dr, double* dU_deps,
+                         double* dU_dsig, double* dU_dq);
+
 /* ---- allocation-free energy entry point -------------------------------- */
 /* No counterpart in the reference.  For hosts that cannot call cudaMalloc in
  * their Monte Carlo move loop (device memory owned by another allocator, or an
