@@ -939,9 +939,42 @@ struct QueryAcc {
   unsigned long long visited = 0, in_cut = 0;
 };
 
+// r^2 to a stored atom, through the row's image shift (folded in full dimensions)
+__device__ __forceinline__ float pair_r2(const BoxF& f, const bool (&full)[3], bool fold_any, float qx, float qy,
+                                         float qz, const float4& a) {
+  float dx = qx - a.x, dy = qy - a.y, dz = qz - a.z;
+  if (fold_any) {
+    if (full[0]) dx = fold(dx, f.hL[0], f.L[0]);
+    if (full[1]) dy = fold(dy, f.hL[1], f.L[1]);
+    if (full[2]) dz = fold(dz, f.hL[2], f.L[2]);
+  }
+  return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+
+// LJ and real-space Ewald energy of one pair inside the selection radius
+template <bool COUNT>
+__device__ __forceinline__ void pair_energy(const BoxViewF& V, QueryAcc& A, const float4& a, int j, float r2,
+                                            const float2* lrow, bool vdw_on, bool qq_on, float rv2, float rq2,
+                                            float qa) {
+  if (COUNT) ++A.in_cut;
+  const int tj = __float_as_int(a.w);
+  if (vdw_on && tj >= 0 && r2 <= rv2) {
+    const float2 es = lrow[tj];
+    const float ev = lj_pair_f(es.x, es.y, r2);
+    A.e.add(ev);
+    A.eabs += fabsf(ev);
+  }
+  if (qq_on && r2 <= rq2) {
+    const float eq = qq_ewald_inter_f(V.f->alpha, qa * V.q32[j], r2);
+    A.e.add(eq);
+    A.eabs += fabsf(eq);
+  }
+}
+
 // FP32 energy of one test atom at p against the box atoms within the cutoff,
 // added to A.  Returns true on core overlap (r^2 < rcut_low^2), as
 // Compute_MoleculePair_Energy (energy_routines.f90:1676-1679) does.
+template <bool COUNT>
 __device__ bool query_f(const BoxViewF& V, QueryAcc& A, float px, float py, float pz, int ta, float qa, bool cbmc,
                         bool want_qq) {
   const BoxF& f = *V.f;
@@ -981,31 +1014,22 @@ __device__ bool query_f(const BoxViewF& V, QueryAcc& A, float px, float py, floa
         const int run = min(hi[0] - cx, nc0 - 1 - wx) + 1;
         const float qx = px + (float)((wx - cx) / nc0) * f.L[0];
         const int j0 = V.cstart[row + wx], j1 = V.cstart[row + wx + run];
-        A.visited += (unsigned long long)(j1 - j0);
-        for (int j = j0; j < j1; ++j) {
-          const float4 a = V.p32[j];
-          float dx = qx - a.x, dy = qy - a.y, dz = qz - a.z;
-          if (fold_any) {
-            if (full[0]) dx = fold(dx, f.hL[0], f.L[0]);
-            if (full[1]) dy = fold(dy, f.hL[1], f.L[1]);
-            if (full[2]) dz = fold(dz, f.hL[2], f.L[2]);
-          }
-          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          if (r2 < low2) return true;
-          if (r2 > rsel2) continue;
-          ++A.in_cut;
-          const int tj = __float_as_int(a.w);
-          if (vdw_on && tj >= 0 && r2 <= rv2) {
-            const float2 es = lrow[tj];
-            const float ev = lj_pair_f(es.x, es.y, r2);
-            A.e.add(ev);
-            A.eabs += fabsf(ev);
-          }
-          if (qq_on && r2 <= rq2) {
-            const float eq = qq_ewald_inter_f(f.alpha, qa * V.q32[j], r2);
-            A.e.add(eq);
-            A.eabs += fabsf(eq);
-          }
+        if (COUNT) A.visited += (unsigned long long)(j1 - j0);
+        // two candidates per iteration: independent distance chains
+        int j = j0;
+        for (; j + 1 < j1; j += 2) {
+          const float4 a0 = V.p32[j], a1 = V.p32[j + 1];
+          const float r20 = pair_r2(f, full, fold_any, qx, qy, qz, a0);
+          const float r21 = pair_r2(f, full, fold_any, qx, qy, qz, a1);
+          if (fminf(r20, r21) < low2) return true;
+          if (r20 <= rsel2) pair_energy<COUNT>(V, A, a0, j, r20, lrow, vdw_on, qq_on, rv2, rq2, qa);
+          if (r21 <= rsel2) pair_energy<COUNT>(V, A, a1, j + 1, r21, lrow, vdw_on, qq_on, rv2, rq2, qa);
+        }
+        if (j < j1) {
+          const float4 a0 = V.p32[j];
+          const float r20 = pair_r2(f, full, fold_any, qx, qy, qz, a0);
+          if (r20 < low2) return true;
+          if (r20 <= rsel2) pair_energy<COUNT>(V, A, a0, j, r20, lrow, vdw_on, qq_on, rv2, rq2, qa);
         }
         cx += run;
       }
@@ -1043,12 +1067,13 @@ struct RecF {
 };
 
 // Energy of atoms `ids` against the box: sum into e, true on overlap
+template <bool COUNT>
 __device__ __forceinline__ bool query_atoms_f(const BoxViewF& V, QueryAcc& A, const SpeciesF& S, const float* r,
                                               const int* ids, int n, float sx, float sy, float sz, bool cbmc,
                                               bool want_qq) {
   for (int i = 0; i < n; ++i) {
     const int a = ids[i];
-    if (query_f(V, A, r[3 * a] + sx, r[3 * a + 1] + sy, r[3 * a + 2] + sz, S.type[a], S.q[a], cbmc, want_qq))
+    if (query_f<COUNT>(V, A, r[3 * a] + sx, r[3 * a + 1] + sy, r[3 * a + 2] + sz, S.type[a], S.q[a], cbmc, want_qq))
       return true;
   }
   return false;
@@ -1057,6 +1082,7 @@ __device__ __forceinline__ bool query_atoms_f(const BoxViewF& V, QueryAcc& A, co
 // One Widom insertion: Widom_Insert (widom_insert.f90:250-447) with the CBMC
 // growth of Build_Molecule (fragment_growth.f90:120-900) and
 // Fragment_Placement (:1449-2132), in FP32
+template <bool COUNT>
 __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const BoxViewF& V,
                                 const float* __restrict__ lib, Lfsr rng, double* xyz_out, QueryAcc& cnt) {
   const BoxF& f = *V.f;
@@ -1157,7 +1183,7 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
     const float ay = (0.5f - draw_f(rng)) * f.L[1];
     const float az = (0.5f - draw_f(rng)) * f.L[2];
     QueryAcc A;
-    bool ov = query_atoms_f(V, A, SF, r, fa_ids, nfa, ax, ay, az, true, cbmc_qq);
+    bool ov = query_atoms_f<COUNT>(V, A, SF, r, fa_ids, nfa, ax, ay, az, true, cbmc_qq);
     cnt.visited += A.visited;
     cnt.in_cut += A.in_cut;
     const float e = A.e.s + A.e.c;
@@ -1299,7 +1325,7 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
           continue;
         }
         QueryAcc A;
-        ov = query_atoms_f(V, A, SF, r, newids, nnew, 0.0f, 0.0f, 0.0f, true, cbmc_qq);
+        ov = query_atoms_f<COUNT>(V, A, SF, r, newids, nnew, 0.0f, 0.0f, 0.0f, true, cbmc_qq);
         cnt.visited += A.visited;
         cnt.in_cut += A.in_cut;
         exist = combined;
@@ -1350,7 +1376,7 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
   QueryAcc A;
   bool ov = false;
   for (int a = 0; a < n && !ov; ++a)
-    ov = query_f(V, A, r[3 * a], r[3 * a + 1], r[3 * a + 2], SF.type[a], SF.q[a], false, true);
+    ov = query_f<COUNT>(V, A, r[3 * a], r[3 * a + 1], r[3 * a + 2], SF.type[a], SF.q[a], false, true);
   cnt.visited += A.visited;
   cnt.in_cut += A.in_cut;
   if (ov) {
@@ -1372,10 +1398,14 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
   return out;
 }
 
-constexpr int kF32Threads = 256;  // two CTAs per SM share nothing but each stages its box once for 8 warps
+// 16 warps per staged box and two CTAs per SM (64 registers): the kernel is
+// latency-bound, and warps per scheduler matter more than the few spills
+constexpr int kF32Threads = 512;
+constexpr int kF32MinBlocks = 2;
+constexpr int kF32Waves = 2;  // CTAs per resident slot: a second wave evens out uneven boxes
 
-template <bool SMEM>
-__global__ void __launch_bounds__(kF32Threads) k_widom_f32(WidomSpecies S, SpeciesF SF, PairTable T, const BoxDev* boxes,
+template <bool SMEM, bool COUNT>
+__global__ void __launch_bounds__(kF32Threads, kF32MinBlocks) k_widom_f32(WidomSpecies S, SpeciesF SF, PairTable T, const BoxDev* boxes,
                                                    const int* box_ids, const float4* c32, const float* cq32,
                                                    const int* cstart, const float* __restrict__ libf, long long n_ins,
                                                    uint64_t seed, WRec* rec, signed char* status, double* xyz,
@@ -1439,7 +1469,7 @@ __global__ void __launch_bounds__(kF32Threads) k_widom_f32(WidomSpecies S, Speci
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n_ins; i += stride) {
     const size_t g = (size_t)k * n_ins + i;
     const Lfsr rng = seed_stream(seed, box_ids[k], i);
-    const RecF o = run_insertion_f(S, SF, V, libf, rng, want_xyz ? xyz + g * 3 * S.natoms : nullptr, cnt);
+    const RecF o = run_insertion_f<COUNT>(S, SF, V, libf, rng, want_xyz ? xyz + g * 3 * S.natoms : nullptr, cnt);
     const double e_int = (double)o.e_inter;
     rec[g] = make_double4_32a((double)o.dE_intra, e_int + s_ec, (double)o.dE_frag, (double)o.ln_pbias);
     status[g] = (signed char)o.status;
@@ -1935,7 +1965,7 @@ extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const
     int per_sm = 1;
     CASS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kF32Threads, use_smem ? max_smem : 0));
     per_sm = std::max(per_sm, 1);
-    long long want = ((long long)dev_sms * per_sm * 2 + nboxes - 1) / nboxes;
+    long long want = ((long long)dev_sms * per_sm * kF32Waves + nboxes - 1) / nboxes;
     long long need = (n_ins + kF32Threads - 1) / kF32Threads;
     int chunks = (int)std::max<long long>(1, std::min(want, need));
     dim3 g(chunks, nboxes);
@@ -1953,7 +1983,8 @@ extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const
     return CASS_OK;
   };
   if (n_ins > 0) {
-    if (f32) rc = use_smem ? launch_f32(k_widom_f32<true>, SF) : launch_f32(k_widom_f32<false>, SF);
+    if (f32 && d_pairs) rc = use_smem ? launch_f32(k_widom_f32<true, true>, SF) : launch_f32(k_widom_f32<false, true>, SF);
+    else if (f32) rc = use_smem ? launch_f32(k_widom_f32<true, false>, SF) : launch_f32(k_widom_f32<false, false>, SF);
     else rc = use_smem ? launch(k_widom<true>) : launch(k_widom<false>);
     if (rc) return rc;
     if (any_recip) {
