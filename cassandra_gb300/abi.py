@@ -135,6 +135,8 @@ SIGNATURES = {
     "mc_sweeps": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.POINTER(CassMCParams), _f64p, _f64p, C.c_uint64,
                             C.POINTER(CassMCResult)]),
     "system_gradient": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(CassEnergy), _f64p, _f64p, _f64p, _f64p]),
+    "cbmc_trial_energies": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _i32p, C.c_int32,
+                                      _f64p, C.c_int32, _f64p, _i32p]),
     # allocation-free energy entry point and run-time extensions of the GPU
     # library (no counterpart in the reference)
     "mol_box_energy_noalloc": (C.c_int, [C.POINTER(CassBoxDesc), C.c_int32, _f64p, _f64p, C.c_void_p, C.c_void_p,
@@ -323,6 +325,17 @@ class Context:
             self._h, len(b), _p(b), C.byref(prm), md.ctypes.data_as(_f64p), mr.ctypes.data_as(_f64p),
             C.c_uint64(seed & (2**64 - 1)), res))
         return [r.as_dict() for r in res], md, mr
+
+    def cbmc_trial_energies(self, ibox: int, is_: int, atoms, xyz, cbmc: bool = True, skip_im: int = 0):
+        """Energies of trial positions [ntrial, nat, 3] of atoms (1-based) of species is_."""
+        at = _i32(atoms)
+        x = np.ascontiguousarray(np.asarray(xyz, dtype=np.float64).reshape(-1, len(at), 3))
+        e = np.zeros(x.shape[0])
+        ov = np.zeros(x.shape[0], dtype=np.int32)
+        self._check("cbmc_trial_energies", self._f["cbmc_trial_energies"](
+            self._h, ibox, is_, skip_im, len(at), _p(at), x.shape[0], x.ctypes.data_as(_f64p), int(cbmc),
+            e.ctypes.data_as(_f64p), ov.ctypes.data_as(_i32p)))
+        return e, ov.astype(bool)
 
     def system_gradient(self, ibox: int, n_atoms_box: int):
         """(energy dict, dU/dr [n_atoms_box, 3], dU/deps [nt, nt], dU/dsig [nt, nt], dU/dq [sum natoms])."""

@@ -169,6 +169,70 @@ __global__ void __launch_bounds__(kBlock) k_mol_inter(BoxDev b, PairTable t, con
 }
 
 // ---------------------------------------------------------------------------
+// K2/K3 trial energies: one CTA per CBMC trial position, threads over the box
+// atoms, the trial's atoms in shared memory; block sum in a fixed order.
+constexpr int kTrialMaxAtoms = 64;
+
+template <bool MIXED>
+__global__ void __launch_bounds__(kBlock) k_trial_energy(BoxDev b, PairTable t, const double4_32a* __restrict__ p64,
+                                                         const int4* __restrict__ meta, int n, int skip_slot,
+                                                         const double4_32a* __restrict__ trial, const int* ttype,
+                                                         int nat, int cbmc, int want_qq, double* e, int* overlap) {
+  __shared__ double4_32a qa[kTrialMaxAtoms];
+  __shared__ int qt[kTrialMaxAtoms];
+  __shared__ double sh[32];
+  __shared__ int ovs;
+  const double4_32a* tr = trial + (size_t)blockIdx.x * nat;
+  for (int a = threadIdx.x; a < nat; a += blockDim.x) {
+    qa[a] = tr[a];
+    qt[a] = ttype[a];
+  }
+  if (threadIdx.x == 0) ovs = 0;
+  __syncthreads();
+  double ev = 0.0, eq = 0.0;
+  KahanF fv, fq;
+  bool ov = false;
+  for (int j = threadIdx.x; j < n && !ov; j += blockDim.x) {
+    const int4 mj = meta[j];
+    if (mj.x == skip_slot) continue;
+    const double4_32a pj = p64[j];
+    for (int a = 0; a < nat; ++a) {
+      const double dx = fold(qa[a].x - pj.x, b.hL[0], b.L[0]);
+      const double dy = fold(qa[a].y - pj.y, b.hL[1], b.L[1]);
+      const double dz = fold(qa[a].z - pj.z, b.hL[2], b.L[2]);
+      const double r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 < b.rcut_lowsq) {
+        ov = true;
+        break;
+      }
+      int m = cutoff_mask(b, r2, cbmc != 0);
+      if (!want_qq) m &= 1;
+      if (MIXED && b.vdw_style == CASS_VDW_LJ) {
+        if ((m & 1) && qt[a] >= 0 && mj.y >= 0) {
+          const int k = pidx(qt[a], mj.y, t.ntypes);
+          fv.add(lj_pair_f(t.epsf[k], t.sig2f[k], (float)r2));
+        }
+      } else if (m & 1) {
+        ev += vdw_pair(t, b, qt[a], mj.y, r2, 1.0);
+      }
+      if (m & 2) {
+        if (MIXED && b.charge_sum_style == CASS_QQ_EWALD)
+          fq.add(qq_ewald_inter_f((float)b.alpha, (float)(qa[a].w * pj.w), (float)r2));
+        else
+          eq += qq_pair_inter(b, qa[a].w * pj.w, r2);
+      }
+    }
+  }
+  if (ov) atomicOr(&ovs, 1);
+  const double s = block_sum(ev + fv.value() + eq + fq.value(), sh);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    overlap[blockIdx.x] = ovs;
+    e[blockIdx.x] = ovs ? 0.0 : s;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // K6a: all inter-molecular pairs of a box (pairs (i,j), j > i, different
 // molecules).  Block (x, y) takes atoms i of row block x against the j tile y,
 // staged in shared memory.  FAST (mixed precision, LJ cut / cut_tail with no
@@ -1115,6 +1179,57 @@ int cass_mol_inter_energy(cass_ctx* c, int32_t im, int32_t is, int32_t cbmc, dou
   *ov = hov ? 1 : 0;
   *ev = hov ? 0.0 : c->h_result[0];
   *eq = hov ? 0.0 : c->h_result[1];
+  return CASS_OK;
+}
+
+int cass_cbmc_trial_energies(cass_ctx* c, int32_t ibox1, int32_t is, int32_t skip_im, int32_t nat,
+                             const int32_t* atoms, int32_t ntrial, const double* xyz, int32_t cbmc, double* e,
+                             int32_t* overlap) {
+  if (!c || ibox1 < 1 || ibox1 > c->nboxes || is < 1 || is > c->nspecies || nat < 1 || !atoms || ntrial < 0 ||
+      (ntrial > 0 && (!xyz || !e || !overlap)))
+    return set_error(CASS_EINVAL, "bad trial arguments");
+  if (!c->pt_set) return set_error(CASS_ESTATE, "nonbond table not set");
+  const SpeciesH& s = c->sp[is - 1];
+  if (!s.defined) return set_error(CASS_ESTATE, "species not defined");
+  if (nat > kTrialMaxAtoms) return set_error(CASS_ECAPACITY, "at most 64 atoms per trial");
+  if (skip_im < 0 || skip_im > c->max_mol[is - 1]) return set_error(CASS_EINVAL, "molecule locate out of range");
+  for (int a = 0; a < nat; ++a)
+    if (atoms[a] < 1 || atoms[a] > s.natoms) return set_error(CASS_EINVAL, "trial atom index out of range");
+  if (ntrial == 0) return CASS_OK;
+  const int ib = ibox1 - 1;
+  int rc;
+  if ((rc = set_device(c)) || (rc = pack_box(c, ib))) return rc;
+  BoxH& B = c->box[ib];
+  std::vector<double4_32a> tr((size_t)ntrial * nat);
+  std::vector<int> tt(nat);
+  for (int a = 0; a < nat; ++a) tt[a] = s.type[atoms[a] - 1];
+  for (int k = 0; k < ntrial; ++k)
+    for (int a = 0; a < nat; ++a) {
+      const double* x = xyz + ((size_t)k * nat + a) * 3;
+      tr[(size_t)k * nat + a] = make_double4_32a(x[0], x[1], x[2], s.q[atoms[a] - 1]);
+    }
+  const size_t tb = tr.size() * sizeof(double4_32a);
+  if ((rc = c->d_trial.reserve(tb + (size_t)nat * sizeof(int) + (size_t)ntrial * (sizeof(double) + sizeof(int)) + 64)))
+    return rc;
+  double4_32a* d_tr = c->d_trial.as<double4_32a>();
+  int* d_tt = reinterpret_cast<int*>(d_tr + tr.size());
+  double* d_e = reinterpret_cast<double*>(reinterpret_cast<char*>(d_tt) + (((size_t)nat * sizeof(int) + 7) & ~(size_t)7));
+  int* d_ov = reinterpret_cast<int*>(d_e + ntrial);
+  CASS_CUDA(h2d(c, d_tr, tr.data(), tb));
+  CASS_CUDA(h2d(c, d_tt, tt.data(), (size_t)nat * sizeof(int)));
+  const int skip_slot = skip_im > 0 ? mol_slot(c, skip_im, is) : -1;
+  const int want_qq = (cbmc && !s.l_coul_cbmc) ? 0 : 1;  // Compute_MoleculePair_Energy, energy_routines.f90:1684-1686
+  if (c->precision == CASS_PREC_MIXED)
+    k_trial_energy<true><<<ntrial, kBlock, 0, c->stream>>>(B.dev, c->pt, B.d_p64.as<double4_32a>(), B.d_meta.as<int4>(),
+                                                           B.npacked, skip_slot, d_tr, d_tt, nat, cbmc, want_qq, d_e, d_ov);
+  else
+    k_trial_energy<false><<<ntrial, kBlock, 0, c->stream>>>(B.dev, c->pt, B.d_p64.as<double4_32a>(), B.d_meta.as<int4>(),
+                                                            B.npacked, skip_slot, d_tr, d_tt, nat, cbmc, want_qq, d_e, d_ov);
+  CASS_CUDA(cudaGetLastError());
+  count_launch(c);
+  CASS_CUDA(d2h(c, e, d_e, (size_t)ntrial * sizeof(double)));
+  CASS_CUDA(d2h(c, overlap, d_ov, (size_t)ntrial * sizeof(int)));
+  CASS_CUDA(cudaStreamSynchronize(c->stream));
   return CASS_OK;
 }
 

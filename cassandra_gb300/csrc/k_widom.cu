@@ -1402,7 +1402,7 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
 // latency-bound, and warps per scheduler matter more than the few spills
 constexpr int kF32Threads = 512;
 constexpr int kF32MinBlocks = 2;
-constexpr int kF32Waves = 2;  // CTAs per resident slot: a second wave evens out uneven boxes
+constexpr int kF32Waves = 8;  // CTAs per resident slot: many short waves even out uneven boxes
 
 template <bool SMEM, bool COUNT>
 __global__ void __launch_bounds__(kF32Threads, kF32MinBlocks) k_widom_f32(WidomSpecies S, SpeciesF SF, PairTable T, const BoxDev* boxes,

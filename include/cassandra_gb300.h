@@ -216,6 +216,19 @@ int cass_ewald_widom(cass_ctx* ctx, int32_t is, int32_t ibox, int32_t n,
                      const double* xyz, double* e_reciprocal);
 
 /* ---- CBMC / Widom ----------------------------------------------------- */
+/* Compute_Molecule_Nonbond_Inter_Energy_Widom (energy_routines.f90:1209-1364)
+ * for a batch of CBMC trial positions, the energy call of every trial in
+ * Build_Molecule (fragment_growth.f90:519-524) and Fragment_Placement
+ * (:1967-2000): ntrial configurations of the nat atoms `atoms` (1-based atom
+ * indices of species is) at xyz [ntrial][nat][3], each against the molecules of
+ * box ibox except molecule (skip_im, is) when skip_im > 0 (the molecule being
+ * deleted or regrown).  cbmc_flag selects rcut_cbmc and drops Coulomb unless
+ * the species' L_Coul_CBMC is set.  e[k] = E_vdw + E_qq of trial k,
+ * overlap[k] = 1 on a core overlap (e[k] = 0). */
+int cass_cbmc_trial_energies(cass_ctx* ctx, int32_t ibox, int32_t is, int32_t skip_im, int32_t nat,
+                             const int32_t* atoms, int32_t ntrial, const double* xyz, int32_t cbmc_flag,
+                             double* e, int32_t* overlap);
+
 /* Widom_Insert (widom_insert.f90:22-594) with Build_Molecule /
  * Fragment_Placement (fragment_growth.f90:72-707,1449-2132) for every
  * insertion, batched over nboxes boxes in one launch.  Insertion k of box b

@@ -1948,6 +1948,39 @@ int orc_widom_insert(orc_ctx* c, int32_t is1, int32_t nboxes, const int32_t* ibo
   return CASS_OK;
 }
 
+// Compute_Molecule_Nonbond_Inter_Energy_Widom for each trial position
+int orc_cbmc_trial_energies(orc_ctx* c, int32_t ibox1, int32_t is1, int32_t skip_im, int32_t nat, const int32_t* atoms,
+                            int32_t ntrial, const double* xyz, int32_t cbmc, double* e, int32_t* overlap) {
+  if (c) refresh_members(c);
+  if (check_ctx(c) || ibox1 < 1 || ibox1 > c->nboxes || is1 < 1 || is1 > c->nspecies || nat < 1 || !atoms ||
+      ntrial < 0 || (ntrial > 0 && (!xyz || !e || !overlap)))
+    return fail(CASS_EINVAL, "bad trial arguments");
+  const Species& s = c->sp[is1 - 1];
+  if (!s.defined) return fail(CASS_ESTATE, "species not defined");
+  for (int a = 0; a < nat; ++a)
+    if (atoms[a] < 1 || atoms[a] > s.natoms) return fail(CASS_EINVAL, "trial atom index out of range");
+  if (skip_im < 0 || skip_im > c->max_mol[is1 - 1]) return fail(CASS_EINVAL, "molecule locate out of range");
+  const int skip = skip_im > 0 ? c->mol_base[is1 - 1] + skip_im - 1 : -1;
+  for (int k = 0; k < ntrial; ++k) {
+    TestMol t;
+    t.is = is1 - 1;
+    t.r.assign(3 * s.natoms, 0.0);
+    t.exist.assign(s.natoms, 0);
+    for (int a = 0; a < nat; ++a) {
+      const int ia = atoms[a] - 1;
+      for (int d = 0; d < 3; ++d) t.r[3 * ia + d] = xyz[((size_t)k * nat + a) * 3 + d];
+      t.exist[ia] = 1;
+    }
+    get_com(c, t.is, t.r.data(), t.exist.data(), t.com);
+    t.max_dcom = max_com_distance(c, t.is, t.r.data(), t.exist.data(), t.com);
+    double ev, eq;
+    const bool ov = mol_inter_energy(c, ibox1 - 1, t.view(), skip, cbmc != 0, ev, eq);
+    overlap[k] = ov ? 1 : 0;
+    e[k] = ov ? 0.0 : ev + eq;
+  }
+  return CASS_OK;
+}
+
 // NVT translate / rotate Monte Carlo, one chain per box (boxes in parallel)
 int orc_mc_sweeps(orc_ctx* c, int32_t nboxes, const int32_t* iboxes, const CassMCParams* p, double* max_disp,
                   double* max_rot, uint64_t seed, CassMCResult* out) {

@@ -294,3 +294,32 @@ def test_widom_edge_cases():
         ro, to = o.widom_insert(2, [1], 64, 12, 12, seed=4, trace=True)
         rg, tg = g.widom_insert(2, [1], 64, 12, 12, seed=4, trace=True)
     assert np.allclose(tg["widom_var"], to["widom_var"], rtol=1e-9)
+
+
+def test_cbmc_trial_energies_match_oracle():
+    s = _butane_batch([300, 500], seed=8)
+    rng = np.random.default_rng(4)
+    L = s.boxes[1].length[0]
+    # 40 random positions of butane's first fragment (atoms 2, 1, 3) in box 2, and
+    # single LJ spheres including one placed on molecule 7 of the box
+    frag = np.array([[0.0, 0.0, 0.0], [1.54, 0.0, 0.0], [-0.63, 1.40, 0.0]])
+    xyz = np.array([frag + (rng.random(3) - 0.5) * L for _ in range(40)])
+    m = s.molecules
+    k7 = [k for k in range(len(m.im)) if m.ibox[k] == 2][6]
+    sph = np.concatenate([(rng.random((15, 1, 3)) - 0.5) * L, m.xyz[k7][None, :, :]])
+    with oracle.open_system(s) as o:
+        with cg.open_system(s, precision=abi.PREC_FP64) as g:
+            for cbmc in (True, False):
+                eo, oo = o.cbmc_trial_energies(2, 2, [2, 1, 3], xyz, cbmc=cbmc)
+                eg, og = g.cbmc_trial_energies(2, 2, [2, 1, 3], xyz, cbmc=cbmc)
+                assert np.array_equal(oo, og)
+                assert np.allclose(eg, eo, rtol=FP64_TOL, atol=1e-9)
+            eo, oo = o.cbmc_trial_energies(2, 1, [1], sph)
+            eg, og = g.cbmc_trial_energies(2, 1, [1], sph)
+            assert np.array_equal(oo, og) and og[-1]
+            assert np.allclose(eg, eo, rtol=FP64_TOL, atol=1e-9)
+            # the same position with the molecule itself excluded (deletion / regrowth)
+            eo, oo = o.cbmc_trial_energies(2, 1, [1], sph[-1:], skip_im=m.im[k7])
+            eg, og = g.cbmc_trial_energies(2, 1, [1], sph[-1:], skip_im=m.im[k7])
+            assert not og[0] and oo[0] == og[0]
+            assert abs(eg[0] - eo[0]) <= FP64_TOL * abs(eo[0])
