@@ -430,8 +430,8 @@ def main():
            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                         "frac": achieved_gbs / hbm_peak, "traffic": traffic,
                         "note": "k_widom_f32; algorithmic bytes = 33 B record per insertion + box staged once per "
-                                "CTA; peak of measured; traffic scaled from the ncu capture of 16 boxes x 4000 "
-                                "insertions"},
+                                "CTA; peak of measured; traffic scaled from the ncu capture of 16 boxes x 16000 "
+                                "insertions (its writes include L2 write-back of the flush buffer)"},
            "compute_roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
                                 "frac": achieved_tf / fp32_peak, "pairs_visited": st["widom_pairs_visited"],
                                 "pairs_in_cutoff": st["widom_pairs_in_cutoff"],

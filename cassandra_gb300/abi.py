@@ -96,6 +96,25 @@ class CassMCResult(C.Structure):
         return d
 
 
+class CassGCMCParams(C.Structure):
+    _fields_ = [("nsteps", C.c_int64), ("is_exchange", C.c_int32), ("kappa_ins", C.c_int32),
+                ("kappa_dih", C.c_int32), ("reserved", C.c_int32), ("cut_translate", C.c_double),
+                ("cut_rotate", C.c_double), ("cut_insert", C.c_double), ("cut_delete", C.c_double),
+                ("cut_regrow", C.c_double)]
+
+
+class CassGCMCResult(C.Structure):
+    _fields_ = [("energy", CassEnergy)] + [(n, C.c_int64) for n in (
+        "n_translate", "n_translate_accepted", "n_rotate", "n_rotate_accepted", "n_insert", "n_insert_accepted",
+        "n_delete", "n_delete_accepted", "n_regrow", "n_regrow_accepted", "n_molecules")] + \
+        [("sum_n_molecules", C.c_double)]
+
+    def as_dict(self) -> dict:
+        d = {n: getattr(self, n) for n, _ in self._fields_ if n != "energy"}
+        d["energy"] = self.energy.as_dict()
+        return d
+
+
 class CassStats(C.Structure):
     _fields_ = [("widom_ms", C.c_double), ("widom_kernel_ms", C.c_double), ("kernel_launches", C.c_int64),
                 ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("widom_pairs_visited", C.c_int64),
@@ -135,6 +154,8 @@ SIGNATURES = {
     "mc_sweeps": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.POINTER(CassMCParams), _f64p, _f64p, C.c_uint64,
                             C.POINTER(CassMCResult)]),
     "system_gradient": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(CassEnergy), _f64p, _f64p, _f64p, _f64p]),
+    "gcmc": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.POINTER(CassGCMCParams), _f64p, _f64p, _f64p, C.c_uint64,
+                       C.POINTER(CassGCMCResult)]),
     "cbmc_trial_energies": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _i32p, C.c_int32,
                                       _f64p, C.c_int32, _f64p, _i32p]),
     # allocation-free energy entry point and run-time extensions of the GPU
@@ -146,7 +167,7 @@ SIGNATURES = {
     "set_count_pairs": (C.c_int, [C.c_void_p, C.c_int32]),
     "set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
-OPTIONAL = {"get_stats", "set_count_pairs", "set_stream", "mol_box_energy_noalloc", "system_gradient"}
+OPTIONAL = {"get_stats", "set_count_pairs", "set_stream", "mol_box_energy_noalloc", "system_gradient", "gcmc"}
 
 
 class CassError(RuntimeError):
@@ -310,6 +331,21 @@ class Context:
 
     def set_stream(self, stream_ptr: int | None) -> None:
         self._check("set_stream", self._f["set_stream"](self._h, C.c_void_p(stream_ptr) if stream_ptr else None))
+
+    def gcmc(self, boxes: Sequence[int], nsteps: int, is_exchange: int, mu_kjmol, max_disp, max_rot, seed: int,
+             kappa_ins: int = 12, kappa_dih: int = 12, cuts=(0.2, 0.4, 0.6, 0.8, 1.0)):
+        """Grand-canonical chains, one per box; cuts are the cumulative probabilities of
+        translate, rotate, insert, delete and regrow."""
+        b = _i32(boxes)
+        mu = np.ascontiguousarray(np.array(mu_kjmol, dtype=np.float64).reshape(len(b)))
+        md = np.ascontiguousarray(np.array(max_disp, dtype=np.float64).reshape(len(b), -1))
+        mr = np.ascontiguousarray(np.array(max_rot, dtype=np.float64).reshape(len(b), -1))
+        prm = CassGCMCParams(nsteps, is_exchange, kappa_ins, kappa_dih, 0, *cuts)
+        res = (CassGCMCResult * len(b))()
+        self._check("gcmc", self._f["gcmc"](
+            self._h, len(b), _p(b), C.byref(prm), mu.ctypes.data_as(_f64p), md.ctypes.data_as(_f64p),
+            mr.ctypes.data_as(_f64p), C.c_uint64(seed & (2**64 - 1)), res))
+        return [r.as_dict() for r in res]
 
     def mc_sweeps(self, boxes: Sequence[int], nsweeps: int, max_disp, max_rot, seed: int,
                   prob_translate: float = 1.0, steps_per_sweep: int = 0, nupdate: int = 0,

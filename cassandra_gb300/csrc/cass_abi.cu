@@ -730,6 +730,8 @@ std::vector<double> count_beads(cass_ctx* c, int ibox) {
 
 namespace cassgpu {
 int pack_box_ext(cass_ctx* c, int ibox) { return pack_box(c, ibox); }
+void invalidate_ext(cass_ctx* c, int ibox) { invalidate(c, ibox); }
+void set_mol_box_ext(cass_ctx* c, int slot, int ibox) { set_mol_box(c, slot, ibox); }
 const std::vector<int>& members_ext(cass_ctx* c, int ibox) { return members(c, ibox); }
 }  // namespace cassgpu
 

@@ -147,6 +147,7 @@ struct cass_ctx_impl {
   DevBuf d_mc;    // Monte Carlo sweep descriptors, outputs and scratch
   DevBuf d_grad;  // adjoint outputs and per-atom parameter derivatives
   DevBuf d_trial; // CBMC trial positions and their energies
+  DevBuf d_gc;    // grand-canonical descriptors, records and outputs
   // structure factors of molecules: [nmol_slots][max nvecs] x2, allocated on first use
   DevBuf d_cos_mol, d_sin_mol, d_cos_mol_old, d_sin_mol_old;
   int cos_mol_stride = 0;

@@ -28,25 +28,10 @@
 #include <vector>
 
 #include "cass_ctx.h"
+#include "cass_cbmc.cuh"
 
 namespace cassgpu {
 
-struct WidomSpecies {
-  int natoms, nfrag, is0;
-  int kappa_ins, kappa_dih;
-  int want_qq_cbmc;  // Coulomb in CBMC trials (L_Coul_CBMC)
-  double ln_kappa_ins, ln_kappa_dih_term;
-  double mass[kMaxAtoms];
-  double q[kMaxAtoms];
-  int type[kMaxAtoms];
-  int frag_natoms[kMaxFrags];
-  signed char frag_atoms[kMaxFrags][kMaxAtoms];
-  int frag_nconnect[kMaxFrags];
-  signed char frag_connect[kMaxFrags][kMaxFrags];
-  int nconfig[kMaxFrags];
-  long long lib_off[kMaxFrags];
-  double prob_ins[kMaxFrags], cum_prob_ins[kMaxFrags], ln_prob_ins[kMaxFrags];
-};
 
 struct BoxSrc {
   const double4_32a* p64;
@@ -255,91 +240,6 @@ __device__ bool query_box(const BoxView& V, const PairTable& T, const double p[3
   }
   eout = acc;
   pc.eabs = eabs;
-  return false;
-}
-
-// ---------------------------------------------------------------------------
-// test-molecule helpers (FP64)
-
-__device__ __forceinline__ void get_com(const WidomSpecies& S, const double* r, unsigned exist, double com[3]) {
-  double tm = 0, x = 0, y = 0, z = 0;
-  for (int k = 0; k < S.natoms; ++k) {
-    if (!((exist >> k) & 1u)) continue;
-    double m = S.mass[k];
-    tm += m;
-    x += m * r[3 * k];
-    y += m * r[3 * k + 1];
-    z += m * r[3 * k + 2];
-  }
-  com[0] = x / tm;
-  com[1] = y / tm;
-  com[2] = z / tm;
-}
-
-// Get_Aligner_Hanger (fragment_growth.f90:2135-2185), row-major
-__device__ void aligner_hanger(double v1[3], double v2[3], double al[9], double hg[9]) {
-  double n1 = sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
-  for (int i = 0; i < 3; ++i) v1[i] = v1[i] / n1;
-  double n2 = sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
-  for (int i = 0; i < 3; ++i) v2[i] = v2[i] / n2;
-  double p1[3] = {v1[1] * v2[2] - v1[2] * v2[1], -v1[0] * v2[2] + v1[2] * v2[0], v1[0] * v2[1] - v1[1] * v2[0]};
-  double np1 = sqrt(p1[0] * p1[0] + p1[1] * p1[1] + p1[2] * p1[2]);
-  for (int i = 0; i < 3; ++i) p1[i] = p1[i] / np1;
-  double p2[3] = {v1[1] * p1[2] - v1[2] * p1[1], -v1[0] * p1[2] + v1[2] * p1[0], v1[0] * p1[1] - v1[1] * p1[0]};
-  double np2 = sqrt(p2[0] * p2[0] + p2[1] * p2[1] + p2[2] * p2[2]);
-  for (int i = 0; i < 3; ++i) p2[i] = p2[i] / np2;
-  for (int i = 0; i < 3; ++i) {
-    al[i] = v1[i];
-    al[3 + i] = p2[i];
-    al[6 + i] = p1[i];
-    hg[i * 3 + 0] = v1[i];
-    hg[i * 3 + 1] = p2[i];
-    hg[i * 3 + 2] = p1[i];
-  }
-}
-
-// Compute_Molecule_Dihedral_Energy over dihedrals whose atoms all exist (RB form)
-__device__ double dihedral_masked(const SpeciesDevHdr& H, const SpeciesPools& P, const double* r, unsigned exist) {
-  double e = 0.0;
-  for (int k = 0; k < H.ndih; ++k) {
-    const int* a = P.ip + H.dih_atoms_off + 4 * k;
-    unsigned m = (1u << a[0]) | (1u << a[1]) | (1u << a[2]) | (1u << a[3]);
-    if ((exist & m) != m) continue;
-    double c1 = dihedral_cos_d(r, a[0], a[1], a[2], a[3]);
-    double cv[6] = {1.0, c1, c1 * c1, 0, 0, 0};
-    cv[3] = cv[1] * cv[2];
-    cv[4] = cv[2] * cv[2];
-    cv[5] = cv[2] * cv[3];
-    double d = 0;
-    for (int j = 0; j < 6; ++j) d += cv[j] * P.dp[H.dih_rb_off + 6 * k + j];
-    e += d;
-  }
-  return e;
-}
-
-// Compute_Atom_Nonbond_Intra_Energy (energy_routines.f90:691-737), CBMC cutoffs
-__device__ bool atom_intra(const SpeciesDevHdr& H, const SpeciesPools& P, const BoxDev& b, const PairTable& T, int ia,
-                           const double* r, unsigned exist, double& eiv, double& eiq, double& eoq) {
-  eiv = eiq = eoq = 0.0;
-  int n = H.natoms;
-  for (int ja = 0; ja < n; ++ja) {
-    if (ja == ia || !((exist >> ja) & 1u)) continue;
-    double vs = P.dp[H.vs_off + ia * n + ja], qs = P.dp[H.qs_off + ia * n + ja];
-    bool nzv = vs > 0.0, nzq = qs > 0.0;
-    if (!(nzv || nzq)) continue;
-    double dx = r[3 * ja] - r[3 * ia], dy = r[3 * ja + 1] - r[3 * ia + 1], dz = r[3 * ja + 2] - r[3 * ia + 2];
-    double r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 < b.rcut_lowsq && nzv) return true;
-    int m = cutoff_mask(b, r2, true);
-    if (!nzv) m &= ~1;
-    if (!nzq) m &= ~2;
-    if (m & 1) eiv += vdw_pair(T, b, P.ip[H.type_off + ja], P.ip[H.type_off + ia], r2, P.dp[H.vs_off + ja * n + ia]);
-    if (m & 2) {
-      double per = 0.0;
-      eiq += qq_pair_intra(b, P.dp[H.q_off + ja] * P.dp[H.q_off + ia], r2, P.dp[H.qs_off + ja * n + ia], &per);
-      eoq += per;
-    }
-  }
   return false;
 }
 
@@ -1727,6 +1627,35 @@ bool species_f(const SpeciesH& s, SpeciesF& F) {
 }  // namespace
 
 namespace cassgpu {
+// Growth tables of species s (0-based is0) for kernels that build molecules
+void fill_growth_species(const SpeciesH& s, int is0, int kappa_ins, int kappa_dih, WidomSpecies& S) {
+  memset(&S, 0, sizeof(S));
+  S.natoms = s.natoms;
+  S.nfrag = s.nfrag;
+  S.is0 = is0;
+  S.kappa_ins = kappa_ins;
+  S.kappa_dih = s.nfrag > 1 ? kappa_dih : 0;
+  S.want_qq_cbmc = s.l_coul_cbmc ? 1 : 0;
+  S.ln_kappa_ins = std::log((double)kappa_ins);
+  S.ln_kappa_dih_term = kappa_dih != 0 ? (double)(s.nfrag - 1) * std::log((double)kappa_dih) : 0.0;
+  for (int a = 0; a < s.natoms; ++a) {
+    S.mass[a] = s.mass[a];
+    S.q[a] = s.q[a];
+    S.type[a] = s.type[a];
+  }
+  for (int f = 0; f < s.nfrag; ++f) {
+    S.frag_natoms[f] = (int)s.frag_atoms[f].size();
+    for (size_t j = 0; j < s.frag_atoms[f].size(); ++j) S.frag_atoms[f][j] = (signed char)s.frag_atoms[f][j];
+    S.frag_nconnect[f] = (int)s.frag_connect[f].size();
+    for (size_t j = 0; j < s.frag_connect[f].size(); ++j) S.frag_connect[f][j] = (signed char)s.frag_connect[f][j];
+    S.nconfig[f] = s.frag_nconfig[f];
+    S.lib_off[f] = s.lib_off[f];
+    S.prob_ins[f] = s.prob_ins[f];
+    S.cum_prob_ins[f] = s.cum_prob_ins[f];
+    S.ln_prob_ins[f] = std::log(s.prob_ins[f]);
+  }
+}
+
 int ensure_pools(cass_ctx* c);
 int pack_box_ext(cass_ctx* c, int ibox);
 const std::vector<int>& members_ext(cass_ctx* c, int ibox);
@@ -1759,33 +1688,8 @@ extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const
   if ((rc = ensure_pools(c))) return rc;
   const int is0 = is1 - 1;
 
-  // test species tables
   WidomSpecies S;
-  memset(&S, 0, sizeof(S));
-  S.natoms = s.natoms;
-  S.nfrag = s.nfrag;
-  S.is0 = is0;
-  S.kappa_ins = kappa_ins;
-  S.kappa_dih = s.nfrag > 1 ? kappa_dih : 0;
-  S.want_qq_cbmc = s.l_coul_cbmc ? 1 : 0;
-  S.ln_kappa_ins = std::log((double)kappa_ins);
-  S.ln_kappa_dih_term = kappa_dih != 0 ? (double)(s.nfrag - 1) * std::log((double)kappa_dih) : 0.0;
-  for (int a = 0; a < s.natoms; ++a) {
-    S.mass[a] = s.mass[a];
-    S.q[a] = s.q[a];
-    S.type[a] = s.type[a];
-  }
-  for (int f = 0; f < s.nfrag; ++f) {
-    S.frag_natoms[f] = (int)s.frag_atoms[f].size();
-    for (size_t j = 0; j < s.frag_atoms[f].size(); ++j) S.frag_atoms[f][j] = (signed char)s.frag_atoms[f][j];
-    S.frag_nconnect[f] = (int)s.frag_connect[f].size();
-    for (size_t j = 0; j < s.frag_connect[f].size(); ++j) S.frag_connect[f][j] = (signed char)s.frag_connect[f][j];
-    S.nconfig[f] = s.frag_nconfig[f];
-    S.lib_off[f] = s.lib_off[f];
-    S.prob_ins[f] = s.prob_ins[f];
-    S.cum_prob_ins[f] = s.cum_prob_ins[f];
-    S.ln_prob_ins[f] = std::log(s.prob_ins[f]);
-  }
+  fill_growth_species(s, is0, kappa_ins, kappa_dih, S);
 
   // per-box constants and cell grids
   std::vector<BoxDev> bd(nboxes);

@@ -87,12 +87,15 @@ def _bend_library(nconfig: int, bond: float, theta0_deg: float, k_K: float, temp
     return out
 
 
-def butane_species(temperature: float = 150.0, nconfig: int = 1000, seed: int = 7) -> Species:
+def butane_species(temperature: float = 150.0, nconfig: int = 1000, seed: int = 7, eps_scale: float = 1.0) -> Species:
     """n-butane, united atom: CH3-CH2-CH2-CH3, fixed 1.54 A bonds, harmonic 114 deg bend
-    (k = 31250 K/rad^2 in the E = k (theta-theta0)^2 form), OPLS dihedral of the pentane fixture."""
+    (k = 31250 K/rad^2 in the E = k (theta-theta0)^2 form), OPLS dihedral of the pentane fixture.
+    eps_scale = 0 gives the ideal (non-interacting) chain."""
     rng = np.random.default_rng(seed)
-    atoms = [Atom("CH3", 15.034, 0.0, ("LJ", 98.0, 3.75)), Atom("CH2", 14.027, 0.0, ("LJ", 46.0, 3.95)),
-             Atom("CH2", 14.027, 0.0, ("LJ", 46.0, 3.95)), Atom("CH3", 15.034, 0.0, ("LJ", 98.0, 3.75))]
+    atoms = [Atom("CH3", 15.034, 0.0, ("LJ", 98.0 * eps_scale, 3.75)),
+             Atom("CH2", 14.027, 0.0, ("LJ", 46.0 * eps_scale, 3.95)),
+             Atom("CH2", 14.027, 0.0, ("LJ", 46.0 * eps_scale, 3.95)),
+             Atom("CH3", 15.034, 0.0, ("LJ", 98.0 * eps_scale, 3.75))]
     sp = Species(atoms=atoms,
                  bonds=[(1, 2, "fixed", 1.54), (2, 3, "fixed", 1.54), (3, 4, "fixed", 1.54)],
                  angles=[(1, 2, 3, "harmonic", 31250.0, 114.0), (2, 3, 4, "harmonic", 31250.0, 114.0)],
@@ -257,3 +260,24 @@ def water_gradient_system(nmol: int = 4096, length: float = 49.7, temperature: f
     bx = BoxSpec(length=(length,) * 3, rcut_vdw=rcut, rcut_coul=rcut, rcut_cbmc=min(6.5, rcut), rcut_low=0.85,
                  charge_style=abi.CHARGE_COUL, charge_sum_style=abi.QQ_EWALD, ewald_tol=tol, temperature=temperature)
     return System([sp], [bx], ms, ff, [nmol])
+
+
+def gcmc_system(nboxes: int = 16, length: float = 40.0, temperature: float = 300.0, rcut: float = 14.0,
+                rcut_cbmc: float = 6.5, rcut_low: float = 1.0, max_per_box: int = 800, seed: int = 2025,
+                nconfig: int = 1000, eps_scale: float = 1.0) -> System:
+    """Empty cubic boxes for grand-canonical runs of the n-butane chain (one species)."""
+    sp = butane_species(temperature, nconfig, seed, eps_scale)
+    ff = ForceField([sp])
+    boxes = [BoxSpec(length=(length,) * 3, rcut_vdw=rcut, rcut_cbmc=rcut_cbmc, rcut_low=rcut_low,
+                     temperature=temperature) for _ in range(nboxes)]
+    return System([sp], boxes, MoleculeSet(), ff, [max_per_box * nboxes])
+
+
+def ideal_gas_system(nboxes: int = 2, length: float = 30.0, temperature: float = 300.0,
+                     max_per_box: int = 400) -> System:
+    """Non-interacting spheres (epsilon 0) for checks of the grand-canonical acceptance rules."""
+    sp = lj_sphere_species(0.0, 3.0, name="IG")
+    ff = ForceField([sp])
+    boxes = [BoxSpec(length=(length,) * 3, rcut_vdw=10.0, rcut_cbmc=6.5, rcut_low=1e-3,
+                     temperature=temperature) for _ in range(nboxes)]
+    return System([sp], boxes, MoleculeSet(), ff, [max_per_box * nboxes])

@@ -274,6 +274,41 @@ typedef struct CassMCResult {
 int cass_mc_sweeps(cass_ctx* ctx, int32_t nboxes, const int32_t* ibox, const CassMCParams* params,
                    double* max_disp, double* max_rot, uint64_t seed, CassMCResult* out);
 
+/* ---- grand-canonical Monte Carlo ---------------------------------------- */
+/* GCMC (gcmc_driver.f90:30-102) of one exchanged species in every listed box,
+ * boxes advancing in lockstep in one launch: Translate, Rotate, CBMC Insertion
+ * (move_insert.f90), CBMC Deletion (move_delete.f90) and CBMC regrowth
+ * (Cut_N_Grow, move_regrow.f90 with Cut_Regrow, fragment_growth.f90:1118-1312),
+ * chosen by the cumulative thresholds below.  Boxes must hold no charges (no
+ * Ewald sum).  The molecule a move picks is the im-th live molecule of its
+ * species in slot order; new molecules take the highest free slot of the
+ * box's share of free slots (free slots of the exchanged species are dealt to
+ * the listed boxes in turn, in ascending slot order).  Box b draws from the
+ * lfsr258 stream seeded by (seed, b, 0).  Requires a prior
+ * cass_system_total_energy of each listed box. */
+typedef struct CassGCMCParams {
+  int64_t nsteps;           /* moves per box */
+  int32_t is_exchange;      /* the inserted / deleted species (1-based) */
+  int32_t kappa_ins, kappa_dih;
+  int32_t reserved;
+  double cut_translate, cut_rotate, cut_insert, cut_delete, cut_regrow;  /* cumulative, <= 1 */
+} CassGCMCParams;
+
+typedef struct CassGCMCResult {
+  CassEnergy energy;         /* energy(ibox) after the last move */
+  int64_t n_translate, n_translate_accepted, n_rotate, n_rotate_accepted;
+  int64_t n_insert, n_insert_accepted, n_delete, n_delete_accepted, n_regrow, n_regrow_accepted;
+  int64_t n_molecules;       /* molecules of the exchanged species after the last move */
+  double sum_n_molecules;    /* that count summed over all moves (for <N>) */
+} CassGCMCResult;
+
+/* mu [nboxes]: chemical potential of the exchanged species, kJ/mol (the .inp
+ * Chemical_Potential_Info value); max_disp, max_rot [nboxes][nspecies] step
+ * sizes (not adapted). */
+int cass_gcmc(cass_ctx* ctx, int32_t nboxes, const int32_t* ibox, const CassGCMCParams* params,
+              const double* mu, const double* max_disp, const double* max_rot, uint64_t seed,
+              CassGCMCResult* out);
+
 /* ---- configuration gradient (adjoint) ---------------------------------- */
 /* The derivatives of the total energy of box ibox, as cass_system_total_energy
  * computes it (and returns it in *energy), for LJ cut / cut_tail boxes with no

@@ -36,6 +36,8 @@ constexpr double ROOTPI = 1.7724538509;
 constexpr double KBOLTZ = 0.8314472;
 constexpr double CHARGE_FACTOR = 138935.4558;
 constexpr double MAX_KBT = 708.0;
+constexpr double H_PLANK = 39.9031268605;
+constexpr double ATOMIC_TO_KJMOL = 0.01;
 
 thread_local std::string g_err;
 
@@ -1442,6 +1444,644 @@ struct McChain {
   }
 };
 
+// ---------------------------------------------------------------------------
+// Grand-canonical moves: Insertion (move_insert.f90), Deletion
+// (move_delete.f90) and Cut_N_Grow (move_regrow.f90), with Build_Molecule,
+// Fragment_Placement and Cut_Regrow (fragment_growth.f90) for a molecule of
+// the box.  del = true computes the Rosenbluth weight of the molecule as it is
+// (trial 1 is its present configuration and is always the one chosen).
+
+// Fold_Molecule, orthorhombic branch (minimum_image_separation.f90:162-235)
+void fold_molecule(const Box& b, Mol& m) {
+  const int n = (int)m.exist.size();
+  for (int k = 0; k < 3; ++k) {
+    if (m.com[k] > b.hL[k]) {
+      m.com[k] = m.com[k] - b.L[k];
+      for (int a = 0; a < n; ++a) m.r[3 * a + k] = m.r[3 * a + k] - b.L[k];
+    } else if (m.com[k] < -b.hL[k]) {
+      m.com[k] = m.com[k] + b.L[k];
+      for (int a = 0; a < n; ++a) m.r[3 * a + k] = m.r[3 * a + k] + b.L[k];
+    }
+  }
+}
+
+// Fragment_Placement (fragment_growth.f90:1449-2132) for the fragments
+// order[first..]; placed[] marks the fragments already in place.  Returns
+// cbmc_overlap.
+bool place_fragments(orc_ctx* c, int ibox, Mol& m, int slot, const std::vector<int>& order, size_t first,
+                     std::vector<int>& placed, bool del, int kappa_dih, double e_prev, double& ln_pbias, Rng& rng) {
+  const Species& s = c->sp[m.is];
+  const Box& b = c->box[ibox];
+  const double beta = b.beta;
+  const int n = s.natoms;
+  std::vector<double> cfg(3 * n, 0.0), ctmp(3 * (size_t)n * kappa_dih, 0.0);
+  std::vector<double> dw(kappa_dih), dn(kappa_dih), dd(kappa_dih);
+  std::vector<char> dov(kappa_dih);
+  for (size_t oi = first; oi < order.size(); ++oi) {
+    const int f = order[oi];
+    const std::vector<int>& atoms = s.frag_atoms[f];
+    const int nf = (int)atoms.size();
+    std::vector<char> grown(m.exist);
+    std::fill(cfg.begin(), cfg.end(), 0.0);
+    if (del) {
+      for (int a : atoms) {
+        m.exist[a] = 1;
+        for (int d = 0; d < 3; ++d) cfg[3 * a + d] = m.r[3 * a + d];
+      }
+    } else {
+      const int nconf = s.frag_nconfig[f];
+      int cf = (int)(rng.next() * nconf);
+      cf = (int)(rng.next() * nconf);  // the duplicated draw of fragment_growth.f90:1578,1584
+      if (cf >= nconf) cf = nconf - 1;
+      for (int j = 0; j < nf; ++j) {
+        const int a = atoms[j];
+        m.exist[a] = 1;
+        for (int d = 0; d < 3; ++d) cfg[3 * a + d] = s.frag_lib[f][(size_t)(cf * nf + j) * 3 + d];
+      }
+    }
+    const std::vector<char> combined(m.exist);
+    std::vector<char> newex(n);
+    for (int a = 0; a < n; ++a) newex[a] = combined[a] && !grown[a];
+    int fc = -1;
+    for (int g : s.frag_connect[f])
+      if (placed[g]) {
+        fc = g;
+        break;
+      }
+    if (fc < 0) return true;
+    const int anc_i = atoms[0], anc_c = s.frag_atoms[fc][0];
+    std::vector<int> atom_id;
+    for (int a : atoms)
+      if (a != anc_i && a != anc_c) atom_id.push_back(a);
+    int atom_ifrag = atoms[nf - 1];
+    for (int a : atoms)
+      if (a != anc_i && a != anc_c) {
+        atom_ifrag = a;
+        break;
+      }
+    int atom_fc = s.frag_atoms[fc].back();
+    for (int a : s.frag_atoms[fc])
+      if (a != anc_i && a != anc_c) {
+        atom_fc = a;
+        break;
+      }
+    double v1[3], v2[3], al_i[9], hg_i[9], al_c[9], hg_c[9];
+    for (int d = 0; d < 3; ++d) {
+      v1[d] = cfg[3 * anc_i + d] - cfg[3 * anc_c + d];
+      v2[d] = cfg[3 * atom_ifrag + d] - cfg[3 * anc_c + d];
+    }
+    aligner_hanger(v1, v2, al_i, hg_i);
+    if (!del) {
+      for (int d = 0; d < 3; ++d) {
+        v1[d] = m.r[3 * anc_i + d] - m.r[3 * anc_c + d];
+        v2[d] = m.r[3 * atom_fc + d] - m.r[3 * anc_c + d];
+      }
+      aligner_hanger(v1, v2, al_c, hg_c);
+    }
+    const double tx = cfg[3 * anc_c], ty = cfg[3 * anc_c + 1], tz = cfg[3 * anc_c + 2];
+    for (int a = 0; a < n; ++a) {
+      cfg[3 * a] -= tx;
+      cfg[3 * a + 1] -= ty;
+      cfg[3 * a + 2] -= tz;
+    }
+    for (int a : atoms) {
+      const double x = cfg[3 * a], y = cfg[3 * a + 1], z = cfg[3 * a + 2];
+      cfg[3 * a] = x * al_i[0] + y * al_i[1] + z * al_i[2];
+      cfg[3 * a + 1] = x * al_i[3] + y * al_i[4] + z * al_i[5];
+      cfg[3 * a + 2] = x * al_i[6] + y * al_i[7] + z * al_i[8];
+    }
+    double theta;
+    if (del) {
+      theta = 0.0;
+      std::copy(hg_i, hg_i + 9, hg_c);
+    } else {
+      theta = TWOPI * rng.next();
+    }
+    for (int ii = 0; ii < kappa_dih; ++ii) {
+      double* ct = &ctmp[(size_t)ii * 3 * n];
+      const double cth = std::cos(theta), sth = std::sin(theta);
+      for (int a : atoms) {
+        const double x = cfg[3 * a], y = cfg[3 * a + 1], z = cfg[3 * a + 2];
+        const double yr = cth * y + sth * z, zr = -sth * y + cth * z;
+        double xn = x * hg_c[0] + yr * hg_c[1] + zr * hg_c[2];
+        double yn = x * hg_c[3] + yr * hg_c[4] + zr * hg_c[5];
+        double zn = x * hg_c[6] + yr * hg_c[7] + zr * hg_c[8];
+        if (a != anc_i && a != anc_c) {
+          xn = xn + m.r[3 * anc_c];
+          yn = yn + m.r[3 * anc_c + 1];
+          zn = zn + m.r[3 * anc_c + 2];
+        }
+        ct[3 * a] = xn;
+        ct[3 * a + 1] = yn;
+        ct[3 * a + 2] = zn;
+      }
+      theta = theta + TWOPI / (double)kappa_dih;
+    }
+    for (int ii = 0; ii < kappa_dih; ++ii) {
+      dn[ii] = 0.0;
+      dd[ii] = 0.0;
+      dov[ii] = 0;
+      const double* ct = &ctmp[(size_t)ii * 3 * n];
+      for (int a : atom_id)
+        for (int d = 0; d < 3; ++d) m.r[3 * a + d] = ct[3 * a + d];
+      for (int a : atom_id) m.exist[a] = 0;
+      double niv = 0, niq = 0, noq = 0;
+      bool ov = false;
+      for (int a : atom_id) {
+        m.exist[a] = 1;
+        double eiv, eiq, eoq;
+        if (atom_intra_energy(c, b, m.is, a, m.r.data(), m.exist.data(), true, eiv, eiq, eoq)) {
+          ov = true;
+          break;
+        }
+        niv += eiv;
+        niq += eiq;
+        noq += eoq;
+      }
+      if (ov) {
+        dw[ii] = ii > 0 ? dw[ii - 1] : 0.0;
+        dov[ii] = 1;
+        for (int a : atom_id) m.exist[a] = 1;
+        continue;
+      }
+      m.exist = newex;
+      get_com(c, m.is, m.r.data(), m.exist.data(), m.com);
+      m.max_dcom = max_com_distance(c, m.is, m.r.data(), m.exist.data(), m.com);
+      double ev = 0.0, eq = 0.0;
+      ov = mol_inter_energy(c, ibox, view_of(m), slot, true, ev, eq);
+      m.exist = combined;
+      if (ov) {
+        dw[ii] = 0.0;
+        dov[ii] = 1;
+      } else {
+        const double ed = dihedral_energy(s, m.r.data(), m.exist.data());
+        dd[ii] = ed;
+        dn[ii] = ed + niv + niq + (ev + eq) + noq - e_prev;
+        const double nk = beta * dn[ii];
+        if (nk >= MAX_KBT) {
+          dw[ii] = 0.0;
+          dov[ii] = 1;
+        } else {
+          dw[ii] = std::exp(-nk);
+        }
+      }
+      if (ii > 0) dw[ii] = dw[ii - 1] + dw[ii];
+    }
+    if (std::all_of(dov.begin(), dov.end(), [](char v) { return v != 0; })) return true;
+    int tr = 0;
+    if (!del) {
+      const double pp = rng.next() * dw[kappa_dih - 1];
+      while (tr < kappa_dih && !(pp < dw[tr])) ++tr;
+      if (tr == kappa_dih) return true;
+    }
+    ln_pbias = ln_pbias - beta * dn[tr] - std::log(dw[kappa_dih - 1]);
+    const double* ct = &ctmp[(size_t)tr * 3 * n];
+    for (int a : atoms)
+      if (a != anc_i && a != anc_c)
+        for (int d = 0; d < 3; ++d) m.r[3 * a + d] = ct[3 * a + d];
+    e_prev = dd[tr];
+    placed[f] = 1;
+  }
+  return false;
+}
+
+// Build_Molecule (fragment_growth.f90:72-707) for molecule m (slot) of box
+// ibox.  Returns cbmc_overlap; sets ln_pseq and ln_pbias.
+bool build_molecule(orc_ctx* c, int ibox, Mol& m, int slot, bool del, int kappa_ins, int kappa_dih, double& ln_pseq,
+                    double& ln_pbias, Rng& rng) {
+  const Species& s = c->sp[m.is];
+  const Box& b = c->box[ibox];
+  const double beta = b.beta;
+  ln_pbias = 0.0;
+  std::fill(m.exist.begin(), m.exist.end(), 0);
+  const double u = rng.next();
+  int fstart = 0;
+  while (fstart < s.nfrag && !(u < s.cum_prob_ins[fstart])) ++fstart;
+  if (fstart >= s.nfrag) fstart = s.nfrag - 1;
+  ln_pseq = std::log(s.prob_ins[fstart]);
+  std::vector<int> order{fstart}, live(s.nfrag, 0);
+  live[fstart] = 1;
+  if (s.nfrag > 1) fragment_order(s, fstart, order, live, ln_pseq, rng);
+  const std::vector<int>& fa = s.frag_atoms[fstart];
+  const int nfa = (int)fa.size();
+  if (!del) {
+    int conf = (int)(rng.next() * s.frag_nconfig[fstart]);
+    if (conf >= s.frag_nconfig[fstart]) conf = s.frag_nconfig[fstart] - 1;
+    for (int i = 0; i < nfa; ++i)
+      for (int d = 0; d < 3; ++d) m.r[3 * fa[i] + d] = s.frag_lib[fstart][(size_t)(conf * nfa + i) * 3 + d];
+  }
+  for (int a : fa) m.exist[a] = 1;
+  get_com(c, m.is, m.r.data(), m.exist.data(), m.com);
+  if (!del) {  // Rotate_Molecule_Eulerian (rotation_routines.f90:41-137)
+    const double theta = std::acos(1.0 - 2.0 * rng.next());
+    const double phi = (1.0 - 2.0 * rng.next()) * PI;
+    const double psi = (1.0 - 2.0 * rng.next()) * PI;
+    const double r11 = std::cos(psi) * std::cos(phi) - std::cos(theta) * std::sin(phi) * std::sin(psi);
+    const double r12 = std::cos(psi) * std::sin(phi) + std::cos(theta) * std::cos(phi) * std::sin(psi);
+    const double r13 = std::sin(psi) * std::sin(theta);
+    const double r21 = -std::sin(psi) * std::cos(phi) - std::cos(theta) * std::sin(phi) * std::cos(psi);
+    const double r22 = -std::sin(psi) * std::sin(phi) + std::cos(theta) * std::cos(phi) * std::cos(psi);
+    const double r23 = std::cos(psi) * std::sin(theta);
+    const double r31 = std::sin(theta) * std::sin(phi);
+    const double r32 = -std::sin(theta) * std::cos(phi);
+    const double r33 = std::cos(theta);
+    for (int a : fa) {
+      const double x = m.r[3 * a] - m.com[0], y = m.r[3 * a + 1] - m.com[1], z = m.r[3 * a + 2] - m.com[2];
+      m.r[3 * a] = (r11 * x + r12 * y + r13 * z) + m.com[0];
+      m.r[3 * a + 1] = (r21 * x + r22 * y + r23 * z) + m.com[1];
+      m.r[3 * a + 2] = (r31 * x + r32 * y + r33 * z) + m.com[2];
+    }
+  }
+  const std::vector<double> r0(m.r);
+  const double com_old[3] = {m.com[0], m.com[1], m.com[2]};
+  std::vector<double> weight(kappa_ins, 0.0), nrg(kappa_ins, 0.0), anchors(3 * kappa_ins, 0.0);
+  std::vector<char> ov_trial(kappa_ins, 0);
+  bool need_max_dcom = true;
+  for (int it = 0; it < kappa_ins; ++it) {
+    double ax, ay, az;
+    if (del && it == 0) {
+      ax = com_old[0];
+      ay = com_old[1];
+      az = com_old[2];
+    } else {
+      ax = (0.5 - rng.next()) * b.L[0];
+      ay = (0.5 - rng.next()) * b.L[1];
+      az = (0.5 - rng.next()) * b.L[2];
+    }
+    for (int a : fa) {
+      m.r[3 * a] = r0[3 * a] - com_old[0] + ax;
+      m.r[3 * a + 1] = r0[3 * a + 1] - com_old[1] + ay;
+      m.r[3 * a + 2] = r0[3 * a + 2] - com_old[2] + az;
+    }
+    anchors[3 * it] = ax;
+    anchors[3 * it + 1] = ay;
+    anchors[3 * it + 2] = az;
+    m.com[0] = ax;
+    m.com[1] = ay;
+    m.com[2] = az;
+    if (need_max_dcom) {
+      m.max_dcom = max_com_distance(c, m.is, m.r.data(), m.exist.data(), m.com);
+      need_max_dcom = false;
+    }
+    double ev = 0.0, eq = 0.0;
+    const bool ov = mol_inter_energy(c, ibox, view_of(m), slot, true, ev, eq);
+    nrg[it] = ev + eq;
+    if (ov) {
+      weight[it] = 0.0;
+      ov_trial[it] = 1;
+    } else {
+      const double nk = beta * nrg[it];
+      if (nk >= MAX_KBT) {
+        weight[it] = 0.0;
+        ov_trial[it] = 1;
+      } else {
+        weight[it] = std::exp(-nk);
+      }
+    }
+    if (it > 0) weight[it] = weight[it - 1] + weight[it];
+  }
+  if (std::all_of(ov_trial.begin(), ov_trial.end(), [](char v) { return v != 0; })) return true;
+  int sel = 0;
+  if (!del) {
+    const double rn = rng.next() * weight[kappa_ins - 1];
+    while (sel < kappa_ins && !(rn < weight[sel])) ++sel;
+    if (sel == kappa_ins) return true;
+  }
+  ln_pbias = ln_pbias - beta * nrg[sel] - std::log(weight[kappa_ins - 1]);
+  for (int a : fa) {
+    m.r[3 * a] = r0[3 * a] - com_old[0] + anchors[3 * sel];
+    m.r[3 * a + 1] = r0[3 * a + 1] - com_old[1] + anchors[3 * sel + 1];
+    m.r[3 * a + 2] = r0[3 * a + 2] - com_old[2] + anchors[3 * sel + 2];
+  }
+  m.com[0] = anchors[3 * sel];
+  m.com[1] = anchors[3 * sel + 1];
+  m.com[2] = anchors[3 * sel + 2];
+  const double e_prev = dihedral_energy(s, m.r.data(), m.exist.data());
+  std::vector<int> placed(s.nfrag, 0);
+  placed[fstart] = 1;
+  if (place_fragments(c, ibox, m, slot, order, 1, placed, del, kappa_dih, e_prev, ln_pbias, rng)) return true;
+  if (order.size() > 1) {
+    get_com(c, m.is, m.r.data(), m.exist.data(), m.com);
+    m.max_dcom = max_com_distance(c, m.is, m.r.data(), m.exist.data(), m.com);
+  }
+  return false;
+}
+
+struct GcmcChain {
+  McChain mc;  // RNG, energy, translate / rotate
+  int is = 0;  // exchanged species (0-based)
+  double mu = 0.0, log_lambda3 = 0.0;
+  const CassGCMCParams* gp = nullptr;
+  std::vector<int> pool;  // free slots of this box, ascending; insertion takes the last
+  std::vector<int> frag_bond_a, frag_bond_b;
+  std::vector<double> prob_del1;
+  CassGCMCResult res{};
+
+  orc_ctx* c() const { return mc.c; }
+  int ibox() const { return mc.ibox; }
+
+  void set_members_changed() {
+    // sp_off after an insertion or deletion (members stay sorted by slot)
+    orc_ctx* cc = mc.c;
+    const std::vector<int>& mem = cc->members[mc.ibox];
+    size_t k = 0;
+    for (int s2 = 0; s2 <= cc->nspecies; ++s2) {
+      const int lim = s2 < cc->nspecies ? cc->mol_base[s2] : INT32_MAX;
+      while (k < mem.size() && mem[k] < lim) ++k;
+      cc->sp_off[mc.ibox][s2] = (int)k;
+    }
+  }
+
+  std::vector<double> beads_with(const Species& s, double sign) const {
+    std::vector<double> nb = count_beads(mc.c, mc.ibox);
+    for (int a = 0; a < s.natoms; ++a)
+      if (s.type[a] >= 0) nb[s.type[a]] += sign;
+    return nb;
+  }
+
+  // Insertion (move_insert.f90)
+  void insert() {
+    orc_ctx* cc = c();
+    const Box& b = cc->box[ibox()];
+    Rng& rng = mc.rng;
+    (void)(int)(rng.next() * 1.0);  // is_rand = INT(rranf() * nspec_insert) + 1
+    if (pool.empty()) {
+      mc.err = fail(CASS_ECAPACITY, "no free molecule slot left for an insertion");
+      return;
+    }
+    ++res.n_insert;
+    const int slot = pool.back();
+    Mol& m = cc->mol[slot];
+    const Species& s = cc->sp[is];
+    m.is = is;
+    m.ibox = ibox();
+    m.r.assign(3 * s.natoms, 0.0);
+    m.exist.assign(s.natoms, 0);
+    double ln_pseq = 0.0, ln_pbias = 0.0;
+    const bool cbmc_ov = build_molecule(cc, ibox(), m, slot, false, gp->kappa_ins, gp->kappa_dih, ln_pseq, ln_pbias, rng);
+    std::fill(m.exist.begin(), m.exist.end(), 1);
+    ln_pbias = ln_pbias + ln_pseq + std::log((double)gp->kappa_ins);
+    if (gp->kappa_dih != 0) ln_pbias = ln_pbias + (double)(s.nfrag - 1) * std::log((double)gp->kappa_dih);
+    if (cbmc_ov) return;
+    fold_molecule(b, m);
+    refresh_com(cc, m);
+    double ev, eq, eiv, eiq, eoq;
+    if (mol_inter_energy(cc, ibox(), view_of(m), slot, false, ev, eq)) return;
+    if (mol_intra_energy(cc, b, is, m.r.data(), m.exist.data(), false, eiv, eiq, eoq)) return;
+    eq = eq + eoq;
+    double dE_inter = ev + eq, dE_intra = eiv + eiq;
+    const double eb = bond_energy(s, m.r.data()), ea = angle_energy(s, m.r.data(), m.exist.data());
+    const double ed = dihedral_energy(s, m.r.data(), m.exist.data()), ei = improper_energy(s, m.r.data());
+    dE_intra = dE_intra + eb + ea + ed + ei;
+    double e_lrc = mc.E.lrc;
+    if (b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) {
+      e_lrc = lr_correction(cc, b, beads_with(s, 1.0));
+      dE_inter = dE_inter + e_lrc - mc.E.lrc;
+    }
+    const double dE = dE_intra + dE_inter;
+    const double dE_frag = ea;
+    const int nmols = mc.nmols(is) + 1;
+    double ln_pacc = b.beta * (dE - dE_frag);
+    ln_pacc = ln_pacc - mu * b.beta;
+    ln_pacc = ln_pacc + ln_pbias;
+    ln_pacc = ln_pacc + std::log((double)nmols) + log_lambda3;
+    ln_pacc = ln_pacc - std::log(b.volume);
+    if (!accept_or_reject(ln_pacc, rng)) return;
+    CassEnergy& E = mc.E;
+    E.total += dE;
+    E.intra += dE_intra;
+    E.inter += dE_inter;
+    E.bond += eb;
+    E.angle += ea;
+    E.dihedral += ed;
+    E.improper += ei;
+    E.intra_vdw += eiv;
+    E.intra_q += eiq;
+    E.inter_vdw += ev;
+    E.inter_q += eq;
+    if (b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) E.lrc = e_lrc;
+    ++res.n_insert_accepted;
+    pool.pop_back();
+    m.live = true;
+    std::vector<int>& mem = cc->members[ibox()];
+    mem.insert(std::lower_bound(mem.begin(), mem.end(), slot), slot);
+    set_members_changed();
+  }
+
+  // Deletion (move_delete.f90)
+  void remove() {
+    orc_ctx* cc = c();
+    const Box& b = cc->box[ibox()];
+    Rng& rng = mc.rng;
+    (void)(int)(rng.next() * 1.0);  // is_rand
+    const int nmols = mc.nmols(is);
+    if (nmols == 0) return;
+    ++res.n_delete;
+    const int im = std::min((int)(rng.next() * nmols) + 1, nmols);
+    const int slot = cc->members[ibox()][cc->sp_off[ibox()][is] + im - 1];
+    Mol& m = cc->mol[slot];
+    const Species& s = cc->sp[is];
+    double ln_pseq = 0.0, ln_pbias = 0.0;
+    const bool cbmc_ov = build_molecule(cc, ibox(), m, slot, true, gp->kappa_ins, gp->kappa_dih, ln_pseq, ln_pbias, rng);
+    std::fill(m.exist.begin(), m.exist.end(), 1);
+    if (cbmc_ov) {
+      mc.err = fail(CASS_ESTATE, "molecule energy too high for a deletion");
+      return;
+    }
+    ln_pbias = ln_pbias + ln_pseq + std::log((double)gp->kappa_ins);
+    if (gp->kappa_dih != 0) ln_pbias = ln_pbias + (double)(s.nfrag - 1) * std::log((double)gp->kappa_dih);
+    refresh_com(cc, m);
+    double ev, eq, eiv, eiq, eoq;
+    mol_inter_energy(cc, ibox(), view_of(m), slot, false, ev, eq);
+    double dE_inter = -ev - eq;
+    const double eb = bond_energy(s, m.r.data()), ea = angle_energy(s, m.r.data(), m.exist.data());
+    const double ed = dihedral_energy(s, m.r.data(), m.exist.data()), ei = improper_energy(s, m.r.data());
+    double dE_intra = -eb - ea - ed - ei;
+    mol_intra_energy(cc, b, is, m.r.data(), m.exist.data(), false, eiv, eiq, eoq);
+    eq = eq + eoq;
+    dE_intra = dE_intra - eiv - eiq;
+    dE_inter = dE_inter - eoq;
+    double e_lrc = mc.E.lrc;
+    if (b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) {
+      e_lrc = lr_correction(cc, b, beads_with(s, -1.0));
+      dE_inter = dE_inter + (e_lrc - mc.E.lrc);
+    }
+    const double dE = dE_intra + dE_inter;
+    const double dE_frag = -ea;
+    double ln_pacc = b.beta * (dE - dE_frag);
+    ln_pacc = ln_pacc + b.beta * mu;
+    ln_pacc = ln_pacc - ln_pbias;
+    ln_pacc = ln_pacc - std::log((double)nmols) - log_lambda3;
+    ln_pacc = ln_pacc + std::log(b.volume);
+    if (!accept_or_reject(ln_pacc, rng)) return;
+    CassEnergy& E = mc.E;
+    E.total += dE;
+    E.intra += dE_intra;
+    E.inter += dE_inter;
+    E.bond -= eb;
+    E.angle -= ea;
+    E.dihedral -= ed;
+    E.improper -= ei;
+    E.intra_vdw -= eiv;
+    E.intra_q -= eiq;
+    E.inter_vdw -= ev;
+    E.inter_q -= eq;
+    if (b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) E.lrc = e_lrc;
+    ++res.n_delete_accepted;
+    m.live = false;
+    std::vector<int>& mem = cc->members[ibox()];
+    mem.erase(std::lower_bound(mem.begin(), mem.end(), slot));
+    set_members_changed();
+    pool.push_back(slot);
+  }
+
+  // energies of molecule m for Cut_N_Grow: bonded + intra + inter (full cutoffs)
+  bool mol_energies(Mol& m, int slot, double& eb, double& ea, double& ed, double& ei, double& eiv, double& eiq,
+                    double& ev, double& eq) {
+    orc_ctx* cc = c();
+    const Species& s = cc->sp[m.is];
+    eb = bond_energy(s, m.r.data());
+    ea = angle_energy(s, m.r.data(), m.exist.data());
+    ed = dihedral_energy(s, m.r.data(), m.exist.data());
+    ei = improper_energy(s, m.r.data());
+    double eoq;
+    mol_intra_energy(cc, cc->box[ibox()], m.is, m.r.data(), m.exist.data(), false, eiv, eiq, eoq);
+    const bool ov = mol_inter_energy(cc, ibox(), view_of(m), slot, false, ev, eq);
+    eq = eq + eoq;
+    return ov;
+  }
+
+  // Cut_Regrow (fragment_growth.f90:1118-1312) on molecule m
+  bool cut_regrow(Mol& m, int slot, bool del, std::vector<int>& order, int& f_live, int& f_dead, double& e_prev,
+                  double& ln_pbias) {
+    orc_ctx* cc = c();
+    const Species& s = cc->sp[m.is];
+    Rng& rng = mc.rng;
+    ln_pbias = 0.0;
+    if (!del) {
+      const int nfb = (int)frag_bond_a.size();
+      const int fb = std::min((int)(rng.next() * nfb), nfb - 1);
+      if (rng.next() < prob_del1[fb]) {
+        f_dead = frag_bond_a[fb];
+        f_live = frag_bond_b[fb];
+      } else {
+        f_dead = frag_bond_b[fb];
+        f_live = frag_bond_a[fb];
+      }
+      std::vector<int> live(s.nfrag, 0);
+      live[f_live] = 1;
+      order.assign(1, f_dead);
+      live[f_dead] = 1;
+      double ln_pseq = 0.0;
+      fragment_order(s, f_dead, order, live, ln_pseq, rng);
+    }
+    std::fill(m.exist.begin(), m.exist.end(), 1);
+    std::vector<int> placed(s.nfrag, 1);
+    for (int f : order) {
+      placed[f] = 0;
+      for (int a : s.frag_atoms[f]) m.exist[a] = 0;
+    }
+    m.exist[s.frag_atoms[f_live][0]] = 1;
+    m.exist[s.frag_atoms[f_dead][0]] = 1;
+    if (!del) e_prev = dihedral_energy(s, m.r.data(), m.exist.data());
+    return place_fragments(cc, ibox(), m, slot, order, 0, placed, del, gp->kappa_dih, e_prev, ln_pbias, rng);
+  }
+
+  // Cut_N_Grow (move_regrow.f90)
+  void regrow() {
+    orc_ctx* cc = c();
+    const Box& b = cc->box[ibox()];
+    Rng& rng = mc.rng;
+    const int nmols = mc.nmols(is);
+    if (nmols == 0) return;
+    (void)rng.next();  // the box choice
+    (void)rng.next();  // the species choice
+    const int im = std::min((int)(rng.next() * nmols) + 1, nmols);
+    const int slot = cc->members[ibox()][cc->sp_off[ibox()][is] + im - 1];
+    Mol& m = cc->mol[slot];
+    const Species& s = cc->sp[is];
+    ++res.n_regrow;
+    if (s.nfrag < 2) return;  // single-fragment regrowth is not on this path
+    const std::vector<double> r_old(m.r);
+    const double com_old[3] = {m.com[0], m.com[1], m.com[2]}, dcom_old = m.max_dcom;
+    std::vector<int> order;
+    int f_live = 0, f_dead = 0;
+    double e_prev = 0.0, ln_pfor = 0.0, ln_prev = 0.0;
+    bool ov = cut_regrow(m, slot, false, order, f_live, f_dead, e_prev, ln_pfor);
+    std::fill(m.exist.begin(), m.exist.end(), 1);
+    refresh_com(cc, m);
+    fold_molecule(b, m);
+    auto revert = [&]() {  // Revert_Old_Cartesian_Coordinates
+      m.r = r_old;
+      std::copy(com_old, com_old + 3, m.com);
+      m.max_dcom = dcom_old;
+    };
+    if (ov) {
+      revert();
+      return;
+    }
+    double eb_n, ea_n, ed_n, ei_n, eiv_n, eiq_n, ev_n, eq_n;
+    if (mol_energies(m, slot, eb_n, ea_n, ed_n, ei_n, eiv_n, eiq_n, ev_n, eq_n)) {
+      revert();
+      return;
+    }
+    double dE_intra = eb_n + ea_n + ed_n + ei_n + eiq_n + eiv_n;
+    double dE_inter = eq_n + ev_n;
+    const std::vector<double> r_new(m.r);
+    const double com_new[3] = {m.com[0], m.com[1], m.com[2]}, dcom_new = m.max_dcom;
+    revert();
+    ov = cut_regrow(m, slot, true, order, f_live, f_dead, e_prev, ln_prev);
+    std::fill(m.exist.begin(), m.exist.end(), 1);
+    if (ov) {
+      mc.err = fail(CASS_ESTATE, "molecule energy too high for a regrowth");
+      return;
+    }
+    refresh_com(cc, m);
+    double eb_o, ea_o, ed_o, ei_o, eiv_o, eiq_o, ev_o, eq_o;
+    mol_energies(m, slot, eb_o, ea_o, ed_o, ei_o, eiv_o, eiq_o, ev_o, eq_o);
+    dE_intra = dE_intra - eb_o - ea_o - ed_o - ei_o - eiq_o - eiv_o;
+    dE_inter = dE_inter - eq_o - ev_o;
+    const double dE = dE_intra + dE_inter;
+    const double dE_frag = ea_n - ea_o;
+    const double ln_pacc = b.beta * (dE - dE_frag) + ln_pfor - ln_prev;
+    if (!accept_or_reject(ln_pacc, rng)) return;
+    m.r = r_new;
+    std::copy(com_new, com_new + 3, m.com);
+    m.max_dcom = dcom_new;
+    CassEnergy& E = mc.E;
+    E.total += dE;
+    E.intra += dE_intra;
+    E.inter += dE_inter;
+    E.bond += eb_n - eb_o;
+    E.angle += ea_n - ea_o;
+    E.dihedral += ed_n - ed_o;
+    E.improper += ei_n - ei_o;
+    E.intra_vdw += eiv_n - eiv_o;
+    E.intra_q += eiq_n - eiq_o;
+    E.inter_vdw += ev_n - ev_o;
+    E.inter_q += eq_n - eq_o;
+    ++res.n_regrow_accepted;
+  }
+
+  void run() {
+    for (int64_t k = 0; k < gp->nsteps && mc.err == CASS_OK; ++k) {
+      const double u = mc.rng.next();  // gcmc_driver.f90:30
+      if (u <= gp->cut_translate) mc.translate();
+      else if (u <= gp->cut_rotate) mc.rotate();
+      else if (u <= gp->cut_insert) insert();
+      else if (u <= gp->cut_delete) remove();
+      else if (u <= gp->cut_regrow) regrow();
+      res.sum_n_molecules += (double)mc.nmols(is);
+    }
+    res.n_translate = mc.res.n_translate;
+    res.n_translate_accepted = mc.res.n_translate_accepted;
+    res.n_rotate = mc.res.n_rotate;
+    res.n_rotate_accepted = mc.res.n_rotate_accepted;
+    res.n_molecules = mc.nmols(is);
+    res.energy = mc.E;
+  }
+};
+
 }  // namespace
 
 extern "C" {
@@ -2017,6 +2657,105 @@ int orc_mc_sweeps(orc_ctx* c, int32_t nboxes, const int32_t* iboxes, const CassM
     out[k] = ch.res;
     errs[k] = ch.err;
     if (ch.err) msgs[k] = g_err;
+  }
+  for (int k = 0; k < nboxes; ++k)
+    if (errs[k]) return fail(errs[k], msgs[k]);
+  return CASS_OK;
+}
+
+// Grand-canonical Monte Carlo, one chain per box (boxes in parallel)
+int orc_gcmc(orc_ctx* c, int32_t nboxes, const int32_t* iboxes, const CassGCMCParams* p, const double* mu,
+             const double* max_disp, const double* max_rot, uint64_t seed, CassGCMCResult* out) {
+  if (c) refresh_members(c);
+  if (check_ctx(c) || nboxes < 1 || !iboxes || !p || !mu || !max_disp || !max_rot || !out || p->nsteps < 0 ||
+      p->is_exchange < 1 || p->is_exchange > c->nspecies || p->kappa_ins < 1)
+    return fail(CASS_EINVAL, "bad gcmc arguments");
+  const int is = p->is_exchange - 1;
+  const Species& s = c->sp[is];
+  if (!s.defined || s.nfrag < 1) return fail(CASS_ESTATE, "exchanged species not defined or without fragments");
+  if (s.nfrag > 1 && p->kappa_dih < 1) return fail(CASS_EINVAL, "kappa_dih must be >= 1");
+  for (int k = 0; k < nboxes; ++k) {
+    const int ib = iboxes[k] - 1;
+    if (ib < 0 || ib >= c->nboxes) return fail(CASS_EINVAL, "box index");
+    for (int j = 0; j < k; ++j)
+      if (iboxes[j] == iboxes[k]) return fail(CASS_EINVAL, "box listed twice");
+    if (!c->box[ib].energy_valid) return fail(CASS_ESTATE, "system energy of box not computed");
+    if (c->box[ib].charge_style != CASS_CHARGE_NONE) return fail(CASS_EUNSUPPORTED, "gcmc boxes hold no charges");
+  }
+  // free slots of the exchanged species, dealt to the boxes in turn
+  std::vector<std::vector<int>> pools(nboxes);
+  int nfree = 0;
+  for (int im = 0; im < c->max_mol[is]; ++im) {
+    const int slot = c->mol_base[is] + im;
+    if (c->mol[slot].live) continue;
+    pools[nfree % nboxes].push_back(slot);
+    ++nfree;
+  }
+  // fragment bonds (f, g), f < g, and prob_del1 (input_routines.f90:3035-3120)
+  std::vector<int> fa, fb;
+  std::vector<double> pd1;
+  for (int f = 0; f < s.nfrag; ++f)
+    for (int g : s.frag_connect[f])
+      if (g > f) {
+        fa.push_back(f);
+        fb.push_back(g);
+        int ndel[2];
+        for (int side = 0; side < 2; ++side) {
+          const int f1 = side ? g : f, f2 = side ? f : g;
+          std::vector<int> live(s.nfrag, 0), order{f1};
+          live[f2] = 1;
+          live[f1] = 1;
+          // every fragment reached from f1 without crossing f2 (the set Fragment_Order visits)
+          for (size_t q = 0; q < order.size(); ++q)
+            for (int h : s.frag_connect[order[q]])
+              if (!live[h]) {
+                live[h] = 1;
+                order.push_back(h);
+              }
+          ndel[side] = 0;
+          for (int h : order) ndel[side] += (int)s.frag_atoms[h].size() - 2;
+        }
+        pd1.push_back((double)ndel[1] / (double)(ndel[0] + ndel[1]));
+      }
+  double mw = 0.0;
+  for (double m : s.mass) mw += m;
+  std::vector<int> errs(nboxes, CASS_OK);
+  std::vector<std::string> msgs(nboxes);
+  std::vector<double> md((size_t)nboxes * c->nspecies), mr((size_t)nboxes * c->nspecies);
+  std::copy(max_disp, max_disp + md.size(), md.begin());
+  std::copy(max_rot, max_rot + mr.size(), mr.begin());
+  CassMCParams mp{};
+  mp.nupdate = 0;
+  mp.target_accept = 0.5;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int k = 0; k < nboxes; ++k) {
+    const int ib = iboxes[k] - 1;
+    const Box& b = c->box[ib];
+    GcmcChain g;
+    g.mc.c = c;
+    g.mc.ibox = ib;
+    g.mc.p = &mp;
+    g.mc.max_disp = md.data() + (size_t)k * c->nspecies;
+    g.mc.max_rot = mr.data() + (size_t)k * c->nspecies;
+    g.mc.rng = seed_stream(seed, iboxes[k], 0);
+    g.mc.E = b.energy;
+    g.mc.nt_disp.assign(c->nspecies, 0);
+    g.mc.ns_disp.assign(c->nspecies, 0);
+    g.mc.nt_rot.assign(c->nspecies, 0);
+    g.mc.ns_rot.assign(c->nspecies, 0);
+    g.is = is;
+    g.gp = p;
+    g.mu = mu[k] / ATOMIC_TO_KJMOL;
+    g.log_lambda3 = 3.0 * std::log(H_PLANK * std::sqrt(b.beta / (TWOPI * mw)));
+    g.pool = pools[k];
+    g.frag_bond_a = fa;
+    g.frag_bond_b = fb;
+    g.prob_del1 = pd1;
+    g.run();
+    c->box[ib].energy = g.mc.E;
+    out[k] = g.res;
+    errs[k] = g.mc.err;
+    if (g.mc.err) msgs[k] = g_err;
   }
   for (int k = 0; k < nboxes; ++k)
     if (errs[k]) return fail(errs[k], msgs[k]);

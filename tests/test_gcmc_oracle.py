@@ -1,0 +1,59 @@
+"""The CPU oracle's grand-canonical chains (move_insert.f90, move_delete.f90,
+move_regrow.f90): energy bookkeeping against a recomputed system energy, and
+the ideal-chain limit <N> = V exp(beta mu) <W> / Lambda^3 with <W> from Widom
+insertions of the same oracle."""
+import math
+
+import numpy as np
+
+from cassandra_gb300 import workloads
+from oracle import oracle
+
+KBOLTZ = 0.8314472
+H_PLANK = 39.9031268605
+
+
+def test_gcmc_bookkeeping_all_moves():
+    s = workloads.gcmc_system(nboxes=2, length=25.0, max_per_box=300)
+    with oracle.open_system(s) as o:
+        for b in (1, 2):
+            o.system_total_energy(b)
+        r = o.gcmc([1, 2], 3000, 1, [-22.0, -26.0], [[1.0], [1.0]], [[0.5], [0.5]], seed=3)
+        for k, x in enumerate(r):
+            for kind in ("translate", "rotate", "insert", "delete", "regrow"):
+                assert x[f"n_{kind}"] > 0
+            assert x["n_insert_accepted"] > 0 and x["n_regrow_accepted"] > 0
+            e, ov = o.system_total_energy(k + 1)
+            assert not ov
+            for comp in ("total", "inter_vdw", "angle", "dihedral", "lrc"):
+                assert abs(x["energy"][comp] - e[comp]) <= 1e-9 * (abs(e["inter_vdw"]) + 1.0), comp
+
+
+def test_gcmc_ideal_chain_matches_widom():
+    s = workloads.gcmc_system(nboxes=2, length=30.0, max_per_box=400, eps_scale=0.0, rcut_low=1e-3)
+    T = s.boxes[0].temperature
+    beta = 1.0 / (KBOLTZ * T)
+    mw = sum(a.mass for a in s.species[0].atoms)
+    lam = H_PLANK * math.sqrt(beta / (2 * math.pi * mw))
+    V = s.boxes[0].volume
+    with oracle.open_system(s) as o:
+        for b in (1, 2):
+            o.system_total_energy(b)
+        _, tr = o.widom_insert(1, [1, 2], 20000, 12, 12, seed=5, trace=True)
+        w = tr["widom_var"].mean()
+        target = 20.0
+        mu = math.log(target * lam ** 3 / (V * w)) / beta * 0.01
+        r = o.gcmc([1, 2], 100000, 1, [mu, mu], [[1.0], [1.0]], [[0.5], [0.5]], seed=3,
+                   cuts=(0.0, 0.0, 0.5, 1.0, 1.0))
+    mean_n = np.mean([x["sum_n_molecules"] / 100000 for x in r])
+    assert abs(mean_n - target) < 0.5, mean_n
+
+
+def test_gcmc_deterministic():
+    s = workloads.gcmc_system(nboxes=1, length=25.0, max_per_box=200)
+    out = []
+    for _ in range(2):
+        with oracle.open_system(s) as o:
+            o.system_total_energy(1)
+            out.append(o.gcmc([1], 500, 1, [-24.0], [[1.0]], [[0.5]], seed=9))
+    assert out[0] == out[1]

@@ -1,0 +1,63 @@
+"""Device grand-canonical chains (cass_gcmc) against the CPU oracle's chains.
+
+The FP64 kernel draws the same lfsr258 numbers in the same order as the
+oracle, so over short runs both make the same decisions and agree in counts,
+molecule numbers and energies.  The mixed kernel (FP32 pair energies against
+the box) follows its own chain; its running energy must match a recomputation
+of its final state."""
+import numpy as np
+import pytest
+
+import cassandra_gb300 as cg
+from cassandra_gb300 import abi, workloads
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+KEYS = ("n_translate", "n_translate_accepted", "n_rotate", "n_rotate_accepted", "n_insert", "n_insert_accepted",
+        "n_delete", "n_delete_accepted", "n_regrow", "n_regrow_accepted", "n_molecules")
+
+
+def _run(open_ctx, s, nsteps, seed, mu=(-22.0, -26.0)):
+    with open_ctx(s) as g:
+        for b in (1, 2):
+            g.system_total_energy(b)
+        r = g.gcmc([1, 2], nsteps, 1, list(mu), [[1.0], [1.0]], [[0.5], [0.5]], seed=seed)
+        again = [g.system_total_energy(b)[0] for b in (1, 2)]
+    return r, again
+
+
+def test_fp64_gcmc_matches_oracle():
+    s = workloads.gcmc_system(nboxes=2, length=25.0, max_per_box=300)
+    ro, eo = _run(oracle.open_system, s, 600, seed=4)
+    rg, eg = _run(lambda x: cg.open_system(x, precision=abi.PREC_FP64), s, 600, seed=4)
+    for a, b in zip(ro, rg):
+        for k in KEYS:
+            assert a[k] == b[k], (k, a[k], b[k])
+        assert abs(a["sum_n_molecules"] - b["sum_n_molecules"]) < 1e-9
+        scale = abs(a["energy"]["inter_vdw"]) + abs(a["energy"]["dihedral"]) + 1.0
+        for k, v in a["energy"].items():
+            assert abs(b["energy"][k] - v) <= 1e-9 * scale, (k, v, b["energy"][k])
+    for x, e in zip(rg, eg):  # the device's running energy against a recomputation of its final state
+        assert abs(x["energy"]["total"] - e["total"]) <= 1e-9 * (abs(e["inter_vdw"]) + 1.0)
+
+
+def test_mixed_gcmc_bookkeeping():
+    s = workloads.gcmc_system(nboxes=2, length=25.0, max_per_box=300)
+    r, again = _run(lambda x: cg.open_system(x, precision=abi.PREC_MIXED), s, 3000, seed=8)
+    for x, e in zip(r, again):
+        assert x["n_insert_accepted"] > 0 and x["n_regrow_accepted"] > 0
+        scale = abs(e["inter_vdw"]) + abs(e["angle"]) + abs(e["dihedral"])
+        assert abs(x["energy"]["total"] - e["total"]) <= 1e-6 * scale, (x["energy"]["total"], e["total"])
+
+
+def test_gcmc_errors():
+    s = workloads.gcmc_system(nboxes=1, length=25.0, max_per_box=5)
+    with cg.open_system(s, precision=abi.PREC_FP64) as g:
+        with pytest.raises(abi.CassError) as e:
+            g.gcmc([1], 10, 1, [-20.0], [[1.0]], [[0.5]], seed=1)
+        assert e.value.code == abi.CASS_ESTATE
+        g.system_total_energy(1)
+        with pytest.raises(abi.CassError) as e:  # five free slots run out at a high chemical potential
+            g.gcmc([1], 5000, 1, [-10.0], [[1.0]], [[0.5]], seed=1, cuts=(0.0, 0.0, 1.0, 1.0, 1.0))
+        assert e.value.code == abi.CASS_ECAPACITY
