@@ -13,7 +13,9 @@ e2e   : the same metric through the public API with host buffers: upload the
         frame, system energies of every box, Widom batch, results back.
 Also reported: the plain-FP64 GPU path on the same workload, the roofline of
 the Widom kernel, and the CPU FP64 oracle (OpenMP, all host cores) on a
-bounded sample.  `--impl reference` times the CPU restatement of the
+bounded sample; NVT MC sweeps/s (500 LJ spheres, 256 waters), grand-canonical
+butane moves/s in 16 boxes with densities against FP64 reruns, and the
+configuration gradient of 4096 waters.  `--impl reference` times the CPU restatement of the
 reference's algorithm (the reference itself is Fortran and cannot be built
 here) on the same workload.
 """
@@ -53,6 +55,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-mc", action="store_true", help="skip the MC-sweep leg")
     p.add_argument("--no-grad", action="store_true", help="skip the configuration-gradient leg")
+    p.add_argument("--no-gcmc", action="store_true", help="skip the grand-canonical leg")
     return p.parse_args()
 
 
@@ -204,6 +207,103 @@ def mc_leg(cg, abi, dev, with_cpu: bool) -> dict:
     if with_cpu:
         out["lj500_translate"]["cpu_baseline"] = cpu(c0, 20, 1.0)
         out["water256_translate_rotate"]["cpu_baseline"] = cpu(c1, 4, 0.5)
+    return out
+
+
+BUTANE_MW = 2 * 15.035 + 2 * 14.027  # g/mol, united-atom CH3-CH2-CH2-CH3
+AVOGADRO = 6.02214076e23
+
+
+def gcmc_leg(cg, abi, dev, with_cpu: bool, eq_steps: int = 60000, blocks: int = 6,
+             block_steps: int = 10000) -> dict:
+    """Grand-canonical butane in 16 boxes of 40 A at 300 K, mu evenly spaced over
+    [-30, -20] kJ/mol, insert/delete 40 %, translate/rotate 40 %, regrow 20 %.
+    Each precision equilibrates from empty boxes, then runs `blocks` production
+    calls whose per-call <N> are block averages; densities of the mixed chains are
+    compared with FP64 reruns of the same boxes through those block errors."""
+    from cassandra_gb300 import workloads
+
+    nb = 16
+    mu = list(np.linspace(-30.0, -20.0, nb))
+    cuts = (0.2, 0.4, 0.6, 0.8, 1.0)
+
+    def chains(precision, boxes_mu, eq, nblk, nstep, seed):
+        n = len(boxes_mu)
+        s = workloads.gcmc_system(nboxes=n, length=40.0, max_per_box=800)
+        boxes = list(range(1, n + 1))
+        md, mr = [[1.0]] * n, [[0.5]] * n
+        g = cg.open_system(s, precision=precision, device=dev)
+        for b in boxes:
+            g.system_total_energy(b)
+        g.gcmc(boxes, eq, 1, boxes_mu, md, mr, seed=seed, cuts=cuts)
+        eq_ms = g.stats()["mc_ms"]
+        means, ms, last = [], 0.0, None
+        for k in range(nblk):
+            last = g.gcmc(boxes, nstep, 1, boxes_mu, md, mr, seed=seed + 1 + k, cuts=cuts)
+            ms += g.stats()["mc_ms"]
+            means.append([r["sum_n_molecules"] / nstep for r in last])
+        means = np.array(means)  # [blocks, boxes]
+        mean_n = means.mean(axis=0)
+        se = means.std(axis=0, ddof=1) / np.sqrt(nblk) if nblk > 1 else np.zeros(n)
+        acc = {k: sum(r[f"n_{k}_accepted"] for r in last) / max(1, sum(r[f"n_{k}"] for r in last))
+               for k in ("translate", "rotate", "insert", "delete", "regrow")}
+        out = {"boxes": n, "equilibration_steps": eq, "production_steps": nblk * nstep,
+               "kernel_ms": ms, "moves_per_s": n * nblk * nstep / (ms / 1e3),
+               "equilibration_moves_per_s": n * eq / (eq_ms / 1e3),
+               "acceptance_last_block": acc, "mean_n": mean_n, "se_n": se}
+        return out, g, s
+
+    def density(n):
+        return float(n * BUTANE_MW / AVOGADRO / (40.0 ** 3 * 1e-24))
+
+    mixed, gm, sysm = chains(abi.PREC_MIXED, mu, eq_steps, blocks, block_steps, seed=11)
+    fp64, gf, _ = chains(abi.PREC_FP64, mu, eq_steps, blocks, block_steps, seed=911)
+    gf.close()
+    z = (mixed["mean_n"] - fp64["mean_n"]) / np.sqrt(np.maximum(mixed["se_n"] ** 2 + fp64["se_n"] ** 2, 1e-12))
+    per_box = [{"mu_kjmol": round(float(m), 4), "mean_n_mixed": float(a), "se_mixed": float(sa),
+                "mean_n_fp64": float(b), "se_fp64": float(sb), "density_g_cm3_mixed": density(a),
+                "density_g_cm3_fp64": density(b), "z": float(zz)}
+               for m, a, sa, b, sb, zz in zip(mu, mixed["mean_n"], mixed["se_n"], fp64["mean_n"], fp64["se_n"], z)]
+    for d in (mixed, fp64):
+        del d["mean_n"], d["se_n"]
+    out = {"workload": "GCMC of united-atom n-butane (CBMC kappa_ins 12, kappa_dih 12) in 16 boxes of 40 A at "
+                       "300 K, mu evenly spaced over [-30, -20] kJ/mol, 14 A cut_tail; insert/delete 40 %, "
+                       "translate/rotate 40 %, regrow 20 %; one CTA per box, all boxes in one launch",
+           "mixed": mixed, "fp64": fp64, "mixed_over_fp64": mixed["moves_per_s"] / fp64["moves_per_s"],
+           "density_check": {"max_abs_z": float(np.max(np.abs(z))), "mean_abs_rel_diff_n": float(
+               np.mean([abs(p["mean_n_mixed"] / max(p["mean_n_fp64"], 1e-9) - 1) for p in per_box])),
+               "note": f"z = (<N>_mixed - <N>_fp64) / combined block standard error ({blocks} blocks of "
+                       f"{block_steps} steps each); independent chains, so |z| ~ N(0,1) when both sample the "
+                       f"same ensemble"},
+           "per_box": per_box}
+    # all SMs busy: 152 boxes (the 16 chemical potentials repeated), mixed precision
+    wide, gw, _ = chains(abi.PREC_MIXED, [mu[k % nb] for k in range(152)], eq_steps // 4, 1, block_steps, seed=77)
+    gw.close()
+    del wide["mean_n"], wide["se_n"]
+    out["mixed_152boxes"] = wide
+    if with_cpu:
+        # the FP64 oracle from the mixed chains' equilibrated state, all boxes, all host threads
+        from oracle import oracle
+        where = gm.molecule_boxes(1)
+        live = [int(k) + 1 for k in np.flatnonzero(where)]
+        xyz = np.concatenate([gm.get_molecule(im, 1).ravel() for im in live])
+        with oracle.open_system(sysm) as o:
+            o.set_molecules(live, [1] * len(live), [int(where[im - 1]) for im in live], xyz)
+            boxes = list(range(1, nb + 1))
+            for b in boxes:
+                o.system_total_energy(b)
+            t0 = time.perf_counter()
+            o.gcmc(boxes, 100, 1, mu, [[1.0]] * nb, [[0.5]] * nb, seed=5, cuts=cuts)
+            per = max(time.perf_counter() - t0, 1e-3) / 100
+            nstep = int(max(200, min(20000, 12.0 / per)))
+            t0 = time.perf_counter()
+            o.gcmc(boxes, nstep, 1, mu, [[1.0]] * nb, [[0.5]] * nb, seed=6, cuts=cuts)
+            dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"moves_per_s": nb * nstep / dt, "cores": min(nb, oracle.num_threads()),
+                               "kind": "port",
+                               "sample": f"{nstep} steps of the 16 chains from the mixed chains' equilibrated "
+                                         f"state, FP64 C++ oracle, boxes in parallel"}
+    gm.close()
     return out
 
 
@@ -464,6 +564,8 @@ def main():
     gctx.close()
     if not args.no_mc:
         out["mc_sweeps"] = mc_leg(cg, abi, dev, rank == 0 and world == 1 and not args.no_cpu_baseline)
+    if not args.no_gcmc:
+        out["gcmc"] = gcmc_leg(cg, abi, dev, rank == 0 and world == 1 and not args.no_cpu_baseline)
     if not args.no_grad:
         out["gradient"] = gradient_leg(cg, abi, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -143,6 +143,7 @@ SIGNATURES = {
     "set_molecules": (C.c_int, [C.c_void_p, C.c_int32, _i32p, _i32p, _i32p, _f64p]),
     "remove_molecule": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "get_molecule": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _f64p]),
+    "get_molecule_boxes": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _i32p]),
     "mol_inter_energy": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _f64p, _f64p, _i32p]),
     "mol_intra_energy": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _f64p, _f64p, _f64p, _i32p]),
     "system_total_energy": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(CassEnergy), _i32p]),
@@ -286,6 +287,12 @@ class Context:
         out = np.zeros(3 * self.natoms[is_])
         self._check("get_molecule", self._f["get_molecule"](self._h, im, is_, _p(out)))
         return out.reshape(-1, 3)
+
+    def molecule_boxes(self, is_: int) -> np.ndarray:
+        """Box of every molecule slot im = 1..max_molecules of species is_ (0: not live)."""
+        out = np.zeros(self.max_molecules[is_ - 1], dtype=np.int32)
+        self._check("get_molecule_boxes", self._f["get_molecule_boxes"](self._h, is_, len(out), _p(out)))
+        return out
 
     # -- energies ------------------------------------------------------
     def mol_inter_energy(self, im: int, is_: int, cbmc: bool = False):

@@ -1144,6 +1144,14 @@ int cass_get_molecule(cass_ctx* c, int32_t im, int32_t is, double* xyz) {
   return CASS_OK;
 }
 
+int cass_get_molecule_boxes(cass_ctx* c, int32_t is, int32_t n, int32_t* which_box) {
+  if (!c || (!which_box && n > 0)) return set_error(CASS_EINVAL, "NULL argument");
+  if (is < 1 || is > c->nspecies) return set_error(CASS_EINVAL, "species index out of range");
+  if (n < 0 || n > c->max_mol[is - 1]) return set_error(CASS_EINVAL, "n out of range");
+  for (int im = 1; im <= n; ++im) which_box[im - 1] = c->mol_box[mol_slot(c, im, is)] + 1;
+  return CASS_OK;
+}
+
 int cass_mol_inter_energy(cass_ctx* c, int32_t im, int32_t is, int32_t cbmc, double* ev, double* eq, int32_t* ov) {
   if (!c || !ev || !eq || !ov) return set_error(CASS_EINVAL, "NULL argument");
   int rc = check_mol(c, im, is);

@@ -187,6 +187,12 @@ int cass_set_molecules(cass_ctx* ctx, int32_t n, const int32_t* im, const int32_
 int cass_remove_molecule(cass_ctx* ctx, int32_t im, int32_t is);
 /* Reads back the coordinates of molecule (im,is). */
 int cass_get_molecule(cass_ctx* ctx, int32_t im, int32_t is, double* xyz);
+/* Box of molecules im = 1..n of species is (molecule_list(im,is)%which_box,
+ * type_definitions.f90:151-153), 0 where the molecule is not live
+ * (molecule_list%live = .FALSE.).  n <= max_molecules[is-1].  Lets the host
+ * rebuild its locate / nmols arrays after cass_gcmc has inserted and deleted
+ * molecules on the device. */
+int cass_get_molecule_boxes(cass_ctx* ctx, int32_t is, int32_t n, int32_t* which_box);
 
 /* ---- energy routines -------------------------------------------------- */
 /* Compute_Molecule_Nonbond_Inter_Energy (energy_routines.f90:1088-1206);

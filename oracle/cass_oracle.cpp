@@ -2308,6 +2308,17 @@ int orc_get_molecule(orc_ctx* c, int32_t im, int32_t is, double* xyz) {
   return CASS_OK;
 }
 
+int orc_get_molecule_boxes(orc_ctx* c, int32_t is, int32_t n, int32_t* which_box) {
+  if (check_ctx(c) || (!which_box && n > 0)) return fail(CASS_EINVAL, "NULL argument");
+  if (is < 1 || is > c->nspecies) return fail(CASS_EINVAL, "species index out of range");
+  if (n < 0 || n > c->max_mol[is - 1]) return fail(CASS_EINVAL, "n out of range");
+  for (int im = 1; im <= n; ++im) {
+    const Mol& m = mol_of(c, is - 1, im - 1);
+    which_box[im - 1] = m.live ? m.ibox + 1 : 0;
+  }
+  return CASS_OK;
+}
+
 int orc_mol_inter_energy(orc_ctx* c, int32_t im, int32_t is, int32_t cbmc, double* ev, double* eq, int32_t* ov) {
   if (c) refresh_members(c);
   int rc = check_ctx(c) ? CASS_EINVAL : check_mol(c, im, is);

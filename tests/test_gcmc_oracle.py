@@ -19,7 +19,10 @@ def test_gcmc_bookkeeping_all_moves():
         for b in (1, 2):
             o.system_total_energy(b)
         r = o.gcmc([1, 2], 3000, 1, [-22.0, -26.0], [[1.0], [1.0]], [[0.5], [0.5]], seed=3)
+        where = o.molecule_boxes(1)
+        assert where.shape == (600,)
         for k, x in enumerate(r):
+            assert int((where == k + 1).sum()) == x["n_molecules"]
             for kind in ("translate", "rotate", "insert", "delete", "regrow"):
                 assert x[f"n_{kind}"] > 0
             assert x["n_insert_accepted"] > 0 and x["n_regrow_accepted"] > 0

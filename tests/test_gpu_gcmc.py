@@ -24,13 +24,20 @@ def _run(open_ctx, s, nsteps, seed, mu=(-22.0, -26.0)):
             g.system_total_energy(b)
         r = g.gcmc([1, 2], nsteps, 1, list(mu), [[1.0], [1.0]], [[0.5], [0.5]], seed=seed)
         again = [g.system_total_energy(b)[0] for b in (1, 2)]
-    return r, again
+        where = g.molecule_boxes(1)
+        for b, x in zip((1, 2), r):
+            assert int((where == b).sum()) == x["n_molecules"]
+        live = np.flatnonzero(where)
+        xyz = np.stack([g.get_molecule(int(k) + 1, 1) for k in live]) if live.size else np.zeros((0, 4, 3))
+    return r, again, (where, xyz)
 
 
 def test_fp64_gcmc_matches_oracle():
     s = workloads.gcmc_system(nboxes=2, length=25.0, max_per_box=300)
-    ro, eo = _run(oracle.open_system, s, 600, seed=4)
-    rg, eg = _run(lambda x: cg.open_system(x, precision=abi.PREC_FP64), s, 600, seed=4)
+    ro, eo, so = _run(oracle.open_system, s, 600, seed=4)
+    rg, eg, sg = _run(lambda x: cg.open_system(x, precision=abi.PREC_FP64), s, 600, seed=4)
+    assert np.array_equal(so[0], sg[0])  # the same molecule slots live in the same boxes
+    assert np.allclose(so[1], sg[1], rtol=0, atol=1e-9)
     for a, b in zip(ro, rg):
         for k in KEYS:
             assert a[k] == b[k], (k, a[k], b[k])
@@ -44,7 +51,7 @@ def test_fp64_gcmc_matches_oracle():
 
 def test_mixed_gcmc_bookkeeping():
     s = workloads.gcmc_system(nboxes=2, length=25.0, max_per_box=300)
-    r, again = _run(lambda x: cg.open_system(x, precision=abi.PREC_MIXED), s, 3000, seed=8)
+    r, again, _ = _run(lambda x: cg.open_system(x, precision=abi.PREC_MIXED), s, 3000, seed=8)
     for x, e in zip(r, again):
         assert x["n_insert_accepted"] > 0 and x["n_regrow_accepted"] > 0
         scale = abs(e["inter_vdw"]) + abs(e["angle"]) + abs(e["dihedral"])
