@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "cass_cbmc.cuh"
+#include "cass_cbmc_f.cuh"
 #include "cass_ctx.h"
 
 namespace cassgpu {
@@ -27,12 +28,12 @@ namespace cassgpu {
 constexpr int kGcThreads = 256;
 constexpr int kGcWarps = kGcThreads / 32;
 constexpr int kGcMaxSpecies = 8;
-constexpr int kGcItems = 256;  // (trial, atom range) items of one batch
 constexpr size_t kGcSmemLimit = 200 * 1024;
 
 struct GcSpecies {
   int natoms, linear;
   double mass[kMaxAtoms];
+  int type[kMaxAtoms];  // nonbond type per atom, -1: none
 };
 
 struct GcArgs {
@@ -47,6 +48,11 @@ struct GcArgs {
   int fb_a[kMaxFrags], fb_b[kMaxFrags];
   double prob_del1[kMaxFrags];
   SpeciesPools P;
+  // FP32 copies for the mixed kernel
+  SpeciesF SF;
+  const float* libf;
+  float prob_del1f[kMaxFrags];
+  float cutf[5];
 };
 
 struct GcBox {
@@ -60,6 +66,10 @@ struct GcBox {
   const double* max_rot;
   double mu, log_lambda3;
   double rcut3, rcut9;    // rcut_vdw^3 and (rcut_vdw^3)^3 of Compute_LR_Correction
+  double lrc_c[kMaxTypes * kMaxTypes];  // 4 eps (sigma^12 / (9 rc^9) - sigma^6 / (3 rc^3)) per type pair
+  double lrc_pref;        // 2 pi / V
+  double log_vol;         // ln V
+  const double* logn;     // ln k, k = 0 .. nrec + 1 (mixed kernel)
   double nb0[kMaxTypes];  // atoms per type at the start
   CassEnergy* energy;
   CassGCMCResult* res;
@@ -74,11 +84,13 @@ struct GrowState {
   int rec, is, na;
   // trial batch
   double trial[kMaxKappa][3 * kMaxAtoms];
+  float trialf[kMaxKappa][3 * kMaxAtoms];  // FP32 copy of the atoms a batch evaluates (mixed kernel)
   int tids[kMaxAtoms], ntid;
   double e[kMaxKappa];
+  float ef[kMaxKappa];
   int ov[kMaxKappa];
-  double part[kGcItems];
-  int povl[kGcItems];
+  double part[kGcWarps * kMaxKappa];  // per-warp trial sums
+  int povl[kGcWarps];                 // per-warp overlap masks
   // growth bookkeeping
   double ln_pseq, ln_pbias, e_prev;
   int order[kMaxFrags], norder;
@@ -96,119 +108,216 @@ struct GrowState {
   int f_live, f_dead;
 };
 
+// The box as a kernel sees it.  Atoms of every record (live molecules and the
+// box's free slots) sit at fixed offsets (roff) in sx/sy/sz; the atoms of the
+// live molecules are also listed compactly in lv (atom index), with apos the
+// inverse map (-1: not listed) and per entry the type (lvt) or, in the mixed
+// kernel, an FP32 copy x, y, z, type bits (lv32).  Pair loops run over lv.
+// lrec holds, per species s from rs0[s], the live records in ascending order.
+// FP32 state of the molecule a mixed-kernel CBMC move grows (shared memory);
+// GrowState holds the integer bookkeeping and the trial batch
+struct GrowF {
+  float r[3 * kMaxAtoms];
+  float com[3];
+  float cfg[3 * kMaxAtoms], hg[9];
+  float theta0;
+  float draws[3 * kMaxKappa];
+  float dn[kMaxKappa], dd[kMaxKappa];
+  float ln_pseq, ln_pbias, e_prev;
+};
+
 struct GcView {
   const BoxDev* b;
   const PairTable* T;
+  const float* epsf;  // FP32 pair table copied to shared memory
+  const float* sig2f;
+  const BoxF* bf;     // FP32 box constants (mixed kernel)
+  const float2* ljp;  // (eps, sigma^2) with row stride kMaxTypes (mixed kernel)
   double *sx, *sy, *sz;
-  int *stype, *srec;
-  int *rlive, *rsp, *roff;
+  int *lv, *apos, *lvt;
+  float4* lv32;
+  int *rlive, *rsp, *roff, *lrec;
+  const int* nlv;
   double* com;
-  float4* s32;
   int natoms, nrec;
 };
 
 // ---------------------------------------------------------------------------
-// block-wide energies of ntr configurations of the atoms gs.tids (taken from
-// gs.trial[t]) against every live atom of records other than skip_rec
+// Sums TG per-lane values over a warp.  The values are halved at each step of
+// a butterfly (the lane keeps one half and adds its partner's copy of it), so
+// TG sums take TG - 1 + log2(32 / TG) shuffles instead of 5 TG.  Returns the
+// warp total of value `which`; every lane gets one, lanes l and l ^ m (m <
+// 32 / TG) the same one.  Fixed order, so the result is deterministic.
+template <int TG>
+__device__ __forceinline__ double warp_multi_sum(double (&v)[TG], int lane, int& which) {
+  which = 0;
+  int off = 16;
+#pragma unroll
+  for (int n = TG; n > 1; n >>= 1) {
+    const bool hi = (lane & off) != 0;
+#pragma unroll
+    for (int u = 0; u < n / 2; ++u) {
+      const double send = hi ? v[u] : v[u + n / 2];
+      const double keep = hi ? v[u + n / 2] : v[u];
+      v[u] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+    }
+    which = 2 * which + (hi ? 1 : 0);
+    off >>= 1;
+  }
+  double s = v[0];
+  for (; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  return s;
+}
 
-template <bool MIXED>
+// Block-wide energies of ntr configurations of the atoms gs.tids (taken from
+// gs.trial[t]) against every listed atom outside the atom range of record
+// skip_rec.  Each lane takes box atoms and evaluates all trials of a group of
+// TG against them, with the sums in registers; the per-warp sums are added
+// in warp order.  gs.e[t] (0 on overlap) and gs.ov[t] on return.
+template <bool MIXED, int TG>
 __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip_rec, bool cbmc,
-                               const int* ttype) {
+                               const int* ttype, bool convert = true) {
   const BoxDev& b = *V.b;
-  const int nch = max(1, kGcWarps / ntr);
-  const int items = ntr * nch;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int it = w; it < items; it += kGcWarps) {
-    const int t = it / nch, ch = it % nch;
-    const int j0 = (int)((long long)V.natoms * ch / nch), j1 = (int)((long long)V.natoms * (ch + 1) / nch);
-    double acc = 0.0;
-    KahanF kacc;
-    int ov = 0;
-    for (int j = j0 + lane; j < j1; j += 32) {
-      const int rj = V.srec[j];
-      if (rj == skip_rec || !V.rlive[rj]) continue;
-      const int tj = V.stype[j];
-      for (int k = 0; k < gs.ntid; ++k) {
-        const int a = gs.tids[k];
-        const int ta = ttype[a];
-        if (MIXED) {
-          const float4 pj = V.s32[j];
-          const float dx = fold((float)gs.trial[t][3 * a] - pj.x, b.hLf[0], b.Lf[0]);
-          const float dy = fold((float)gs.trial[t][3 * a + 1] - pj.y, b.hLf[1], b.Lf[1]);
-          const float dz = fold((float)gs.trial[t][3 * a + 2] - pj.z, b.hLf[2], b.Lf[2]);
-          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          if (r2 < (float)b.rcut_lowsq) {
-            ov = 1;
-            continue;
+  const int ntid = gs.ntid;
+  if (MIXED && convert) {  // else the caller wrote gs.trialf
+    for (int q = threadIdx.x; q < ntr * ntid * 3; q += blockDim.x) {
+      const int t = q / (3 * ntid), r = q % (3 * ntid), a = gs.tids[r / 3];
+      gs.trialf[t][3 * a + r % 3] = (float)gs.trial[t][3 * a + r % 3];
+    }
+    __syncthreads();
+  }
+  int s0 = -1, s1 = -1;
+  if (skip_rec >= 0) {
+    s0 = V.roff[skip_rec];
+    s1 = s0 + gs.na;
+  }
+  const int nlv = *V.nlv;
+  unsigned ovall = 0u;
+  for (int t0 = 0; t0 < ntr; t0 += TG) {
+    double accd[TG];
+    float accf[TG];
+#pragma unroll
+    for (int u = 0; u < TG; ++u) {
+      accd[u] = 0.0;
+      accf[u] = 0.0f;
+    }
+    unsigned ovm = 0u;
+    for (int i = threadIdx.x; i < nlv; i += blockDim.x) {
+      const int j = V.lv[i];
+      if (j >= s0 && j < s1) continue;
+      if (MIXED) {
+        const float4 pj = V.lv32[i];
+        const int tj = __float_as_int(pj.w);
+        const float rlow2 = (float)b.rcut_lowsq, rc2 = cbmc ? (float)b.rcut_cbmcsq : (float)b.rcut_vdwsq;
+        for (int k = 0; k < ntid; ++k) {
+          const int a = gs.tids[k], ta = ttype[a];
+          const bool has = ta >= 0 && tj >= 0;
+          const int kk = has ? pidx(ta, tj, V.T->ntypes) : 0;
+          const float eps = V.epsf[kk], s2 = V.sig2f[kk];
+#pragma unroll
+          for (int u = 0; u < TG; ++u) {
+            if (t0 + u < ntr) {
+              const float* tr = gs.trialf[t0 + u] + 3 * a;
+              const float dx = fold(tr[0] - pj.x, b.hLf[0], b.Lf[0]);
+              const float dy = fold(tr[1] - pj.y, b.hLf[1], b.Lf[1]);
+              const float dz = fold(tr[2] - pj.z, b.hLf[2], b.Lf[2]);
+              const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+              if (r2 < rlow2) ovm |= 1u << u;
+              else if (r2 <= rc2 && has) accf[u] += lj_pair_f(eps, s2, r2);
+            }
           }
-          const float rc2 = cbmc ? (float)b.rcut_cbmcsq : (float)b.rcut_vdwsq;
-          if (r2 <= rc2 && ta >= 0 && tj >= 0) {
-            const int kk = pidx(ta, tj, V.T->ntypes);
-            kacc.add(lj_pair_f(V.T->epsf[kk], V.T->sig2f[kk], r2));
+        }
+      } else {
+        const double xj = V.sx[j], yj = V.sy[j], zj = V.sz[j];
+        const int tj = V.lvt[i];
+        for (int k = 0; k < ntid; ++k) {
+          const int a = gs.tids[k], ta = ttype[a];
+#pragma unroll
+          for (int u = 0; u < TG; ++u) {
+            if (t0 + u < ntr) {
+              const double* tr = gs.trial[t0 + u] + 3 * a;
+              const double dx = fold(tr[0] - xj, b.hL[0], b.L[0]);
+              const double dy = fold(tr[1] - yj, b.hL[1], b.L[1]);
+              const double dz = fold(tr[2] - zj, b.hL[2], b.L[2]);
+              const double r2 = dx * dx + dy * dy + dz * dz;
+              if (r2 < b.rcut_lowsq) ovm |= 1u << u;
+              else if (cutoff_mask(b, r2, cbmc) & 1) accd[u] += vdw_pair(*V.T, b, ta, tj, r2, 1.0);
+            }
           }
-        } else {
-          const double dx = fold(gs.trial[t][3 * a] - V.sx[j], b.hL[0], b.L[0]);
-          const double dy = fold(gs.trial[t][3 * a + 1] - V.sy[j], b.hL[1], b.L[1]);
-          const double dz = fold(gs.trial[t][3 * a + 2] - V.sz[j], b.hL[2], b.L[2]);
-          const double r2 = dx * dx + dy * dy + dz * dz;
-          if (r2 < b.rcut_lowsq) {
-            ov = 1;
-            continue;
-          }
-          if (cutoff_mask(b, r2, cbmc) & 1) acc += vdw_pair(*V.T, b, ta, tj, r2, 1.0);
         }
       }
     }
-    if (MIXED) acc = kacc.value();
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    ov = __any_sync(0xffffffffu, ov);
-    if (lane == 0) {
-      gs.part[it] = acc;
-      gs.povl[it] = ov;
+    if (MIXED) {
+#pragma unroll
+      for (int u = 0; u < TG; ++u) accd[u] = (double)accf[u];
     }
+    int which;
+    const double tot = warp_multi_sum<TG>(accd, lane, which);
+    if ((lane & (32 / TG - 1)) == 0 && t0 + which < ntr) gs.part[w * kMaxKappa + t0 + which] = tot;
+    ovall |= __reduce_or_sync(0xffffffffu, ovm) << t0;
   }
+  if (lane == 0) gs.povl[w] = (int)ovall;
   __syncthreads();
   if (threadIdx.x < ntr) {
     double e = 0.0;
     int o = 0;
-    for (int ch = 0; ch < nch; ++ch) {
-      e += gs.part[threadIdx.x * nch + ch];
-      o |= gs.povl[threadIdx.x * nch + ch];
+    for (int ww = 0; ww < kGcWarps; ++ww) {
+      e += gs.part[ww * kMaxKappa + threadIdx.x];
+      o |= (gs.povl[ww] >> threadIdx.x) & 1;
     }
     gs.e[threadIdx.x] = o ? 0.0 : e;
+    if (MIXED) gs.ef[threadIdx.x] = o ? 0.0f : (float)e;
     gs.ov[threadIdx.x] = o;
   }
   __syncthreads();
 }
 
-// the k-th (1-based) live molecule of species is in record order; all threads
-__device__ int nth_live(const GcView& V, int is, int k, int* scratch) {
-  const int per = (V.nrec + kGcThreads - 1) / kGcThreads;
-  const int r0 = threadIdx.x * per, r1 = min(V.nrec, r0 + per);
-  int cnt = 0;
-  for (int r = r0; r < r1; ++r) cnt += (V.rlive[r] && V.rsp[r] == is);
-  scratch[threadIdx.x] = cnt;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int acc = 0, found = -1;
-    for (int t = 0; t < kGcThreads && found < 0; ++t) {
-      if (acc + scratch[t] >= k) {
-        int need = k - acc;
-        const int a0 = t * per, a1 = min(V.nrec, a0 + per);
-        for (int r = a0; r < a1; ++r)
-          if (V.rlive[r] && V.rsp[r] == is && --need == 0) {
-            found = r;
-            break;
-          }
-      }
-      acc += scratch[t];
-    }
-    scratch[kGcThreads] = found;
+// the live-atom list and the sorted live records (thread 0)
+template <bool MIXED>
+__device__ void list_add(const GcView& V, int* nlv, int r, int na, const int* types) {
+  for (int a = 0; a < na; ++a) {
+    const int j = V.roff[r] + a, i = (*nlv)++;
+    V.apos[j] = i;
+    V.lv[i] = j;
+    if (MIXED) V.lv32[i] = make_float4((float)V.sx[j], (float)V.sy[j], (float)V.sz[j], __int_as_float(types[a]));
+    else V.lvt[i] = types[a];
   }
-  __syncthreads();
-  const int r = scratch[kGcThreads];
-  __syncthreads();
-  return r;
+}
+
+template <bool MIXED>
+__device__ void list_remove(const GcView& V, int* nlv, int r, int na) {
+  for (int a = 0; a < na; ++a) {
+    const int j = V.roff[r] + a, i = V.apos[j], last = --(*nlv);
+    if (i != last) {
+      const int jl = V.lv[last];
+      V.lv[i] = jl;
+      V.apos[jl] = i;
+      if (MIXED) V.lv32[i] = V.lv32[last];
+      else V.lvt[i] = V.lvt[last];
+    }
+    V.apos[j] = -1;
+  }
+}
+
+// n: live records of the species before the change
+__device__ void lrec_insert(int* lrec, int base, int n, int r) {
+  int p = n;
+  while (p > 0 && lrec[base + p - 1] > r) {
+    lrec[base + p] = lrec[base + p - 1];
+    --p;
+  }
+  lrec[base + p] = r;
+}
+
+__device__ void lrec_remove(int* lrec, int base, int n, int r) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (lrec[base + mid] < r) lo = mid + 1;
+    else hi = mid;
+  }
+  for (int p = lo; p + 1 < n; ++p) lrec[base + p] = lrec[base + p + 1];
 }
 
 __device__ __forceinline__ bool gc_accept(double ln_pacc, Lfsr& rng) {
@@ -416,7 +525,7 @@ __device__ bool gc_place_fragments(const GcArgs& A, const GcView& V, GrowState& 
         if ((gs.newex >> a) & 1u) gs.tids[gs.ntid++] = a;
     }
     __syncthreads();
-    batch_energies<MIXED>(V, gs, kd, gs.rec, true, S.type);
+    batch_energies<MIXED, 16>(V, gs, kd, gs.rec, true, S.type);
     if (threadIdx.x == 0) {
       const double beta = b.beta;
       double w[kMaxKappa];
@@ -538,7 +647,7 @@ __device__ bool gc_build(const GcArgs& A, const GcView& V, GrowState& gs, bool d
       for (int d = 0; d < 3; ++d) gs.trial[it][3 * a + d] = gs.r[3 * a + d] - gs.com[d] + gs.draws[3 * it + d];
     }
   __syncthreads();
-  batch_energies<MIXED>(V, gs, ki, gs.rec, true, S.type);
+  batch_energies<MIXED, 16>(V, gs, ki, gs.rec, true, S.type);
   if (threadIdx.x == 0) {
     const double beta = b.beta;
     double w[kMaxKappa];
@@ -596,7 +705,7 @@ __device__ void gc_mol_energies(const GcArgs& A, const GcView& V, GrowState& gs,
     }
   }
   __syncthreads();
-  batch_energies<MIXED>(V, gs, 1, gs.rec, false, ttype);
+  batch_energies<MIXED, 2>(V, gs, 1, gs.rec, false, ttype);
   if (threadIdx.x == 0) {
     IntraOut io{0, 0, 0, 0, 0, 0, 0, false};
     if (with_intra) io = molecule_intra(A.P, gs.is, *V.b, *V.T, gs.r);
@@ -614,69 +723,542 @@ __device__ void gc_mol_energies(const GcArgs& A, const GcView& V, GrowState& gs,
   __syncthreads();
 }
 
-__device__ double gc_lrc(const BoxDev& b, const PairTable& T, const double* nb, double rcut3, double rcut9) {
+// Compute_LR_Correction (energy_routines.f90:2956-3023) for type counts nb,
+// with the per-pair coefficients computed on the host
+__device__ double gc_lrc(const GcBox& G, int ntypes, const double* nb) {
   double e = 0.0;
-  for (int ia = 0; ia < T.ntypes; ++ia) {
+  for (int ia = 0; ia < ntypes; ++ia) {
     double eij = 0.0;
-    for (int ja = 0; ja < T.ntypes; ++ja) {
-      const double eps = T.eps[pidx(ia, ja, T.ntypes)], s2 = T.sig2[pidx(ia, ja, T.ntypes)];
-      const double s6 = s2 * s2 * s2, s12 = s6 * s6;
-      eij = eij + nb[ja] * 4.0 * eps * (s12 / (9.0 * rcut9) - (s6 / (3.0 * rcut3)));
-    }
+    for (int ja = 0; ja < ntypes; ++ja) eij = eij + nb[ja] * G.lrc_c[ia * ntypes + ja];
     e = e + nb[ia] * eij;
   }
-  return 2.0 * kPI * e / b.volume;
+  return G.lrc_pref * e;
+}
+
+
+// ---------------------------------------------------------------------------
+// FP32 CBMC growth of the mixed kernel: the steps of gc_fragment_order,
+// gc_place_fragments and gc_build with FP32 geometry, draws (top 23 bits of
+// the same lfsr258 numbers), trial intramolecular energies and Boltzmann
+// weights (shifted by the lowest trial energy).  ln P_bias is accumulated in
+// FP32; the acceptance exponent it enters is formed in FP64.
+
+// weights of k trials with energies u (ovm: overlapping trials), the rule
+// "rand * sum < cumulative sum" with pick = rand (pick < 0: no draw, trial 0)
+// and ln of the weight sum shifted by the lowest energy: returns the trial,
+// -1 if all overlap; *dlnw = beta (U_sel - U_min) + ln sum exp(-beta (U - U_min))
+__device__ __forceinline__ int gc_select_f(int k, const float* u, unsigned ovm, float beta, Lfsr& rng, bool del,
+                                           float* dlnw) {
+  float umin = 3.0e38f;
+  for (int t = 0; t < k; ++t)
+    if (!((ovm >> t) & 1u)) umin = fminf(umin, u[t]);
+  if (umin == 3.0e38f) return -1;
+  float w[kMaxKappa];
+  float cum = 0.0f;
+  for (int t = 0; t < k; ++t) {
+    cum += ((ovm >> t) & 1u) ? 0.0f : __expf(-beta * (u[t] - umin));
+    w[t] = cum;
+  }
+  int sel = 0;
+  if (!del) {
+    const float x = draw_f(rng) * cum;
+    while (sel < k && !(x < w[sel])) ++sel;
+    if (sel == k) return -1;
+  }
+  *dlnw = beta * (u[sel] - umin) + __logf(cum);
+  return sel;
+}
+
+// Fragment_Order (fragment_growth.f90:1317-1446), FP32; thread 0
+__device__ void gc_fragment_order_f(const WidomSpecies& S, GrowState& gs, GrowF& g, unsigned live, Lfsr& rng) {
+  const int f0 = gs.order[0];
+  int hang[kMaxFrags];
+  int nh = 0;
+  for (int k = 0; k < S.frag_nconnect[f0]; ++k) {
+    const int f = S.frag_connect[f0][k];
+    if (!((live >> f) & 1u)) hang[nh++] = f;
+  }
+  while (nh > 0) {
+    float tot = 0.0f;
+    for (int k = 0; k < nh; ++k) tot += (float)(S.frag_natoms[hang[k]] - 2);
+    const float u = draw_f(rng);
+    int k = 0;
+    float cum = 0.0f;
+    for (; k < nh; ++k) {
+      cum += (float)(S.frag_natoms[hang[k]] - 2) / tot;
+      if (u < cum) break;
+    }
+    if (k >= nh) k = nh - 1;
+    const int f = hang[k];
+    if (nh > 1) g.ln_pseq += __logf((float)(S.frag_natoms[f] - 2) / tot);
+    gs.order[gs.norder++] = f;
+    live |= 1u << f;
+    for (int q = k; q + 1 < nh; ++q) hang[q] = hang[q + 1];
+    --nh;
+    for (int q = 0; q < S.frag_nconnect[f]; ++q) {
+      const int h = S.frag_connect[f][q];
+      if (!((live >> h) & 1u) && nh < kMaxFrags) hang[nh++] = h;
+    }
+  }
+}
+
+// Cut_Regrow (fragment_growth.f90:1118-1312) masks; thread 0
+__device__ void gc_cut_f(const WidomSpecies& S, GrowState& gs, GrowF& g) {
+  gs.exist = (1u << S.natoms) - 1u;
+  gs.placed = (1u << S.nfrag) - 1u;
+  for (int k = 0; k < gs.norder; ++k) {
+    const int f = gs.order[k];
+    gs.placed &= ~(1u << f);
+    for (int j = 0; j < S.frag_natoms[f]; ++j) gs.exist &= ~(1u << S.frag_atoms[f][j]);
+  }
+  gs.exist |= 1u << S.frag_atoms[gs.f_live][0];
+  gs.exist |= 1u << S.frag_atoms[gs.f_dead][0];
+  g.ln_pbias = 0.0f;
+  gs.flag = 0;
+}
+
+// Fragment_Placement (fragment_growth.f90:1449-2132) for gs.order[first..], FP32; all threads
+__device__ bool gc_place_fragments_f(const GcArgs& A, const GcView& V, GrowState& gs, GrowF& g, int first, bool del,
+                                     Lfsr& rng) {
+  const WidomSpecies& S = A.S;
+  const SpeciesF& F = A.SF;
+  const BoxF& bf = *V.bf;
+  const int kd = S.kappa_dih;
+  for (int oi = first; oi < gs.norder; ++oi) {
+    if (threadIdx.x == 0) {
+      const int f = gs.order[oi];
+      const int nf = S.frag_natoms[f];
+      const unsigned grown = gs.exist;
+      for (int i = 0; i < 3 * kMaxAtoms; ++i) g.cfg[i] = 0.0f;
+      if (del) {
+        for (int j = 0; j < nf; ++j) {
+          const int a = S.frag_atoms[f][j];
+          gs.exist |= 1u << a;
+          for (int d = 0; d < 3; ++d) g.cfg[3 * a + d] = g.r[3 * a + d];
+        }
+      } else {
+        const int nconf = S.nconfig[f];
+        int cf = (int)(draw_f(rng) * (float)nconf);
+        cf = (int)(draw_f(rng) * (float)nconf);  // the duplicated draw of fragment_growth.f90:1578,1584
+        if (cf >= nconf) cf = nconf - 1;
+        const float* L = A.libf + S.lib_off[f] + (size_t)cf * nf * 3;
+        for (int j = 0; j < nf; ++j) {
+          const int a = S.frag_atoms[f][j];
+          gs.exist |= 1u << a;
+          for (int d = 0; d < 3; ++d) g.cfg[3 * a + d] = L[3 * j + d];
+        }
+      }
+      gs.combined = gs.exist;
+      gs.newex = gs.combined & ~grown;
+      int fc = -1;
+      for (int q = 0; q < S.frag_nconnect[f]; ++q) {
+        const int h = S.frag_connect[f][q];
+        if ((gs.placed >> h) & 1u) {
+          fc = h;
+          break;
+        }
+      }
+      gs.flag = fc < 0 ? 1 : 0;
+      if (fc >= 0) {
+        const int anc_i = S.frag_atoms[f][0], anc_c = S.frag_atoms[fc][0];
+        gs.anc_i = anc_i;
+        gs.anc_c = anc_c;
+        gs.ntid = 0;
+        gs.idmask = 0u;
+        for (int j = 0; j < nf; ++j) {
+          const int a = S.frag_atoms[f][j];
+          if (a != anc_i && a != anc_c) {
+            gs.tids[gs.ntid++] = a;
+            gs.idmask |= 1u << a;
+          }
+        }
+        const int atom_ifrag = gs.ntid > 0 ? gs.tids[0] : S.frag_atoms[f][nf - 1];
+        int atom_fc = S.frag_atoms[fc][S.frag_natoms[fc] - 1];
+        for (int j = 0; j < S.frag_natoms[fc]; ++j) {
+          const int a = S.frag_atoms[fc][j];
+          if (a != anc_i && a != anc_c) {
+            atom_fc = a;
+            break;
+          }
+        }
+        float v1[3], v2[3], al_i[9], hg_i[9], al_c[9], hg_c[9];
+        for (int d = 0; d < 3; ++d) {
+          v1[d] = g.cfg[3 * anc_i + d] - g.cfg[3 * anc_c + d];
+          v2[d] = g.cfg[3 * atom_ifrag + d] - g.cfg[3 * anc_c + d];
+        }
+        aligner_hanger_f(v1, v2, al_i, hg_i);
+        if (!del) {
+          for (int d = 0; d < 3; ++d) {
+            v1[d] = g.r[3 * anc_i + d] - g.r[3 * anc_c + d];
+            v2[d] = g.r[3 * atom_fc + d] - g.r[3 * anc_c + d];
+          }
+          aligner_hanger_f(v1, v2, al_c, hg_c);
+        }
+        const float tx = g.cfg[3 * anc_c], ty = g.cfg[3 * anc_c + 1], tz = g.cfg[3 * anc_c + 2];
+        for (int j = 0; j < nf; ++j) {
+          const int a = S.frag_atoms[f][j];
+          const float x = g.cfg[3 * a] - tx, y = g.cfg[3 * a + 1] - ty, z = g.cfg[3 * a + 2] - tz;
+          g.cfg[3 * a] = x * al_i[0] + y * al_i[1] + z * al_i[2];
+          g.cfg[3 * a + 1] = x * al_i[3] + y * al_i[4] + z * al_i[5];
+          g.cfg[3 * a + 2] = x * al_i[6] + y * al_i[7] + z * al_i[8];
+        }
+        if (del) {
+          g.theta0 = 0.0f;
+          for (int i = 0; i < 9; ++i) g.hg[i] = hg_i[i];
+        } else {
+          g.theta0 = (float)kTWOPI * draw_f(rng);
+          for (int i = 0; i < 9; ++i) g.hg[i] = hg_c[i];
+        }
+      }
+    }
+    __syncthreads();
+    if (gs.flag) return true;
+    // trial geometry, intramolecular and dihedral energies: trial ii on lane ii of warp 0
+    if (threadIdx.x < kd) {
+      const int ii = threadIdx.x;
+      const float theta = g.theta0 + (float)ii * ((float)kTWOPI / (float)kd);
+      float sth, cth;
+      sincosf(theta, &sth, &cth);
+      float r[3 * kMaxAtoms];
+      for (int i = 0; i < 3 * S.natoms; ++i) r[i] = g.r[i];
+      const int f = gs.order[oi];
+      const float ax = g.r[3 * gs.anc_c], ay = g.r[3 * gs.anc_c + 1], az = g.r[3 * gs.anc_c + 2];
+      for (int j = 0; j < S.frag_natoms[f]; ++j) {
+        const int a = S.frag_atoms[f][j];
+        if (a == gs.anc_i || a == gs.anc_c) continue;
+        const float x = g.cfg[3 * a], y = g.cfg[3 * a + 1], z = g.cfg[3 * a + 2];
+        const float yr = cth * y + sth * z, zr = -sth * y + cth * z;
+        r[3 * a] = (x * g.hg[0] + yr * g.hg[1] + zr * g.hg[2]) + ax;
+        r[3 * a + 1] = (x * g.hg[3] + yr * g.hg[4] + zr * g.hg[5]) + ay;
+        r[3 * a + 2] = (x * g.hg[6] + yr * g.hg[7] + zr * g.hg[8]) + az;
+      }
+      for (int i = 0; i < 3 * S.natoms; ++i) gs.trialf[ii][i] = r[i];
+      unsigned ex = gs.combined & ~gs.idmask;
+      float niv = 0.0f, niq = 0.0f, noq = 0.0f;
+      bool ov = false;
+      for (int k = 0; k < gs.ntid && !ov; ++k) {
+        ex |= 1u << gs.tids[k];
+        float eiv, eiq, eoq;
+        ov = atom_intra_f(F, bf, V.ljp, gs.tids[k], r, ex, eiv, eiq, eoq);
+        niv += eiv;
+        niq += eiq;
+        noq += eoq;
+      }
+      gs.dov[ii] = ov ? 1 : 0;
+      g.dd[ii] = ov ? 0.0f : dihedral_f(F, r, gs.combined);
+      g.dn[ii] = niv + niq + noq;  // completed with the inter and dihedral energies below
+    }
+    __syncthreads();
+    // inter energies of the new atoms (Compute_Molecule_Nonbond_Inter_Energy with new_exist)
+    if (threadIdx.x == 0) {
+      gs.ntid = 0;
+      for (int a = 0; a < S.natoms; ++a)
+        if ((gs.newex >> a) & 1u) gs.tids[gs.ntid++] = a;
+    }
+    __syncthreads();
+    batch_energies<true, 16>(V, gs, kd, gs.rec, true, S.type, false);
+    if (threadIdx.x == 0) {
+      unsigned ovm = 0u;
+      float u[kMaxKappa];
+      for (int ii = 0; ii < kd; ++ii) {
+        u[ii] = 0.0f;
+        bool ov = gs.dov[ii] || gs.ov[ii];
+        if (!ov) {
+          u[ii] = g.dd[ii] + g.dn[ii] + gs.ef[ii] - g.e_prev;
+          if (u[ii] >= bf.kmaxE) ov = true;
+        }
+        if (ov) {
+          ovm |= 1u << ii;
+          gs.dov[ii] = 1;
+        }
+      }
+      float dlnw = 0.0f;
+      const int tr = gc_select_f(kd, u, ovm, bf.beta, rng, del, &dlnw);
+      if (tr < 0) {
+        gs.flag = 1;
+      } else {
+        g.ln_pbias = g.ln_pbias - dlnw;
+        const int f = gs.order[oi];
+        for (int j = 0; j < S.frag_natoms[f]; ++j) {
+          const int a = S.frag_atoms[f][j];
+          if (a != gs.anc_i && a != gs.anc_c)
+            for (int d = 0; d < 3; ++d) g.r[3 * a + d] = gs.trialf[tr][3 * a + d];
+        }
+        g.e_prev = g.dd[tr];
+        gs.placed |= 1u << f;
+        gs.exist = gs.combined;
+      }
+    }
+    __syncthreads();
+    if (gs.flag) return true;
+  }
+  return false;
+}
+
+// Build_Molecule (fragment_growth.f90:72-707) for record gs.rec, FP32; all threads
+__device__ bool gc_build_f(const GcArgs& A, const GcView& V, GrowState& gs, GrowF& g, bool del, Lfsr& rng) {
+  const WidomSpecies& S = A.S;
+  const SpeciesF& F = A.SF;
+  const BoxF& bf = *V.bf;
+  const int ki = S.kappa_ins;
+  if (threadIdx.x == 0) {
+    g.ln_pbias = 0.0f;
+    gs.exist = 0u;
+    gs.flag = 0;
+    const float u = draw_f(rng);
+    int fstart = 0;
+    while (fstart < S.nfrag && !(u < F.cum_prob_ins[fstart])) ++fstart;
+    if (fstart >= S.nfrag) fstart = S.nfrag - 1;
+    g.ln_pseq = (float)S.ln_prob_ins[fstart];
+    gs.order[0] = fstart;
+    gs.norder = 1;
+    if (S.nfrag > 1) gc_fragment_order_f(S, gs, g, 1u << fstart, rng);
+    const int nfa = S.frag_natoms[fstart];
+    if (!del) {
+      const int nconf = S.nconfig[fstart];
+      int conf = (int)(draw_f(rng) * (float)nconf);
+      if (conf >= nconf) conf = nconf - 1;
+      const float* L0 = A.libf + S.lib_off[fstart] + (size_t)conf * nfa * 3;
+      for (int i = 0; i < nfa; ++i)
+        for (int d = 0; d < 3; ++d) g.r[3 * S.frag_atoms[fstart][i] + d] = L0[3 * i + d];
+    }
+    gs.ntid = nfa;
+    for (int i = 0; i < nfa; ++i) {
+      gs.tids[i] = S.frag_atoms[fstart][i];
+      gs.exist |= 1u << gs.tids[i];
+    }
+    get_com_f(F, g.r, gs.exist, g.com);
+    if (!del) {  // Rotate_Molecule_Eulerian
+      const float theta = acosf(1.0f - 2.0f * draw_f(rng));
+      const float phi = (1.0f - 2.0f * draw_f(rng)) * (float)kPI;
+      const float psi = (1.0f - 2.0f * draw_f(rng)) * (float)kPI;
+      float st, ct, sp, cp, ss, cs;
+      sincosf(theta, &st, &ct);
+      sincosf(phi, &sp, &cp);
+      sincosf(psi, &ss, &cs);
+      const float r11 = cs * cp - ct * sp * ss, r12 = cs * sp + ct * cp * ss, r13 = ss * st;
+      const float r21 = -ss * cp - ct * sp * cs, r22 = -ss * sp + ct * cp * cs, r23 = cs * st;
+      const float r31 = st * sp, r32 = -st * cp, r33 = ct;
+      for (int i = 0; i < nfa; ++i) {
+        const int a = gs.tids[i];
+        const float x = g.r[3 * a] - g.com[0], y = g.r[3 * a + 1] - g.com[1], z = g.r[3 * a + 2] - g.com[2];
+        g.r[3 * a] = (r11 * x + r12 * y + r13 * z) + g.com[0];
+        g.r[3 * a + 1] = (r21 * x + r22 * y + r23 * z) + g.com[1];
+        g.r[3 * a + 2] = (r31 * x + r32 * y + r33 * z) + g.com[2];
+      }
+    }
+    for (int it = 0; it < ki; ++it) {
+      if (del && it == 0) {
+        g.draws[0] = g.com[0];
+        g.draws[1] = g.com[1];
+        g.draws[2] = g.com[2];
+      } else {
+        g.draws[3 * it] = (0.5f - draw_f(rng)) * bf.L[0];
+        g.draws[3 * it + 1] = (0.5f - draw_f(rng)) * bf.L[1];
+        g.draws[3 * it + 2] = (0.5f - draw_f(rng)) * bf.L[2];
+      }
+    }
+  }
+  __syncthreads();
+  // trial positions: rtrial(0) - COM + anchor
+  for (int q = threadIdx.x; q < ki * gs.ntid; q += blockDim.x) {
+    const int it = q / gs.ntid, a = gs.tids[q % gs.ntid];
+    for (int d = 0; d < 3; ++d) gs.trialf[it][3 * a + d] = g.r[3 * a + d] - g.com[d] + g.draws[3 * it + d];
+  }
+  __syncthreads();
+  batch_energies<true, 16>(V, gs, ki, gs.rec, true, S.type, false);
+  if (threadIdx.x == 0) {
+    unsigned ovm = 0u;
+    float u[kMaxKappa];
+    for (int it = 0; it < ki; ++it) {
+      u[it] = gs.ef[it];
+      if (gs.ov[it] || u[it] >= bf.kmaxE) ovm |= 1u << it;
+    }
+    float dlnw = 0.0f;
+    const int sel = gc_select_f(ki, u, ovm, bf.beta, rng, del, &dlnw);
+    if (sel < 0) {
+      gs.flag = 1;
+    } else {
+      g.ln_pbias = g.ln_pbias - dlnw;
+      for (int k = 0; k < gs.ntid; ++k) {
+        const int a = gs.tids[k];
+        for (int d = 0; d < 3; ++d) g.r[3 * a + d] = gs.trialf[sel][3 * a + d];
+      }
+      for (int d = 0; d < 3; ++d) g.com[d] = g.draws[3 * sel + d];
+      g.e_prev = dihedral_f(F, g.r, gs.exist);
+      gs.placed = 1u << gs.order[0];
+    }
+  }
+  __syncthreads();
+  if (gs.flag) return true;
+  if (gc_place_fragments_f(A, V, gs, g, 1, del, rng)) return true;
+  if (threadIdx.x == 0 && gs.norder > 1) get_com_f(F, g.r, gs.exist, g.com);
+  __syncthreads();
+  return false;
+}
+
+// energies of the whole molecule g.r (record gs.rec), FP32 geometry: inter
+// (full cutoffs, block-wide) plus intra and bonded (thread 0); out[0..7] as
+// gc_mol_energies
+__device__ void gc_mol_energies_f(const GcArgs& A, const GcView& V, GrowState& gs, GrowF& g, const int* ttype,
+                                  double* out, int* ovs) {
+  if (threadIdx.x == 0) {
+    gs.ntid = gs.na;
+    for (int a = 0; a < gs.na; ++a) {
+      gs.tids[a] = a;
+      for (int d = 0; d < 3; ++d) gs.trialf[0][3 * a + d] = g.r[3 * a + d];
+    }
+  }
+  __syncthreads();
+  batch_energies<true, 2>(V, gs, 1, gs.rec, false, ttype, false);
+  if (threadIdx.x == 0) {
+    const IntraF io = molecule_intra_f(A.SF, *V.bf, V.ljp, g.r);
+    out[0] = gs.e[0];
+    out[1] = io.pqq;
+    out[2] = io.bond;
+    out[3] = io.angle;
+    out[4] = io.dih;
+    out[5] = io.imp;
+    out[6] = io.ivdw;
+    out[7] = io.iqq;
+    ovs[0] = gs.ov[0];
+    ovs[1] = io.overlap ? 1 : 0;
+  }
+  __syncthreads();
+}
+
+// Fold_Molecule of g (FP32); thread 0
+__device__ __forceinline__ void gc_fold_f(const BoxF& bf, GrowF& g, int na) {
+  for (int k = 0; k < 3; ++k) {
+    float sh = 0.0f;
+    if (g.com[k] > bf.hL[k]) sh = -bf.L[k];
+    else if (g.com[k] < -bf.hL[k]) sh = bf.L[k];
+    if (sh != 0.0f) {
+      g.com[k] += sh;
+      for (int a = 0; a < na; ++a) g.r[3 * a + k] += sh;
+    }
+  }
+}
+
+// min((int)(u n) + 1, n) for a uniform draw u (the molecule pick of the
+// move routines); the mixed kernel takes u from the top 23 bits
+template <bool MIXED>
+__device__ __forceinline__ int gc_pick(Lfsr& rng, int n) {
+  if constexpr (MIXED) return min((int)(draw_f(rng) * (float)n) + 1, n);
+  else return min((int)(rng.next() * n) + 1, n);
+}
+
+// a draw whose value is not used (the box and species choices of the reference)
+template <bool MIXED>
+__device__ __forceinline__ void gc_skip_draw(Lfsr& rng) {
+  if constexpr (MIXED) rng.next_bits();
+  else (void)rng.next();
 }
 
 template <bool MIXED>
-__global__ void __launch_bounds__(kGcThreads) k_gcmc(GcArgs A, GcBox* boxes, PairTable T) {
+__global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, PairTable T) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ BoxDev b;
   __shared__ GrowState gs;
-  __shared__ int scratch[kGcThreads + 1];
   __shared__ double em[10];
   __shared__ int eov[2];
-  __shared__ int mv_kind, mv_rec, mv_skip, mv_acc, mv_stop;
+  __shared__ int mv_kind, mv_rec, mv_is, mv_skip, mv_acc, mv_stop, s_nlv;
+  __shared__ int rs0[kGcMaxSpecies];
   __shared__ double old_r[3 * kMaxAtoms], old_com[3];
   __shared__ int ttype[kMaxAtoms];
+  __shared__ float s_epsf[kMaxTypes * kMaxTypes], s_sig2f[kMaxTypes * kMaxTypes];
   __shared__ double rg_new[3 * kMaxAtoms], rg_new_com[3], rg_en[8], rg_e_prev, rg_ln_pfor;
+  __shared__ GrowF gf;
+  __shared__ BoxF bf;
+  __shared__ float2 s_ljp[kMaxTypes * kMaxTypes];
+  __shared__ float rgf_new[3 * kMaxAtoms], rgf_new_com[3], rgf_e_prev, rgf_ln_pfor;
   GcBox& G = boxes[blockIdx.x];
-  if (threadIdx.x == 0) b = G.b;
+  if (threadIdx.x == 0) {
+    b = G.b;
+    if (MIXED) {  // FP32 box constants
+      for (int d = 0; d < 3; ++d) {
+        bf.L[d] = (float)G.b.L[d];
+        bf.hL[d] = (float)G.b.hL[d];
+        bf.cinv[d] = 0.0f;
+        bf.nc[d] = 1;
+      }
+      bf.rcb2 = (float)G.b.rcut_cbmcsq;
+      bf.rv2 = (float)G.b.rcut_vdwsq;
+      bf.rq2 = (float)G.b.rcut_coulsq;
+      bf.low2 = (float)G.b.rcut_lowsq;
+      bf.rc_cbmc = (float)sqrt(G.b.rcut_cbmcsq);
+      bf.rc_full = (float)sqrt(G.b.rcut_vdwsq);
+      bf.beta = (float)G.b.beta;
+      bf.kmaxE = (float)(kMAX_KBT / G.b.beta);
+      bf.alpha = (float)G.b.alpha;
+      bf.charge_on = 0;
+    }
+  }
+  for (int i = threadIdx.x; i < kMaxTypes * kMaxTypes; i += blockDim.x) {
+    const int ta = i / kMaxTypes, tb = i % kMaxTypes;
+    const bool ok = ta < T.ntypes && tb < T.ntypes;
+    s_ljp[i] = ok ? make_float2(T.epsf[ta * T.ntypes + tb], T.sig2f[ta * T.ntypes + tb]) : make_float2(0.f, 0.f);
+  }
   const int N = G.natoms, R = G.nrec;
   double* sx = reinterpret_cast<double*>(smem);
   double* sy = sx + N;
   double* sz = sy + N;
   double* scom = sz + N;  // [R][3]
-  int* stype = reinterpret_cast<int*>(scom + 3 * R);
-  int* srec = stype + N;
-  int* rlive = srec + N;
+  int* lv = reinterpret_cast<int*>(scom + 3 * R);
+  int* apos = lv + N;
+  int* lvt = apos + N;  // FP64 kernel only
+  int* rlive = lvt + (MIXED ? 0 : N);
   int* rsp = rlive + R;
   int* roff = rsp + R;
   int* pool = roff + R;
-  float4* s32 = reinterpret_cast<float4*>(reinterpret_cast<unsigned char*>(smem) +
-                                          ((((size_t)(pool + R) - (size_t)smem) + 15) & ~(size_t)15));
+  int* lrec = pool + R;
+  float4* lv32 = reinterpret_cast<float4*>(reinterpret_cast<unsigned char*>(smem) +
+                                           ((((size_t)(lrec + R) - (size_t)smem) + 15) & ~(size_t)15));
   for (int j = threadIdx.x; j < N; j += blockDim.x) {
     const double4_32a p = G.xyzq[j];
     sx[j] = p.x;
     sy[j] = p.y;
     sz[j] = p.z;
-    stype[j] = G.atype[j];
-    if (MIXED) {
-      int tb = G.atype[j];
-      float tf;
-      memcpy(&tf, &tb, sizeof(float));
-      s32[j] = make_float4((float)p.x, (float)p.y, (float)p.z, tf);
-    }
+    apos[j] = -1;
   }
   for (int r = threadIdx.x; r < R; r += blockDim.x) {
     const int4 ri = G.rec[r];
     rlive[r] = ri.w;
     rsp[r] = ri.y;
     roff[r] = ri.z;
-    for (int a = 0; a < A.sp[ri.y].natoms; ++a) srec[ri.z + a] = r;
   }
   for (int k = threadIdx.x; k < G.npool; k += blockDim.x) pool[k] = G.pool[k];
+  for (int k = threadIdx.x; k < kMaxTypes * kMaxTypes; k += blockDim.x) {
+    s_epsf[k] = T.epsf[k];
+    s_sig2f[k] = T.sig2f[k];
+  }
   __syncthreads();
+  if (threadIdx.x == 0) {
+    // the list of live atoms (record order) and the sorted live records per
+    // species (records are in slot order, so each species is one range)
+    int n = 0;
+    for (int k = 0; k < kGcMaxSpecies; ++k) rs0[k] = 0;
+    for (int r = R - 1; r >= 0; --r) rs0[rsp[r]] = r;
+    int cnt[kGcMaxSpecies] = {0};
+    for (int r = 0; r < R; ++r) {
+      if (!rlive[r]) continue;
+      const int sp = rsp[r];
+      lrec[rs0[sp] + cnt[sp]++] = r;
+      for (int a = 0; a < A.sp[sp].natoms; ++a) {
+        const int j = roff[r] + a;
+        apos[j] = n;
+        lv[n++] = j;
+      }
+    }
+    s_nlv = n;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < s_nlv; i += blockDim.x) {
+    const int j = lv[i];
+    const int tj = G.atype[j];
+    if (MIXED) lv32[i] = make_float4((float)sx[j], (float)sy[j], (float)sz[j], __int_as_float(tj));
+    else lvt[i] = tj;
+  }
   for (int r = threadIdx.x; r < R; r += blockDim.x) {  // Get_COM
     const GcSpecies& s = A.sp[rsp[r]];
     double tm = 0, x = 0, y = 0, z = 0;
@@ -695,16 +1277,23 @@ __global__ void __launch_bounds__(kGcThreads) k_gcmc(GcArgs A, GcBox* boxes, Pai
   GcView V;
   V.b = &b;
   V.T = &T;
+  V.epsf = s_epsf;
+  V.sig2f = s_sig2f;
+  V.bf = &bf;
+  V.ljp = s_ljp;
   V.sx = sx;
   V.sy = sy;
   V.sz = sz;
-  V.stype = stype;
-  V.srec = srec;
+  V.lv = lv;
+  V.apos = apos;
+  V.lvt = lvt;
+  V.lv32 = lv32;
   V.rlive = rlive;
   V.rsp = rsp;
   V.roff = roff;
+  V.lrec = lrec;
+  V.nlv = &s_nlv;
   V.com = scom;
-  V.s32 = s32;
   V.natoms = N;
   V.nrec = R;
   // thread-0 state
@@ -712,6 +1301,7 @@ __global__ void __launch_bounds__(kGcThreads) k_gcmc(GcArgs A, GcBox* boxes, Pai
   CassEnergy E;
   CassGCMCResult RS;
   int npool = G.npool, status = 0;
+  long long sum_n = 0;
   int nmol[kGcMaxSpecies];
   double nb[kMaxTypes];
   if (threadIdx.x == 0) {
@@ -729,11 +1319,15 @@ __global__ void __launch_bounds__(kGcThreads) k_gcmc(GcArgs A, GcBox* boxes, Pai
   for (long long step = 0; step < A.nsteps; ++step) {
     // ---- move kind (gcmc_driver.f90:30) and the molecule
     if (threadIdx.x == 0) {
-      const double u = rng.next();
-      mv_kind = u <= A.cut_t ? 0 : (u <= A.cut_r ? 1 : (u <= A.cut_i ? 2 : (u <= A.cut_d ? 3 : (u <= A.cut_g ? 4 : 5))));
+      if constexpr (MIXED) {
+        const float u = draw_f(rng);
+        mv_kind = u <= A.cutf[0] ? 0 : (u <= A.cutf[1] ? 1 : (u <= A.cutf[2] ? 2 : (u <= A.cutf[3] ? 3 : (u <= A.cutf[4] ? 4 : 5))));
+      } else {
+        const double u = rng.next();
+        mv_kind = u <= A.cut_t ? 0 : (u <= A.cut_r ? 1 : (u <= A.cut_i ? 2 : (u <= A.cut_d ? 3 : (u <= A.cut_g ? 4 : 5))));
+      }
       mv_skip = 0;
       mv_stop = 0;
-      scratch[kGcThreads] = 0;
       int is = -1, im = 0;
       if (mv_kind == 0 || mv_kind == 1) {  // species choice of Translate / Rotate
         const double* step_sz = mv_kind == 0 ? G.max_disp : G.max_rot;
@@ -743,21 +1337,32 @@ __global__ void __launch_bounds__(kGcThreads) k_gcmc(GcArgs A, GcBox* boxes, Pai
         if (ntot == 0) {
           mv_skip = 1;
         } else {
-          const double v = rng.next();
-          double x = 0.0;
           int last = 0;
-          for (int k = 0; k < A.nspecies; ++k) {
-            x = (step_sz[k] > 0.0 ? (double)nmol[k] / (double)ntot : 0.0) + (k > 0 ? x : 0.0);
-            if (step_sz[k] > 0.0 && nmol[k] > 0) last = k;
-            if (is < 0 && v <= x) is = k;
+          if constexpr (MIXED) {
+            const float v = draw_f(rng) * (float)ntot;
+            int cum = 0;
+            for (int k = 0; k < A.nspecies; ++k) {
+              if (!(step_sz[k] > 0.0)) continue;
+              cum += nmol[k];
+              if (nmol[k] > 0) last = k;
+              if (is < 0 && v <= (float)cum) is = k;
+            }
+          } else {
+            const double v = rng.next();
+            double x = 0.0;
+            for (int k = 0; k < A.nspecies; ++k) {
+              x = (step_sz[k] > 0.0 ? (double)nmol[k] / (double)ntot : 0.0) + (k > 0 ? x : 0.0);
+              if (step_sz[k] > 0.0 && nmol[k] > 0) last = k;
+              if (is < 0 && v <= x) is = k;
+            }
           }
           if (is < 0) is = last;
-          im = min((int)(rng.next() * nmol[is]) + 1, nmol[is]);
+          im = gc_pick<MIXED>(rng, nmol[is]);
           if (mv_kind == 0) ++RS.n_translate;
           else ++RS.n_rotate;
         }
       } else if (mv_kind == 2) {
-        (void)rng.next();  // is_rand
+        gc_skip_draw<MIXED>(rng);  // is_rand
         if (npool == 0) {
           mv_stop = 1;
           status = 2;
@@ -766,21 +1371,21 @@ __global__ void __launch_bounds__(kGcThreads) k_gcmc(GcArgs A, GcBox* boxes, Pai
           is = ise;
         }
       } else if (mv_kind == 3) {
-        (void)rng.next();  // is_rand
+        gc_skip_draw<MIXED>(rng);  // is_rand
         if (nmol[ise] == 0) {
           mv_skip = 1;
         } else {
           ++RS.n_delete;
           is = ise;
-          im = min((int)(rng.next() * nmol[ise]) + 1, nmol[ise]);
+          im = gc_pick<MIXED>(rng, nmol[ise]);
         }
       } else if (mv_kind == 4) {
         if (nmol[ise] == 0) {
           mv_skip = 1;
         } else {
-          (void)rng.next();  // the box choice
-          (void)rng.next();  // the species choice
-          im = min((int)(rng.next() * nmol[ise]) + 1, nmol[ise]);
+          gc_skip_draw<MIXED>(rng);  // the box choice
+          gc_skip_draw<MIXED>(rng);  // the species choice
+          im = gc_pick<MIXED>(rng, nmol[ise]);
           is = ise;
           ++RS.n_regrow;
           if (S.nfrag < 2) mv_skip = 1;  // single-fragment regrowth is not on this path
@@ -788,27 +1393,12 @@ __global__ void __launch_bounds__(kGcThreads) k_gcmc(GcArgs A, GcBox* boxes, Pai
       } else {
         mv_skip = 1;
       }
-      scratch[kGcThreads - 1] = is;
-      scratch[kGcThreads - 2] = im;
-    }
-    __syncthreads();
-    if (mv_stop) break;
-    const int is = scratch[kGcThreads - 1], im = scratch[kGcThreads - 2];
-    __syncthreads();
-    if (!mv_skip) {
-      int rec;
-      if (mv_kind == 2) {
-        if (threadIdx.x == 0) mv_rec = pool[npool - 1];  // npool > 0: checked when the move was chosen
-        __syncthreads();
-        rec = mv_rec;
-      } else {
-        rec = nth_live(V, is, im, scratch);
-      }
-      if (rec < 0) {  // the live count and the records disagree: stop the chain
-        if (threadIdx.x == 0) status = 1;
-        break;
-      }
-      if (threadIdx.x == 0) {
+      // the molecule: a free record for an insertion, else the im-th live
+      // molecule of species is in slot order
+      if (!mv_skip && !mv_stop) {
+        const int rec = mv_kind == 2 ? pool[npool - 1] : lrec[rs0[is] + im - 1];
+        mv_rec = rec;
+        mv_is = is;
         gs.rec = rec;
         gs.is = is;
         gs.na = A.sp[is].natoms;
@@ -819,21 +1409,18 @@ __global__ void __launch_bounds__(kGcThreads) k_gcmc(GcArgs A, GcBox* boxes, Pai
         }
         for (int d = 0; d < 3; ++d) gs.com[d] = scom[3 * rec + d];
       }
-      __syncthreads();
+    }
+    __syncthreads();
+    if (mv_stop) break;
+    if (!mv_skip) {
+      const int is = mv_is;
       if (mv_kind <= 1) {
-        // ---- Translate / Rotate: old and trial energies of the molecule
+        // ---- Translate / Rotate: the trial position first (no draw depends on
+        // the old energy), then old and trial energies in one pass
         if (threadIdx.x == 0) {
           for (int i = 0; i < 3 * gs.na; ++i) old_r[i] = gs.r[i];
           for (int d = 0; d < 3; ++d) old_com[d] = gs.com[d];
-        }
-        __syncthreads();
-        gc_mol_energies<MIXED>(A, V, gs, stype + roff[rec], em, eov, false);
-        if (threadIdx.x == 0) {
-          if (eov[0]) {
-            mv_stop = 1;
-            status = 1;
-          } else {
-            em[8] = em[0];  // old inter vdW
+          {
             const double step_sz = mv_kind == 0 ? G.max_disp[is] : G.max_rot[is];
             const GcSpecies& s = A.sp[is];
             if (mv_kind == 0) {
@@ -891,15 +1478,24 @@ __global__ void __launch_bounds__(kGcThreads) k_gcmc(GcArgs A, GcBox* boxes, Pai
               }
             }
           }
+          gs.ntid = gs.na;
+          for (int a = 0; a < gs.na; ++a) {
+            gs.tids[a] = a;
+            for (int d = 0; d < 3; ++d) {
+              gs.trial[0][3 * a + d] = old_r[3 * a + d];
+              gs.trial[1][3 * a + d] = gs.r[3 * a + d];
+            }
+          }
         }
         __syncthreads();
-        if (mv_stop) break;
-        const double ev_old = em[8];
-        gc_mol_energies<MIXED>(A, V, gs, stype + roff[rec], em, eov, false);
+        batch_energies<MIXED, 2>(V, gs, 2, gs.rec, false, A.sp[is].type);
         if (threadIdx.x == 0) {
           mv_acc = 0;
-          if (!eov[0]) {
-            const double dv = em[0] - ev_old;
+          if (gs.ov[0]) {  // the molecule overlapped before the move
+            mv_stop = 1;
+            status = 1;
+          } else if (!gs.ov[1]) {
+            const double dv = gs.e[1] - gs.e[0];
             if (gc_accept(b.beta * dv, rng)) {
               mv_acc = 1;
               E.total = E.total + dv;
@@ -928,237 +1524,485 @@ __global__ void __launch_bounds__(kGcThreads) k_gcmc(GcArgs A, GcBox* boxes, Pai
             for (int d = 0; d < 3; ++d) gs.com[d] = old_com[d];
           }
         }
+        __syncthreads();
+        if (mv_stop) break;
       } else if (mv_kind == 2) {
-        // ---- Insertion
-        const bool ov = gc_build<MIXED>(A, V, gs, false, rng);
-        if (threadIdx.x == 0) {
-          gs.flag = ov ? 1 : 0;
-          gs.ln_pbias = gs.ln_pbias + gs.ln_pseq + S.ln_kappa_ins + S.ln_kappa_dih_term;
-          if (!ov) {  // Fold_Molecule, Get_COM
-            for (int k = 0; k < 3; ++k) {
-              double sh = 0.0;
-              if (gs.com[k] > b.hL[k]) sh = -b.L[k];
-              else if (gs.com[k] < -b.hL[k]) sh = b.L[k];
-              if (sh != 0.0) {
-                gs.com[k] = gs.com[k] + sh;
-                for (int a = 0; a < gs.na; ++a) gs.r[3 * a + k] = gs.r[3 * a + k] + sh;
+        if constexpr (MIXED) {
+          // ---- Insertion (FP32 growth)
+          if (threadIdx.x == 0) mv_acc = 0;
+          const bool ov = gc_build_f(A, V, gs, gf, false, rng);
+          if (threadIdx.x == 0) {
+            gs.flag = ov ? 1 : 0;
+            if (!ov) {
+              gc_fold_f(bf, gf, gs.na);
+              get_com_f(A.SF, gf.r, (1u << gs.na) - 1u, gf.com);
+            }
+          }
+          __syncthreads();
+          if (!gs.flag) {
+            gc_mol_energies_f(A, V, gs, gf, ttype, em, eov);
+            if (threadIdx.x == 0 && !eov[0] && !eov[1]) {
+              const double ev = em[0], eq = em[1];
+              const double eb = em[2], ea = em[3], ed = em[4], ei = em[5], eiv = em[6], eiq = em[7];
+              double dE_inter = ev + eq, dE_intra = eiv + eiq + eb + ea + ed + ei;
+              double nbn[kMaxTypes];
+              for (int t = 0; t < kMaxTypes; ++t) nbn[t] = nb[t];
+              for (int a = 0; a < gs.na; ++a)
+                if (S.type[a] >= 0) nbn[S.type[a]] += 1.0;
+              double e_lrc = E.lrc;
+              const bool tail = b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL;
+              if (tail) {
+                e_lrc = gc_lrc(G, T.ntypes, nbn);
+                dE_inter = dE_inter + e_lrc - E.lrc;
+              }
+              const double dE = dE_intra + dE_inter;
+              const double ln_pbias = (double)(gf.ln_pbias + gf.ln_pseq) + (S.ln_kappa_ins + S.ln_kappa_dih_term);
+              const double ln_pacc = b.beta * (dE - ea - G.mu) + ln_pbias + G.logn[nmol[ise] + 1] + G.log_lambda3 -
+                                     G.log_vol;
+              if (gc_accept(ln_pacc, rng)) {
+                mv_acc = 1;
+                E.total += dE;
+                E.intra += dE_intra;
+                E.inter += dE_inter;
+                E.bond += eb;
+                E.angle += ea;
+                E.dihedral += ed;
+                E.improper += ei;
+                E.intra_vdw += eiv;
+                E.intra_q += eiq;
+                E.inter_vdw += ev;
+                E.inter_q += eq;
+                if (tail) E.lrc = e_lrc;
+                for (int t = 0; t < kMaxTypes; ++t) nb[t] = nbn[t];
+                ++RS.n_insert_accepted;
+                ++nmol[ise];
+                --npool;
+                // the new molecule: coordinates, live lists
+                const int rec = gs.rec;
+                rlive[rec] = 1;
+                for (int a = 0; a < gs.na; ++a) {
+                  const int j = roff[rec] + a;
+                  sx[j] = (double)gf.r[3 * a];
+                  sy[j] = (double)gf.r[3 * a + 1];
+                  sz[j] = (double)gf.r[3 * a + 2];
+                }
+                for (int d = 0; d < 3; ++d) scom[3 * rec + d] = (double)gf.com[d];
+                lrec_insert(lrec, rs0[ise], nmol[ise] - 1, rec);
+                for (int a = 0; a < gs.na; ++a) {
+                  const int j = roff[rec] + a, i = s_nlv++;
+                  apos[j] = i;
+                  lv[i] = j;
+                  lv32[i] = make_float4(gf.r[3 * a], gf.r[3 * a + 1], gf.r[3 * a + 2], __int_as_float(S.type[a]));
+                }
               }
             }
-            get_com(S, gs.r, (1u << gs.na) - 1u, gs.com);
+          }
+        } else {
+          // ---- Insertion
+          const bool ov = gc_build<MIXED>(A, V, gs, false, rng);
+          if (threadIdx.x == 0) {
+            gs.flag = ov ? 1 : 0;
+            gs.ln_pbias = gs.ln_pbias + gs.ln_pseq + S.ln_kappa_ins + S.ln_kappa_dih_term;
+            if (!ov) {  // Fold_Molecule, Get_COM
+              for (int k = 0; k < 3; ++k) {
+                double sh = 0.0;
+                if (gs.com[k] > b.hL[k]) sh = -b.L[k];
+                else if (gs.com[k] < -b.hL[k]) sh = b.L[k];
+                if (sh != 0.0) {
+                  gs.com[k] = gs.com[k] + sh;
+                  for (int a = 0; a < gs.na; ++a) gs.r[3 * a + k] = gs.r[3 * a + k] + sh;
+                }
+              }
+              get_com(S, gs.r, (1u << gs.na) - 1u, gs.com);
+            }
+          }
+          if (threadIdx.x == 0) mv_acc = 0;
+          __syncthreads();
+          if (!gs.flag) {
+            gc_mol_energies<MIXED>(A, V, gs, ttype, em, eov);
+            if (threadIdx.x == 0 && !eov[0] && !eov[1]) {
+              const double ev = em[0], eq = em[1];
+              const double eb = em[2], ea = em[3], ed = em[4], ei = em[5], eiv = em[6], eiq = em[7];
+              double dE_inter = ev + eq, dE_intra = eiv + eiq + eb + ea + ed + ei;
+              double nbn[kMaxTypes];
+              for (int t = 0; t < kMaxTypes; ++t) nbn[t] = nb[t];
+              for (int a = 0; a < gs.na; ++a)
+                if (S.type[a] >= 0) nbn[S.type[a]] += 1.0;
+              double e_lrc = E.lrc;
+              const bool tail = b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL;
+              if (tail) {
+                e_lrc = gc_lrc(G, T.ntypes, nbn);
+                dE_inter = dE_inter + e_lrc - E.lrc;
+              }
+              const double dE = dE_intra + dE_inter;
+              double ln_pacc = b.beta * (dE - ea);
+              ln_pacc = ln_pacc - G.mu * b.beta;
+              ln_pacc = ln_pacc + gs.ln_pbias;
+              ln_pacc = ln_pacc + log((double)(nmol[ise] + 1)) + G.log_lambda3;
+              ln_pacc = ln_pacc - G.log_vol;
+              if (gc_accept(ln_pacc, rng)) {
+                mv_acc = 1;
+                E.total += dE;
+                E.intra += dE_intra;
+                E.inter += dE_inter;
+                E.bond += eb;
+                E.angle += ea;
+                E.dihedral += ed;
+                E.improper += ei;
+                E.intra_vdw += eiv;
+                E.intra_q += eiq;
+                E.inter_vdw += ev;
+                E.inter_q += eq;
+                if (tail) E.lrc = e_lrc;
+                for (int t = 0; t < kMaxTypes; ++t) nb[t] = nbn[t];
+                ++RS.n_insert_accepted;
+                ++nmol[ise];
+                --npool;
+              }
+            }
+          }
+          if (threadIdx.x == 0 && mv_acc) {
+            rlive[gs.rec] = 1;
+            lrec_insert(lrec, rs0[ise], nmol[ise] - 1, gs.rec);
+            list_add<MIXED>(V, &s_nlv, gs.rec, gs.na, S.type);  // coordinates follow in the commit below
           }
         }
-        if (threadIdx.x == 0) mv_acc = 0;
-        __syncthreads();
-        if (!gs.flag) {
-          gc_mol_energies<MIXED>(A, V, gs, ttype, em, eov);
-          if (threadIdx.x == 0 && !eov[0] && !eov[1]) {
+      } else if (mv_kind == 3) {
+        if constexpr (MIXED) {
+          // ---- Deletion (FP32 old-weight pass from the stored coordinates)
+          if (threadIdx.x == 0) {
+            mv_acc = 0;
+            for (int i = 0; i < 3 * gs.na; ++i) gf.r[i] = (float)gs.r[i];
+            for (int d = 0; d < 3; ++d) gf.com[d] = (float)gs.com[d];
+          }
+          __syncthreads();
+          const bool ov = gc_build_f(A, V, gs, gf, true, rng);
+          if (threadIdx.x == 0) {
+            gs.flag = ov ? 1 : 0;
+            if (ov) {
+              mv_stop = 1;
+              status = 1;
+            }
+            get_com_f(A.SF, gf.r, (1u << gs.na) - 1u, gf.com);
+          }
+          __syncthreads();
+          if (mv_stop) break;
+          gc_mol_energies_f(A, V, gs, gf, ttype, em, eov);
+          if (threadIdx.x == 0) {
             const double ev = em[0], eq = em[1];
             const double eb = em[2], ea = em[3], ed = em[4], ei = em[5], eiv = em[6], eiq = em[7];
-            double dE_inter = ev + eq, dE_intra = eiv + eiq + eb + ea + ed + ei;
+            double dE_inter = -ev - eq;
+            double dE_intra = -eb - ea - ed - ei - eiv - eiq;
             double nbn[kMaxTypes];
             for (int t = 0; t < kMaxTypes; ++t) nbn[t] = nb[t];
             for (int a = 0; a < gs.na; ++a)
-              if (S.type[a] >= 0) nbn[S.type[a]] += 1.0;
+              if (S.type[a] >= 0) nbn[S.type[a]] -= 1.0;
             double e_lrc = E.lrc;
             const bool tail = b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL;
             if (tail) {
-              e_lrc = gc_lrc(b, T, nbn, G.rcut3, G.rcut9);
-              dE_inter = dE_inter + e_lrc - E.lrc;
+              e_lrc = gc_lrc(G, T.ntypes, nbn);
+              dE_inter = dE_inter + (e_lrc - E.lrc);
             }
             const double dE = dE_intra + dE_inter;
-            double ln_pacc = b.beta * (dE - ea);
-            ln_pacc = ln_pacc - G.mu * b.beta;
-            ln_pacc = ln_pacc + gs.ln_pbias;
-            ln_pacc = ln_pacc + log((double)(nmol[ise] + 1)) + G.log_lambda3;
-            ln_pacc = ln_pacc - log(b.volume);
+            const double ln_pbias = (double)(gf.ln_pbias + gf.ln_pseq) + (S.ln_kappa_ins + S.ln_kappa_dih_term);
+            const double ln_pacc = b.beta * (dE + ea + G.mu) - ln_pbias - G.logn[nmol[ise]] - G.log_lambda3 +
+                                   G.log_vol;
             if (gc_accept(ln_pacc, rng)) {
               mv_acc = 1;
               E.total += dE;
               E.intra += dE_intra;
               E.inter += dE_inter;
-              E.bond += eb;
-              E.angle += ea;
-              E.dihedral += ed;
-              E.improper += ei;
-              E.intra_vdw += eiv;
-              E.intra_q += eiq;
-              E.inter_vdw += ev;
-              E.inter_q += eq;
+              E.bond -= eb;
+              E.angle -= ea;
+              E.dihedral -= ed;
+              E.improper -= ei;
+              E.intra_vdw -= eiv;
+              E.intra_q -= eiq;
+              E.inter_vdw -= ev;
+              E.inter_q -= eq;
               if (tail) E.lrc = e_lrc;
               for (int t = 0; t < kMaxTypes; ++t) nb[t] = nbn[t];
-              ++RS.n_insert_accepted;
-              ++nmol[ise];
-              --npool;
+              ++RS.n_delete_accepted;
+              --nmol[ise];
+              rlive[gs.rec] = 0;
+              pool[npool++] = gs.rec;
+              lrec_remove(lrec, rs0[ise], nmol[ise] + 1, gs.rec);
+              list_remove<MIXED>(V, &s_nlv, gs.rec, gs.na);
             }
+            // a rejected deletion leaves the stored coordinates as they were
           }
-        }
-        if (threadIdx.x == 0 && mv_acc) rlive[gs.rec] = 1;
-      } else if (mv_kind == 3) {
-        // ---- Deletion
-        const bool ov = gc_build<MIXED>(A, V, gs, true, rng);
-        if (threadIdx.x == 0) {
-          gs.flag = ov ? 1 : 0;
-          if (ov) {
-            mv_stop = 1;
-            status = 1;
-          }
-          gs.ln_pbias = gs.ln_pbias + gs.ln_pseq + S.ln_kappa_ins + S.ln_kappa_dih_term;
-          get_com(S, gs.r, (1u << gs.na) - 1u, gs.com);
-        }
-        __syncthreads();
-        if (mv_stop) break;
-        gc_mol_energies<MIXED>(A, V, gs, ttype, em, eov);
-        if (threadIdx.x == 0) {
-          mv_acc = 0;
-          const double ev = em[0], eq = em[1];
-          const double eb = em[2], ea = em[3], ed = em[4], ei = em[5], eiv = em[6], eiq = em[7];
-          double dE_inter = -ev;
-          double dE_intra = -eb - ea - ed - ei;
-          dE_intra = dE_intra - eiv - eiq;
-          dE_inter = dE_inter - eq;
-          double nbn[kMaxTypes];
-          for (int t = 0; t < kMaxTypes; ++t) nbn[t] = nb[t];
-          for (int a = 0; a < gs.na; ++a)
-            if (S.type[a] >= 0) nbn[S.type[a]] -= 1.0;
-          double e_lrc = E.lrc;
-          const bool tail = b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL;
-          if (tail) {
-            e_lrc = gc_lrc(b, T, nbn, G.rcut3, G.rcut9);
-            dE_inter = dE_inter + (e_lrc - E.lrc);
-          }
-          const double dE = dE_intra + dE_inter;
-          double ln_pacc = b.beta * (dE + ea);
-          ln_pacc = ln_pacc + b.beta * G.mu;
-          ln_pacc = ln_pacc - gs.ln_pbias;
-          ln_pacc = ln_pacc - log((double)nmol[ise]) - G.log_lambda3;
-          ln_pacc = ln_pacc + log(b.volume);
-          if (gc_accept(ln_pacc, rng)) {
-            mv_acc = 1;
-            E.total += dE;
-            E.intra += dE_intra;
-            E.inter += dE_inter;
-            E.bond -= eb;
-            E.angle -= ea;
-            E.dihedral -= ed;
-            E.improper -= ei;
-            E.intra_vdw -= eiv;
-            E.intra_q -= eiq;
-            E.inter_vdw -= ev;
-            E.inter_q -= eq;
-            if (tail) E.lrc = e_lrc;
-            for (int t = 0; t < kMaxTypes; ++t) nb[t] = nbn[t];
-            ++RS.n_delete_accepted;
-            --nmol[ise];
-            rlive[gs.rec] = 0;
-            pool[npool++] = gs.rec;
-          }
-          // a rejected deletion keeps the coordinates its Rosenbluth pass left
-        }
-      } else {
-        // ---- Cut_N_Grow: Cut_Regrow for the new configuration, then for the old one
-        if (threadIdx.x == 0) {
-          mv_acc = 0;
-          for (int i = 0; i < 3 * gs.na; ++i) old_r[i] = gs.r[i];
-          for (int d = 0; d < 3; ++d) old_com[d] = gs.com[d];
-          const int fb = min((int)(rng.next() * A.nfbond), A.nfbond - 1);
-          if (rng.next() < A.prob_del1[fb]) {
-            gs.f_dead = A.fb_a[fb];
-            gs.f_live = A.fb_b[fb];
-          } else {
-            gs.f_dead = A.fb_b[fb];
-            gs.f_live = A.fb_a[fb];
-          }
-          gs.order[0] = gs.f_dead;
-          gs.norder = 1;
-          gs.ln_pseq = 0.0;
-          gc_fragment_order(S, gs, (1u << gs.f_live) | (1u << gs.f_dead), rng);
-          gc_cut(S, gs);
-          rg_e_prev = dihedral_masked(A.P.hdr[S.is0], A.P, gs.r, gs.exist);
-          gs.e_prev = rg_e_prev;
-        }
-        __syncthreads();
-        bool ov = gc_place_fragments<MIXED>(A, V, gs, 0, false, rng, A.lib);
-        if (threadIdx.x == 0) {
-          if (ov) {  // Revert_Old_Cartesian_Coordinates
-            for (int i = 0; i < 3 * gs.na; ++i) gs.r[i] = old_r[i];
-            for (int d = 0; d < 3; ++d) gs.com[d] = old_com[d];
-          } else {  // Get_COM, Fold_Molecule
-            rg_ln_pfor = gs.ln_pbias;
-            get_com(S, gs.r, (1u << gs.na) - 1u, gs.com);
-            for (int k = 0; k < 3; ++k) {
-              double sh = 0.0;
-              if (gs.com[k] > b.hL[k]) sh = -b.L[k];
-              else if (gs.com[k] < -b.hL[k]) sh = b.L[k];
-              if (sh != 0.0) {
-                gs.com[k] = gs.com[k] + sh;
-                for (int a = 0; a < gs.na; ++a) gs.r[3 * a + k] = gs.r[3 * a + k] + sh;
-              }
-            }
-          }
-        }
-        __syncthreads();
-        if (!ov) {
-          gc_mol_energies<MIXED>(A, V, gs, ttype, em, eov);
+        } else {
+          // ---- Deletion
+          const bool ov = gc_build<MIXED>(A, V, gs, true, rng);
           if (threadIdx.x == 0) {
-            if (eov[0]) {
-              ov = true;
-              for (int i = 0; i < 3 * gs.na; ++i) gs.r[i] = old_r[i];
-              for (int d = 0; d < 3; ++d) gs.com[d] = old_com[d];
-            } else {
-              for (int k = 0; k < 8; ++k) rg_en[k] = em[k];
-              for (int i = 0; i < 3 * gs.na; ++i) {
-                rg_new[i] = gs.r[i];
-                gs.r[i] = old_r[i];
-              }
-              for (int d = 0; d < 3; ++d) {
-                rg_new_com[d] = gs.com[d];
-                gs.com[d] = old_com[d];
-              }
-              gc_cut(S, gs);
-              gs.e_prev = rg_e_prev;
-              gs.ln_pbias = 0.0;
-            }
             gs.flag = ov ? 1 : 0;
+            if (ov) {
+              mv_stop = 1;
+              status = 1;
+            }
+            gs.ln_pbias = gs.ln_pbias + gs.ln_pseq + S.ln_kappa_ins + S.ln_kappa_dih_term;
+            get_com(S, gs.r, (1u << gs.na) - 1u, gs.com);
           }
           __syncthreads();
-          if (!gs.flag) {
-            const bool ov_old = gc_place_fragments<MIXED>(A, V, gs, 0, true, rng, A.lib);
+          if (mv_stop) break;
+          gc_mol_energies<MIXED>(A, V, gs, ttype, em, eov);
+          if (threadIdx.x == 0) {
+            mv_acc = 0;
+            const double ev = em[0], eq = em[1];
+            const double eb = em[2], ea = em[3], ed = em[4], ei = em[5], eiv = em[6], eiq = em[7];
+            double dE_inter = -ev;
+            double dE_intra = -eb - ea - ed - ei;
+            dE_intra = dE_intra - eiv - eiq;
+            dE_inter = dE_inter - eq;
+            double nbn[kMaxTypes];
+            for (int t = 0; t < kMaxTypes; ++t) nbn[t] = nb[t];
+            for (int a = 0; a < gs.na; ++a)
+              if (S.type[a] >= 0) nbn[S.type[a]] -= 1.0;
+            double e_lrc = E.lrc;
+            const bool tail = b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL;
+            if (tail) {
+              e_lrc = gc_lrc(G, T.ntypes, nbn);
+              dE_inter = dE_inter + (e_lrc - E.lrc);
+            }
+            const double dE = dE_intra + dE_inter;
+            double ln_pacc = b.beta * (dE + ea);
+            ln_pacc = ln_pacc + b.beta * G.mu;
+            ln_pacc = ln_pacc - gs.ln_pbias;
+            ln_pacc = ln_pacc - log((double)nmol[ise]) - G.log_lambda3;
+            ln_pacc = ln_pacc + G.log_vol;
+            if (gc_accept(ln_pacc, rng)) {
+              mv_acc = 1;
+              E.total += dE;
+              E.intra += dE_intra;
+              E.inter += dE_inter;
+              E.bond -= eb;
+              E.angle -= ea;
+              E.dihedral -= ed;
+              E.improper -= ei;
+              E.intra_vdw -= eiv;
+              E.intra_q -= eiq;
+              E.inter_vdw -= ev;
+              E.inter_q -= eq;
+              if (tail) E.lrc = e_lrc;
+              for (int t = 0; t < kMaxTypes; ++t) nb[t] = nbn[t];
+              ++RS.n_delete_accepted;
+              --nmol[ise];
+              rlive[gs.rec] = 0;
+              pool[npool++] = gs.rec;
+              lrec_remove(lrec, rs0[ise], nmol[ise] + 1, gs.rec);
+              list_remove<MIXED>(V, &s_nlv, gs.rec, gs.na);
+            }
+            // a rejected deletion keeps the coordinates its Rosenbluth pass left
+          }
+        }
+      } else {
+        if constexpr (MIXED) {
+          // ---- Cut_N_Grow (FP32 growth): new configuration, then the old one
+          if (threadIdx.x == 0) {
+            mv_acc = 0;
+            for (int i = 0; i < 3 * gs.na; ++i) gf.r[i] = (float)gs.r[i];
+            for (int d = 0; d < 3; ++d) gf.com[d] = (float)gs.com[d];
+            const int fb = min((int)(draw_f(rng) * (float)A.nfbond), A.nfbond - 1);
+            if (draw_f(rng) < A.prob_del1f[fb]) {
+              gs.f_dead = A.fb_a[fb];
+              gs.f_live = A.fb_b[fb];
+            } else {
+              gs.f_dead = A.fb_b[fb];
+              gs.f_live = A.fb_a[fb];
+            }
+            gs.order[0] = gs.f_dead;
+            gs.norder = 1;
+            gf.ln_pseq = 0.0f;
+            gc_fragment_order_f(S, gs, gf, (1u << gs.f_live) | (1u << gs.f_dead), rng);
+            gc_cut_f(S, gs, gf);
+            rgf_e_prev = dihedral_f(A.SF, gf.r, gs.exist);
+            gf.e_prev = rgf_e_prev;
+          }
+          __syncthreads();
+          bool ov = gc_place_fragments_f(A, V, gs, gf, 0, false, rng);
+          if (threadIdx.x == 0 && !ov) {
+            rgf_ln_pfor = gf.ln_pbias;
+            get_com_f(A.SF, gf.r, (1u << gs.na) - 1u, gf.com);
+            gc_fold_f(bf, gf, gs.na);
+          }
+          __syncthreads();
+          if (!ov) {
+            gc_mol_energies_f(A, V, gs, gf, ttype, em, eov);
             if (threadIdx.x == 0) {
-              if (ov_old) {
-                mv_stop = 1;
-                status = 1;
+              if (eov[0]) {
+                ov = true;
               } else {
-                get_com(S, gs.r, (1u << gs.na) - 1u, gs.com);
+                for (int k = 0; k < 8; ++k) rg_en[k] = em[k];
+                for (int i = 0; i < 3 * gs.na; ++i) {
+                  rgf_new[i] = gf.r[i];
+                  gf.r[i] = (float)gs.r[i];
+                }
+                for (int d = 0; d < 3; ++d) {
+                  rgf_new_com[d] = gf.com[d];
+                  gf.com[d] = (float)gs.com[d];
+                }
+                gc_cut_f(S, gs, gf);
+                gf.e_prev = rgf_e_prev;
               }
+              gs.flag = ov ? 1 : 0;
             }
             __syncthreads();
-            if (mv_stop) break;
+            if (!gs.flag) {
+              const bool ov_old = gc_place_fragments_f(A, V, gs, gf, 0, true, rng);
+              if (threadIdx.x == 0) {
+                if (ov_old) {
+                  mv_stop = 1;
+                  status = 1;
+                } else {
+                  get_com_f(A.SF, gf.r, (1u << gs.na) - 1u, gf.com);
+                }
+              }
+              __syncthreads();
+              if (mv_stop) break;
+              gc_mol_energies_f(A, V, gs, gf, ttype, em, eov);
+              if (threadIdx.x == 0) {
+                const double* en = rg_en;  // ev, eq, eb, ea, ed, ei, eiv, eiq of the new configuration
+                double dE_intra = en[2] + en[3] + en[4] + en[5] + en[7] + en[6];
+                double dE_inter = en[1] + en[0];
+                dE_intra = dE_intra - em[2] - em[3] - em[4] - em[5] - em[7] - em[6];
+                dE_inter = dE_inter - em[1] - em[0];
+                const double dE = dE_intra + dE_inter;
+                const double dE_frag = en[3] - em[3];
+                const double ln_pacc = b.beta * (dE - dE_frag) + (double)(rgf_ln_pfor - gf.ln_pbias);
+                if (gc_accept(ln_pacc, rng)) {
+                  mv_acc = 1;
+                  E.total += dE;
+                  E.intra += dE_intra;
+                  E.inter += dE_inter;
+                  E.bond += en[2] - em[2];
+                  E.angle += en[3] - em[3];
+                  E.dihedral += en[4] - em[4];
+                  E.improper += en[5] - em[5];
+                  E.intra_vdw += en[6] - em[6];
+                  E.intra_q += en[7] - em[7];
+                  E.inter_vdw += en[0] - em[0];
+                  E.inter_q += en[1] - em[1];
+                  ++RS.n_regrow_accepted;
+                  const int rec = gs.rec;
+                  for (int a = 0; a < gs.na; ++a) {
+                    const int j = roff[rec] + a;
+                    sx[j] = (double)rgf_new[3 * a];
+                    sy[j] = (double)rgf_new[3 * a + 1];
+                    sz[j] = (double)rgf_new[3 * a + 2];
+                    const int i = apos[j];
+                    lv32[i] = make_float4(rgf_new[3 * a], rgf_new[3 * a + 1], rgf_new[3 * a + 2], lv32[i].w);
+                  }
+                  for (int d = 0; d < 3; ++d) scom[3 * rec + d] = (double)rgf_new_com[d];
+                }
+              }
+            }
+          }
+        } else {
+          // ---- Cut_N_Grow: Cut_Regrow for the new configuration, then for the old one
+          if (threadIdx.x == 0) {
+            mv_acc = 0;
+            for (int i = 0; i < 3 * gs.na; ++i) old_r[i] = gs.r[i];
+            for (int d = 0; d < 3; ++d) old_com[d] = gs.com[d];
+            const int fb = min((int)(rng.next() * A.nfbond), A.nfbond - 1);
+            if (rng.next() < A.prob_del1[fb]) {
+              gs.f_dead = A.fb_a[fb];
+              gs.f_live = A.fb_b[fb];
+            } else {
+              gs.f_dead = A.fb_b[fb];
+              gs.f_live = A.fb_a[fb];
+            }
+            gs.order[0] = gs.f_dead;
+            gs.norder = 1;
+            gs.ln_pseq = 0.0;
+            gc_fragment_order(S, gs, (1u << gs.f_live) | (1u << gs.f_dead), rng);
+            gc_cut(S, gs);
+            rg_e_prev = dihedral_masked(A.P.hdr[S.is0], A.P, gs.r, gs.exist);
+            gs.e_prev = rg_e_prev;
+          }
+          __syncthreads();
+          bool ov = gc_place_fragments<MIXED>(A, V, gs, 0, false, rng, A.lib);
+          if (threadIdx.x == 0) {
+            if (ov) {  // Revert_Old_Cartesian_Coordinates
+              for (int i = 0; i < 3 * gs.na; ++i) gs.r[i] = old_r[i];
+              for (int d = 0; d < 3; ++d) gs.com[d] = old_com[d];
+            } else {  // Get_COM, Fold_Molecule
+              rg_ln_pfor = gs.ln_pbias;
+              get_com(S, gs.r, (1u << gs.na) - 1u, gs.com);
+              for (int k = 0; k < 3; ++k) {
+                double sh = 0.0;
+                if (gs.com[k] > b.hL[k]) sh = -b.L[k];
+                else if (gs.com[k] < -b.hL[k]) sh = b.L[k];
+                if (sh != 0.0) {
+                  gs.com[k] = gs.com[k] + sh;
+                  for (int a = 0; a < gs.na; ++a) gs.r[3 * a + k] = gs.r[3 * a + k] + sh;
+                }
+              }
+            }
+          }
+          __syncthreads();
+          if (!ov) {
             gc_mol_energies<MIXED>(A, V, gs, ttype, em, eov);
             if (threadIdx.x == 0) {
-              const double* en = rg_en;  // ev, eq, eb, ea, ed, ei, eiv, eiq of the new configuration
-              double dE_intra = en[2] + en[3] + en[4] + en[5] + en[7] + en[6];
-              double dE_inter = en[1] + en[0];
-              dE_intra = dE_intra - em[2] - em[3] - em[4] - em[5] - em[7] - em[6];
-              dE_inter = dE_inter - em[1] - em[0];
-              const double dE = dE_intra + dE_inter;
-              const double dE_frag = en[3] - em[3];
-              const double ln_pacc = b.beta * (dE - dE_frag) + rg_ln_pfor - gs.ln_pbias;
-              if (gc_accept(ln_pacc, rng)) {
-                mv_acc = 1;
-                for (int i = 0; i < 3 * gs.na; ++i) gs.r[i] = rg_new[i];
-                for (int d = 0; d < 3; ++d) gs.com[d] = rg_new_com[d];
-                E.total += dE;
-                E.intra += dE_intra;
-                E.inter += dE_inter;
-                E.bond += en[2] - em[2];
-                E.angle += en[3] - em[3];
-                E.dihedral += en[4] - em[4];
-                E.improper += en[5] - em[5];
-                E.intra_vdw += en[6] - em[6];
-                E.intra_q += en[7] - em[7];
-                E.inter_vdw += en[0] - em[0];
-                E.inter_q += en[1] - em[1];
-                ++RS.n_regrow_accepted;
+              if (eov[0]) {
+                ov = true;
+                for (int i = 0; i < 3 * gs.na; ++i) gs.r[i] = old_r[i];
+                for (int d = 0; d < 3; ++d) gs.com[d] = old_com[d];
+              } else {
+                for (int k = 0; k < 8; ++k) rg_en[k] = em[k];
+                for (int i = 0; i < 3 * gs.na; ++i) {
+                  rg_new[i] = gs.r[i];
+                  gs.r[i] = old_r[i];
+                }
+                for (int d = 0; d < 3; ++d) {
+                  rg_new_com[d] = gs.com[d];
+                  gs.com[d] = old_com[d];
+                }
+                gc_cut(S, gs);
+                gs.e_prev = rg_e_prev;
+                gs.ln_pbias = 0.0;
+              }
+              gs.flag = ov ? 1 : 0;
+            }
+            __syncthreads();
+            if (!gs.flag) {
+              const bool ov_old = gc_place_fragments<MIXED>(A, V, gs, 0, true, rng, A.lib);
+              if (threadIdx.x == 0) {
+                if (ov_old) {
+                  mv_stop = 1;
+                  status = 1;
+                } else {
+                  get_com(S, gs.r, (1u << gs.na) - 1u, gs.com);
+                }
+              }
+              __syncthreads();
+              if (mv_stop) break;
+              gc_mol_energies<MIXED>(A, V, gs, ttype, em, eov);
+              if (threadIdx.x == 0) {
+                const double* en = rg_en;  // ev, eq, eb, ea, ed, ei, eiv, eiq of the new configuration
+                double dE_intra = en[2] + en[3] + en[4] + en[5] + en[7] + en[6];
+                double dE_inter = en[1] + en[0];
+                dE_intra = dE_intra - em[2] - em[3] - em[4] - em[5] - em[7] - em[6];
+                dE_inter = dE_inter - em[1] - em[0];
+                const double dE = dE_intra + dE_inter;
+                const double dE_frag = en[3] - em[3];
+                const double ln_pacc = b.beta * (dE - dE_frag) + rg_ln_pfor - gs.ln_pbias;
+                if (gc_accept(ln_pacc, rng)) {
+                  mv_acc = 1;
+                  for (int i = 0; i < 3 * gs.na; ++i) gs.r[i] = rg_new[i];
+                  for (int d = 0; d < 3; ++d) gs.com[d] = rg_new_com[d];
+                  E.total += dE;
+                  E.intra += dE_intra;
+                  E.inter += dE_inter;
+                  E.bond += en[2] - em[2];
+                  E.angle += en[3] - em[3];
+                  E.dihedral += en[4] - em[4];
+                  E.improper += en[5] - em[5];
+                  E.intra_vdw += en[6] - em[6];
+                  E.intra_q += en[7] - em[7];
+                  E.inter_vdw += en[0] - em[0];
+                  E.inter_q += en[1] - em[1];
+                  ++RS.n_regrow_accepted;
+                }
               }
             }
           }
@@ -1168,19 +2012,20 @@ __global__ void __launch_bounds__(kGcThreads) k_gcmc(GcArgs A, GcBox* boxes, Pai
       // commit the molecule's coordinates (rejected deletions and regrowths keep
       // the coordinates of their Rosenbluth pass, as the reference does)
       if (threadIdx.x == 0) {
-        if (mv_kind != 2 || mv_acc) {
+        if (MIXED ? (mv_kind <= 1 && mv_acc) : (mv_kind != 2 || mv_acc)) {
           for (int a = 0; a < gs.na; ++a) {
             const int j = roff[gs.rec] + a;
             sx[j] = gs.r[3 * a];
             sy[j] = gs.r[3 * a + 1];
             sz[j] = gs.r[3 * a + 2];
-            if (MIXED) s32[j] = make_float4((float)gs.r[3 * a], (float)gs.r[3 * a + 1], (float)gs.r[3 * a + 2], s32[j].w);
+            const int i = apos[j];
+            if (MIXED && i >= 0) lv32[i] = make_float4((float)gs.r[3 * a], (float)gs.r[3 * a + 1], (float)gs.r[3 * a + 2], lv32[i].w);
           }
           for (int d = 0; d < 3; ++d) scom[3 * gs.rec + d] = gs.com[d];
         }
       }
     }
-    if (threadIdx.x == 0) RS.sum_n_molecules += (double)nmol[ise];
+    if (threadIdx.x == 0) sum_n += nmol[ise];
     __syncthreads();
   }
   __syncthreads();
@@ -1195,6 +2040,7 @@ __global__ void __launch_bounds__(kGcThreads) k_gcmc(GcArgs A, GcBox* boxes, Pai
   if (threadIdx.x == 0) {
     RS.energy = E;
     RS.n_molecules = nmol[ise];
+    RS.sum_n_molecules = (double)sum_n;
     *G.res = RS;
     *G.energy = E;
     *G.status = status;
@@ -1211,8 +2057,11 @@ void fill_growth_species(const SpeciesH& s, int is0, int kappa_ins, int kappa_di
 void invalidate_ext(cass_ctx* c, int ibox);
 void set_mol_box_ext(cass_ctx* c, int slot, int ibox);
 
+// the dynamic shared memory layout of k_gcmc: sx, sy, sz, scom, lv, apos,
+// [lvt], rlive, rsp, roff, pool, lrec, [lv32]
 size_t gc_smem_bytes(int natoms, int nrec, bool mixed) {
-  size_t s = (size_t)natoms * (3 * sizeof(double) + 2 * sizeof(int)) + (size_t)nrec * (3 * sizeof(double) + 4 * sizeof(int));
+  size_t s = (size_t)natoms * (3 * sizeof(double) + (mixed ? 2 : 3) * sizeof(int)) +
+             (size_t)nrec * (3 * sizeof(double) + 5 * sizeof(int));
   s = (s + 15) & ~(size_t)15;
   if (mixed) s += (size_t)natoms * sizeof(float4);
   return s;
@@ -1265,7 +2114,11 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
     for (size_t q = 0; q < t.angle_kind.size(); ++q)
       if (t.angle_kind[q] != CASS_BONDED_FIXED || t.angle_param[2 * q] != 180.0) lin = false;
     A.sp[k].linear = lin ? 1 : 0;
-    for (int a = 0; a < t.natoms && a < kMaxAtoms; ++a) A.sp[k].mass[a] = t.mass[a];
+    for (int a = 0; a < kMaxAtoms; ++a) A.sp[k].type[a] = -1;
+    for (int a = 0; a < t.natoms && a < kMaxAtoms; ++a) {
+      A.sp[k].mass[a] = t.mass[a];
+      A.sp[k].type[a] = t.type[a];
+    }
   }
   A.nsteps = p->nsteps;
   A.cut_t = p->cut_translate;
@@ -1276,6 +2129,14 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
   A.seed = seed;
   A.lib = s.d_library.as<double>();
   A.P = c->pools;
+  A.cutf[0] = (float)p->cut_translate;
+  A.cutf[1] = (float)p->cut_rotate;
+  A.cutf[2] = (float)p->cut_insert;
+  A.cutf[3] = (float)p->cut_delete;
+  A.cutf[4] = (float)p->cut_regrow;
+  // the mixed kernel grows molecules in FP32 from FP32 copies of the species and library
+  mixed = mixed && species_f(s, A.SF) && s.d_library_f.p != nullptr;
+  A.libf = s.d_library_f.as<float>();
   // fragment bonds (f, g), f < g, and the probability of deleting f when the bond is cut
   // (input_routines.f90:3035-3120): atoms beyond the bond on g's side over both sides
   for (int f = 0; f < s.nfrag; ++f)
@@ -1298,6 +2159,7 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
       A.fb_a[A.nfbond] = f;
       A.fb_b[A.nfbond] = g;
       A.prob_del1[A.nfbond] = (double)ndel[1] / (double)(ndel[0] + ndel[1]);
+      A.prob_del1f[A.nfbond] = (float)A.prob_del1[A.nfbond];
       ++A.nfbond;
     }
   double mw = 0.0;
@@ -1358,6 +2220,17 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
     g.log_lambda3 = 3.0 * std::log(39.9031268605 * std::sqrt(B.dev.beta / (kTWOPI * mw)));  // de Broglie
     g.rcut3 = B.rcut3;
     g.rcut9 = B.rcut9;
+    {
+      const int nt = c->pt.ntypes;
+      for (int ia = 0; ia < nt; ++ia)
+        for (int ja = 0; ja < nt; ++ja) {
+          const double eps = c->pt.eps[ia * nt + ja], s2 = c->pt.sig2[ia * nt + ja];
+          const double s6 = s2 * s2 * s2, s12 = s6 * s6;
+          g.lrc_c[ia * nt + ja] = 4.0 * eps * (s12 / (9.0 * B.rcut9) - (s6 / (3.0 * B.rcut3)));
+        }
+      g.lrc_pref = 2.0 * kPI / B.dev.volume;
+      g.log_vol = std::log(B.dev.volume);
+    }
     for (int t = 0; t < kMaxTypes; ++t) g.nb0[t] = nb0[t];
     smem = std::max(smem, gc_smem_bytes(g.natoms, g.nrec, mixed));
     tot_atoms += (size_t)off;
@@ -1366,7 +2239,10 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
   if (smem > kGcSmemLimit)
     return set_error(CASS_ECAPACITY, "gcmc holds a box's molecules and free slots in shared memory: too many atoms");
   const size_t nsp = (size_t)c->nspecies;
-  const size_t bytes = nboxes * sizeof(GcBox) + tot_atoms * (sizeof(double4_32a) + sizeof(int)) +
+  size_t max_rec = 0;
+  for (const HostBox& h : hb) max_rec = std::max(max_rec, h.slots.size());
+  const size_t nlog = max_rec + 2;
+  const size_t bytes = nboxes * sizeof(GcBox) + nlog * sizeof(double) + tot_atoms * (sizeof(double4_32a) + sizeof(int)) +
                        tot_rec * (sizeof(int4) + sizeof(int)) + 2 * nboxes * nsp * sizeof(double) +
                        nboxes * (sizeof(CassEnergy) + sizeof(CassGCMCResult) + sizeof(int)) + 1024;
   if ((rc = c->d_gc.reserve(bytes))) return rc;
@@ -1383,6 +2259,13 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
   int* d_status = reinterpret_cast<int*>(carve(nboxes * sizeof(int), 16));
   double* d_md = reinterpret_cast<double*>(carve(nboxes * nsp * sizeof(double), 16));
   double* d_mr = reinterpret_cast<double*>(carve(nboxes * nsp * sizeof(double), 16));
+  double* d_logn = reinterpret_cast<double*>(carve(nlog * sizeof(double), 16));
+  {
+    std::vector<double> logn(nlog);
+    logn[0] = 0.0;  // never read: ln N is taken for N >= 1
+    for (size_t k = 1; k < nlog; ++k) logn[k] = std::log((double)k);
+    CASS_CUDA(h2d(c, d_logn, logn.data(), nlog * sizeof(double)));
+  }
   std::vector<CassEnergy> hE(nboxes);
   std::vector<double4_32a*> d_xyz(nboxes);
   std::vector<int4*> d_rec(nboxes);
@@ -1403,6 +2286,7 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
     g.atype = d_at;
     g.rec = d_rec[k];
     g.pool = d_pool;
+    g.logn = d_logn;
     g.max_disp = d_md + k * nsp;
     g.max_rot = d_mr + k * nsp;
     g.energy = d_E + k;
