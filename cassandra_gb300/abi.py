@@ -120,7 +120,7 @@ class CassStats(C.Structure):
                 ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("widom_pairs_visited", C.c_int64),
                 ("widom_pairs_in_cutoff", C.c_int64), ("widom_grid_x", C.c_int32), ("widom_grid_y", C.c_int32),
                 ("widom_block", C.c_int32), ("widom_smem_bytes", C.c_int32), ("mc_ms", C.c_double),
-                ("mc_moves", C.c_int64)]
+                ("mc_moves", C.c_int64), ("gcmc_cluster", C.c_int32), ("reserved", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_}

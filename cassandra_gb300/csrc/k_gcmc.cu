@@ -12,6 +12,16 @@
 // geometry and intramolecular energies of a stage run one trial per lane of
 // warp 0.  FP64 kernel: the reference arithmetic; mixed kernel: FP32 pair
 // energies against the box, everything else FP64.
+//
+// A box may be run by a thread-block cluster of C CTAs (C = 1, 2, 4 or 8,
+// chosen so that all boxes run at once).  Every CTA of the cluster holds the
+// whole box and runs the same serial steps from the same lfsr258 stream, so
+// all make the same decisions; the pair loops of a batch are split over the
+// CTAs, whose per-trial partial sums are exchanged through distributed shared
+// memory and added in rank order after one cluster barrier per batch (two
+// partial buffers alternate, so a buffer is rewritten only after every CTA
+// has read it).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -25,10 +35,10 @@
 
 namespace cassgpu {
 
-constexpr int kGcThreads = 256;
+constexpr int kGcThreads = 512;
 constexpr int kGcWarps = kGcThreads / 32;
 constexpr int kGcMaxSpecies = 8;
-constexpr size_t kGcSmemLimit = 200 * 1024;
+constexpr size_t kGcSmemLimit = 190 * 1024;  // dynamic; the static part is about 35 KB of the 227 KB
 
 struct GcSpecies {
   int natoms, linear;
@@ -89,7 +99,12 @@ struct GrowState {
   double e[kMaxKappa];
   float ef[kMaxKappa];
   int ov[kMaxKappa];
+  double cpart[2][kMaxKappa];  // per-CTA trial sums read by the cluster (alternating buffers)
+  float cpartf[2][kMaxKappa];
+  int covl[2][kMaxKappa];
+  int cbuf;
   double part[kGcWarps * kMaxKappa];  // per-warp trial sums
+  float partf[kGcWarps * kMaxKappa];  // the same in FP32 (mixed CBMC batches)
   int povl[kGcWarps];                 // per-warp overlap masks
   // growth bookkeeping
   double ln_pseq, ln_pbias, e_prev;
@@ -140,6 +155,7 @@ struct GcView {
   const int* nlv;
   double* com;
   int natoms, nrec;
+  int crank, csize;  // rank of this CTA in the box's cluster, cluster size
 };
 
 // ---------------------------------------------------------------------------
@@ -148,8 +164,8 @@ struct GcView {
 // TG sums take TG - 1 + log2(32 / TG) shuffles instead of 5 TG.  Returns the
 // warp total of value `which`; every lane gets one, lanes l and l ^ m (m <
 // 32 / TG) the same one.  Fixed order, so the result is deterministic.
-template <int TG>
-__device__ __forceinline__ double warp_multi_sum(double (&v)[TG], int lane, int& which) {
+template <int TG, class R>
+__device__ __forceinline__ R warp_multi_sum(R (&v)[TG], int lane, int& which) {
   which = 0;
   int off = 16;
 #pragma unroll
@@ -157,14 +173,14 @@ __device__ __forceinline__ double warp_multi_sum(double (&v)[TG], int lane, int&
     const bool hi = (lane & off) != 0;
 #pragma unroll
     for (int u = 0; u < n / 2; ++u) {
-      const double send = hi ? v[u] : v[u + n / 2];
-      const double keep = hi ? v[u + n / 2] : v[u];
+      const R send = hi ? v[u] : v[u + n / 2];
+      const R keep = hi ? v[u + n / 2] : v[u];
       v[u] = keep + __shfl_xor_sync(0xffffffffu, send, off);
     }
     which = 2 * which + (hi ? 1 : 0);
     off >>= 1;
   }
-  double s = v[0];
+  R s = v[0];
   for (; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
   return s;
 }
@@ -173,7 +189,11 @@ __device__ __forceinline__ double warp_multi_sum(double (&v)[TG], int lane, int&
 // gs.trial[t]) against every listed atom outside the atom range of record
 // skip_rec.  Each lane takes box atoms and evaluates all trials of a group of
 // TG against them, with the sums in registers; the per-warp sums are added
-// in warp order.  gs.e[t] (0 on overlap) and gs.ov[t] on return.
+// in warp order.  gs.e[t] (0 on overlap) and gs.ov[t] on return.  In the
+// mixed kernel a lane's sum and the sum over a warp are FP32 (the FP64 pipe
+// of GB300 issues at 1/64 of the FP32 rate); CBMC trial batches (TG > 2) stay
+// FP32 to the end and fill gs.ef only, molecule energies (TG = 2) add the
+// per-warp sums in FP64 and fill both gs.e and gs.ef.
 template <bool MIXED, int TG>
 __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip_rec, bool cbmc,
                                const int* ttype, bool convert = true) {
@@ -193,6 +213,7 @@ __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip
     s1 = s0 + gs.na;
   }
   const int nlv = *V.nlv;
+  const float rlow2 = (float)b.rcut_lowsq, rc2 = cbmc ? (float)b.rcut_cbmcsq : (float)b.rcut_vdwsq;
   unsigned ovall = 0u;
   for (int t0 = 0; t0 < ntr; t0 += TG) {
     double accd[TG];
@@ -203,13 +224,12 @@ __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip
       accf[u] = 0.0f;
     }
     unsigned ovm = 0u;
-    for (int i = threadIdx.x; i < nlv; i += blockDim.x) {
+    for (int i = threadIdx.x + V.crank * blockDim.x; i < nlv; i += blockDim.x * V.csize) {
       const int j = V.lv[i];
       if (j >= s0 && j < s1) continue;
       if (MIXED) {
         const float4 pj = V.lv32[i];
         const int tj = __float_as_int(pj.w);
-        const float rlow2 = (float)b.rcut_lowsq, rc2 = cbmc ? (float)b.rcut_cbmcsq : (float)b.rcut_vdwsq;
         for (int k = 0; k < ntid; ++k) {
           const int a = gs.tids[k], ta = ttype[a];
           const bool has = ta >= 0 && tj >= 0;
@@ -248,29 +268,77 @@ __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip
         }
       }
     }
-    if (MIXED) {
-#pragma unroll
-      for (int u = 0; u < TG; ++u) accd[u] = (double)accf[u];
-    }
     int which;
-    const double tot = warp_multi_sum<TG>(accd, lane, which);
-    if ((lane & (32 / TG - 1)) == 0 && t0 + which < ntr) gs.part[w * kMaxKappa + t0 + which] = tot;
+    if (MIXED) {
+      const float tot = warp_multi_sum<TG>(accf, lane, which);
+      if ((lane & (32 / TG - 1)) == 0 && t0 + which < ntr) {
+        if (TG > 2) gs.partf[w * kMaxKappa + t0 + which] = tot;
+        else gs.part[w * kMaxKappa + t0 + which] = (double)tot;
+      }
+    } else {
+      const double tot = warp_multi_sum<TG>(accd, lane, which);
+      if ((lane & (32 / TG - 1)) == 0 && t0 + which < ntr) gs.part[w * kMaxKappa + t0 + which] = tot;
+    }
     ovall |= __reduce_or_sync(0xffffffffu, ovm) << t0;
   }
   if (lane == 0) gs.povl[w] = (int)ovall;
   __syncthreads();
-  if (threadIdx.x < ntr) {
-    double e = 0.0;
-    int o = 0;
-    for (int ww = 0; ww < kGcWarps; ++ww) {
-      e += gs.part[ww * kMaxKappa + threadIdx.x];
-      o |= (gs.povl[ww] >> threadIdx.x) & 1;
+  constexpr bool kF = MIXED && TG > 2;  // FP32 to the end
+  const int t = threadIdx.x;
+  if (V.csize == 1) {
+    if (t < ntr) {
+      int o = 0;
+      for (int ww = 0; ww < kGcWarps; ++ww) o |= (gs.povl[ww] >> t) & 1;
+      if (kF) {
+        float e = 0.0f;
+        for (int ww = 0; ww < kGcWarps; ++ww) e += gs.partf[ww * kMaxKappa + t];
+        gs.ef[t] = o ? 0.0f : e;
+      } else {
+        double e = 0.0;
+        for (int ww = 0; ww < kGcWarps; ++ww) e += gs.part[ww * kMaxKappa + t];
+        gs.e[t] = o ? 0.0 : e;
+        if (MIXED) gs.ef[t] = o ? 0.0f : (float)e;
+      }
+      gs.ov[t] = o;
     }
-    gs.e[threadIdx.x] = o ? 0.0 : e;
-    if (MIXED) gs.ef[threadIdx.x] = o ? 0.0f : (float)e;
-    gs.ov[threadIdx.x] = o;
+  } else {
+    // this CTA's sums, then the cluster's in rank order
+    namespace cgr = cooperative_groups;
+    cgr::cluster_group cl = cgr::this_cluster();
+    const int buf = gs.cbuf;
+    if (t < ntr) {
+      int o = 0;
+      for (int ww = 0; ww < kGcWarps; ++ww) o |= (gs.povl[ww] >> t) & 1;
+      if (kF) {
+        float e = 0.0f;
+        for (int ww = 0; ww < kGcWarps; ++ww) e += gs.partf[ww * kMaxKappa + t];
+        gs.cpartf[buf][t] = e;
+      } else {
+        double e = 0.0;
+        for (int ww = 0; ww < kGcWarps; ++ww) e += gs.part[ww * kMaxKappa + t];
+        gs.cpart[buf][t] = e;
+      }
+      gs.covl[buf][t] = o;
+    }
+    cl.sync();
+    if (t < ntr) {
+      int o = 0;
+      for (int r = 0; r < V.csize; ++r) o |= *cl.map_shared_rank(&gs.covl[buf][t], r);
+      if (kF) {
+        float e = 0.0f;
+        for (int r = 0; r < V.csize; ++r) e += *cl.map_shared_rank(&gs.cpartf[buf][t], r);
+        gs.ef[t] = o ? 0.0f : e;
+      } else {
+        double e = 0.0;
+        for (int r = 0; r < V.csize; ++r) e += *cl.map_shared_rank(&gs.cpart[buf][t], r);
+        gs.e[t] = o ? 0.0 : e;
+        if (MIXED) gs.ef[t] = o ? 0.0f : (float)e;
+      }
+      gs.ov[t] = o;
+    }
   }
   __syncthreads();
+  if (t == 0) gs.cbuf ^= 1;
 }
 
 // the live-atom list and the sorted live records (thread 0)
@@ -1156,7 +1224,7 @@ __device__ __forceinline__ void gc_skip_draw(Lfsr& rng) {
 }
 
 template <bool MIXED>
-__global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, PairTable T) {
+__global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, PairTable T, int csize) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ BoxDev b;
   __shared__ GrowState gs;
@@ -1171,9 +1239,12 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
   __shared__ GrowF gf;
   __shared__ BoxF bf;
   __shared__ float2 s_ljp[kMaxTypes * kMaxTypes];
+  __shared__ PairTable sT;  // the pair table in shared memory (its address is passed to device functions)
   __shared__ float rgf_new[3 * kMaxAtoms], rgf_new_com[3], rgf_e_prev, rgf_ln_pfor;
-  GcBox& G = boxes[blockIdx.x];
+  const int crank = (int)(blockIdx.x % (unsigned)csize);
+  GcBox& G = boxes[blockIdx.x / csize];
   if (threadIdx.x == 0) {
+    gs.cbuf = 0;
     b = G.b;
     if (MIXED) {  // FP32 box constants
       for (int d = 0; d < 3; ++d) {
@@ -1193,6 +1264,11 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
       bf.alpha = (float)G.b.alpha;
       bf.charge_on = 0;
     }
+  }
+  {
+    const int* src = reinterpret_cast<const int*>(&T);
+    int* dst = reinterpret_cast<int*>(&sT);
+    for (int i = threadIdx.x; i < (int)(sizeof(PairTable) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
   }
   for (int i = threadIdx.x; i < kMaxTypes * kMaxTypes; i += blockDim.x) {
     const int ta = i / kMaxTypes, tb = i % kMaxTypes;
@@ -1276,7 +1352,7 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
   if (threadIdx.x < kMaxAtoms) ttype[threadIdx.x] = threadIdx.x < A.S.natoms ? A.S.type[threadIdx.x] : -1;
   GcView V;
   V.b = &b;
-  V.T = &T;
+  V.T = &sT;
   V.epsf = s_epsf;
   V.sig2f = s_sig2f;
   V.bf = &bf;
@@ -1296,6 +1372,8 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
   V.com = scom;
   V.natoms = N;
   V.nrec = R;
+  V.crank = crank;
+  V.csize = csize;
   // thread-0 state
   Lfsr rng;
   CassEnergy E;
@@ -2029,6 +2107,8 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
     __syncthreads();
   }
   __syncthreads();
+  if (csize > 1) cooperative_groups::this_cluster().sync();  // no CTA leaves while its shared memory may be read
+  if (crank != 0) return;
   for (int j = threadIdx.x; j < N; j += blockDim.x) {
     double4_32a p = G.xyzq[j];
     p.x = sx[j];
@@ -2300,8 +2380,43 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
   CASS_CUDA(h2d(c, d_mr, max_rot, nboxes * nsp * sizeof(double)));
   auto kern = mixed ? k_gcmc<true> : k_gcmc<false>;
   CASS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // cluster size: the largest of 8, 4, 2 for which every box's cluster can be
+  // resident at once; else one CTA per box
+  int csize = 1;
+  for (int cs = 8; cs >= 2; cs >>= 1) {
+    cudaLaunchConfig_t q = {};
+    cudaLaunchAttribute qa[1];
+    qa[0].id = cudaLaunchAttributeClusterDimension;
+    qa[0].val.clusterDim.x = cs;
+    qa[0].val.clusterDim.y = 1;
+    qa[0].val.clusterDim.z = 1;
+    q.gridDim = dim3(nboxes * cs);
+    q.blockDim = dim3(kGcThreads);
+    q.dynamicSmemBytes = smem;
+    q.attrs = qa;
+    q.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &q) == cudaSuccess && nclusters >= nboxes) {
+      csize = cs;
+      break;
+    }
+    (void)cudaGetLastError();
+  }
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = csize;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(nboxes * csize);
+  cfg.blockDim = dim3(kGcThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = c->stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  c->stats.gcmc_cluster = csize;
   CASS_CUDA(cudaEventRecord(c->ev[0], c->stream));
-  kern<<<nboxes, kGcThreads, smem, c->stream>>>(A, d_box, c->pt);
+  CASS_CUDA(cudaLaunchKernelEx(&cfg, kern, A, d_box, c->pt, csize));
   CASS_CUDA(cudaGetLastError());
   CASS_CUDA(cudaEventRecord(c->ev[1], c->stream));
   count_launch(c);

@@ -371,8 +371,10 @@ typedef struct CassStats {
   int64_t widom_pairs_in_cutoff; /* of which inside a cutoff */
   int32_t widom_grid_x, widom_grid_y, widom_block;
   int32_t widom_smem_bytes;
-  double mc_ms;             /* the most recent cass_mc_sweeps: its kernel */
+  double mc_ms;             /* the most recent cass_mc_sweeps or cass_gcmc: its kernel */
   int64_t mc_moves;         /* moves it ran, all boxes */
+  int32_t gcmc_cluster;     /* CTAs per box of the most recent cass_gcmc (a thread-block cluster) */
+  int32_t reserved;
 } CassStats;
 int cass_get_stats(cass_ctx* ctx, CassStats* out);
 /* count_pairs != 0 makes the Widom kernel count visited / in-cutoff pairs. */

@@ -27,7 +27,7 @@ def test_struct_layouts():
     assert ctypes.sizeof(abi.CassWidomTrace) == 48
     assert ctypes.sizeof(abi.CassMCParams) == 8 + 2 * 4 + 2 * 8
     assert ctypes.sizeof(abi.CassMCResult) == 14 * 8 + 5 * 8
-    assert ctypes.sizeof(abi.CassStats) == 2 * 8 + 5 * 8 + 4 * 4 + 8 + 8
+    assert ctypes.sizeof(abi.CassStats) == 2 * 8 + 5 * 8 + 4 * 4 + 8 + 8 + 2 * 4
     assert ctypes.sizeof(abi.CassBoxDesc) == 3 * 8 + 2 * 4 + 6 * 8 + 2 * 4 + 3 * 8
 
 
