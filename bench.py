@@ -214,8 +214,8 @@ BUTANE_MW = 2 * 15.035 + 2 * 14.027  # g/mol, united-atom CH3-CH2-CH2-CH3
 AVOGADRO = 6.02214076e23
 
 
-def gcmc_leg(cg, abi, dev, with_cpu: bool, eq_steps: int = 60000, blocks: int = 6,
-             block_steps: int = 10000) -> dict:
+def gcmc_leg(cg, abi, dev, with_cpu: bool, eq_steps: int = 150000, blocks: int = 8,
+             block_steps: int = 15000) -> dict:
     """Grand-canonical butane in 16 boxes of 40 A at 300 K, mu evenly spaced over
     [-30, -20] kJ/mol, insert/delete 40 %, translate/rotate 40 %, regrow 20 %.
     Each precision equilibrates from empty boxes, then runs `blocks` production
@@ -237,6 +237,7 @@ def gcmc_leg(cg, abi, dev, with_cpu: bool, eq_steps: int = 60000, blocks: int = 
             g.system_total_energy(b)
         g.gcmc(boxes, eq, 1, boxes_mu, md, mr, seed=seed, cuts=cuts)
         eq_ms = g.stats()["mc_ms"]
+        cluster = g.stats()["gcmc_cluster"]
         means, ms, last = [], 0.0, None
         for k in range(nblk):
             last = g.gcmc(boxes, nstep, 1, boxes_mu, md, mr, seed=seed + 1 + k, cuts=cuts)
@@ -247,7 +248,7 @@ def gcmc_leg(cg, abi, dev, with_cpu: bool, eq_steps: int = 60000, blocks: int = 
         se = means.std(axis=0, ddof=1) / np.sqrt(nblk) if nblk > 1 else np.zeros(n)
         acc = {k: sum(r[f"n_{k}_accepted"] for r in last) / max(1, sum(r[f"n_{k}"] for r in last))
                for k in ("translate", "rotate", "insert", "delete", "regrow")}
-        out = {"boxes": n, "equilibration_steps": eq, "production_steps": nblk * nstep,
+        out = {"boxes": n, "ctas_per_box": cluster, "equilibration_steps": eq, "production_steps": nblk * nstep,
                "kernel_ms": ms, "moves_per_s": n * nblk * nstep / (ms / 1e3),
                "equilibration_moves_per_s": n * eq / (eq_ms / 1e3),
                "acceptance_last_block": acc, "mean_n": mean_n, "se_n": se}
