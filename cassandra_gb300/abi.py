@@ -115,6 +115,10 @@ class CassGCMCResult(C.Structure):
         return d
 
 
+class CassCBMCOptions(C.Structure):
+    _fields_ = [("energy_table_res", C.c_int32), ("sector_overlap", C.c_int32), ("rmin_u_max", C.c_double)]
+
+
 class CassStats(C.Structure):
     _fields_ = [("widom_ms", C.c_double), ("widom_kernel_ms", C.c_double), ("kernel_launches", C.c_int64),
                 ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("widom_pairs_visited", C.c_int64),
@@ -144,6 +148,7 @@ SIGNATURES = {
     "remove_molecule": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "get_molecule": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _f64p]),
     "get_molecule_boxes": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _i32p]),
+    "set_cbmc_options": (C.c_int, [C.c_void_p, C.POINTER(CassCBMCOptions)]),
     "mol_inter_energy": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _f64p, _f64p, _i32p]),
     "mol_intra_energy": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _f64p, _f64p, _f64p, _i32p]),
     "system_total_energy": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(CassEnergy), _i32p]),
@@ -287,6 +292,12 @@ class Context:
         out = np.zeros(3 * self.natoms[is_])
         self._check("get_molecule", self._f["get_molecule"](self._h, im, is_, _p(out)))
         return out.reshape(-1, 3)
+
+    def set_cbmc_options(self, energy_table_res: int = 0, sector_overlap: bool = False,
+                         rmin_u_max: float = 0.0) -> None:
+        """CBMC_Info energy_table N, Cell_List_Overlap and Rcutoff_Low adaptive U of the input file."""
+        o = CassCBMCOptions(energy_table_res, int(sector_overlap), rmin_u_max)
+        self._check("set_cbmc_options", self._f["set_cbmc_options"](self._h, C.byref(o)))
 
     def molecule_boxes(self, is_: int) -> np.ndarray:
         """Box of every molecule slot im = 1..max_molecules of species is_ (0: not live)."""

@@ -130,6 +130,7 @@ __global__ void __launch_bounds__(kBlock) k_mol_inter(BoxDev b, PairTable t, con
   double ev = 0.0, eq = 0.0;
   KahanF fv, fq;
   bool ov = false;
+  const bool table = cbmc && b.tab_res > 0;
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
     int4 mj = meta[j];
     if (mj.x == qslot) continue;
@@ -139,6 +140,10 @@ __global__ void __launch_bounds__(kBlock) k_mol_inter(BoxDev b, PairTable t, con
       double dy = fold(qa[a].y - pj.y, b.hL[1], b.L[1]);
       double dz = fold(qa[a].z - pj.z, b.hL[2], b.L[2]);
       double r2 = dx * dx + dy * dy + dz * dz;
+      if (table) {  // Estimate_MoleculePair_Energy: the combined energy goes to the vdW sum
+        if (table_pair(b, t.ntypes, r2, qt[a], mj.y, qa[a].w, pj.w, ev) == 2) ov = true;
+        continue;
+      }
       if (r2 < b.rcut_lowsq) {
         ov = true;
         continue;
@@ -192,6 +197,7 @@ __global__ void __launch_bounds__(kBlock) k_trial_energy(BoxDev b, PairTable t, 
   double ev = 0.0, eq = 0.0;
   KahanF fv, fq;
   bool ov = false;
+  const bool table = cbmc && b.tab_res > 0;
   for (int j = threadIdx.x; j < n && !ov; j += blockDim.x) {
     const int4 mj = meta[j];
     if (mj.x == skip_slot) continue;
@@ -201,6 +207,13 @@ __global__ void __launch_bounds__(kBlock) k_trial_energy(BoxDev b, PairTable t, 
       const double dy = fold(qa[a].y - pj.y, b.hL[1], b.L[1]);
       const double dz = fold(qa[a].z - pj.z, b.hL[2], b.L[2]);
       const double r2 = dx * dx + dy * dy + dz * dz;
+      if (table) {  // Estimate_MoleculePair_Energy
+        if (table_pair(b, t.ntypes, r2, qt[a], mj.y, qa[a].w, pj.w, ev) == 2) {
+          ov = true;
+          break;
+        }
+        continue;
+      }
       if (r2 < b.rcut_lowsq) {
         ov = true;
         break;
@@ -733,6 +746,194 @@ int pack_box_ext(cass_ctx* c, int ibox) { return pack_box(c, ibox); }
 void invalidate_ext(cass_ctx* c, int ibox) { invalidate(c, ibox); }
 void set_mol_box_ext(cass_ctx* c, int slot, int ibox) { set_mol_box(c, slot, ibox); }
 const std::vector<int>& members_ext(cass_ctx* c, int ibox) { return members(c, ibox); }
+
+namespace {
+// AtomPair_VdW_Energy_Vector (energy_routines.f90:1733-1829) at r^2 = rsq:
+// the box's vdW pair energy without a cutoff test
+double table_vdw(const cass_ctx_impl* c, const BoxDev& b, int it, int jt, double rsq) {
+  const PairTable& t = c->pt;
+  const int k = it * t.ntypes + jt;
+  const double eps = t.eps[k];
+  if (b.vdw_style == CASS_VDW_LJ) {
+    const double s2 = t.sig2[k] / rsq, s6 = s2 * s2 * s2, s12 = s6 * s6;
+    double e = 4.0 * eps * (s12 - s6);
+    if (b.vdw_sum_style == CASS_VDW_SUM_CUT_SHIFT) {
+      const double c2 = t.sig2[k] / b.rcut_vdwsq, c6 = c2 * c2 * c2, c12 = c6 * c6;
+      e = e - 4.0 * eps * (c12 - c6);
+    } else if (b.vdw_sum_style == CASS_VDW_SUM_CUT_SWITCH) {
+      if (rsq >= b.ron_switch_sq) {
+        if (rsq > b.roff_switch_sq) {
+          e = 0.0;
+        } else {
+          const double d = b.roff_switch_sq - rsq;
+          e = d * d * (b.switch_factor2 + 2.0 * rsq) * b.switch_factor1 * e;
+        }
+      }
+    } else if (b.vdw_sum_style == CASS_VDW_SUM_CHARMM) {
+      e = eps * (s12 - 2.0 * s6);
+    } else if (b.vdw_sum_style == CASS_VDW_SUM_CUT_SHIFT_FORCE) {
+      const double c2 = t.sig2[k] / b.rcut_vdwsq, c6 = c2 * c2 * c2, c12 = c6 * c6;
+      const double rc = std::sqrt(b.rcut_vdwsq);
+      const double dedr = -24.0 * eps * (2.0 * c12 - c6) / rc;
+      e = e - 4.0 * eps * (c12 - c6) - (std::sqrt(rsq) - rc) * dedr;
+    }
+    return e;
+  }
+  if (b.vdw_style == CASS_VDW_MIE) {
+    const double sig = c->pt_sig[k], n = t.mie_n[k], m = t.mie_m[k], rc = std::sqrt(b.rcut_vdwsq);
+    const double sr = sig / std::sqrt(rsq);
+    double e = t.mie_c[k] * eps * (std::pow(sr, n) - std::pow(sr, m));
+    if (b.vdw_sum_style == CASS_VDW_SUM_CUT_SHIFT) {
+      const double sc = sig / rc;
+      e = e - t.mie_c[k] * eps * (std::pow(sc, n) - std::pow(sc, m));
+    }
+    return e;
+  }
+  return 0.0;
+}
+}  // namespace
+
+// The tables of the CBMC options: r_min^2 per type pair
+// (create_nonbond_table.f90:219-220, 285-303, 396-418, with the charge range of
+// each type of :144-153) and, per box, the atom-pair energy table
+// (atompair_nrg_table_routines.f90:149-261; rsq_step and rsq_shifter of
+// :163-168).  One device buffer: r_min^2 (FP64, FP32), then per box the vdW
+// part [ntypes][ntypes][res] and the Coulomb kernel [res] in FP64 and FP32.
+int ensure_cbmc(cass_ctx_impl* c) {
+  const CassCBMCOptions& o = c->cbmc_opt;
+  const bool on = o.energy_table_res > 0 || o.sector_overlap;
+  if (!on) {
+    for (BoxH& B : c->box) {
+      B.dev.tab_res = 0;
+      B.dev.sector = 0;
+    }
+    return CASS_OK;
+  }
+  if (!c->cbmc_dirty) return CASS_OK;
+  if (!c->pt_set) return set_error(CASS_ESTATE, "nonbond table not set");
+  const int nt = c->ntypes, res = o.energy_table_res;
+  double rlow = -1.0, max_cbmcsq = 0.0, min_beta = 0.0;
+  int charge_style1 = CASS_CHARGE_NONE, nbox = 0;
+  for (int ib = 0; ib < c->nboxes; ++ib) {
+    const BoxH& B = c->box[ib];
+    if (!B.defined) continue;
+    if (nbox == 0) {
+      rlow = B.dev.rcut_lowsq;
+      min_beta = B.dev.beta;
+    } else if (B.dev.rcut_lowsq != rlow) {
+      return set_error(CASS_EUNSUPPORTED, "CBMC options need one rcut_low for all boxes");
+    }
+    if (ib == 0) charge_style1 = B.desc.charge_style;
+    max_cbmcsq = std::max(max_cbmcsq, B.dev.rcut_cbmcsq);
+    min_beta = std::min(min_beta, B.dev.beta);
+    ++nbox;
+  }
+  if (nbox == 0) return set_error(CASS_ESTATE, "CBMC options need a box");
+  std::vector<double> rmin((size_t)nt * nt, rlow);
+  if (o.rmin_u_max > 0.0) {
+    std::vector<double> qmin(nt, 0.0), qmax(nt, 0.0);
+    std::vector<char> seen(nt, 0);
+    for (const SpeciesH& sp : c->sp) {
+      if (!sp.defined) continue;
+      for (int a = 0; a < sp.natoms; ++a) {
+        const int t = sp.type[a];
+        if (t < 0) continue;
+        qmin[t] = seen[t] ? std::min(qmin[t], sp.q[a]) : sp.q[a];
+        qmax[t] = seen[t] ? std::max(qmax[t], sp.q[a]) : sp.q[a];
+        seen[t] = 1;
+      }
+    }
+    const double u_base = o.rmin_u_max / min_beta, rcut_low = std::sqrt(rlow);
+    for (int i = 0; i < nt; ++i)
+      for (int j = 0; j < nt; ++j) {
+        const double eps = c->pt.eps[i * nt + j], sig = c->pt_sig[i * nt + j];
+        if (!(eps > 0.0)) continue;
+        double min_uq = 0.0;
+        if (charge_style1 != CASS_CHARGE_NONE) {
+          double qp = std::min(qmin[i] * qmax[j], qmax[i] * qmin[j]);
+          if (qp <= 0.0) {
+            min_uq = qp * kCHARGE_FACTOR / rcut_low;
+          } else {
+            qp = std::min(qmin[i] * qmin[j], qmax[i] * qmax[j]);
+            min_uq = qp * kCHARGE_FACTOR / sig;
+          }
+        }
+        const double umax = std::max(u_base - min_uq, 0.0);
+        const double lambda = 0.5 * (1.0 + std::sqrt(1.0 + umax / eps));
+        rmin[(size_t)i * nt + j] = sig * sig / std::pow(lambda, 1.0 / 3.0);
+      }
+  }
+  if (o.sector_overlap)
+    for (const BoxH& B : c->box)
+      if (B.defined)
+        for (double r2 : rmin)
+          if (r2 > B.dev.rcut_cbmcsq) return set_error(CASS_EUNSUPPORTED, "r_min exceeds rcut_cbmc");
+  // host image of the device buffer
+  const size_t nn = (size_t)nt * nt;
+  const size_t per_box = res > 0 ? (nn * res + res) * (sizeof(double) + sizeof(float)) : 0;
+  const size_t head = ((nn * (sizeof(double) + sizeof(float)) + 255) & ~(size_t)255);
+  const size_t box_stride = (per_box + 255) & ~(size_t)255;
+  std::vector<unsigned char> img(head + box_stride * c->nboxes, 0);
+  double* h_rmin = reinterpret_cast<double*>(img.data());
+  float* h_rminf = reinterpret_cast<float*>(h_rmin + nn);
+  for (size_t k = 0; k < nn; ++k) {
+    h_rmin[k] = rmin[k];
+    h_rminf[k] = (float)rmin[k];
+  }
+  std::vector<double> step(c->nboxes, 0.0), shift(c->nboxes, 0.0);
+  if (res > 0)
+    for (int ib = 0; ib < c->nboxes; ++ib) {
+      const BoxH& B = c->box[ib];
+      if (!B.defined) continue;
+      const BoxDev& b = B.dev;
+      double* v = reinterpret_cast<double*>(img.data() + head + box_stride * ib);
+      double* f2 = v + nn * res;
+      float* vf = reinterpret_cast<float*>(f2 + res);
+      float* f2f = vf + nn * res;
+      step[ib] = (max_cbmcsq - rlow) / res;
+      shift[ib] = rlow - step[ib];
+      for (int i = 1; i <= res; ++i) {
+        const double mp = (shift[ib] + step[ib] * i) + 0.5 * step[ib];
+        const double rij = std::sqrt(mp);
+        double k2 = 0.0;
+        if (b.charge_style == CASS_CHARGE_COUL) {
+          if (b.charge_sum_style == CASS_QQ_EWALD) k2 = std::erfc(b.alpha * rij) / rij;
+          else if (b.charge_sum_style == CASS_QQ_DSF)
+            k2 = b.dsf_factor2 * (rij - b.rcut_coul) - b.dsf_factor1 + std::erfc(b.alpha_dsf * rij) / rij;
+          else if (b.charge_sum_style == CASS_QQ_CUT) k2 = 1.0 / rij;
+        }
+        f2[i - 1] = k2;
+        f2f[i - 1] = (float)k2;
+        for (int ti = 0; ti < nt; ++ti)
+          for (int tj = 0; tj < nt; ++tj) {
+            const double e = table_vdw(c, b, ti, tj, mp);
+            v[((size_t)ti * nt + tj) * res + (i - 1)] = e;
+            vf[((size_t)ti * nt + tj) * res + (i - 1)] = (float)e;
+          }
+      }
+    }
+  CASS_CUDA(cudaSetDevice(c->device));
+  if (int rc = c->d_cbmc_tab.reserve(img.size())) return rc;
+  CASS_CUDA(h2d(c, c->d_cbmc_tab.p, img.data(), img.size()));
+  CASS_CUDA(cudaStreamSynchronize(c->stream));
+  unsigned char* base = static_cast<unsigned char*>(c->d_cbmc_tab.p);
+  for (int ib = 0; ib < c->nboxes; ++ib) {
+    BoxDev& b = c->box[ib].dev;
+    b.sector = o.sector_overlap ? 1 : 0;
+    b.rminsq = reinterpret_cast<const double*>(base);
+    b.rminsqf = reinterpret_cast<const float*>(base + nn * sizeof(double));
+    b.tab_res = (res > 0 && c->box[ib].defined) ? res : 0;
+    b.tab_step = step[ib];
+    b.tab_shift = shift[ib];
+    const double* v = reinterpret_cast<const double*>(base + head + box_stride * ib);
+    b.tab_v = v;
+    b.tab_f2 = v + nn * res;
+    b.tab_vf = reinterpret_cast<const float*>(b.tab_f2 + res);
+    b.tab_f2f = b.tab_vf + nn * res;
+  }
+  c->cbmc_dirty = false;
+  return CASS_OK;
+}
 }  // namespace cassgpu
 
 // ===========================================================================
@@ -845,6 +1046,8 @@ int cass_set_nonbond_table(cass_ctx* c, int32_t nt, const double* eps, const dou
     t.sig2f[i] = (float)t.sig2[i];
   }
   c->pt_set = true;
+  c->pt_sig.assign(sig, sig + nt * nt);
+  c->cbmc_dirty = true;
   for (int b = 0; b < c->nboxes; ++b) c->box[b].energy_valid = false;
   return CASS_OK;
 }
@@ -961,6 +1164,7 @@ int cass_set_species(cass_ctx* c, int32_t is, const CassSpeciesDesc* d) {
     CASS_CUDA(h2d(c, s.d_library_f.p, lf.data(), lf.size() * sizeof(float)));
   }
   s.defined = true;
+  c->cbmc_dirty = true;
   c->members_dirty = true;
   c->pools_dirty = true;
   for (int b = 0; b < c->nboxes; ++b) invalidate(c, b);
@@ -975,6 +1179,7 @@ int cass_set_box(cass_ctx* c, int32_t ibox, const CassBoxDesc* d) {
   B.desc = *d;
   BoxDev& v = B.dev;
   memset(&v, 0, sizeof(v));
+  c->cbmc_dirty = true;
   for (int k = 0; k < 3; ++k) {
     v.L[k] = d->length[k];
     v.hL[k] = 0.5 * d->length[k];
@@ -1152,6 +1357,14 @@ int cass_get_molecule_boxes(cass_ctx* c, int32_t is, int32_t n, int32_t* which_b
   return CASS_OK;
 }
 
+int cass_set_cbmc_options(cass_ctx* c, const CassCBMCOptions* o) {
+  if (!c || !o || o->energy_table_res < 0 || o->energy_table_res > (1 << 20) || !(o->rmin_u_max >= 0.0))
+    return set_error(CASS_EINVAL, "bad CBMC options");
+  c->cbmc_opt = *o;
+  c->cbmc_dirty = true;
+  return CASS_OK;
+}
+
 int cass_mol_inter_energy(cass_ctx* c, int32_t im, int32_t is, int32_t cbmc, double* ev, double* eq, int32_t* ov) {
   if (!c || !ev || !eq || !ov) return set_error(CASS_EINVAL, "NULL argument");
   int rc = check_mol(c, im, is);
@@ -1161,6 +1374,7 @@ int cass_mol_inter_energy(cass_ctx* c, int32_t im, int32_t is, int32_t cbmc, dou
   int ibox = c->mol_box[slot];
   if (ibox < 0) return set_error(CASS_ESTATE, "molecule not live");
   if ((rc = set_device(c)) || (rc = pack_box(c, ibox))) return rc;
+  if (cbmc && (rc = ensure_cbmc(c))) return rc;
   BoxH& B = c->box[ibox];
   const int qoff = B.pk_mol_off[c->pk_index[slot]];
   const SpeciesH& s = c->sp[is - 1];
@@ -1209,6 +1423,7 @@ int cass_cbmc_trial_energies(cass_ctx* c, int32_t ibox1, int32_t is, int32_t ski
   const int ib = ibox1 - 1;
   int rc;
   if ((rc = set_device(c)) || (rc = pack_box(c, ib))) return rc;
+  if (cbmc && (rc = ensure_cbmc(c))) return rc;
   BoxH& B = c->box[ib];
   std::vector<double4_32a> tr((size_t)ntrial * nat);
   std::vector<int> tt(nat);

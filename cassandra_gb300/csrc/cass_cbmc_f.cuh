@@ -31,7 +31,32 @@ struct BoxF {
   int nc[3];
   float rcb2, rv2, rq2, low2, rc_cbmc, rc_full, beta, kmaxE, alpha;
   int charge_on;
+  // CBMC options: the FP32 atom-pair energy table and the r_min^2 test
+  int tab_res, sector, ntypes;
+  float tab_shift, tab_rcs, tab_step, tab_inv_step;  // tab_rcs = rcut_cbmc^2 - tab_shift
+  const float* tab_v;
+  const float* tab_f2;
+  float rmin2[kMaxTypes * kMaxTypes];  // row stride kMaxTypes
 };
+
+// the CBMC-option fields of f from the box's BoxDev; thread 0 then all threads
+__device__ inline void boxf_options(BoxF& f, const BoxDev& b, int ntypes) {
+  if (threadIdx.x == 0) {
+    f.tab_res = b.tab_res;
+    f.sector = b.sector;
+    f.ntypes = ntypes;
+    f.tab_shift = (float)b.tab_shift;
+    f.tab_rcs = (float)(b.rcut_cbmcsq - b.tab_shift);
+    f.tab_step = (float)b.tab_step;
+    f.tab_inv_step = b.tab_res > 0 ? (float)(1.0 / b.tab_step) : 0.0f;
+    f.tab_v = b.tab_vf;
+    f.tab_f2 = b.tab_f2f;
+  }
+  for (int i = threadIdx.x; i < kMaxTypes * kMaxTypes; i += blockDim.x) {
+    const int ta = i / kMaxTypes, tb = i % kMaxTypes;
+    f.rmin2[i] = (b.sector && ta < ntypes && tb < ntypes) ? b.rminsqf[ta * ntypes + tb] : (float)b.rcut_lowsq;
+  }
+}
 
 // uniform in [0, 1) from an lfsr258 draw without the FP64 unit: the reference
 // value x*2^-64 + 0.5 (x signed) equals (x ^ 2^63) / 2^64; keep its top 23 bits

@@ -133,6 +133,7 @@ struct cass_ctx_impl {
   std::vector<SpeciesH> sp;
   std::vector<BoxH> box;
   PairTable pt{};
+  std::vector<double> pt_sig;  // mixed sigma per type pair, as given
   bool pt_set = false;
   std::vector<int> mol_box;  // -1 = not live
   std::vector<int> slot_sp;  // species (0-based) of each molecule slot
@@ -162,7 +163,14 @@ struct cass_ctx_impl {
   DevBuf d_c64, d_c32, d_cq32, d_cell_start, d_cell_count, d_cell_of, d_boxdev, d_widom_out, d_widom_xyz,
       d_trace, d_box_sums;
   std::vector<int> widom_boxes;
+  // CBMC options and the tables they derive (energy table per box, r_min^2)
+  CassCBMCOptions cbmc_opt{};
+  bool cbmc_dirty = true;
+  DevBuf d_cbmc_tab;
 };
+
+// builds the CBMC-option tables if needed and points each box's BoxDev at them
+int ensure_cbmc(cass_ctx_impl* c);
 
 // copies that keep the byte counters of CassStats
 cudaError_t h2d(cass_ctx_impl* c, void* dst, const void* src, size_t n);

@@ -60,6 +60,16 @@ struct BoxDev {
   int nvecs, kvec_off;
   // Widom per-box constants
   double e_inter_constant, prefactor;
+  // CBMC options (cass_set_cbmc_options): the atom-pair energy table (0 bins:
+  // off) and the r_min^2 overlap test of Widom growth (sector != 0)
+  int tab_res, sector;
+  double tab_step, tab_shift;
+  const double* tab_v;   // [ntypes][ntypes][tab_res] vdW part
+  const double* tab_f2;  // [tab_res] Coulomb kernel, times (q_i cf) q_j
+  const float* tab_vf;   // FP32 copies
+  const float* tab_f2f;
+  const double* rminsq;  // [ntypes][ntypes]
+  const float* rminsqf;
 };
 
 __host__ __device__ inline int pidx(int i, int j, int nt) { return i * nt + j; }
@@ -259,6 +269,41 @@ __device__ __forceinline__ double qq_pair_intra(const BoxDev& b, double qiqj, do
     return Eij - (1.0 - qscale) * (cfqq / rij);
   }
   return qscale * kCHARGE_FACTOR * qiqj / sqrt(r2);
+}
+
+// Estimate_MoleculePair_Energy for one atom pair (energy_routines.f90:
+// 1563-1583): the table bin of r^2 - rsq_shifter.  Returns 0 beyond
+// rcut_cbmc, 2 on overlap (below rcut_low), else 1 with the entry added to e.
+__device__ __forceinline__ int table_pair(const BoxDev& b, int nt, double r2, int ti, int tj, double qi, double qj,
+                                          double& e) {
+  const double rs = r2 - b.tab_shift;
+  if (rs >= b.rcut_cbmcsq - b.tab_shift) return 0;
+  if (rs < b.tab_step) return 2;
+  int bin = (int)(rs / b.tab_step);  // 1-based; res at most, except within rounding of the cutoff
+  if (bin > b.tab_res) bin = b.tab_res;
+  const double ev = (ti >= 0 && tj >= 0) ? b.tab_v[((size_t)ti * nt + tj) * b.tab_res + (bin - 1)] : 0.0;
+  e += ev + b.tab_f2[bin - 1] * ((qi * kCHARGE_FACTOR) * qj);
+  return 1;
+}
+
+// the same in FP32 from the FP32 table (mixed kernels); rcs = rcut_cbmc^2 - shift;
+// the term is returned in e
+__device__ __forceinline__ int table_pair_f(const float* v, const float* f2, int res, float shift, float rcs,
+                                            float step, float inv_step, int nt, float r2, int ti, int tj, float qicf,
+                                            float qj, float& e) {
+  const float rs = r2 - shift;
+  if (rs >= rcs) return 0;
+  if (rs < step) return 2;
+  int bin = (int)(rs * inv_step);
+  bin = min(max(bin, 1), res);
+  const float ev = (ti >= 0 && tj >= 0) ? __ldg(&v[(ti * nt + tj) * res + (bin - 1)]) : 0.0f;
+  e = ev + __ldg(&f2[bin - 1]) * (qicf * qj);
+  return 1;
+}
+
+// r_min^2 of check_overlap (sector_routines.f90:160-233) for a type pair
+__device__ __forceinline__ double rmin2_pair(const BoxDev& b, int nt, int ti, int tj) {
+  return (ti >= 0 && tj >= 0) ? b.rminsq[ti * nt + tj] : b.rcut_lowsq;
 }
 
 // FP32 LJ (cut / cut_tail / minimum_image) used by the mixed path; other vdw

@@ -214,6 +214,9 @@ __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip
   }
   const int nlv = *V.nlv;
   const float rlow2 = (float)b.rcut_lowsq, rc2 = cbmc ? (float)b.rcut_cbmcsq : (float)b.rcut_vdwsq;
+  const bool tab = cbmc && b.tab_res > 0;
+  const int ntypes = V.T->ntypes;
+  const BoxF& bf = *V.bf;
   unsigned ovall = 0u;
   for (int t0 = 0; t0 < ntr; t0 += TG) {
     double accd[TG];
@@ -243,8 +246,17 @@ __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip
               const float dy = fold(tr[1] - pj.y, b.hLf[1], b.Lf[1]);
               const float dz = fold(tr[2] - pj.z, b.hLf[2], b.Lf[2]);
               const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-              if (r2 < rlow2) ovm |= 1u << u;
-              else if (r2 <= rc2 && has) accf[u] += lj_pair_f(eps, s2, r2);
+              if (tab) {  // Estimate_MoleculePair_Energy from the FP32 table
+                float et;
+                const int kt = table_pair_f(bf.tab_v, bf.tab_f2, bf.tab_res, bf.tab_shift, bf.tab_rcs, bf.tab_step,
+                                            bf.tab_inv_step, ntypes, r2, ta, tj, 0.0f, 0.0f, et);
+                if (kt == 2) ovm |= 1u << u;
+                else if (kt == 1) accf[u] += et;
+              } else if (r2 < rlow2) {
+                ovm |= 1u << u;
+              } else if (r2 <= rc2 && has) {
+                accf[u] += lj_pair_f(eps, s2, r2);
+              }
             }
           }
         }
@@ -261,8 +273,13 @@ __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip
               const double dy = fold(tr[1] - yj, b.hL[1], b.L[1]);
               const double dz = fold(tr[2] - zj, b.hL[2], b.L[2]);
               const double r2 = dx * dx + dy * dy + dz * dz;
-              if (r2 < b.rcut_lowsq) ovm |= 1u << u;
-              else if (cutoff_mask(b, r2, cbmc) & 1) accd[u] += vdw_pair(*V.T, b, ta, tj, r2, 1.0);
+              if (tab) {  // Estimate_MoleculePair_Energy (the boxes hold no charges)
+                if (table_pair(b, ntypes, r2, ta, tj, 0.0, 0.0, accd[u]) == 2) ovm |= 1u << u;
+              } else if (r2 < b.rcut_lowsq) {
+                ovm |= 1u << u;
+              } else if (cutoff_mask(b, r2, cbmc) & 1) {
+                accd[u] += vdw_pair(*V.T, b, ta, tj, r2, 1.0);
+              }
             }
           }
         }
@@ -1270,6 +1287,7 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
     int* dst = reinterpret_cast<int*>(&sT);
     for (int i = threadIdx.x; i < (int)(sizeof(PairTable) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
   }
+  if (MIXED) boxf_options(bf, G.b, T.ntypes);
   for (int i = threadIdx.x; i < kMaxTypes * kMaxTypes; i += blockDim.x) {
     const int ta = i / kMaxTypes, tb = i % kMaxTypes;
     const bool ok = ta < T.ntypes && tb < T.ntypes;
@@ -2182,6 +2200,7 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
   int rc;
   CASS_CUDA(cudaSetDevice(c->device));
   if ((rc = ensure_pools(c))) return rc;
+  if ((rc = ensure_cbmc(c))) return rc;
   GcArgs A;
   memset(&A, 0, sizeof(A));
   fill_growth_species(s, is, p->kappa_ins, p->kappa_dih, A.S);

@@ -220,6 +220,18 @@ __device__ bool query_box(const BoxView& V, const PairTable& T, const double p[3
           double dy = fold(p[1] - a.y, b.hL[1], b.L[1]);
           double dz = fold(p[2] - a.z, b.hL[2], b.L[2]);
           double r2 = dx * dx + dy * dy + dz * dz;
+          if (cbmc && b.sector && r2 < rmin2_pair(b, T.ntypes, qt, V.ptype[j])) return true;  // check_overlap
+          if (cbmc && b.tab_res > 0) {  // Estimate_MoleculePair_Energy
+            double et = 0.0;
+            const int k = table_pair(b, T.ntypes, r2, qt, V.ptype[j], qch, a.w, et);
+            if (k == 2) return true;
+            if (k == 1) {
+              ++pc.in_cut;
+              acc += et;
+              eabs += fabs(et);
+            }
+            continue;
+          }
           if (r2 < b.rcut_lowsq) return true;
           int m = cutoff_mask(b, r2, cbmc);
           if (!qq_on) m &= 1;
@@ -696,9 +708,76 @@ __device__ __forceinline__ void pair_energy(const BoxViewF& V, QueryAcc& A, cons
 // FP32 energy of one test atom at p against the box atoms within the cutoff,
 // added to A.  Returns true on core overlap (r^2 < rcut_low^2), as
 // Compute_MoleculePair_Energy (energy_routines.f90:1676-1679) does.
-template <bool COUNT>
+// A CBMC query with the CBMC options: check_overlap against r_min^2 of the
+// type pair and, with the energy table, Estimate_MoleculePair_Energy per pair
+// (FP32 table; a pair's bin can differ from FP64 within rounding of a bin edge)
+__device__ bool query_f_opt(const BoxViewF& V, QueryAcc& A, float px, float py, float pz, int ta, float qa) {
+  const BoxF& f = *V.f;
+  const float rc = f.rc_cbmc;
+  const float p[3] = {px, py, pz};
+  int lo[3], hi[3];
+  bool full[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float w = fminf(rc * f.cinv[d], 1.0e5f);
+    const float ul = fminf(fmaxf((p[d] + f.hL[d]) * f.cinv[d] - w - 1e-3f, -1.0e6f), 1.0e6f);
+    const float uh = fminf(fmaxf((p[d] + f.hL[d]) * f.cinv[d] + w + 1e-3f, -1.0e6f), 1.0e6f);
+    const int l = (int)floorf(ul), h = (int)floorf(uh);
+    full[d] = h - l + 1 >= f.nc[d];
+    lo[d] = full[d] ? 0 : l;
+    hi[d] = full[d] ? f.nc[d] - 1 : h;
+  }
+  const bool fold_any = full[0] || full[1] || full[2];
+  const bool vdw_on = ta >= 0;
+  const bool qq_on = f.charge_on && qa != 0.0f;
+  const float rsel2 = f.rcb2;
+  const float2* lrow = V.ljp + (vdw_on ? ta : 0) * kMaxTypes;
+  const float* rmrow = f.rmin2 + (vdw_on ? ta : 0) * kMaxTypes;
+  const float qicf = qa * (float)kCHARGE_FACTOR;
+  const int nc0 = f.nc[0], nc1 = f.nc[1], nc2 = f.nc[2];
+  for (int cz = lo[2]; cz <= hi[2]; ++cz) {
+    const int wz = wrapc(cz, nc2);
+    const float qz = pz + (float)((wz - cz) / nc2) * f.L[2];
+    for (int cy = lo[1]; cy <= hi[1]; ++cy) {
+      const int wy = wrapc(cy, nc1);
+      const float qy = py + (float)((wy - cy) / nc1) * f.L[1];
+      const int row = (wz * nc1 + wy) * nc0;
+      int cx = lo[0];
+      while (cx <= hi[0]) {
+        const int wx = wrapc(cx, nc0);
+        const int run = min(hi[0] - cx, nc0 - 1 - wx) + 1;
+        const float qx = px + (float)((wx - cx) / nc0) * f.L[0];
+        const int j0 = V.cstart[row + wx], j1 = V.cstart[row + wx + run];
+        for (int j = j0; j < j1; ++j) {
+          const float4 a = V.p32[j];
+          const float r2 = pair_r2(f, full, fold_any, qx, qy, qz, a);
+          const int tj = __float_as_int(a.w);
+          if (f.sector && r2 < (vdw_on && tj >= 0 ? rmrow[tj] : f.low2)) return true;
+          if (f.tab_res > 0) {
+            float e = 0.0f;
+            const int k = table_pair_f(f.tab_v, f.tab_f2, f.tab_res, f.tab_shift, f.tab_rcs, f.tab_step,
+                                       f.tab_inv_step, f.ntypes, r2, ta, tj, qicf, qq_on ? V.q32[j] : 0.0f, e);
+            if (k == 2) return true;
+            if (k == 1) {
+              A.e.add(e);
+              A.eabs += fabsf(e);
+            }
+          } else {
+            if (r2 < f.low2) return true;
+            if (r2 <= rsel2) pair_energy<false>(V, A, a, j, r2, lrow, vdw_on, qq_on, f.rcb2, f.rcb2, qa);
+          }
+        }
+        cx += run;
+      }
+    }
+  }
+  return false;
+}
+
+template <bool COUNT, bool OPT = false>
 __device__ bool query_f(const BoxViewF& V, QueryAcc& A, float px, float py, float pz, int ta, float qa, bool cbmc,
                         bool want_qq) {
+  if (OPT && cbmc) return query_f_opt(V, A, px, py, pz, ta, qa);
   const BoxF& f = *V.f;
   const float rc = cbmc ? f.rc_cbmc : f.rc_full;
   const float p[3] = {px, py, pz};
@@ -767,13 +846,13 @@ struct RecF {
 };
 
 // Energy of atoms `ids` against the box: sum into e, true on overlap
-template <bool COUNT>
+template <bool COUNT, bool OPT>
 __device__ __forceinline__ bool query_atoms_f(const BoxViewF& V, QueryAcc& A, const SpeciesF& S, const float* r,
                                               const int* ids, int n, float sx, float sy, float sz, bool cbmc,
                                               bool want_qq) {
   for (int i = 0; i < n; ++i) {
     const int a = ids[i];
-    if (query_f<COUNT>(V, A, r[3 * a] + sx, r[3 * a + 1] + sy, r[3 * a + 2] + sz, S.type[a], S.q[a], cbmc, want_qq))
+    if (query_f<COUNT, OPT>(V, A, r[3 * a] + sx, r[3 * a + 1] + sy, r[3 * a + 2] + sz, S.type[a], S.q[a], cbmc, want_qq))
       return true;
   }
   return false;
@@ -782,7 +861,7 @@ __device__ __forceinline__ bool query_atoms_f(const BoxViewF& V, QueryAcc& A, co
 // One Widom insertion: Widom_Insert (widom_insert.f90:250-447) with the CBMC
 // growth of Build_Molecule (fragment_growth.f90:120-900) and
 // Fragment_Placement (:1449-2132), in FP32
-template <bool COUNT>
+template <bool COUNT, bool OPT>
 __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const BoxViewF& V,
                                 const float* __restrict__ lib, Lfsr rng, double* xyz_out, QueryAcc& cnt) {
   const BoxF& f = *V.f;
@@ -883,7 +962,7 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
     const float ay = (0.5f - draw_f(rng)) * f.L[1];
     const float az = (0.5f - draw_f(rng)) * f.L[2];
     QueryAcc A;
-    bool ov = query_atoms_f<COUNT>(V, A, SF, r, fa_ids, nfa, ax, ay, az, true, cbmc_qq);
+    bool ov = query_atoms_f<COUNT, OPT>(V, A, SF, r, fa_ids, nfa, ax, ay, az, true, cbmc_qq);
     cnt.visited += A.visited;
     cnt.in_cut += A.in_cut;
     const float e = A.e.s + A.e.c;
@@ -1025,7 +1104,7 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
           continue;
         }
         QueryAcc A;
-        ov = query_atoms_f<COUNT>(V, A, SF, r, newids, nnew, 0.0f, 0.0f, 0.0f, true, cbmc_qq);
+        ov = query_atoms_f<COUNT, OPT>(V, A, SF, r, newids, nnew, 0.0f, 0.0f, 0.0f, true, cbmc_qq);
         cnt.visited += A.visited;
         cnt.in_cut += A.in_cut;
         exist = combined;
@@ -1104,7 +1183,7 @@ constexpr int kF32Threads = 512;
 constexpr int kF32MinBlocks = 2;
 constexpr int kF32Waves = 8;  // CTAs per resident slot: many short waves even out uneven boxes
 
-template <bool SMEM, bool COUNT>
+template <bool SMEM, bool COUNT, bool OPT>
 __global__ void __launch_bounds__(kF32Threads, kF32MinBlocks) k_widom_f32(WidomSpecies S, SpeciesF SF, PairTable T, const BoxDev* boxes,
                                                    const int* box_ids, const float4* c32, const float* cq32,
                                                    const int* cstart, const float* __restrict__ libf, long long n_ins,
@@ -1140,6 +1219,7 @@ __global__ void __launch_bounds__(kF32Threads, kF32MinBlocks) k_widom_f32(WidomS
     s_natoms = b.natoms;
     s_ec = b.e_inter_constant;
   }
+  if (OPT) boxf_options(sf, boxes[k], T.ntypes);
   for (int i = threadIdx.x; i < kMaxTypes * kMaxTypes; i += blockDim.x) {
     const int a = i / kMaxTypes, c = i % kMaxTypes;
     const bool ok = a < T.ntypes && c < T.ntypes;
@@ -1169,7 +1249,7 @@ __global__ void __launch_bounds__(kF32Threads, kF32MinBlocks) k_widom_f32(WidomS
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n_ins; i += stride) {
     const size_t g = (size_t)k * n_ins + i;
     const Lfsr rng = seed_stream(seed, box_ids[k], i);
-    const RecF o = run_insertion_f<COUNT>(S, SF, V, libf, rng, want_xyz ? xyz + g * 3 * S.natoms : nullptr, cnt);
+    const RecF o = run_insertion_f<COUNT, OPT>(S, SF, V, libf, rng, want_xyz ? xyz + g * 3 * S.natoms : nullptr, cnt);
     const double e_int = (double)o.e_inter;
     rec[g] = make_double4_32a((double)o.dE_intra, e_int + s_ec, (double)o.dE_frag, (double)o.ln_pbias);
     status[g] = (signed char)o.status;
@@ -1489,6 +1569,7 @@ extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const
   int rc;
   CASS_CUDA(cudaSetDevice(c->device));
   if ((rc = ensure_pools(c))) return rc;
+  if ((rc = ensure_cbmc(c))) return rc;
   const int is0 = is1 - 1;
 
   WidomSpecies S;
@@ -1690,8 +1771,10 @@ extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const
     return CASS_OK;
   };
   if (n_ins > 0) {
-    if (f32 && d_pairs) rc = use_smem ? launch_f32(k_widom_f32<true, true>, SF) : launch_f32(k_widom_f32<false, true>, SF);
-    else if (f32) rc = use_smem ? launch_f32(k_widom_f32<true, false>, SF) : launch_f32(k_widom_f32<false, false>, SF);
+    const bool opt = c->cbmc_opt.energy_table_res > 0 || c->cbmc_opt.sector_overlap;  // no pair counts with options
+    if (f32 && opt) rc = use_smem ? launch_f32(k_widom_f32<true, false, true>, SF) : launch_f32(k_widom_f32<false, false, true>, SF);
+    else if (f32 && d_pairs) rc = use_smem ? launch_f32(k_widom_f32<true, true, false>, SF) : launch_f32(k_widom_f32<false, true, false>, SF);
+    else if (f32) rc = use_smem ? launch_f32(k_widom_f32<true, false, false>, SF) : launch_f32(k_widom_f32<false, false, false>, SF);
     else rc = use_smem ? launch(k_widom<true>) : launch(k_widom<false>);
     if (rc) return rc;
     if (any_recip) {

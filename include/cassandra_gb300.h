@@ -221,6 +221,36 @@ int cass_ewald_restore(cass_ctx* ctx, int32_t im, int32_t is, int32_t ibox);
 int cass_ewald_widom(cass_ctx* ctx, int32_t is, int32_t ibox, int32_t n,
                      const double* xyz, double* e_reciprocal);
 
+/* ---- CBMC options ----------------------------------------------------- */
+/* Input-file options that change how CBMC trial energies and trial overlaps
+ * are computed; they apply to the calls that follow.
+ *   energy_table_res > 0 ("# CBMC_Info ... energy_table N",
+ *     input_routines.f90:6041-6050): every CBMC trial energy
+ *     (Compute_Molecule_Nonbond_Inter_Energy / _Widom with cbmc_flag,
+ *     energy_routines.f90:1182-1191,1275-1278) becomes the atom-pair table
+ *     lookup of Estimate_MoleculePair_Energy (energy_routines.f90:1528-1587)
+ *     over the table of Create_Atompair_Nrg_table
+ *     (atompair_nrg_table_routines.f90:149-261): N bins in r^2 from
+ *     rcut_low^2 to the largest rcut_cbmc^2 of the context's boxes, each the
+ *     vdW + real-space Coulomb pair energy at the bin's midpoint.  Used by
+ *     cass_widom_insert, cass_cbmc_trial_energies, cass_mol_inter_energy with
+ *     cbmc_flag and cass_gcmc.  0: off.
+ *   sector_overlap != 0 ("# Cell_List_Overlap true"): in cass_widom_insert a
+ *     trial atom closer than r_min(type pair) to a box atom makes its trial
+ *     overlap (check_overlap, sector_routines.f90:160-233, called from
+ *     fragment_growth.f90:475-488 and 1930-1949).
+ *   rmin_u_max > 0 ("# Rcutoff_Low ... adaptive U", input_routines.f90:
+ *     6941-7102): r_min^2 per type pair from U_max = U k T_max
+ *     (create_nonbond_table.f90:285-303,396-418); 0: r_min = rcut_low.
+ * The boxes must share one rcut_low (the reference has a single one) and
+ * r_min may not exceed a box's rcut_cbmc (CASS_EUNSUPPORTED at use). */
+typedef struct CassCBMCOptions {
+  int32_t energy_table_res;
+  int32_t sector_overlap;
+  double rmin_u_max;
+} CassCBMCOptions;
+int cass_set_cbmc_options(cass_ctx* ctx, const CassCBMCOptions* opt);
+
 /* ---- CBMC / Widom ----------------------------------------------------- */
 /* Compute_Molecule_Nonbond_Inter_Energy_Widom (energy_routines.f90:1209-1364)
  * for a batch of CBMC trial positions, the energy call of every trial in

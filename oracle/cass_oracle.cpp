@@ -98,6 +98,16 @@ struct Mol {
   std::vector<double> cos_mol, sin_mol, cos_mol_old, sin_mol_old;
 };
 
+// CBMC atom-pair energy table of one box (Create_Atompair_Nrg_table,
+// atompair_nrg_table_routines.f90:149-261): bin i (1-based) holds the pair
+// energy at the midpoint of [rcut_low^2 + (i-1) step, rcut_low^2 + i step).
+struct CbmcTab {
+  int res = 0;
+  double step = 0, shift = 0;   // rsq_step, rsq_shifter
+  std::vector<double> v;        // [ntypes][ntypes][res] vdW part
+  std::vector<double> f2;       // [res] Coulomb kernel, times (q_i cf) q_j
+};
+
 }  // namespace
 
 struct orc_ctx {
@@ -113,6 +123,12 @@ struct orc_ctx {
   // is the first member of species is
   std::vector<std::vector<int>> members, sp_off;
   bool members_dirty = true;
+  // CBMC options (cass_set_cbmc_options) and what they derive
+  CassCBMCOptions opt{};
+  bool cbmc_dirty = true;
+  std::vector<CbmcTab> tab;     // per box, when opt.energy_table_res > 0
+  std::vector<double> rminsq;   // [ntypes][ntypes] r_min^2 of check_overlap
+  double rlowsq = 0.0;          // rcut_low^2 shared by the boxes
 };
 
 namespace {
@@ -379,6 +395,207 @@ bool molpair_energy(const orc_ctx* c, const Box& b, const MolView& a, const MolV
   return false;
 }
 
+// AtomPair_VdW_Energy_Vector (energy_routines.f90:1733-1829) at one r^2:
+// the vdW pair energy of the box's style with no cutoff test
+double vdw_vector_entry(const orc_ctx* c, const Box& b, int it, int jt, double rsq) {
+  if (it < 0 || jt < 0) return 0.0;
+  const int k = it * c->ntypes + jt;
+  const double eps = c->eps[k], sig = c->sig[k];
+  if (b.vdw_style == CASS_VDW_LJ) {
+    const double s2 = (sig * sig) / rsq, s6 = s2 * s2 * s2, s12 = s6 * s6;
+    double e = 4.0 * eps * (s12 - s6);
+    if (b.vdw_sum_style == CASS_VDW_SUM_CUT_SHIFT) {
+      const double c2 = sig * sig / b.rcut_vdwsq, c6 = c2 * c2 * c2, c12 = c6 * c6;
+      e = e - 4.0 * eps * (c12 - c6);
+    } else if (b.vdw_sum_style == CASS_VDW_SUM_CUT_SWITCH) {
+      if (rsq < b.ron_switch_sq) {
+      } else if (rsq > b.roff_switch_sq) {
+        e = 0.0;
+      } else {
+        const double d = b.roff_switch_sq - rsq;
+        e = d * d * (b.switch_factor2 + 2.0 * rsq) * b.switch_factor1 * e;
+      }
+    } else if (b.vdw_sum_style == CASS_VDW_SUM_CHARMM) {
+      e = eps * (s12 - 2.0 * s6);
+    } else if (b.vdw_sum_style == CASS_VDW_SUM_CUT_SHIFT_FORCE) {
+      const double c2 = sig * sig / b.rcut_vdwsq, c6 = c2 * c2 * c2, c12 = c6 * c6;
+      const double rc = std::sqrt(b.rcut_vdwsq);
+      const double dedr = -24.0 * eps * (2.0 * c12 - c6) / rc;
+      e = e - 4.0 * eps * (c12 - c6) - (std::sqrt(rsq) - rc) * dedr;
+    }
+    return e;
+  }
+  if (b.vdw_style == CASS_VDW_MIE) {
+    const double n = c->mie_n[k], m = c->mie_m[k];
+    const double rc = std::sqrt(b.rcut_vdwsq);
+    const double coeff = n / (n - m) * std::pow(n / m, m / (n - m));
+    const double sr = sig / std::sqrt(rsq);
+    double e = coeff * eps * (std::pow(sr, n) - std::pow(sr, m));
+    if (b.vdw_sum_style == CASS_VDW_SUM_CUT_SHIFT) {
+      const double sc = sig / rc;
+      e = e - coeff * eps * (std::pow(sc, n) - std::pow(sc, m));
+    }
+    return e;
+  }
+  return 0.0;
+}
+
+// The tables the CBMC options derive: the energy table per box
+// (atompair_nrg_table_routines.f90:149-261, with rsq_step and rsq_shifter of
+// :163-168) and r_min^2 per type pair (create_nonbond_table.f90:219-220,
+// 285-303, 396-418 with the type charge ranges of :144-153)
+int build_cbmc(orc_ctx* c) {
+  if (!c->cbmc_dirty) return CASS_OK;
+  const int nt = c->ntypes;
+  double rlow = -1.0, max_cbmcsq = 0.0, min_beta = 0.0;
+  int charge_style1 = CASS_CHARGE_NONE;
+  bool first = true;
+  for (int ib = 0; ib < c->nboxes; ++ib) {
+    const Box& b = c->box[ib];
+    if (!b.defined) continue;
+    if (first) {
+      rlow = b.rcut_lowsq;
+      min_beta = b.beta;
+      first = false;
+    } else if (b.rcut_lowsq != rlow) {
+      return fail(CASS_EUNSUPPORTED, "CBMC options need one rcut_low for all boxes");
+    }
+    if (ib == 0) charge_style1 = b.charge_style;
+    max_cbmcsq = std::max(max_cbmcsq, b.rcut_cbmcsq);
+    min_beta = std::min(min_beta, b.beta);
+  }
+  if (first) return fail(CASS_ESTATE, "CBMC options need a box");
+  c->rlowsq = rlow;
+  // r_min^2 per type pair
+  c->rminsq.assign((size_t)nt * nt, rlow);
+  if (c->opt.rmin_u_max > 0.0) {
+    std::vector<double> qmin(nt, 0.0), qmax(nt, 0.0);
+    std::vector<char> seen(nt, 0);
+    for (const Species& sp : c->sp) {
+      if (!sp.defined) continue;
+      for (int a = 0; a < sp.natoms; ++a) {
+        const int t = sp.type[a];
+        if (t < 0) continue;
+        if (seen[t]) {
+          qmin[t] = std::min(qmin[t], sp.q[a]);
+          qmax[t] = std::max(qmax[t], sp.q[a]);
+        } else {
+          qmin[t] = qmax[t] = sp.q[a];
+          seen[t] = 1;
+        }
+      }
+    }
+    const double u_base = c->opt.rmin_u_max / min_beta;
+    const double rcut_low = std::sqrt(rlow);
+    for (int i = 0; i < nt; ++i)
+      for (int j = 0; j < nt; ++j) {
+        const double eps = c->eps[i * nt + j], sig = c->sig[i * nt + j];
+        if (!(eps > 0.0)) continue;
+        double min_uq = 0.0;
+        if (charge_style1 != CASS_CHARGE_NONE) {
+          double qp = std::min(qmin[i] * qmax[j], qmax[i] * qmin[j]);
+          if (qp <= 0.0) {
+            min_uq = qp * CHARGE_FACTOR / rcut_low;
+          } else {
+            qp = std::min(qmin[i] * qmin[j], qmax[i] * qmax[j]);
+            min_uq = qp * CHARGE_FACTOR / sig;
+          }
+        }
+        const double umax = std::max(u_base - min_uq, 0.0);
+        const double lambda = 0.5 * (1.0 + std::sqrt(1.0 + umax / eps));
+        c->rminsq[i * nt + j] = sig * sig / std::pow(lambda, 1.0 / 3.0);
+      }
+  }
+  if (c->opt.sector_overlap)
+    for (int ib = 0; ib < c->nboxes; ++ib) {
+      const Box& b = c->box[ib];
+      if (!b.defined) continue;
+      for (double r2 : c->rminsq)
+        if (r2 > b.rcut_cbmcsq) return fail(CASS_EUNSUPPORTED, "r_min exceeds rcut_cbmc");
+    }
+  // energy tables
+  c->tab.assign(c->nboxes, CbmcTab{});
+  const int res = c->opt.energy_table_res;
+  if (res > 0)
+    for (int ib = 0; ib < c->nboxes; ++ib) {
+      const Box& b = c->box[ib];
+      if (!b.defined) continue;
+      CbmcTab& T = c->tab[ib];
+      T.res = res;
+      T.step = (max_cbmcsq - rlow) / res;
+      T.shift = rlow - T.step;
+      T.v.assign((size_t)nt * nt * res, 0.0);
+      T.f2.assign(res, 0.0);
+      for (int i = 1; i <= res; ++i) {
+        const double lb = T.shift + T.step * i;
+        const double mp = lb + 0.5 * T.step;
+        const double rij = std::sqrt(mp);
+        double f2 = 0.0;
+        if (b.charge_style == CASS_CHARGE_COUL) {
+          if (b.charge_sum_style == CASS_QQ_EWALD) f2 = std::erfc(b.alpha_ewald * rij) / rij;
+          else if (b.charge_sum_style == CASS_QQ_DSF)
+            f2 = b.dsf_factor2 * (rij - b.rcut_coul) - b.dsf_factor1 + std::erfc(b.alpha_dsf * rij) / rij;
+          else if (b.charge_sum_style == CASS_QQ_CUT) f2 = 1.0 / rij;
+        }
+        T.f2[i - 1] = f2;
+        for (int ti = 0; ti < nt; ++ti)
+          for (int tj = 0; tj < nt; ++tj) T.v[((size_t)ti * nt + tj) * res + (i - 1)] = vdw_vector_entry(c, b, ti, tj, mp);
+      }
+    }
+  c->cbmc_dirty = false;
+  return CASS_OK;
+}
+
+// Estimate_MoleculePair_Energy (energy_routines.f90:1528-1587): the combined
+// vdW + Coulomb energy of molecule a (the solute) with m (the solvent) from
+// the box's table; true on overlap (a pair below rcut_low inside rcut_cbmc)
+bool molpair_estimate(const orc_ctx* c, int ibox, const MolView& a, const MolView& m, double& e) {
+  const Box& b = c->box[ibox];
+  const CbmcTab& T = c->tab[ibox];
+  const Species& sa = c->sp[a.is];
+  const Species& sm = c->sp[m.is];
+  const int nt = c->ntypes;
+  const double rcs = b.rcut_cbmcsq - T.shift;
+  e = 0.0;
+  for (int ia = 0; ia < sa.natoms; ++ia) {
+    if (!a.exist[ia]) continue;
+    for (int ja = 0; ja < sm.natoms; ++ja) {
+      if (!m.exist[ja]) continue;
+      double dx = a.r[3 * ia] - m.r[3 * ja], dy = a.r[3 * ia + 1] - m.r[3 * ja + 1], dz = a.r[3 * ia + 2] - m.r[3 * ja + 2];
+      min_image(b, dx, dy, dz);
+      const double rs = dx * dx + dy * dy + dz * dz - T.shift;
+      if (rs >= rcs) continue;
+      if (rs < T.step) return true;
+      int bin = (int)(rs / T.step);  // 1-based; at most res except within rounding of the cutoff
+      if (bin > T.res) bin = T.res;
+      const int ta = sa.type[ia], tj = sm.type[ja];
+      const double ev = (ta >= 0 && tj >= 0) ? T.v[((size_t)ta * nt + tj) * T.res + (bin - 1)] : 0.0;
+      e += ev + T.f2[bin - 1] * ((sa.q[ia] * CHARGE_FACTOR) * sm.q[ja]);
+    }
+  }
+  return false;
+}
+
+// check_overlap (sector_routines.f90:160-233) for atom ia of species is at
+// p: true if a box atom lies closer than r_min(type pair)
+bool check_overlap_atom(const orc_ctx* c, int ibox, int is, int ia, const double* p) {
+  const Box& b = c->box[ibox];
+  const int nt = c->ntypes, ta = c->sp[is].type[ia];
+  for (int slot : c->members[ibox]) {
+    const Mol& m = c->mol[slot];
+    const Species& sm = c->sp[m.is];
+    for (int ja = 0; ja < sm.natoms; ++ja) {
+      if (!m.exist[ja]) continue;
+      double dx = m.r[3 * ja] - p[0], dy = m.r[3 * ja + 1] - p[1], dz = m.r[3 * ja + 2] - p[2];
+      min_image(b, dx, dy, dz);
+      const int tj = sm.type[ja];
+      const double rmin2 = (ta >= 0 && tj >= 0) ? c->rminsq[(size_t)ta * nt + tj] : c->rlowsq;
+      if (dx * dx + dy * dy + dz * dz < rmin2) return true;
+    }
+  }
+  return false;
+}
+
 MolView view_of(const Mol& m) { return MolView{m.is, m.r.data(), m.exist.data(), m.com, m.max_dcom}; }
 
 // Get_COM (get_com.f90:45-105)
@@ -428,7 +645,13 @@ bool mol_inter_energy(const orc_ctx* c, int ibox, const MolView& a, int skip, bo
     MolView mv = view_of(m);
     if (!check_molpair_cutoff(b, a, mv, cbmc)) continue;
     double vlj, vqq;
-    if (molpair_energy(c, b, a, mv, cbmc, vlj, vqq, eabs)) return true;
+    if (cbmc && c->opt.energy_table_res > 0) {
+      // the estimate is the combined vdW + Coulomb energy (energy_routines.f90:1182-1191)
+      if (molpair_estimate(c, ibox, a, mv, vlj)) return true;
+      vqq = 0.0;
+    } else if (molpair_energy(c, b, a, mv, cbmc, vlj, vqq, eabs)) {
+      return true;
+    }
     evdw += vlj;
     eqq += vqq;
   }
@@ -906,7 +1129,10 @@ InsertionOut widom_one(const orc_ctx* c, int is, int ibox, int kappa_ins, int ka
       need_max_dcom = false;
     }
     double e = 0.0;
-    bool ov = widom_inter(c, ibox, t, true, e);
+    bool ov = false;
+    if (c->opt.sector_overlap)  // check_overlap of each placed atom (fragment_growth.f90:475-488)
+      for (int i = 0; i < nfa && !ov; ++i) ov = check_overlap_atom(c, ibox, is, fa[i], &t.r[3 * fa[i]]);
+    if (!ov) ov = widom_inter(c, ibox, t, true, e);
     nrg[it] = nrg[it] + e;
     if (ov) {
       weight[it] = 0.0;
@@ -1041,6 +1267,16 @@ InsertionOut widom_one(const orc_ctx* c, int is, int ibox, int kappa_ins, int ka
         const double* ct = &ctmp[(size_t)ii * 3 * s.natoms];
         for (int a : atom_id)
           for (int d = 0; d < 3; ++d) t.r[3 * a + d] = ct[3 * a + d];
+        if (c->opt.sector_overlap) {  // check_overlap of the fragment's atoms (fragment_growth.f90:1930-1949)
+          bool sov = false;
+          for (int a : atom_id)
+            if (!sov) sov = check_overlap_atom(c, ibox, is, a, &t.r[3 * a]);
+          if (sov) {
+            dw[ii] = ii > 0 ? dw[ii - 1] : 0.0;
+            dov[ii] = 1;
+            continue;
+          }
+        }
         for (int a : atom_id) t.exist[a] = 0;
         double niv = 0, niq = 0, noq = 0;
         bool ov = false;
@@ -2127,6 +2363,7 @@ int orc_set_nonbond_table(orc_ctx* c, int32_t nt, const double* eps, const doubl
   c->sig.assign(sig, sig + nt * nt);
   if (mn) c->mie_n.assign(mn, mn + nt * nt);
   if (mm) c->mie_m.assign(mm, mm + nt * nt);
+  c->cbmc_dirty = true;
   return CASS_OK;
 }
 
@@ -2140,6 +2377,7 @@ int orc_set_species(orc_ctx* c, int32_t is, const CassSpeciesDesc* d) {
     if (d->frag_natoms[f] < 1 || d->frag_natoms[f] > d->natoms) return fail(CASS_EINVAL, "bad fragment sizes");
   Species& s = c->sp[is - 1];
   int n = d->natoms;
+  c->cbmc_dirty = true;
   s = Species();
   s.natoms = n;
   s.type.resize(n);
@@ -2215,6 +2453,7 @@ int orc_set_box(orc_ctx* c, int32_t ibox, const CassBoxDesc* d) {
   if (check_ctx(c) || ibox < 1 || ibox > c->nboxes || !d) return fail(CASS_EINVAL, "bad box");
   Box& b = c->box[ibox - 1];
   b = Box();
+  c->cbmc_dirty = true;
   for (int k = 0; k < 3; ++k) {
     b.L[k] = d->length[k];
     b.hL[k] = 0.5 * d->length[k];
@@ -2319,10 +2558,25 @@ int orc_get_molecule_boxes(orc_ctx* c, int32_t is, int32_t n, int32_t* which_box
   return CASS_OK;
 }
 
+// the tables of the CBMC options, rebuilt after a change of boxes, species,
+// pair table or options
+static int cbmc_ready(orc_ctx* c) {
+  if (c->opt.energy_table_res <= 0 && !c->opt.sector_overlap) return CASS_OK;
+  return build_cbmc(c);
+}
+
+int orc_set_cbmc_options(orc_ctx* c, const CassCBMCOptions* o) {
+  if (check_ctx(c) || !o || o->energy_table_res < 0 || o->rmin_u_max < 0.0) return fail(CASS_EINVAL, "bad CBMC options");
+  c->opt = *o;
+  c->cbmc_dirty = true;
+  return CASS_OK;
+}
+
 int orc_mol_inter_energy(orc_ctx* c, int32_t im, int32_t is, int32_t cbmc, double* ev, double* eq, int32_t* ov) {
   if (c) refresh_members(c);
   int rc = check_ctx(c) ? CASS_EINVAL : check_mol(c, im, is);
   if (rc) return rc;
+  if (cbmc && (rc = cbmc_ready(c))) return rc;
   Mol& m = mol_of(c, is - 1, im - 1);
   if (!m.live) return fail(CASS_ESTATE, "molecule not live");
   int slot = c->mol_base[is - 1] + im - 1;
@@ -2534,6 +2788,7 @@ int orc_widom_insert(orc_ctx* c, int32_t is1, int32_t nboxes, const int32_t* ibo
   int is = is1 - 1;
   const Species& s = c->sp[is];
   if (s.nfrag < 1) return fail(CASS_EINVAL, "species has no fragments");
+  if (int rc = cbmc_ready(c)) return rc;
   if (s.nfrag > 1 && kappa_dih < 1) return fail(CASS_EINVAL, "kappa_dih must be >= 1");
   for (int k = 0; k < nboxes; ++k) {
     int ib = iboxes[k] - 1;
@@ -2608,6 +2863,8 @@ int orc_cbmc_trial_energies(orc_ctx* c, int32_t ibox1, int32_t is1, int32_t skip
     return fail(CASS_EINVAL, "bad trial arguments");
   const Species& s = c->sp[is1 - 1];
   if (!s.defined) return fail(CASS_ESTATE, "species not defined");
+  if (cbmc)
+    if (int rc = cbmc_ready(c)) return rc;
   for (int a = 0; a < nat; ++a)
     if (atoms[a] < 1 || atoms[a] > s.natoms) return fail(CASS_EINVAL, "trial atom index out of range");
   if (skip_im < 0 || skip_im > c->max_mol[is1 - 1]) return fail(CASS_EINVAL, "molecule locate out of range");
@@ -2684,6 +2941,7 @@ int orc_gcmc(orc_ctx* c, int32_t nboxes, const int32_t* iboxes, const CassGCMCPa
   const int is = p->is_exchange - 1;
   const Species& s = c->sp[is];
   if (!s.defined || s.nfrag < 1) return fail(CASS_ESTATE, "exchanged species not defined or without fragments");
+  if (int rc = cbmc_ready(c)) return rc;
   if (s.nfrag > 1 && p->kappa_dih < 1) return fail(CASS_EINVAL, "kappa_dih must be >= 1");
   for (int k = 0; k < nboxes; ++k) {
     const int ib = iboxes[k] - 1;

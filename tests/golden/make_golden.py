@@ -10,6 +10,8 @@ Sources (paths inside the Cassandra tree):
   Scripts/testSuite/Test7_Water.py + Resources/inputFiles/test7.water{1..4}.xyz
   Scripts/testSuite/Resources/exampleResources/Widom/{pentane,water_spce}/  (trajectories, .mcf, .inp)
   Scripts/testSuite/Resources/exampleResults/Widom/{pentane,water_spce}/*.prp  (per-frame Energy_Total)
+  Scripts/testSuite/Resources/exampleResults/Widom/pentane/*.wprp, *.wprp2, *.log  (Widom statistics)
+  Scripts/testSuite/Resources/exampleResources/Widom/pentane/species1/frag*/frag*.dat  (fragment libraries)
 """
 from __future__ import annotations
 
@@ -138,11 +140,34 @@ def pregen(name, traj, prp, mcf, inp):
     np.savez_compressed(os.path.join(OUT, f"pregen_{name}.npz"), **data)
 
 
+def widom_pentane():
+    """The pentane Widom fixture's statistics: per-frame averages of widom_var
+    (.spec1.wprp), the three sub-interval averages per frame (.spec1.wprp2),
+    the shifted chemical potential of the log, and the fragment libraries the
+    run used (species1/frag*/frag*.dat, as arrays)."""
+    base = os.path.join(TS, "Resources", "exampleResources", "Widom", "pentane")
+    res = os.path.join(TS, "Resources", "exampleResults", "Widom", "pentane")
+    wprp = np.loadtxt(os.path.join(res, "pentane_widom.out.spec1.wprp"), skiprows=1)
+    wprp2 = np.loadtxt(os.path.join(res, "pentane_widom.out.spec1.wprp2"))
+    log = open(os.path.join(res, "pentane_widom.out.log")).read()
+    mu = float(re.search(r"Shifted chemical potential for species 1 in box 1 is\s+([-0-9.Ee+]+)", log).group(1))
+    data = {"widom_var_mean": wprp[:, 1], "widom_var_sub": wprp2, "n_overlaps": wprp[:, 3], "mu_prime_kjmol": mu}
+    for f in (1, 2, 3):
+        rows = []
+        for ln in open(os.path.join(base, "species1", f"frag{f}", f"frag{f}.dat")):
+            parts = ln.split()
+            if len(parts) == 4:
+                rows.append([float(v) for v in parts[1:]])
+        data[f"frag{f}"] = np.array(rows).reshape(-1, 3, 3)
+    np.savez_compressed(os.path.join(OUT, "widom_pentane.npz"), **data)
+
+
 if __name__ == "__main__":
     nist_lj()
     nist_spce()
     pregen("water_spce", "spce_traj", "spce_widom.out.prp", "spce.mcf", "spce_widom.inp")
     pregen("pentane", "pentane_traj", "pentane_widom.out.prp", "pentane.mcf", "pentane_widom.inp")
+    widom_pentane()
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

@@ -98,3 +98,22 @@ def pregen_system(name: str, frame: int) -> System:
     for m in range(nmol):
         ms.add(m + 1, 1, 1, xyz[na * m:na * (m + 1)])
     return System([sp], [bx], ms, ff, [nmol + 1])
+
+
+def pentane_widom_system(frame: int) -> System:
+    """A frame of the reference's pentane Widom fixture with its fragment libraries
+    (exampleResources/Widom/pentane: 60 united-atom pentanes in a 100 A box, 336 K,
+    rcut_low 2 A, rcut_cbmc 6.5 A, 14 A cut_tail)."""
+    s = pregen_system("pentane", frame)
+    d = golden("widom_pentane.npz")
+    s.species[0].libraries = [d["frag1"], d["frag2"], d["frag3"]]
+    return s
+
+
+def de_broglie(system: System, is_: int = 1, ibox: int = 1) -> float:
+    """h / sqrt(2 pi m kT) in A with the reference's h_plank and kboltz (input_routines.f90:4265-4268)."""
+    import math
+    T = system.boxes[ibox - 1].temperature
+    beta = 1.0 / (0.8314472 * T)
+    mw = sum(a.mass for a in system.species[is_ - 1].atoms)
+    return 39.9031268605 * math.sqrt(beta / (2.0 * math.pi * mw))
