@@ -149,6 +149,8 @@ SIGNATURES = {
     "get_molecule": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _f64p]),
     "get_molecule_boxes": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _i32p]),
     "set_cbmc_options": (C.c_int, [C.c_void_p, C.POINTER(CassCBMCOptions)]),
+    "volume_scale": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.POINTER(CassEnergy), _i32p]),
+    "volume_restore": (C.c_int, [C.c_void_p, C.c_int32]),
     "mol_inter_energy": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _f64p, _f64p, _i32p]),
     "mol_intra_energy": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _f64p, _f64p, _f64p, _i32p]),
     "system_total_energy": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(CassEnergy), _i32p]),
@@ -298,6 +300,16 @@ class Context:
         """CBMC_Info energy_table N, Cell_List_Overlap and Rcutoff_Low adaptive U of the input file."""
         o = CassCBMCOptions(energy_table_res, int(sector_overlap), rmin_u_max)
         self._check("set_cbmc_options", self._f["set_cbmc_options"](self._h, C.byref(o)))
+
+    def volume_scale(self, ibox: int, new_length: float):
+        """Scale cubic box ibox to edge new_length (COMs kept fractional); returns (energy dict, overlap)."""
+        e = CassEnergy()
+        ov = C.c_int32()
+        self._check("volume_scale", self._f["volume_scale"](self._h, ibox, new_length, C.byref(e), C.byref(ov)))
+        return e.as_dict(), bool(ov.value)
+
+    def volume_restore(self, ibox: int) -> None:
+        self._check("volume_restore", self._f["volume_restore"](self._h, ibox))
 
     def molecule_boxes(self, is_: int) -> np.ndarray:
         """Box of every molecule slot im = 1..max_molecules of species is_ (0: not live)."""

@@ -680,7 +680,11 @@ int sync_result(cass_ctx* c, int n) {
 
 int ensure_cos_mol(cass_ctx* c, int nv) {
   if (nv <= c->cos_mol_stride && c->d_cos_mol.p) return CASS_OK;
-  int stride = std::max(nv, c->cos_mol_stride);
+  // a quarter more k-vectors than needed, so that volume moves rarely regrow the rows
+  int stride = std::max(nv + nv / 4, c->cos_mol_stride);
+  if (c->d_cos_mol.p)  // the rows of every molecule are lost: boxes with an Ewald sum must be recomputed
+    for (BoxH& B : c->box)
+      if (B.desc.charge_style == CASS_CHARGE_COUL && B.desc.charge_sum_style == CASS_QQ_EWALD) B.energy_valid = false;
   size_t bytes = (size_t)std::max(1, c->nmol_slots) * stride * sizeof(double);
   int rc = c->d_cos_mol.reserve(bytes);
   if (!rc) rc = c->d_sin_mol.reserve(bytes);
@@ -1354,6 +1358,89 @@ int cass_get_molecule_boxes(cass_ctx* c, int32_t is, int32_t n, int32_t* which_b
   if (is < 1 || is > c->nspecies) return set_error(CASS_EINVAL, "species index out of range");
   if (n < 0 || n > c->max_mol[is - 1]) return set_error(CASS_EINVAL, "n out of range");
   for (int im = 1; im <= n; ++im) which_box[im - 1] = c->mol_box[mol_slot(c, im, is)] + 1;
+  return CASS_OK;
+}
+
+// Volume_Change (move_volume.f90:24-679), cubic boxes, up to its acceptance
+// test: every live molecule of the box keeps the fractional coordinates of
+// its COM and moves rigidly (:296-336), the box gets the new edge and its
+// k-vectors (:374) and the system energy is recomputed (:426).  The old state
+// is kept for cass_volume_restore.
+int cass_volume_scale(cass_ctx* c, int32_t ibox1, double new_length, CassEnergy* e_new, int32_t* overlap) {
+  if (!c || ibox1 < 1 || ibox1 > c->nboxes || !e_new || !overlap || !(new_length > 0.0))
+    return set_error(CASS_EINVAL, "bad volume move arguments");
+  BoxH& B = c->box[ibox1 - 1];
+  if (!B.defined) return set_error(CASS_ESTATE, "box not defined");
+  if (!B.energy_valid) return set_error(CASS_ESTATE, "system energy of box not computed");
+  const CassBoxDesc d0 = B.desc;
+  if (d0.length[0] != d0.length[1] || d0.length[0] != d0.length[2])
+    return set_error(CASS_EUNSUPPORTED, "volume moves need a cubic box");
+  const double half = 0.5 * new_length;
+  if (half < d0.rcut_vdw || (d0.charge_style == CASS_CHARGE_COUL && half < d0.rcut_coul) ||
+      (d0.vdw_sum_style == CASS_VDW_SUM_CUT_SWITCH && half < d0.roff_switch))
+    return set_error(CASS_EINVAL, "cutoff greater than half the new box length (move_volume.f90:283-292)");
+  const double L0 = d0.length[0];
+  B.vol_saved = true;
+  B.vol_desc = d0;
+  B.vol_energy = B.energy;
+  B.vol_im.clear();
+  B.vol_is.clear();
+  B.vol_xyz.clear();
+  std::vector<double> xyz_new;
+  for (int slot : members(c, ibox1 - 1)) {
+    const int sp = c->slot_sp[slot];
+    const SpeciesH& s = c->sp[sp];
+    const int im = slot - c->mol_base[sp] + 1;
+    const double* x = &s.pos[(size_t)(im - 1) * 3 * s.natoms];
+    double tm = 0.0, com[3] = {0.0, 0.0, 0.0};  // Get_COM (get_com.f90:45-105)
+    for (int a = 0; a < s.natoms; ++a) {
+      tm += s.mass[a];
+      for (int k = 0; k < 3; ++k) com[k] += s.mass[a] * x[3 * a + k];
+    }
+    double sh[3];
+    for (int k = 0; k < 3; ++k) {
+      com[k] = com[k] / tm;
+      sh[k] = new_length * (com[k] / L0) - com[k];  // fractional COM kept (:300-323)
+    }
+    B.vol_im.push_back(im);
+    B.vol_is.push_back(sp + 1);
+    for (int a = 0; a < 3 * s.natoms; ++a) {
+      B.vol_xyz.push_back(x[a]);
+      xyz_new.push_back(x[a] + sh[a % 3]);
+    }
+  }
+  const int n = (int)B.vol_im.size();
+  std::vector<int32_t> boxes(n, ibox1);
+  int rc;
+  if (n > 0 && (rc = cass_set_molecules(c, n, B.vol_im.data(), B.vol_is.data(), boxes.data(), xyz_new.data())))
+    return rc;
+  CassBoxDesc d1 = d0;
+  d1.length[0] = d1.length[1] = d1.length[2] = new_length;
+  if ((rc = cass_set_box(c, ibox1, &d1))) return rc;
+  return cass_system_total_energy(c, ibox1, 1, e_new, overlap);
+}
+
+// Reset_Coords (move_volume.f90:555-677): the coordinates, box and energy
+// saved by the last cass_volume_scale of the box.  The structure factors are
+// recomputed from the restored coordinates; energy(ibox) is the saved value.
+int cass_volume_restore(cass_ctx* c, int32_t ibox1) {
+  if (!c || ibox1 < 1 || ibox1 > c->nboxes) return set_error(CASS_EINVAL, "bad box");
+  BoxH& B = c->box[ibox1 - 1];
+  if (!B.vol_saved) return set_error(CASS_ESTATE, "no volume move to restore");
+  const int n = (int)B.vol_im.size();
+  std::vector<int32_t> boxes(n, ibox1);
+  int rc;
+  if (n > 0 && (rc = cass_set_molecules(c, n, B.vol_im.data(), B.vol_is.data(), boxes.data(), B.vol_xyz.data())))
+    return rc;
+  const CassBoxDesc d0 = B.vol_desc;
+  const CassEnergy e0 = B.vol_energy;
+  if ((rc = cass_set_box(c, ibox1, &d0))) return rc;
+  CassEnergy e;
+  int32_t ov = 0;
+  if ((rc = cass_system_total_energy(c, ibox1, 1, &e, &ov))) return rc;
+  BoxH& B2 = c->box[ibox1 - 1];
+  B2.energy = e0;
+  B2.vol_saved = false;
   return CASS_OK;
 }
 

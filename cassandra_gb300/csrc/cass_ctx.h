@@ -113,6 +113,12 @@ struct BoxH {
   DevBuf d_p64, d_p32, d_meta, d_molinfo;
   DevBuf d_kvec, d_cos_sum, d_sin_sum, d_cos_old, d_sin_old;
   bool cell_dirty = true;
+  // the state cass_volume_scale keeps for cass_volume_restore
+  bool vol_saved = false;
+  CassBoxDesc vol_desc{};
+  CassEnergy vol_energy{};
+  std::vector<int> vol_im, vol_is;
+  std::vector<double> vol_xyz;
 };
 
 // in-place coordinate update of one packed atom (charge and type stay)

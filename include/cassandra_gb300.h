@@ -221,6 +221,21 @@ int cass_ewald_restore(cass_ctx* ctx, int32_t im, int32_t is, int32_t ibox);
 int cass_ewald_widom(cass_ctx* ctx, int32_t is, int32_t ibox, int32_t n,
                      const double* xyz, double* e_reciprocal);
 
+/* ---- volume moves ------------------------------------------------------ */
+/* Volume_Change (move_volume.f90:24-679) for a cubic box, split at its
+ * acceptance test so that the host keeps the random draw, the acceptance
+ * rule (:440-446) and the counters.  cass_volume_scale gives every live
+ * molecule of ibox the same fractional COM in the box of edge new_length and
+ * moves it rigidly (:296-336), sets the new edge and its k-vectors
+ * (Ewald_Reciprocal_Lattice_Vector_Setup, :374) and recomputes the system
+ * energy on the device (Compute_System_Total_Energy, :426); energy(ibox) is
+ * then the new energy.  The previous coordinates, box and energy are kept:
+ * cass_volume_restore brings them back (Reset_Coords, :555-677) after a
+ * rejection or an overlap.  The new half edge must not be shorter than the
+ * cutoffs (CASS_EINVAL, as :283-292 abort). */
+int cass_volume_scale(cass_ctx* ctx, int32_t ibox, double new_length, CassEnergy* energy, int32_t* overlap);
+int cass_volume_restore(cass_ctx* ctx, int32_t ibox);
+
 /* ---- CBMC options ----------------------------------------------------- */
 /* Input-file options that change how CBMC trial energies and trial overlaps
  * are computed; they apply to the calls that follow.

@@ -72,6 +72,7 @@ struct Species {
 
 struct Box {
   bool defined = false;
+  CassBoxDesc desc{};
   double L[3] = {0, 0, 0}, hL[3] = {0, 0, 0}, volume = 0;
   int vdw_style = 0, vdw_sum_style = 0, charge_style = 0, charge_sum_style = 0;
   double rcut_vdw = 0, rcut_coul = 0, rcut_cbmc = 0, rcut_low = 0, rcut_max = 0;
@@ -129,6 +130,15 @@ struct orc_ctx {
   std::vector<CbmcTab> tab;     // per box, when opt.energy_table_res > 0
   std::vector<double> rminsq;   // [ntypes][ntypes] r_min^2 of check_overlap
   double rlowsq = 0.0;          // rcut_low^2 shared by the boxes
+  // the state orc_volume_scale keeps for orc_volume_restore, per box
+  struct VolSave {
+    bool saved = false;
+    CassBoxDesc desc{};
+    CassEnergy energy{};
+    std::vector<int> im, is;
+    std::vector<double> xyz;
+  };
+  std::vector<VolSave> vol;
 };
 
 namespace {
@@ -2453,6 +2463,7 @@ int orc_set_box(orc_ctx* c, int32_t ibox, const CassBoxDesc* d) {
   if (check_ctx(c) || ibox < 1 || ibox > c->nboxes || !d) return fail(CASS_EINVAL, "bad box");
   Box& b = c->box[ibox - 1];
   b = Box();
+  b.desc = *d;
   c->cbmc_dirty = true;
   for (int k = 0; k < 3; ++k) {
     b.L[k] = d->length[k];
@@ -2563,6 +2574,80 @@ int orc_get_molecule_boxes(orc_ctx* c, int32_t is, int32_t n, int32_t* which_box
 static int cbmc_ready(orc_ctx* c) {
   if (c->opt.energy_table_res <= 0 && !c->opt.sector_overlap) return CASS_OK;
   return build_cbmc(c);
+}
+
+int orc_system_total_energy(orc_ctx* c, int32_t ibox1, int32_t intra_flag, CassEnergy* out, int32_t* overlap);
+
+// Volume_Change (move_volume.f90:24-679), cubic box, up to its acceptance
+// test: fractional COMs kept and molecules moved rigidly (:296-336), new edge
+// and k-vectors (:374), system energy recomputed (:426); the old state kept.
+int orc_volume_scale(orc_ctx* c, int32_t ibox1, double new_length, CassEnergy* e_new, int32_t* overlap) {
+  if (c) refresh_members(c);
+  if (check_ctx(c) || ibox1 < 1 || ibox1 > c->nboxes || !e_new || !overlap || !(new_length > 0.0))
+    return fail(CASS_EINVAL, "bad volume move arguments");
+  const Box& b = c->box[ibox1 - 1];
+  if (!b.defined) return fail(CASS_ESTATE, "box not defined");
+  if (!b.energy_valid) return fail(CASS_ESTATE, "system energy of box not computed");
+  const CassBoxDesc d0 = b.desc;
+  if (d0.length[0] != d0.length[1] || d0.length[0] != d0.length[2]) return fail(CASS_EUNSUPPORTED, "volume moves need a cubic box");
+  const double half = 0.5 * new_length;
+  if (half < d0.rcut_vdw || (d0.charge_style == CASS_CHARGE_COUL && half < d0.rcut_coul) ||
+      (d0.vdw_sum_style == CASS_VDW_SUM_CUT_SWITCH && half < d0.roff_switch))
+    return fail(CASS_EINVAL, "cutoff greater than half the new box length");
+  if ((int)c->vol.size() < c->nboxes) c->vol.resize(c->nboxes);
+  orc_ctx::VolSave& v = c->vol[ibox1 - 1];
+  v = orc_ctx::VolSave();
+  v.saved = true;
+  v.desc = d0;
+  v.energy = b.energy;
+  const double L0 = d0.length[0];
+  std::vector<double> xyz_new;
+  for (int slot : c->members[ibox1 - 1]) {
+    const Mol& m = c->mol[slot];
+    const Species& sp = c->sp[m.is];
+    double tm = 0.0, com[3] = {0.0, 0.0, 0.0};  // Get_COM (get_com.f90:45-105)
+    for (int a = 0; a < sp.natoms; ++a) {
+      tm += sp.mass[a];
+      for (int k = 0; k < 3; ++k) com[k] += sp.mass[a] * m.r[3 * a + k];
+    }
+    double sh[3];
+    for (int k = 0; k < 3; ++k) {
+      com[k] = com[k] / tm;
+      sh[k] = new_length * (com[k] / L0) - com[k];
+    }
+    v.im.push_back(slot - c->mol_base[m.is] + 1);
+    v.is.push_back(m.is + 1);
+    for (int a = 0; a < 3 * sp.natoms; ++a) {
+      v.xyz.push_back(m.r[a]);
+      xyz_new.push_back(m.r[a] + sh[a % 3]);
+    }
+  }
+  const int n = (int)v.im.size();
+  std::vector<int32_t> boxes(n, ibox1);
+  int rc;
+  if (n > 0 && (rc = orc_set_molecules(c, n, v.im.data(), v.is.data(), boxes.data(), xyz_new.data()))) return rc;
+  CassBoxDesc d1 = d0;
+  d1.length[0] = d1.length[1] = d1.length[2] = new_length;
+  if ((rc = orc_set_box(c, ibox1, &d1))) return rc;
+  return orc_system_total_energy(c, ibox1, 1, e_new, overlap);
+}
+
+// Reset_Coords (move_volume.f90:555-677)
+int orc_volume_restore(orc_ctx* c, int32_t ibox1) {
+  if (check_ctx(c) || ibox1 < 1 || ibox1 > c->nboxes) return fail(CASS_EINVAL, "bad box");
+  if ((int)c->vol.size() < c->nboxes || !c->vol[ibox1 - 1].saved) return fail(CASS_ESTATE, "no volume move to restore");
+  orc_ctx::VolSave v = c->vol[ibox1 - 1];
+  const int n = (int)v.im.size();
+  std::vector<int32_t> boxes(n, ibox1);
+  int rc;
+  if (n > 0 && (rc = orc_set_molecules(c, n, v.im.data(), v.is.data(), boxes.data(), v.xyz.data()))) return rc;
+  if ((rc = orc_set_box(c, ibox1, &v.desc))) return rc;
+  CassEnergy e;
+  int32_t ov = 0;
+  if ((rc = orc_system_total_energy(c, ibox1, 1, &e, &ov))) return rc;
+  c->box[ibox1 - 1].energy = v.energy;
+  c->vol[ibox1 - 1].saved = false;
+  return CASS_OK;
 }
 
 int orc_set_cbmc_options(orc_ctx* c, const CassCBMCOptions* o) {
