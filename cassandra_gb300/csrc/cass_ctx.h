@@ -152,6 +152,7 @@ struct cass_ctx_impl {
   std::vector<PatchRec> h_patch;
   DevBuf d_patch;
   DevBuf d_mc;    // Monte Carlo sweep descriptors, outputs and scratch
+  DevBuf d_mc_box;  // box layouts of MC sweeps too large for shared memory
   DevBuf d_grad;  // adjoint outputs and per-atom parameter derivatives
   DevBuf d_trial; // CBMC trial positions and their energies
   DevBuf d_gc;    // grand-canonical descriptors, records and outputs

@@ -75,6 +75,7 @@ struct McBox {
   CassEnergy* energy;  // in/out
   CassMCResult* res;   // out
   int* status;         // out: 0 ok, 1 overlapping molecule before a move
+  unsigned char* gbox; // the box layout in global memory (boxes too large for shared memory)
 };
 
 // the move thread 0 prepared for the block
@@ -127,9 +128,11 @@ __device__ __forceinline__ V block_sum_mc(V v, V* red, int slot) {
   return v;
 }
 
-template <bool MIXED>
+// GMEM: the box layout lives in a per-box global buffer (L2-resident) instead
+// of shared memory, for boxes above the shared-memory limit; same code
+template <bool MIXED, bool GMEM>
 __global__ void __launch_bounds__(kMcThreads) k_mc_sweeps(McArgs A, McBox* boxes, PairTable T) {
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ BoxDev b;
   __shared__ McMove mv;
   __shared__ double red[kMcWarps * 8];
@@ -143,6 +146,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_sweeps(McArgs A, McBox* boxes
     ljp[i] = ok ? make_float2(T.epsf[a * T.ntypes + c], T.sig2f[a * T.ntypes + c]) : make_float2(0.f, 0.f);
   }
   const int N = G.natoms, M = G.nmols;
+  unsigned char* smem = GMEM ? G.gbox : dsmem;
   // shared layout: x y z q (double), type, mol (int), [x y z type (float4), q (float)], COM (double x3), first, nat
   double* sx = reinterpret_cast<double*>(smem);
   double* sy = sx + N;
@@ -637,8 +641,8 @@ extern "C" int cass_mc_sweeps(cass_ctx* c, int32_t nboxes, const int32_t* iboxes
       max_nv = std::max(max_nv, B.nvecs);
     }
   }
-  if (smem > kMcSmemLimit)
-    return set_error(CASS_ECAPACITY, "mc sweeps hold a box in shared memory: at most about 4000 atoms per box");
+  // boxes above the shared-memory limit run with their layout in global memory
+  const bool gmem = smem > kMcSmemLimit;
   if (any_ewald && !c->d_cos_mol.p) return set_error(CASS_ESTATE, "structure factors not computed");
   A.cos_mol = c->d_cos_mol.as<double>();
   A.sin_mol = c->d_sin_mol.as<double>();
@@ -693,13 +697,25 @@ extern "C" int cass_mc_sweeps(cass_ctx* c, int32_t nboxes, const int32_t* iboxes
     g.status = d_status + k;
     hE[k] = B.energy;
   }
+  if (gmem) {
+    std::vector<size_t> off(nboxes);
+    size_t tot = 0;
+    for (int k = 0; k < nboxes; ++k) {
+      off[k] = tot;
+      tot += (mc_smem_bytes(hb[k].natoms, hb[k].nmols, mixed) + 255) & ~(size_t)255;
+    }
+    if ((rc = c->d_mc_box.reserve(std::max<size_t>(tot, 256)))) return rc;
+    for (int k = 0; k < nboxes; ++k) hb[k].gbox = static_cast<unsigned char*>(c->d_mc_box.p) + off[k];
+  }
   CASS_CUDA(h2d(c, d_box, hb.data(), nboxes * sizeof(McBox)));
   CASS_CUDA(h2d(c, d_E, hE.data(), nboxes * sizeof(CassEnergy)));
   CASS_CUDA(h2d(c, d_md, max_disp, nboxes * nsp * sizeof(double)));
   CASS_CUDA(h2d(c, d_mr, max_rot, nboxes * nsp * sizeof(double)));
   size_t dyn = 0;
   for (int k = 0; k < nboxes; ++k) dyn = std::max(dyn, mc_smem_bytes(hb[k].natoms, hb[k].nmols, mixed));
-  auto kern = mixed ? k_mc_sweeps<true> : k_mc_sweeps<false>;
+  auto kern = gmem ? (mixed ? k_mc_sweeps<true, true> : k_mc_sweeps<false, true>)
+                   : (mixed ? k_mc_sweeps<true, false> : k_mc_sweeps<false, false>);
+  if (gmem) dyn = 0;
   CASS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
   CASS_CUDA(cudaEventRecord(c->ev[0], c->stream));
   kern<<<nboxes, kMcThreads, dyn, c->stream>>>(A, d_box, c->pt);
