@@ -29,6 +29,7 @@ def test_volume_scale_matches_oracle_and_restores(factor):
             assert abs(eg[k] - eo[k]) <= 1e-10 * (abs(eo[k]) + 1.0), k
         assert np.allclose(_coords(g, s), _coords(o, s), rtol=0, atol=1e-12)
         g.volume_restore(1)
+        o.volume_restore(1)
         assert np.array_equal(_coords(g, s), x0)
         e2, _ = g.system_total_energy(1)
         assert abs(e2["total"] - eg0["total"]) <= 1e-10 * abs(eg0["total"])
