@@ -56,6 +56,10 @@ def parse():
     p.add_argument("--no-mc", action="store_true", help="skip the MC-sweep leg")
     p.add_argument("--no-grad", action="store_true", help="skip the configuration-gradient leg")
     p.add_argument("--no-gcmc", action="store_true", help="skip the grand-canonical leg")
+    p.add_argument("--no-npt", action="store_true", help="skip the NPT / fluctuation-formula leg")
+    p.add_argument("--npt-chains", type=int, default=32)
+    p.add_argument("--npt-eq-blocks", type=int, default=6)
+    p.add_argument("--npt-blocks", type=int, default=4, help="production blocks (configurations per chain)")
     return p.parse_args()
 
 
@@ -306,6 +310,73 @@ def gcmc_leg(cg, abi, dev, with_cpu: bool, eq_steps: int = 150000, blocks: int =
                                          f"state, FP64 C++ oracle, boxes in parallel"}
     gm.close()
     return out
+
+
+def npt_leg(cg, abi, dev, nchains: int, eq_blocks: int, prod_blocks: int) -> dict:
+    """NPT sampling of 4096 rigid waters (12,288 atoms, Ewald 1e-6, 12 A) at 298 K
+    and 1 bar -- mixed-precision translate/rotate sweeps on the device, volume moves
+    rebuilt on the device with the host's acceptance rule -- in `nchains`
+    independent chains, one configuration per chain after each block of one sweep
+    and one volume move; the fluctuation formula d<rho>/d(eps_O) =
+    -beta (<rho U'> - <rho><U'>) over the saved configurations, with
+    U' = dU/d(eps_OO) from the running LJ energy (LJ energies are linear in eps)
+    checked against the FP64 adjoint (cass_system_gradient) at the final
+    configurations of four chains."""
+    from cassandra_gb300 import npt, workloads
+    from cassandra_gb300.autograd import fluctuation_sensitivity
+    nmol, T = 4096, 298.0
+    s = workloads.water_gradient_system(nboxes=nchains)
+    boxes = list(range(1, nchains + 1))
+    eps_oo = float(s.ff.eps[0, 0])  # internal units (eps/k times kboltz)
+    mw = 15.999 + 2 * 1.008
+    rho, dud = [], []
+    with cg.open_system(s, precision=abi.PREC_MIXED, device=dev) as g:
+        ch = npt.NPTChains(g, boxes, [nmol] * nchains, T, 1.0, 400.0, [[0.25]] * nchains, [[0.25]] * nchains,
+                           seed=21)
+        ch.start([b.length[0] for b in s.boxes])
+        t0 = time.perf_counter()
+        sweep_ms = 0.0
+        for _ in range(eq_blocks):
+            ch.sweeps(1, prob_translate=0.5)
+            sweep_ms += g.stats()["mc_ms"]
+            ch.volume_moves()
+        t1 = time.perf_counter()
+        for _ in range(prod_blocks):
+            ch.sweeps(1, prob_translate=0.5)
+            sweep_ms += g.stats()["mc_ms"]
+            ch.volume_moves()
+            d = ch.densities(mw)
+            for k in range(nchains):
+                e = ch.components[k]
+                rho.append(d[k])
+                dud.append((e["inter_vdw"] + e["lrc"]) / eps_oo)
+        t2 = time.perf_counter()
+        check = []
+        for b in boxes[:4]:
+            e, _, de, _, _ = g.system_gradient(b, 3 * nmol)
+            k = b - 1
+            check.append(abs(de[0, 0] - dud[-nchains + k]) / abs(de[0, 0]))
+    rho, dud = np.array(rho), np.array(dud)
+    beta = 1.0 / (0.8314472 * T)
+    sens = fluctuation_sensitivity(rho, dud, beta) * 0.8314472  # per K of eps/k
+    # jackknife over chains (configurations of one chain are correlated)
+    per = np.arange(len(rho)) % nchains
+    jk = np.array([fluctuation_sensitivity(rho[per != c], dud[per != c], beta) * 0.8314472 for c in range(nchains)])
+    err = float(np.sqrt((nchains - 1) / nchains * np.sum((jk - jk.mean()) ** 2)))
+    blocks = eq_blocks + prod_blocks
+    return {"workload": f"NPT of 4096 rigid waters (12,288 atoms, 49.7 A start, Ewald tol 1e-6, 12 A) at 298 K and "
+                        f"1 bar, {nchains} chains, blocks of one sweep (4096 translate/rotate moves) and one volume "
+                        f"move per chain, mixed precision",
+            "configurations": int(len(rho)), "equilibration_blocks": eq_blocks, "production_blocks": prod_blocks,
+            "wall_s": t2 - t0, "production_configs_per_s": len(rho) / (t2 - t1),
+            "sweeps_per_s": nchains * blocks / (sweep_ms / 1e3),
+            "volume_acceptance": float(ch.n_vol_acc.sum() / max(1, ch.n_vol.sum())),
+            "mean_density_g_cm3": float(rho.mean()),
+            "d_rho_d_eps_O": {"value": sens, "jackknife_err": err, "unit": "g/cm^3 per K of eps_O/k",
+                              "formula": "-beta (<rho dU/deps> - <rho><dU/deps>)"},
+            "adjoint_check_max_rel_diff": float(max(check)),
+            "note": "configurations after short equilibration from the lattice start; the full 2000-configuration "
+                    "run is --npt-chains 32 --npt-blocks 63"}
 
 
 def gradient_leg(cg, abi, dev) -> dict:
@@ -569,6 +640,8 @@ def main():
         out["gcmc"] = gcmc_leg(cg, abi, dev, rank == 0 and world == 1 and not args.no_cpu_baseline)
     if not args.no_grad:
         out["gradient"] = gradient_leg(cg, abi, dev)
+    if not args.no_npt:
+        out["npt_fluctuation"] = npt_leg(cg, abi, dev, args.npt_chains, args.npt_eq_blocks, args.npt_blocks)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(system, args)
     if rank == 0:

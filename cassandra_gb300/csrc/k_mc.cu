@@ -34,6 +34,7 @@ namespace cassgpu {
 
 constexpr int kMcThreads = 128;
 constexpr int kMcWarps = kMcThreads / 32;
+constexpr int kMcThreadsG = 512;  // boxes in global memory: more lanes for their longer loops
 constexpr int kMaxSpeciesMC = 8;
 constexpr size_t kMcSmemLimit = 200 * 1024;
 
@@ -131,12 +132,13 @@ __device__ __forceinline__ V block_sum_mc(V v, V* red, int slot) {
 // GMEM: the box layout lives in a per-box global buffer (L2-resident) instead
 // of shared memory, for boxes above the shared-memory limit; same code
 template <bool MIXED, bool GMEM>
-__global__ void __launch_bounds__(kMcThreads) k_mc_sweeps(McArgs A, McBox* boxes, PairTable T) {
+__global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(McArgs A, McBox* boxes, PairTable T) {
+  constexpr int NW = (GMEM ? kMcThreadsG : kMcThreads) / 32;
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ BoxDev b;
   __shared__ McMove mv;
-  __shared__ double red[kMcWarps * 8];
-  __shared__ int redi[kMcWarps * 2];
+  __shared__ double red[NW * 8];
+  __shared__ int redi[NW * 2];
   __shared__ float2 ljp[kMaxTypes * kMaxTypes];
   McBox& G = boxes[blockIdx.x];
   if (threadIdx.x == 0) b = G.b;
@@ -407,7 +409,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_sweeps(McArgs A, McBox* boxes
     if (threadIdx.x == 0) {
       dv = dq = 0.0;
       int o = 0, n = 0;
-      for (int w = 0; w < kMcWarps; ++w) {
+      for (int w = 0; w < NW; ++w) {
         dv += red[w * 8];
         dq += red[w * 8 + 1];
         o |= redi[2 * w];
@@ -460,7 +462,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_sweeps(McArgs A, McBox* boxes
       block_sum_mc(part, red, 4);
       __syncthreads();
       if (threadIdx.x == 0) {
-        for (int w = 0; w < kMcWarps; ++w) e_recip += red[w * 8 + 4];
+        for (int w = 0; w < NW; ++w) e_recip += red[w * 8 + 4];
         e_recip *= kCHARGE_FACTOR;
       }
     }
@@ -718,7 +720,7 @@ extern "C" int cass_mc_sweeps(cass_ctx* c, int32_t nboxes, const int32_t* iboxes
   if (gmem) dyn = 0;
   CASS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
   CASS_CUDA(cudaEventRecord(c->ev[0], c->stream));
-  kern<<<nboxes, kMcThreads, dyn, c->stream>>>(A, d_box, c->pt);
+  kern<<<nboxes, gmem ? kMcThreadsG : kMcThreads, dyn, c->stream>>>(A, d_box, c->pt);
   CASS_CUDA(cudaGetLastError());
   CASS_CUDA(cudaEventRecord(c->ev[1], c->stream));
   count_launch(c);

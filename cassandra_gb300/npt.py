@@ -45,7 +45,8 @@ class NPTChains:
         self.seed = seed
         self.block = 0
         self.length = [None] * len(self.boxes)
-        self.energy = [None] * len(self.boxes)
+        self.energy = [None] * len(self.boxes)   # running total energy of each box
+        self.components = [None] * len(self.boxes)  # its components (CassEnergy as a dict)
         self.n_vol = np.zeros(len(self.boxes), dtype=np.int64)
         self.n_vol_acc = np.zeros(len(self.boxes), dtype=np.int64)
 
@@ -55,6 +56,7 @@ class NPTChains:
             if ov:
                 raise RuntimeError(f"box {b} starts with an overlap")
             self.energy[k] = e["total"]
+            self.components[k] = e
             self.length[k] = float(lengths[k])
 
     def sweeps(self, nsweeps: int, prob_translate: float = 1.0) -> None:
@@ -64,6 +66,7 @@ class NPTChains:
         self.block += 1
         for k, r in enumerate(res):
             self.energy[k] = r["energy"]["total"]
+            self.components[k] = r["energy"]
 
     def volume_moves(self) -> None:
         for k, b in enumerate(self.boxes):
@@ -86,6 +89,7 @@ class NPTChains:
                 self.n_vol_acc[k] += 1
                 self.length[k] = L_new
                 self.energy[k] = e_new["total"]
+                self.components[k] = e_new
             else:
                 self.ctx.volume_restore(b)
 

@@ -223,10 +223,12 @@ def water_nvt_system(nboxes: int = 1, nmol: int = 256, length: float = 19.7, tem
 
 
 def water_gradient_system(nmol: int = 4096, length: float = 49.7, temperature: float = 298.0, rcut: float = 12.0,
-                          tol: float = 1e-6, min_inter: float = 1.5, seed: int = 13) -> System:
+                          tol: float = 1e-6, min_inter: float = 1.5, seed: int = 13, nboxes: int = 1) -> System:
     """Rigid 3-site waters on a cubic lattice with random orientations, each
     orientation redrawn until its atoms are at least min_inter from every atom
-    of the molecules already placed; one Ewald box (the gradient workload)."""
+    of the molecules already placed; one Ewald box (the gradient workload).
+    With nboxes > 1 the further boxes are copies of the first shifted by a
+    random periodic translation (replicas for independent chains)."""
     rng = np.random.default_rng(seed)
     sp = water_species()
     ff = ForceField([sp])
@@ -257,9 +259,18 @@ def water_gradient_system(nmol: int = 4096, length: float = 49.7, temperature: f
                 placed[(ix, iy, iz)] = xyz
                 ms.add(k + 1, 1, 1, xyz)
                 k += 1
-    bx = BoxSpec(length=(length,) * 3, rcut_vdw=rcut, rcut_coul=rcut, rcut_cbmc=min(6.5, rcut), rcut_low=0.85,
-                 charge_style=abi.CHARGE_COUL, charge_sum_style=abi.QQ_EWALD, ewald_tol=tol, temperature=temperature)
-    return System([sp], [bx], ms, ff, [nmol])
+    boxes = [BoxSpec(length=(length,) * 3, rcut_vdw=rcut, rcut_coul=rcut, rcut_cbmc=min(6.5, rcut), rcut_low=0.85,
+                     charge_style=abi.CHARGE_COUL, charge_sum_style=abi.QQ_EWALD, ewald_tol=tol,
+                     temperature=temperature) for _ in range(nboxes)]
+    first = list(ms.xyz)
+    for b in range(2, nboxes + 1):
+        shift = rng.uniform(-0.5 * length, 0.5 * length, 3)
+        for m, xyz in enumerate(first):
+            x = xyz + shift
+            c = x.mean(0)
+            x = x - length * np.round(c / length)  # fold by the molecule's centre
+            ms.add(m + 1 + (b - 1) * nmol, 1, b, x)
+    return System([sp], boxes, ms, ff, [nmol * nboxes])
 
 
 def gcmc_system(nboxes: int = 16, length: float = 40.0, temperature: float = 300.0, rcut: float = 14.0,
