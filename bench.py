@@ -57,6 +57,8 @@ def parse():
     p.add_argument("--no-grad", action="store_true", help="skip the configuration-gradient leg")
     p.add_argument("--no-gcmc", action="store_true", help="skip the grand-canonical leg")
     p.add_argument("--no-npt", action="store_true", help="skip the NPT / fluctuation-formula leg")
+    p.add_argument("--no-pregen", action="store_true", help="skip the trajectory-fed Widom leg")
+    p.add_argument("--pregen-frames", type=int, default=4)
     p.add_argument("--npt-chains", type=int, default=32)
     p.add_argument("--npt-eq-blocks", type=int, default=6)
     p.add_argument("--npt-blocks", type=int, default=4, help="production blocks (configurations per chain)")
@@ -379,6 +381,71 @@ def npt_leg(cg, abi, dev, nchains: int, eq_blocks: int, prod_blocks: int) -> dic
                     "run is --npt-chains 32 --npt-blocks 63"}
 
 
+def pregen_leg(cg, abi, system, n_per_box: int, kappa: int, nframes: int, seed: int) -> dict:
+    """The headline Widom workload streamed from trajectory files, as the pregen
+    driver runs it: per box an .xyz/.H trajectory of `nframes` frames (the frozen
+    box with every atom displaced by N(0, 0.05 A) per frame, written to a
+    temporary directory), read by the library's reader threads one frame ahead;
+    per frame cass_load_next_frame, the system energy of every box and one
+    batched Widom call.  The first frame is untimed."""
+    import shutil
+    import tempfile
+    from cassandra_gb300 import io, pregen
+    boxes = list(range(1, len(system.boxes) + 1))
+    rng = np.random.default_rng(seed)
+    ms = system.molecules
+    xyz_all = ms.flat_xyz().reshape(-1, 3)
+    td = tempfile.mkdtemp(prefix="cass_pregen_")
+    try:
+        t0 = time.perf_counter()
+        paths = []
+        for b in boxes:
+            x0 = xyz_all[np.asarray(ms.ibox) == b]
+            L = system.boxes[b - 1].length
+            xp, hp = os.path.join(td, f"box{b}.xyz"), os.path.join(td, f"box{b}.H")
+            with open(xp, "w") as fx, open(hp, "w") as fh:
+                for k in range(nframes + 1):
+                    x = x0 + rng.normal(scale=0.05, size=x0.shape)
+                    io.write_xyz_frame(fx, x, ["LJ"] * len(x), k)
+                    io.write_H_frame(fh, L, [len(x), 0])
+            paths.append((xp, hp))
+        t_write = time.perf_counter() - t0
+        text_bytes = sum(os.path.getsize(p) for pair in paths for p in pair)
+        with cg.open_system(system, precision=abi.PREC_MIXED) as ctx:
+            trajs = [cg.open_trajectory(xp, hp, [1, 4]) for xp, hp in paths]
+            try:
+                pregen.pregen_widom(ctx, trajs, [2], n_per_box, kappa, kappa, seed=seed, max_frames=1)
+                s0 = ctx.stats()
+                p0 = sum(t.stats()["parse_s"] for t in trajs)
+                t0 = time.perf_counter()
+                recs = pregen.pregen_widom(ctx, trajs, [2], n_per_box, kappa, kappa, seed=seed + 1,
+                                           max_frames=nframes)
+                wall = time.perf_counter() - t0
+                s1 = ctx.stats()
+                parse = sum(t.stats()["parse_s"] for t in trajs) - p0
+            finally:
+                for t in trajs:
+                    t.close()
+        nf = len(recs)
+        trials = n_per_box * len(boxes) * 2 * kappa * nf
+        return {"workload": f"{len(boxes)} LJ boxes streamed from .xyz/.H trajectories, {n_per_box * len(boxes)} "
+                            f"butane insertions per frame (kappa {kappa}/{kappa}), mixed precision",
+                "frames": nf, "value": trials / wall, "unit": UNIT, "frames_per_s": nf / wall,
+                "load_s_per_frame": float(np.mean([r["load_s"] for r in recs])),
+                "energy_s_per_frame": float(np.mean([r["energy_s"] for r in recs])),
+                "widom_s_per_frame": float(np.mean([r["widom_s"] for r in recs])),
+                "reader_parse_s_per_frame": parse / nf, "reader_threads": len(trajs),
+                "text_mb_per_frame": text_bytes / (nframes + 1) / 1e6,
+                "h2d_bytes_per_frame": int((s1["h2d_bytes"] - s0["h2d_bytes"]) / nf),
+                "d2h_bytes_per_frame": int((s1["d2h_bytes"] - s0["d2h_bytes"]) / nf),
+                "write_s": t_write,
+                "note": "host wall clock per frame: load (waits for the reader only if it is behind; repack and "
+                        "pinned upload), system energies, Widom; reader_parse_s_per_frame is summed over the "
+                        "reader threads and runs during the previous frame's device work"}
+    finally:
+        shutil.rmtree(td, ignore_errors=True)
+
+
 def gradient_leg(cg, abi, dev) -> dict:
     """Configuration gradients/s of 4096 rigid waters with Ewald (FP64 adjoint),
     spot-checked against central differences of the FP64 GPU energy."""
@@ -634,6 +701,8 @@ def main():
                       "note": "per step: set_molecules of all boxes, system_total_energy of each box, widom_insert; "
                               "host wall clock"}
     gctx.close()
+    if not args.no_pregen:
+        out["pregen_feed"] = pregen_leg(cg, abi, system, n_per_box, args.kappa, args.pregen_frames, args.seed + 31)
     if not args.no_mc:
         out["mc_sweeps"] = mc_leg(cg, abi, dev, rank == 0 and world == 1 and not args.no_cpu_baseline)
     if not args.no_gcmc:

@@ -39,6 +39,11 @@ def open_system(system, precision: int = abi.PREC_MIXED, device: int = 0, max_kv
     return system.open(functions(), precision=precision, device=device, max_kvectors=max_kvectors)
 
 
+def open_trajectory(xyz_path: str, h_path: str | None, natoms, nmols=None, box=None) -> abi.Trajectory:
+    """Open a pregenerated trajectory (.xyz and, optionally, .H) for cass_load_next_frame."""
+    return abi.Trajectory(functions(), xyz_path, h_path, natoms, nmols, box)
+
+
 def header_functions() -> list:
     """Names of the entry points declared in include/cassandra_gb300.h."""
     import re

@@ -130,6 +130,12 @@ class CassStats(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class CassFrame(C.Structure):
+    _fields_ = [("status", C.c_int32), ("natoms", C.c_int32), ("index", C.c_int64), ("box", C.c_double * 9),
+                ("nmols", C.POINTER(C.c_int32)), ("xyz", C.POINTER(C.c_double)), ("pinned", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
 TRACE_DTYPE = np.dtype([("widom_var", "f8"), ("ln_pbias", "f8"), ("e_inter", "f8"),
                         ("e_first_trial_sum", "f8"), ("e_inter_abs", "f8"), ("selected_trial", "i4"),
                         ("overlap", "i4")])
@@ -171,11 +177,17 @@ SIGNATURES = {
     "mol_box_energy_noalloc": (C.c_int, [C.POINTER(CassBoxDesc), C.c_int32, _f64p, _f64p, C.c_void_p, C.c_void_p,
                                          C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32,
                                          C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "traj_open": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, _i32p, _i32p, _f64p, C.POINTER(C.c_void_p)]),
+    "traj_next": (C.c_int, [C.c_void_p, C.POINTER(CassFrame)]),
+    "traj_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
+    "traj_close": (C.c_int, [C.c_void_p]),
+    "load_next_frame": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), _i32p]),
     "get_stats": (C.c_int, [C.c_void_p, C.POINTER(CassStats)]),
     "set_count_pairs": (C.c_int, [C.c_void_p, C.c_int32]),
     "set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
-OPTIONAL = {"get_stats", "set_count_pairs", "set_stream", "mol_box_energy_noalloc", "system_gradient", "gcmc"}
+OPTIONAL = {"get_stats", "set_count_pairs", "set_stream", "mol_box_energy_noalloc", "system_gradient", "gcmc",
+            "traj_open", "traj_next", "traj_stats", "traj_close", "load_next_frame"}
 
 
 class CassError(RuntimeError):
@@ -311,6 +323,13 @@ class Context:
     def volume_restore(self, ibox: int) -> None:
         self._check("volume_restore", self._f["volume_restore"](self._h, ibox))
 
+    def load_next_frame(self, trajectories) -> bool:
+        """Load_Next_Frame: the next frame of trajectories[k] into box k+1; True at the end of a trajectory."""
+        hs = (C.c_void_p * len(trajectories))(*[t._h for t in trajectories])
+        end = np.zeros(1, dtype=np.int32)
+        self._check("load_next_frame", self._f["load_next_frame"](self._h, len(trajectories), hs, _p(end)))
+        return bool(end[0])
+
     def molecule_boxes(self, is_: int) -> np.ndarray:
         """Box of every molecule slot im = 1..max_molecules of species is_ (0: not live)."""
         out = np.zeros(self.max_molecules[is_ - 1], dtype=np.int32)
@@ -428,3 +447,61 @@ class Context:
         if trace:
             return out, tr.reshape(len(b), n_insertions)
         return out
+
+
+class Trajectory:
+    """A pregenerated trajectory of one box (.xyz + optional .H), read one frame
+    ahead by the library's reader thread into pinned host memory."""
+
+    def __init__(self, fns: dict, xyz_path: str, h_path: str | None, natoms: Sequence[int],
+                 nmols: Sequence[int] | None = None, box=None):
+        self._f = fns
+        self.natoms = _i32(natoms)
+        self._nm = _i32(nmols) if nmols is not None else None
+        self._box = None
+        if box is not None:
+            b = np.asarray(box, dtype=np.float64)
+            self._box = _f64(np.diag(b) if b.shape == (3,) else b.reshape(3, 3))
+        h = C.c_void_p()
+        rc = fns["traj_open"](xyz_path.encode(), h_path.encode() if h_path else None, len(self.natoms),
+                              _p(self.natoms), _p(self._nm), _p(self._box), C.byref(h))
+        if rc != CASS_OK:
+            raise CassError("traj_open", rc, fns["last_error"]().decode(errors="replace"))
+        self._h = h
+        self.nspecies = len(self.natoms)
+
+    def next(self) -> dict | None:
+        """The next frame as arrays (copied), or None at the end of the trajectory."""
+        fr = CassFrame()
+        rc = self._f["traj_next"](self._h, C.byref(fr))
+        if rc != CASS_OK:
+            raise CassError("traj_next", rc, self._f["last_error"]().decode(errors="replace"))
+        if fr.status != 0:
+            return None
+        xyz = np.ctypeslib.as_array(fr.xyz, shape=(fr.natoms * 3,)).reshape(-1, 3).copy() if fr.natoms else \
+            np.zeros((0, 3))
+        return {"index": fr.index, "box": np.array(fr.box[:]).reshape(3, 3),
+                "nmols": np.ctypeslib.as_array(fr.nmols, shape=(self.nspecies,)).copy(), "xyz": xyz,
+                "pinned": bool(fr.pinned)}
+
+    def stats(self) -> dict:
+        n, t = C.c_int64(), C.c_double()
+        self._f["traj_stats"](self._h, C.byref(n), C.byref(t))
+        return {"frames": n.value, "parse_s": t.value}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._f["traj_close"](self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -13,10 +13,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcassgpu.so")
-SOURCES = ["cass_abi.cu", "k_widom.cu", "k_mc.cu", "k_grad.cu", "k_gcmc.cu", "cass_noalloc.cu"]
+SOURCES = ["cass_abi.cu", "k_widom.cu", "k_mc.cu", "k_grad.cu", "k_gcmc.cu", "cass_noalloc.cu", "cass_traj.cu"]
 HEADERS = ["cass_device.cuh", "cass_molecule.cuh", "cass_cbmc.cuh", "cass_cbmc_f.cuh", "cass_ctx.h"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3", "-std=c++17",
-              "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
+              "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off"]
 
 
 def _nvcc() -> str:

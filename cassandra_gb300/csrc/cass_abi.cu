@@ -622,50 +622,55 @@ void set_mol_box(cass_ctx* c, int slot, int ibox) {
   c->mol_box[slot] = ibox;
 }
 
-// Packs the live molecules of a box (species-major, locate order) and uploads.
+// Packs the live molecules of a box (species-major, locate order) into the
+// context's pinned staging buffer and uploads it.
 int pack_box(cass_ctx* c, int ibox) {
   BoxH& B = c->box[ibox];
   if (!B.pack_dirty) return CASS_OK;
-  std::vector<double4_32a> p64;
-  std::vector<float4> p32;
-  std::vector<int4> meta;
-  std::vector<int4> molinfo;
-  B.pk_mol.clear();
-  B.pk_mol_off.clear();
-  for (int slot : members(c, ibox)) {
-    {
-      const int is = c->slot_sp[slot], im = slot - c->mol_base[is];
-      const SpeciesH& s = c->sp[is];
-      c->pk_index[slot] = (int)B.pk_mol.size();
-      B.pk_mol.push_back(slot);
-      B.pk_mol_off.push_back((int)p64.size());
-      molinfo.push_back(make_int4(slot, is, (int)p64.size(), s.natoms));
-      const double* r = &s.pos[(size_t)im * 3 * s.natoms];
-      for (int a = 0; a < s.natoms; ++a) {
-        p64.push_back(make_double4_32a(r[3 * a], r[3 * a + 1], r[3 * a + 2], s.q[a]));
-        float tf;
-        int ty = s.type[a];
-        memcpy(&tf, &ty, sizeof(float));
-        p32.push_back(make_float4((float)r[3 * a], (float)r[3 * a + 1], (float)r[3 * a + 2], tf));
-        meta.push_back(make_int4(slot, s.type[a], is, a));
-      }
-    }
-  }
-  B.npacked = (int)p64.size();
-  B.npacked_mols = (int)molinfo.size();
-  size_t n = std::max<size_t>(1, p64.size());
+  const std::vector<int>& mem = members(c, ibox);
+  size_t na = 0;
+  for (int slot : mem) na += (size_t)c->sp[c->slot_sp[slot]].natoms;
+  const size_t nm = mem.size();
+  const size_t n = std::max<size_t>(1, na), m = std::max<size_t>(1, nm);
   int rc = B.d_p64.reserve(n * sizeof(double4_32a));
   if (!rc) rc = B.d_p32.reserve(n * sizeof(float4));
   if (!rc) rc = B.d_meta.reserve(n * sizeof(int4));
-  if (!rc) rc = B.d_molinfo.reserve(std::max<size_t>(1, molinfo.size()) * sizeof(int4));
+  if (!rc) rc = B.d_molinfo.reserve(m * sizeof(int4));
+  if (!rc) rc = c->h_pack.reserve(n * (sizeof(double4_32a) + sizeof(float4) + sizeof(int4)) + m * sizeof(int4));
   if (rc) return rc;
-  if (!p64.empty()) {
-    CASS_CUDA(h2d(c, B.d_p64.p, p64.data(), p64.size() * sizeof(double4_32a)));
-    CASS_CUDA(h2d(c, B.d_p32.p, p32.data(), p32.size() * sizeof(float4)));
-    CASS_CUDA(h2d(c, B.d_meta.p, meta.data(), meta.size() * sizeof(int4)));
-    CASS_CUDA(h2d(c, B.d_molinfo.p, molinfo.data(), molinfo.size() * sizeof(int4)));
+  double4_32a* p64 = c->h_pack.as<double4_32a>();
+  float4* p32 = reinterpret_cast<float4*>(p64 + na);
+  int4* meta = reinterpret_cast<int4*>(p32 + na);
+  int4* molinfo = meta + na;
+  B.pk_mol.clear();
+  B.pk_mol_off.clear();
+  int k = 0;
+  for (int slot : mem) {
+    const int is = c->slot_sp[slot], im = slot - c->mol_base[is];
+    const SpeciesH& s = c->sp[is];
+    c->pk_index[slot] = (int)B.pk_mol.size();
+    molinfo[B.pk_mol.size()] = make_int4(slot, is, k, s.natoms);
+    B.pk_mol.push_back(slot);
+    B.pk_mol_off.push_back(k);
+    const double* r = &s.pos[(size_t)im * 3 * s.natoms];
+    for (int a = 0; a < s.natoms; ++a, ++k) {
+      p64[k] = make_double4_32a(r[3 * a], r[3 * a + 1], r[3 * a + 2], s.q[a]);
+      float tf;
+      int ty = s.type[a];
+      memcpy(&tf, &ty, sizeof(float));
+      p32[k] = make_float4((float)r[3 * a], (float)r[3 * a + 1], (float)r[3 * a + 2], tf);
+      meta[k] = make_int4(slot, s.type[a], is, a);
+    }
   }
-  // pageable host vectors go out of scope below: wait for the copies
+  B.npacked = (int)na;
+  B.npacked_mols = (int)nm;
+  if (na > 0) {
+    CASS_CUDA(h2d(c, B.d_p64.p, p64, na * sizeof(double4_32a)));
+    CASS_CUDA(h2d(c, B.d_p32.p, p32, na * sizeof(float4)));
+    CASS_CUDA(h2d(c, B.d_meta.p, meta, na * sizeof(int4)));
+    CASS_CUDA(h2d(c, B.d_molinfo.p, molinfo, nm * sizeof(int4)));
+  }
+  // the staging buffer is refilled by the next pack: wait for the copies
   CASS_CUDA(cudaStreamSynchronize(c->stream));
   B.pack_dirty = false;
   return CASS_OK;

@@ -69,6 +69,37 @@ struct DevBuf {
   }
 };
 
+// Owning page-locked host buffer (cudaHostAlloc): the source of
+// asynchronous uploads.
+struct PinnedBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  PinnedBuf() = default;
+  PinnedBuf(const PinnedBuf&) = delete;
+  PinnedBuf& operator=(const PinnedBuf&) = delete;
+  ~PinnedBuf() { release(); }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  // grows (never shrinks, contents not kept); returns a CASS status
+  int reserve(size_t n) {
+    if (n <= bytes) return CASS_OK;
+    release();
+    if (cudaHostAlloc(&p, n, cudaHostAllocDefault) != cudaSuccess) {
+      p = nullptr;
+      return set_error(CASS_ENOMEM, "pinned host allocation failed");
+    }
+    bytes = n;
+    return CASS_OK;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
 struct SpeciesH {
   bool defined = false;
   int natoms = 0;
@@ -174,6 +205,8 @@ struct cass_ctx_impl {
   CassCBMCOptions cbmc_opt{};
   bool cbmc_dirty = true;
   DevBuf d_cbmc_tab;
+  // pinned staging of the packed-box uploads
+  PinnedBuf h_pack;
 };
 
 // builds the CBMC-option tables if needed and points each box's BoxDev at them

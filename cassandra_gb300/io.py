@@ -5,6 +5,9 @@ Bond_Info, Angle_Info, Dihedral_Info, Improper_Info, Intra_Scaling,
 Fragment_Info, Fragment_Connectivity); units are converted later, in
 cassandra_gb300.system.  read_frag_library reads a fragment library .dat as
 written by Cassandra's fragment runs (coordinates per conformation).
+write_xyz_frame / write_H_frame write the two files of a pregenerated
+trajectory in the layout Load_Next_Frame reads (load_next_frame.f90:184-228,
+307-328); the trajectory itself is read by the library (cass_traj_open).
 """
 from __future__ import annotations
 
@@ -93,3 +96,26 @@ def read_frag_library(text: str, natoms: int) -> np.ndarray:
                 continue
     arr = np.asarray(rows, dtype=np.float64)
     return arr.reshape(-1, natoms, 3)
+
+
+def write_xyz_frame(f, xyz, elements, step: int = 0) -> None:
+    """One .xyz frame: the atom count, a comment record, 'element x y z' per atom
+    (17 significant digits, so that a read gives back the same doubles)."""
+    xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
+    f.write(f"{len(xyz):12d}\n MC_STEP: {step:12d}\n")
+    for e, (x, y, z) in zip(elements, xyz):
+        f.write(f"{e:<4s}{x:26.17e}{y:26.17e}{z:26.17e}\n")
+
+
+def write_H_frame(f, box, nmols) -> None:
+    """One .H frame: the volume, the three rows of the box matrix, a blank record,
+    the number of species and one 'species nmols' record each."""
+    b = np.asarray(box, dtype=np.float64)
+    m = np.diag(b) if b.shape == (3,) else b.reshape(3, 3)
+    f.write(f"{abs(np.linalg.det(m)):26.17e}\n")
+    for r in m:
+        f.write("".join(f"{v:26.17e}" for v in r) + "\n")
+    f.write("\n")
+    f.write(f"{len(nmols):12d}\n")
+    for k, n in enumerate(nmols):
+        f.write(f"{k + 1:12d}{int(n):12d}\n")

@@ -404,6 +404,54 @@ int cass_mol_box_energy_noalloc(const CassBoxDesc* box, int32_t ntypes, const do
                                 int32_t skip_mol, int32_t cbmc_flag, int32_t l_coul_cbmc, int32_t precision,
                                 double* out, void* stream);
 
+/* ---- trajectory feed (the pregen driver's frames) ---------------------- */
+/* A pregenerated trajectory of one box, as Load_Next_Frame reads it
+ * (load_next_frame.f90:5-330; files opened by Get_Pregen_Info,
+ * input_routines.f90:5717-5880).  The .xyz file holds, per frame, an atom-count
+ * record, a comment record and one "element x y z" record per atom
+ * (Read_xyz_frame, :307-328); the .H file holds, per frame, a volume record,
+ * the three rows of the box matrix, one skipped record, the number of species
+ * listed and one "species nmols" record each (Read_H_frame, :184-228).
+ * Without an .H file the molecule counts `nmols` and the box `box` (3 x 3,
+ * rows) are fixed for every frame (the "# Pregen_Info" entries).  A reader
+ * thread parses the next frame into pinned host memory while the caller uses
+ * the current one. */
+typedef struct cass_traj cass_traj;
+typedef struct CassFrame {
+  int32_t status;         /* 0: a frame; 1: the end of the trajectory was reached */
+  int32_t natoms;         /* atoms of the frame (natoms_to_read) */
+  int64_t index;          /* 0-based frame number */
+  double box[9];          /* box_list%length, row-major (Read_H_frame) */
+  const int32_t* nmols;   /* [nspecies] molecules of each species (nmols_to_read) */
+  const double* xyz;      /* [natoms][3] species-major, in pinned host memory;
+                             valid until the next cass_traj_next or cass_load_next_frame */
+  int32_t pinned;         /* 1 when xyz is page-locked */
+  int32_t reserved;
+} CassFrame;
+/* natoms[is-1] = atoms per molecule of species is.  h_path may be NULL (then
+ * nmols and box are required).  Fails with CASS_EINVAL when a file cannot be
+ * opened. */
+int cass_traj_open(const char* xyz_path, const char* h_path, int32_t nspecies, const int32_t* natoms,
+                   const int32_t* nmols, const double* box, cass_traj** out);
+/* The next frame (status 1 at the end).  A malformed record fails with
+ * CASS_EINVAL and the record's line number in cass_last_error(). */
+int cass_traj_next(cass_traj* t, CassFrame* frame);
+/* Frames parsed and the reader thread's parse time, for measurement. */
+int cass_traj_stats(cass_traj* t, int64_t* frames, double* parse_seconds);
+int cass_traj_close(cass_traj* t);
+/* Load_Next_Frame (load_next_frame.f90:5-330): takes the next frame of
+ * traj[k] for box k+1 (nboxes = the context's box count); every molecule is
+ * first made not live; the molecules of box ibox are locates
+ * base+1..base+nmols_to_read of each species, base = those of the same species
+ * in lower boxes (:239-246); each molecule's COM is folded into the box with
+ * Apply_PBC_Anint and its atoms shifted rigidly (:257-283); a box whose
+ * matrix changed gets the new edges and k-vectors (Set_Frame_Box, :57-102;
+ * orthorhombic matrices only).  The packed coordinates are uploaded from
+ * pinned memory.  The energies are then rebuilt by cass_system_total_energy
+ * (pregen_driver.f90:187).  On the end of any trajectory, *end_reached = 1 and
+ * the context is unchanged. */
+int cass_load_next_frame(cass_ctx* ctx, int32_t nboxes, cass_traj* const* traj, int32_t* end_reached);
+
 /* ---- run-time extensions (no counterpart in the reference) ------------- */
 /* Counters of a context, for measurement.  Times are CUDA-event durations on
  * the context's stream of the most recent cass_widom_insert call. */

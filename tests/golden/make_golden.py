@@ -12,6 +12,7 @@ Sources (paths inside the Cassandra tree):
   Scripts/testSuite/Resources/exampleResults/Widom/{pentane,water_spce}/*.prp  (per-frame Energy_Total)
   Scripts/testSuite/Resources/exampleResults/Widom/pentane/*.wprp, *.wprp2, *.log  (Widom statistics)
   Scripts/testSuite/Resources/exampleResources/Widom/pentane/species1/frag*/frag*.dat  (fragment libraries)
+  Scripts/testSuite/Resources/exampleResources/Widom/{water_spce,pentane}/*_traj.{xyz,H}  (raw text, reader pin)
 """
 from __future__ import annotations
 
@@ -162,12 +163,30 @@ def widom_pentane():
     np.savez_compressed(os.path.join(OUT, "widom_pentane.npz"), **data)
 
 
+def traj_text():
+    """Raw text of the reference's pregenerated trajectories, to pin the
+    library's .xyz/.H reader: all .H records and the first .xyz frames of the
+    water_spce and pentane Widom examples."""
+    base = os.path.join(TS, "Resources", "exampleResources", "Widom")
+    data = {}
+    for name, traj, nfr in (("water_spce", "spce_traj", 3), ("pentane", "pentane_traj", 2)):
+        lines = open(os.path.join(base, name, traj + ".xyz")).read().split("\n")
+        pos = 0
+        for _ in range(nfr):
+            pos += 2 + int(lines[pos].split()[0])
+        data[f"{name}_xyz"] = "\n".join(lines[:pos]) + "\n"
+        data[f"{name}_H"] = open(os.path.join(base, name, traj + ".H")).read()
+        data[f"{name}_nframes_xyz"] = nfr
+    np.savez_compressed(os.path.join(OUT, "traj_text.npz"), **data)
+
+
 if __name__ == "__main__":
     nist_lj()
     nist_spce()
     pregen("water_spce", "spce_traj", "spce_widom.out.prp", "spce.mcf", "spce_widom.inp")
     pregen("pentane", "pentane_traj", "pentane_widom.out.prp", "pentane.mcf", "pentane_widom.inp")
     widom_pentane()
+    traj_text()
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

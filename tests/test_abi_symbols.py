@@ -29,6 +29,7 @@ def test_struct_layouts():
     assert ctypes.sizeof(abi.CassMCResult) == 14 * 8 + 5 * 8
     assert ctypes.sizeof(abi.CassStats) == 2 * 8 + 5 * 8 + 4 * 4 + 8 + 8 + 2 * 4
     assert ctypes.sizeof(abi.CassBoxDesc) == 3 * 8 + 2 * 4 + 6 * 8 + 2 * 4 + 3 * 8
+    assert ctypes.sizeof(abi.CassFrame) == 4 + 4 + 8 + 9 * 8 + 8 + 8 + 4 + 4
 
 
 def test_errors_are_status_codes_without_a_device():
