@@ -58,6 +58,9 @@ def parse():
     p.add_argument("--no-gcmc", action="store_true", help="skip the grand-canonical leg")
     p.add_argument("--no-npt", action="store_true", help="skip the NPT / fluctuation-formula leg")
     p.add_argument("--no-pregen", action="store_true", help="skip the trajectory-fed Widom leg")
+    p.add_argument("--gcmc-eq-steps", type=int, default=150000)
+    p.add_argument("--gcmc-blocks", type=int, default=8)
+    p.add_argument("--gcmc-block-steps", type=int, default=15000)
     p.add_argument("--pregen-frames", type=int, default=4)
     p.add_argument("--npt-chains", type=int, default=32)
     p.add_argument("--npt-eq-blocks", type=int, default=6)
@@ -386,8 +389,9 @@ def pregen_leg(cg, abi, system, n_per_box: int, kappa: int, nframes: int, seed: 
     driver runs it: per box an .xyz/.H trajectory of `nframes` frames (the frozen
     box with every atom displaced by N(0, 0.05 A) per frame, written to a
     temporary directory), read by the library's reader threads one frame ahead;
-    per frame cass_load_next_frame, the system energy of every box and one
-    batched Widom call.  The first frame is untimed."""
+    per frame cass_load_next_frame and one batched Widom call, once without and
+    once with the system energy of every box each frame.  The first frame of each
+    pass is untimed."""
     import shutil
     import tempfile
     from cassandra_gb300 import io, pregen
@@ -411,37 +415,43 @@ def pregen_leg(cg, abi, system, n_per_box: int, kappa: int, nframes: int, seed: 
             paths.append((xp, hp))
         t_write = time.perf_counter() - t0
         text_bytes = sum(os.path.getsize(p) for pair in paths for p in pair)
-        with cg.open_system(system, precision=abi.PREC_MIXED) as ctx:
-            trajs = [cg.open_trajectory(xp, hp, [1, 4]) for xp, hp in paths]
-            try:
-                pregen.pregen_widom(ctx, trajs, [2], n_per_box, kappa, kappa, seed=seed, max_frames=1)
-                s0 = ctx.stats()
-                p0 = sum(t.stats()["parse_s"] for t in trajs)
-                t0 = time.perf_counter()
-                recs = pregen.pregen_widom(ctx, trajs, [2], n_per_box, kappa, kappa, seed=seed + 1,
-                                           max_frames=nframes)
-                wall = time.perf_counter() - t0
-                s1 = ctx.stats()
-                parse = sum(t.stats()["parse_s"] for t in trajs) - p0
-            finally:
-                for t in trajs:
-                    t.close()
-        nf = len(recs)
-        trials = n_per_box * len(boxes) * 2 * kappa * nf
+
+        def run(energy_every):
+            with cg.open_system(system, precision=abi.PREC_MIXED) as ctx:
+                trajs = [cg.open_trajectory(xp, hp, [1, 4]) for xp, hp in paths]
+                try:
+                    pregen.pregen_widom(ctx, trajs, [2], n_per_box, kappa, kappa, seed=seed, max_frames=1,
+                                        energy_every=energy_every)
+                    s0 = ctx.stats()
+                    p0 = sum(t.stats()["parse_s"] for t in trajs)
+                    t0 = time.perf_counter()
+                    recs = pregen.pregen_widom(ctx, trajs, [2], n_per_box, kappa, kappa, seed=seed + 1,
+                                               max_frames=nframes, energy_every=energy_every)
+                    wall = time.perf_counter() - t0
+                    s1 = ctx.stats()
+                    parse = sum(t.stats()["parse_s"] for t in trajs) - p0
+                finally:
+                    for t in trajs:
+                        t.close()
+            nf = len(recs)
+            trials = n_per_box * len(boxes) * 2 * kappa * nf
+            return {"frames": nf, "value": trials / wall, "unit": UNIT, "frames_per_s": nf / wall,
+                    "load_s_per_frame": float(np.mean([r["load_s"] for r in recs])),
+                    "energy_s_per_frame": float(np.mean([r["energy_s"] for r in recs])),
+                    "widom_s_per_frame": float(np.mean([r["widom_s"] for r in recs])),
+                    "reader_parse_s_per_frame": parse / nf,
+                    "h2d_bytes_per_frame": int((s1["h2d_bytes"] - s0["h2d_bytes"]) / nf),
+                    "d2h_bytes_per_frame": int((s1["d2h_bytes"] - s0["d2h_bytes"]) / nf)}
+
         return {"workload": f"{len(boxes)} LJ boxes streamed from .xyz/.H trajectories, {n_per_box * len(boxes)} "
                             f"butane insertions per frame (kappa {kappa}/{kappa}), mixed precision",
-                "frames": nf, "value": trials / wall, "unit": UNIT, "frames_per_s": nf / wall,
-                "load_s_per_frame": float(np.mean([r["load_s"] for r in recs])),
-                "energy_s_per_frame": float(np.mean([r["energy_s"] for r in recs])),
-                "widom_s_per_frame": float(np.mean([r["widom_s"] for r in recs])),
-                "reader_parse_s_per_frame": parse / nf, "reader_threads": len(trajs),
-                "text_mb_per_frame": text_bytes / (nframes + 1) / 1e6,
-                "h2d_bytes_per_frame": int((s1["h2d_bytes"] - s0["h2d_bytes"]) / nf),
-                "d2h_bytes_per_frame": int((s1["d2h_bytes"] - s0["d2h_bytes"]) / nf),
-                "write_s": t_write,
-                "note": "host wall clock per frame: load (waits for the reader only if it is behind; repack and "
-                        "pinned upload), system energies, Widom; reader_parse_s_per_frame is summed over the "
-                        "reader threads and runs during the previous frame's device work"}
+                "widom_only": run(0), "with_total_energies": run(1), "reader_threads": len(paths),
+                "text_mb_per_frame": text_bytes / (nframes + 1) / 1e6, "write_s": t_write,
+                "note": "host wall clock per frame: load (waits for a reader only if it is behind; repack, pinned "
+                        "upload, long-range correction), system energies of every box (with_total_energies: "
+                        "every frame, as a pregen run printing thermo data each frame), Widom; "
+                        "reader_parse_s_per_frame is summed over the reader threads and overlaps the previous "
+                        "frame's device work"}
     finally:
         shutil.rmtree(td, ignore_errors=True)
 
@@ -702,11 +712,22 @@ def main():
                               "host wall clock"}
     gctx.close()
     if not args.no_pregen:
-        out["pregen_feed"] = pregen_leg(cg, abi, system, n_per_box, args.kappa, args.pregen_frames, args.seed + 31)
+        pf = pregen_leg(cg, abi, system, n_per_box, args.kappa, args.pregen_frames, args.seed + 31)
+        out["pregen_feed"] = pf
+        w = pf["widom_only"]
+        if "e2e" in out:
+            out["e2e_set_molecules"] = out.pop("e2e")
+        out["e2e"] = {"value": w["value"], "unit": UNIT, "h2d_bytes_per_step": w["h2d_bytes_per_frame"],
+                      "d2h_bytes_per_step": w["d2h_bytes_per_frame"], "steps": w["frames"],
+                      "note": "the headline workload through the public API from trajectory files: per step "
+                              "(frame) cass_load_next_frame of all 64 boxes (text parsed by reader threads into "
+                              "pinned buffers, pinned upload) and one cass_widom_insert, results read back; "
+                              "host wall clock"}
     if not args.no_mc:
         out["mc_sweeps"] = mc_leg(cg, abi, dev, rank == 0 and world == 1 and not args.no_cpu_baseline)
     if not args.no_gcmc:
-        out["gcmc"] = gcmc_leg(cg, abi, dev, rank == 0 and world == 1 and not args.no_cpu_baseline)
+        out["gcmc"] = gcmc_leg(cg, abi, dev, rank == 0 and world == 1 and not args.no_cpu_baseline,
+                               eq_steps=args.gcmc_eq_steps, blocks=args.gcmc_blocks, block_steps=args.gcmc_block_steps)
     if not args.no_grad:
         out["gradient"] = gradient_leg(cg, abi, dev)
     if not args.no_npt:

@@ -599,6 +599,7 @@ int mol_slot(cass_ctx* c, int im, int is) { return c->mol_base[is - 1] + im - 1;
 void invalidate(cass_ctx* c, int ibox) {
   if (ibox < 0 || ibox >= c->nboxes) return;
   c->box[ibox].energy_valid = false;
+  c->box[ibox].frame_ready = false;
   c->box[ibox].pack_dirty = true;
   c->box[ibox].cell_dirty = true;
 }
@@ -689,7 +690,8 @@ int ensure_cos_mol(cass_ctx* c, int nv) {
   int stride = std::max(nv + nv / 4, c->cos_mol_stride);
   if (c->d_cos_mol.p)  // the rows of every molecule are lost: boxes with an Ewald sum must be recomputed
     for (BoxH& B : c->box)
-      if (B.desc.charge_style == CASS_CHARGE_COUL && B.desc.charge_sum_style == CASS_QQ_EWALD) B.energy_valid = false;
+      if (B.desc.charge_style == CASS_CHARGE_COUL && B.desc.charge_sum_style == CASS_QQ_EWALD)
+        B.energy_valid = B.frame_ready = false;
   size_t bytes = (size_t)std::max(1, c->nmol_slots) * stride * sizeof(double);
   int rc = c->d_cos_mol.reserve(bytes);
   if (!rc) rc = c->d_sin_mol.reserve(bytes);
@@ -1057,7 +1059,7 @@ int cass_set_nonbond_table(cass_ctx* c, int32_t nt, const double* eps, const dou
   c->pt_set = true;
   c->pt_sig.assign(sig, sig + nt * nt);
   c->cbmc_dirty = true;
-  for (int b = 0; b < c->nboxes; ++b) c->box[b].energy_valid = false;
+  for (int b = 0; b < c->nboxes; ++b) c->box[b].energy_valid = c->box[b].frame_ready = false;
   return CASS_OK;
 }
 
@@ -1313,6 +1315,7 @@ int cass_set_molecules(cass_ctx* c, int32_t n, const int32_t* im, const int32_t*
       c->h_patch.push_back(q);
     }
     B.energy_valid = false;
+    B.frame_ready = false;
     B.cell_dirty = true;
   }
   const int np = (int)c->h_patch.size();
@@ -1581,6 +1584,45 @@ int cass_mol_intra_energy(cass_ctx* c, int32_t im, int32_t is, int32_t cbmc, dou
   return CASS_OK;
 }
 
+// Compute_System_Ewald_Reciprocal_Energy (energy_routines.f90:4111-4231): every
+// molecule's cos_mol/sin_mol row, the box's cos_sum/sin_sum and the reciprocal
+// energy, on the device.
+static int box_reciprocal(cass_ctx* c, int ibox, double* e_recip) {
+  BoxH& B = c->box[ibox];
+  int rc;
+  int nv = B.nvecs;
+  if ((rc = ensure_cos_mol(c, nv))) return rc;
+  DevBuf& part = c->d_box_sums;
+  int nchunks = std::max(1, (B.npacked_mols + kSfacMolChunk - 1) / kSfacMolChunk);
+  if ((rc = part.reserve((size_t)nchunks * nv * sizeof(double2)))) return rc;
+  std::vector<int> charged(c->nspecies);
+  for (int is = 0; is < c->nspecies; ++is) charged[is] = c->sp[is].has_charge ? 1 : 0;
+  DevBuf& dch = c->d_cell_count;  // small reuse: species charged flags
+  if ((rc = dch.reserve(std::max(c->nspecies, 1) * sizeof(int) + 256))) return rc;
+  CASS_CUDA(h2d(c, dch.p, charged.data(), c->nspecies * sizeof(int)));
+  if (B.npacked_mols > 0) {
+    dim3 g((nv + 127) / 128, nchunks);
+    k_sfac<<<g, 128, 0, c->stream>>>(B.d_kvec.as<double4_32a>(), nv, B.d_p64.as<double4_32a>(), B.d_molinfo.as<int4>(),
+                                     B.npacked_mols, dch.as<int>(), c->d_cos_mol.as<double>(),
+                                     c->d_sin_mol.as<double>(), c->cos_mol_stride, part.as<double2>());
+    CASS_CUDA(cudaGetLastError());
+  count_launch(c);
+  } else {
+    CASS_CUDA(cudaMemsetAsync(part.p, 0, (size_t)nv * sizeof(double2), c->stream));
+  }
+  int nblk = std::max(1, std::min(148, (nv + kBlock - 1) / kBlock));
+  if ((rc = ensure_scratch(c, nblk, 1))) return rc;
+  k_sfac_reduce<<<nblk, kBlock, 0, c->stream>>>(B.d_kvec.as<double4_32a>(), nv, part.as<double2>(), nchunks,
+                                                B.d_cos_sum.as<double>(), B.d_sin_sum.as<double>(),
+                                                c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
+                                                c->d_result.as<double>());
+  CASS_CUDA(cudaGetLastError());
+  count_launch(c);
+  if ((rc = sync_result(c, 1))) return rc;
+  *e_recip = c->h_result[0] * kCHARGE_FACTOR;
+  return CASS_OK;
+}
+
 int cass_system_total_energy(cass_ctx* c, int32_t ibox1, int32_t intra_flag, CassEnergy* out, int32_t* overlap) {
   if (!c || ibox1 < 1 || ibox1 > c->nboxes || !out || !overlap) return set_error(CASS_EINVAL, "bad arguments");
   if (!c->pt_set) return set_error(CASS_ESTATE, "nonbond table not set");
@@ -1646,41 +1688,13 @@ int cass_system_total_energy(cass_ctx* c, int32_t ibox1, int32_t intra_flag, Cas
   if (hov) {
     *overlap = 1;
     B.energy_valid = false;
+    B.frame_ready = false;
     return CASS_OK;
   }
   E.inter = E.inter_q + E.inter_vdw;
   if (B.desc.charge_style == CASS_CHARGE_COUL) {
     if (box_has_ewald(B) && B.nvecs > 0) {
-      int nv = B.nvecs;
-      if ((rc = ensure_cos_mol(c, nv))) return rc;
-      DevBuf& part = c->d_box_sums;
-      int nchunks = std::max(1, (B.npacked_mols + kSfacMolChunk - 1) / kSfacMolChunk);
-      if ((rc = part.reserve((size_t)nchunks * nv * sizeof(double2)))) return rc;
-      std::vector<int> charged(c->nspecies);
-      for (int is = 0; is < c->nspecies; ++is) charged[is] = c->sp[is].has_charge ? 1 : 0;
-      DevBuf& dch = c->d_cell_count;  // small reuse: species charged flags
-      if ((rc = dch.reserve(std::max(c->nspecies, 1) * sizeof(int) + 256))) return rc;
-      CASS_CUDA(h2d(c, dch.p, charged.data(), c->nspecies * sizeof(int)));
-      if (B.npacked_mols > 0) {
-        dim3 g((nv + 127) / 128, nchunks);
-        k_sfac<<<g, 128, 0, c->stream>>>(B.d_kvec.as<double4_32a>(), nv, B.d_p64.as<double4_32a>(), B.d_molinfo.as<int4>(),
-                                         B.npacked_mols, dch.as<int>(), c->d_cos_mol.as<double>(),
-                                         c->d_sin_mol.as<double>(), c->cos_mol_stride, part.as<double2>());
-        CASS_CUDA(cudaGetLastError());
-  count_launch(c);
-      } else {
-        CASS_CUDA(cudaMemsetAsync(part.p, 0, (size_t)nv * sizeof(double2), c->stream));
-      }
-      int nblk = std::max(1, std::min(148, (nv + kBlock - 1) / kBlock));
-      if ((rc = ensure_scratch(c, nblk, 1))) return rc;
-      k_sfac_reduce<<<nblk, kBlock, 0, c->stream>>>(B.d_kvec.as<double4_32a>(), nv, part.as<double2>(), nchunks,
-                                                    B.d_cos_sum.as<double>(), B.d_sin_sum.as<double>(),
-                                                    c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
-                                                    c->d_result.as<double>());
-      CASS_CUDA(cudaGetLastError());
-  count_launch(c);
-      if ((rc = sync_result(c, 1))) return rc;
-      E.reciprocal = c->h_result[0] * kCHARGE_FACTOR;
+      if ((rc = box_reciprocal(c, ibox, &E.reciprocal))) return rc;
       E.inter = E.inter + E.reciprocal;
     }
     // Compute_System_Self_Energy (energy_routines.f90:2553-2601), O(nmol) host sum of charges squared
@@ -1701,6 +1715,7 @@ int cass_system_total_energy(cass_ctx* c, int32_t ibox1, int32_t intra_flag, Cas
   E.total = E.intra + E.inter;
   B.energy = E;
   B.energy_valid = true;
+  B.frame_ready = true;
   *out = E;
   return CASS_OK;
 }
@@ -1741,6 +1756,7 @@ int cass_ewald_update(cass_ctx* c, int32_t im, int32_t is, int32_t ibox1, int32_
   if ((rc = sync_result(c, 1))) return rc;
   *e_recip = c->h_result[0] * kCHARGE_FACTOR;
   B.energy_valid = false;
+  B.frame_ready = false;
   return CASS_OK;
 }
 
@@ -1791,3 +1807,21 @@ int cass_ewald_widom(cass_ctx* c, int32_t is, int32_t ibox1, int32_t n, const do
 }
 
 }  // extern "C"
+
+namespace cassgpu {
+// The box set-up at the end of Set_Frame_Coords (load_next_frame.f90:290-301):
+// the long-range correction (Compute_LR_Correction) and, for Ewald boxes, the
+// structure factors and reciprocal energy (Compute_System_Ewald_Reciprocal_Energy).
+// Enough for Widom insertions; the other energy components are left to
+// cass_system_total_energy.
+int frame_setup_ext(cass_ctx* c, int ibox) {
+  BoxH& B = c->box[ibox];
+  int rc;
+  if ((rc = pack_box(c, ibox))) return rc;
+  if (B.desc.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) B.energy.lrc = lr_correction(c, B, count_beads(c, ibox));
+  if (box_has_ewald(B) && B.nvecs > 0 && (rc = box_reciprocal(c, ibox, &B.energy.reciprocal))) return rc;
+  B.frame_ready = true;
+  return CASS_OK;
+}
+}  // namespace cassgpu
+

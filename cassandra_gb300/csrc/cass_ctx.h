@@ -135,6 +135,9 @@ struct BoxH {
   std::vector<double> kvec;  // [nvecs][4] = hx, hy, hz, Cn
   int nvecs = 0;
   bool energy_valid = false;
+  // energy.lrc / energy.reciprocal and the structure factors are current
+  // (a frame load sets them up without the other components)
+  bool frame_ready = false;
   CassEnergy energy{};
   // packed atoms of the live molecules of this box, molecule-contiguous
   bool pack_dirty = true;

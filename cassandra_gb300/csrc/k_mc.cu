@@ -763,7 +763,7 @@ extern "C" int cass_mc_sweeps(cass_ctx* c, int32_t nboxes, const int32_t* iboxes
   c->stats.mc_moves = moves;
   for (int k = 0; k < nboxes; ++k)
     if (hs[k]) {
-      c->box[iboxes[k] - 1].energy_valid = false;
+      c->box[iboxes[k] - 1].energy_valid = c->box[iboxes[k] - 1].frame_ready = false;
       return set_error(CASS_ESTATE, "a molecule overlapped another before its move (energy too high)");
     }
   return CASS_OK;

@@ -1564,7 +1564,8 @@ extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const
   for (int k = 0; k < nboxes; ++k) {
     int ib = iboxes[k] - 1;
     if (ib < 0 || ib >= c->nboxes) return set_error(CASS_EINVAL, "box index out of range");
-    if (!c->box[ib].energy_valid) return set_error(CASS_ESTATE, "system energy of box not computed");
+    if (!c->box[ib].energy_valid && !c->box[ib].frame_ready)
+      return set_error(CASS_ESTATE, "system energy of box not computed");
   }
   int rc;
   CASS_CUDA(cudaSetDevice(c->device));

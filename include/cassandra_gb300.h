@@ -285,7 +285,8 @@ int cass_cbmc_trial_energies(cass_ctx* ctx, int32_t ibox, int32_t is, int32_t sk
  * insertion, batched over nboxes boxes in one launch.  Insertion k of box b
  * draws its random numbers from an lfsr258 stream seeded by (seed, b, k)
  * (the same stream in the CPU oracle).  Requires a prior
- * cass_system_total_energy of each listed box.  trace may be NULL; else it
+ * cass_system_total_energy or cass_load_next_frame of each listed box (the
+ * long-range correction and the structure factors).  trace may be NULL; else it
  * receives nboxes*n_insertions records, box-major. */
 int cass_widom_insert(cass_ctx* ctx, int32_t is, int32_t nboxes, const int32_t* ibox,
                       int64_t n_insertions, int32_t kappa_ins, int32_t kappa_dih,
@@ -447,9 +448,12 @@ int cass_traj_close(cass_traj* t);
  * Apply_PBC_Anint and its atoms shifted rigidly (:257-283); a box whose
  * matrix changed gets the new edges and k-vectors (Set_Frame_Box, :57-102;
  * orthorhombic matrices only).  The packed coordinates are uploaded from
- * pinned memory.  The energies are then rebuilt by cass_system_total_energy
- * (pregen_driver.f90:187).  On the end of any trajectory, *end_reached = 1 and
- * the context is unchanged. */
+ * pinned memory.  As at the end of Set_Frame_Coords (:290-301), each box gets
+ * its long-range correction and, with Ewald, its structure factors and
+ * reciprocal energy: enough for cass_widom_insert.  The other energy
+ * components come from cass_system_total_energy (pregen_driver.f90:187),
+ * which the MC entry points require.  On the end of any trajectory,
+ * *end_reached = 1 and the context is unchanged. */
 int cass_load_next_frame(cass_ctx* ctx, int32_t nboxes, cass_traj* const* traj, int32_t* end_reached);
 
 /* ---- run-time extensions (no counterpart in the reference) ------------- */

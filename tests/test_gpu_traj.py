@@ -176,3 +176,29 @@ def test_pregen_widom_matches_frame_by_frame_contexts(tmp_path):
         assert np.allclose(gtr["widom_var"], wtr["widom_var"], rtol=1e-9, atol=0)
         assert _close(got[0]["widom_sum"], want[0]["widom_sum"], 1e-9, 0.0)
         assert _close(r["energy"][0]["total"] * KJ, d["energy_total_kjmol"][f], 5e-8, 1e-4)
+
+
+@pytest.mark.parametrize("prec", [abi.PREC_FP64, abi.PREC_MIXED])
+@pytest.mark.parametrize("name", ["water_spce", "pentane"])
+def test_widom_after_frame_load_needs_no_total_energy(tmp_path, name, prec):
+    """cass_load_next_frame sets up the long-range correction and the structure
+    factors as Set_Frame_Coords does; Widom right after it equals Widom after a
+    full cass_system_total_energy of the same frame."""
+    from cassandra_gb300 import workloads
+    xp, hp, d = write_fixture_traj(tmp_path, name)
+    s = helpers.pregen_system(name, 0) if name == "water_spce" else helpers.pentane_widom_system(0)
+    if name == "water_spce":
+        s.species[0].libraries = [workloads.water_species().libraries[0] * 1.0]
+    kd = 0 if name == "water_spce" else 4
+    with cg.open_system(s, precision=prec) as g, cg.open_trajectory(xp, hp, [len(ELEMENTS[name])]) as t:
+        for f in range(3):
+            assert not g.load_next_frame([t])
+            a, ta = g.widom_insert(1, [1], 400, 8, kd, seed=5 + f, trace=True)
+            with pytest.raises(abi.CassError, match="system energy"):
+                g.mc_sweeps([1], 1, [[0.1]], [[0.1]], seed=1)  # MC needs the full energy
+            e, _ = g.system_total_energy(1)
+            b, tb = g.widom_insert(1, [1], 400, 8, kd, seed=5 + f, trace=True)
+            assert a[0]["n_overlaps"] == b[0]["n_overlaps"]
+            assert np.array_equal(ta["selected_trial"], tb["selected_trial"])
+            assert np.array_equal(ta["widom_var"], tb["widom_var"])
+            assert a[0]["widom_sum"] == b[0]["widom_sum"]
