@@ -1033,6 +1033,13 @@ int cass_set_count_pairs(cass_ctx* c, int32_t on) {
   return CASS_OK;
 }
 
+int cass_set_widom_cells(cass_ctx* c, double cells_per_cutoff) {
+  if (!c || !(cells_per_cutoff >= 0.0 && cells_per_cutoff <= 8.0))
+    return set_error(CASS_EINVAL, "cells_per_cutoff must be in [0, 8]");
+  c->widom_cells = cells_per_cutoff;
+  return CASS_OK;
+}
+
 int cass_set_stream(cass_ctx* c, void* stream) {
   if (!c) return set_error(CASS_EINVAL, "NULL context");
   CASS_CUDA(cudaStreamSynchronize(c->stream));

@@ -28,6 +28,7 @@ struct SpeciesF {
 // FP32 constants of the CTA's box
 struct BoxF {
   float L[3], hL[3], cinv[3];
+  float ch[3];  // cell edge L / nc (Widom stencils)
   int nc[3];
   float rcb2, rv2, rq2, low2, rc_cbmc, rc_full, beta, kmaxE, alpha;
   int charge_on;

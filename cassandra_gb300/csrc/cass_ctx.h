@@ -166,6 +166,7 @@ struct cass_ctx_impl {
   cudaStream_t stream = nullptr, own_stream = nullptr;
   CassStats stats{};
   int count_pairs = 0;
+  double widom_cells = 0.0;  // cells per rcut_cbmc in the Widom cell lists (0: default)
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   int nspecies = 0, ntypes = 0, nboxes = 0, max_kvec = 100000;
   std::vector<int> max_mol, mol_base;

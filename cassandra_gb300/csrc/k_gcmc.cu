@@ -2263,15 +2263,22 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
     }
   double mw = 0.0;
   for (double m : s.mass) mw += m;
-  // free slots of the exchanged species, dealt to the boxes in turn
+  // free slots of the exchanged species, in ascending order, each to the box
+  // holding the fewest atoms so far (live molecules of every species plus the
+  // slots dealt; ties to the first listed box): the boxes' shares even out
   std::vector<std::vector<int>> pools(nboxes);
   {
-    int nfree = 0;
+    std::vector<long long> load(nboxes, 0);
+    for (int k = 0; k < nboxes; ++k)
+      for (int slot : members_ext(c, iboxes[k] - 1)) load[k] += c->sp[c->slot_sp[slot]].natoms;
     for (int im = 0; im < c->max_mol[is]; ++im) {
       const int slot = c->mol_base[is] + im;
       if (c->mol_box[slot] >= 0) continue;
-      pools[nfree % nboxes].push_back(slot);
-      ++nfree;
+      int kmin = 0;
+      for (int k = 1; k < nboxes; ++k)
+        if (load[k] < load[kmin]) kmin = k;
+      pools[kmin].push_back(slot);
+      load[kmin] += s.natoms;
     }
   }
   // per-box records: the live molecules and the box's free slots, in slot order

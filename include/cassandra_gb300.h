@@ -476,6 +476,10 @@ typedef struct CassStats {
 int cass_get_stats(cass_ctx* ctx, CassStats* out);
 /* count_pairs != 0 makes the Widom kernel count visited / in-cutoff pairs. */
 int cass_set_count_pairs(cass_ctx* ctx, int32_t count_pairs);
+/* Edge of the cells of the Widom cell lists, as a divisor of rcut_cbmc: the
+ * edge is rcut_cbmc / cells_per_cutoff (0 restores the default of the
+ * context's precision).  Results do not depend on it beyond summation order. */
+int cass_set_widom_cells(cass_ctx* ctx, double cells_per_cutoff);
 /* Runs the context's work on a caller-owned cudaStream_t (NULL: its own). */
 int cass_set_stream(cass_ctx* ctx, void* stream);
 

@@ -3036,14 +3036,24 @@ int orc_gcmc(orc_ctx* c, int32_t nboxes, const int32_t* iboxes, const CassGCMCPa
     if (!c->box[ib].energy_valid) return fail(CASS_ESTATE, "system energy of box not computed");
     if (c->box[ib].charge_style != CASS_CHARGE_NONE) return fail(CASS_EUNSUPPORTED, "gcmc boxes hold no charges");
   }
-  // free slots of the exchanged species, dealt to the boxes in turn
+  // free slots of the exchanged species, in ascending order, each to the box
+  // holding the fewest atoms so far (live molecules of every species plus the
+  // slots dealt; ties to the first listed box): the boxes' shares even out
   std::vector<std::vector<int>> pools(nboxes);
-  int nfree = 0;
-  for (int im = 0; im < c->max_mol[is]; ++im) {
-    const int slot = c->mol_base[is] + im;
-    if (c->mol[slot].live) continue;
-    pools[nfree % nboxes].push_back(slot);
-    ++nfree;
+  {
+    std::vector<long long> load(nboxes, 0);
+    for (int k = 0; k < nboxes; ++k)
+      for (int slot = 0; slot < (int)c->mol.size(); ++slot)
+        if (c->mol[slot].live && c->mol[slot].ibox == iboxes[k] - 1) load[k] += c->sp[c->mol[slot].is].natoms;
+    for (int im = 0; im < c->max_mol[is]; ++im) {
+      const int slot = c->mol_base[is] + im;
+      if (c->mol[slot].live) continue;
+      int kmin = 0;
+      for (int k = 1; k < nboxes; ++k)
+        if (load[k] < load[kmin]) kmin = k;
+      pools[kmin].push_back(slot);
+      load[kmin] += c->sp[is].natoms;
+    }
   }
   // fragment bonds (f, g), f < g, and prob_del1 (input_routines.f90:3035-3120)
   std::vector<int> fa, fb;
