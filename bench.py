@@ -62,7 +62,7 @@ def parse():
     p.add_argument("--gcmc-blocks", type=int, default=8)
     p.add_argument("--gcmc-block-steps", type=int, default=15000)
     p.add_argument("--pregen-frames", type=int, default=4)
-    p.add_argument("--npt-chains", type=int, default=32)
+    p.add_argument("--npt-chains", type=int, default=64)
     p.add_argument("--npt-eq-blocks", type=int, default=6)
     p.add_argument("--npt-blocks", type=int, default=4, help="production blocks (configurations per chain)")
     return p.parse_args()
@@ -381,7 +381,7 @@ def npt_leg(cg, abi, dev, nchains: int, eq_blocks: int, prod_blocks: int) -> dic
                               "formula": "-beta (<rho dU/deps> - <rho><dU/deps>)"},
             "adjoint_check_max_rel_diff": float(max(check)),
             "note": "configurations after short equilibration from the lattice start; the full 2000-configuration "
-                    "run is --npt-chains 32 --npt-blocks 63"}
+                    "run is --npt-chains 64 --npt-blocks 32"}
 
 
 def pregen_leg(cg, abi, system, n_per_box: int, kappa: int, nframes: int, seed: int) -> dict:

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -254,11 +255,14 @@ __global__ void __launch_bounds__(kBlock) k_trial_energy(BoxDev b, PairTable t, 
 constexpr int kTileJ = 512;
 
 template <bool FAST>
+// pre2 (FP64 kernel): an FP32 bound on r^2 beyond every cutoff of the box with
+// a margin far above FP32 rounding; pairs past it skip the FP64 arithmetic,
+// which decides every cutoff exactly (FLT_MAX where a style has no cutoff)
 __global__ void __launch_bounds__(kBlock) k_pair_total(BoxDev b, PairTable t, const double4_32a* __restrict__ p64,
-                                                       const int4* __restrict__ meta, int n, double* partial,
+                                                       const int4* __restrict__ meta, int n, float pre2, double* partial,
                                                        unsigned* counter, double* out, int* ovflag) {
   __shared__ double4_32a sj[FAST ? 1 : kBlock];
-  __shared__ float4 sf[FAST ? kBlock : 1];
+  __shared__ float4 sf[kBlock];
   __shared__ int2 sm[kBlock];  // molecule slot, type
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const double4_32a pi = i < n ? p64[i] : make_double4_32a(0, 0, 0, 0);
@@ -288,8 +292,8 @@ __global__ void __launch_bounds__(kBlock) k_pair_total(BoxDev b, PairTable t, co
       if (jj < j1) {
         const double4_32a pj = p64[jj];
         const int4 mj = meta[jj];
-        if (FAST) sf[threadIdx.x] = make_float4((float)pj.x, (float)pj.y, (float)pj.z, (float)pj.w);
-        else sj[threadIdx.x] = pj;
+        sf[threadIdx.x] = make_float4((float)pj.x, (float)pj.y, (float)pj.z, (float)pj.w);
+        if (!FAST) sj[threadIdx.x] = pj;
         sm[threadIdx.x] = make_int2(mj.x, mj.y);
       }
       __syncthreads();
@@ -322,6 +326,12 @@ __global__ void __launch_bounds__(kBlock) k_pair_total(BoxDev b, PairTable t, co
           }
           if (qq_on && r2 <= rq2f) fq.add(qq_ewald_inter_f(alphaf, pif.w * pj.w, r2));
         } else {
+          {
+            const float4 q = sf[k];
+            const float ex = fold(pif.x - q.x, b.hLf[0], b.Lf[0]), ey = fold(pif.y - q.y, b.hLf[1], b.Lf[1]),
+                        ez = fold(pif.z - q.z, b.hLf[2], b.Lf[2]);
+            if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > pre2) continue;
+          }
           const double4_32a pj = sj[k];
           const double dx = fold(pi.x - pj.x, b.hL[0], b.L[0]);
           const double dy = fold(pi.y - pj.y, b.hL[1], b.L[1]);
@@ -378,6 +388,9 @@ __global__ void __launch_bounds__(kBlock) k_intra_total(BoxDev b, PairTable t, S
 // Ewald structure factors.  kvec[k] = (hx, hy, hz, Cn).
 constexpr int kSfacMolChunk = 64;
 
+// F32: the mixed path's FP32 phases (a molecule's sums in FP32, stored and
+// accumulated in FP64), as its MC moves compute the rows of moved molecules
+template <bool F32>
 __global__ void __launch_bounds__(128) k_sfac(const double4_32a* __restrict__ kvec, int nv, const double4_32a* __restrict__ p64,
                                               const MolInfo* __restrict__ mols, int nm, const int* __restrict__ charged,
                                               double* cos_mol, double* sin_mol, int stride, double2* part) {
@@ -385,11 +398,24 @@ __global__ void __launch_bounds__(128) k_sfac(const double4_32a* __restrict__ kv
   int m0 = blockIdx.y * kSfacMolChunk, m1 = min(nm, m0 + kSfacMolChunk);
   if (k >= nv) return;
   double4_32a h = kvec[k];
+  const float hx = (float)h.x, hy = (float)h.y, hz = (float)h.z;
   double cs = 0.0, sn = 0.0;
   for (int m = m0; m < m1; ++m) {
     MolInfo mi = mols[m];
     if (!charged[mi.y]) continue;
     double c = 0.0, s = 0.0;
+    if (F32) {
+      float cf = 0.0f, sf = 0.0f;
+      for (int a = 0; a < mi.w; ++a) {
+        double4_32a p = p64[mi.z + a];
+        float sv, cv;
+        sincosf(hx * (float)p.x + hy * (float)p.y + hz * (float)p.z, &sv, &cv);
+        cf += (float)p.w * cv;
+        sf += (float)p.w * sv;
+      }
+      c = (double)cf;
+      s = (double)sf;
+    } else
     for (int a = 0; a < mi.w; ++a) {
       double4_32a p = p64[mi.z + a];
       double hdotr = h.x * p.x + h.y * p.y + h.z * p.z;
@@ -1609,9 +1635,10 @@ static int box_reciprocal(cass_ctx* c, int ibox, double* e_recip) {
   CASS_CUDA(h2d(c, dch.p, charged.data(), c->nspecies * sizeof(int)));
   if (B.npacked_mols > 0) {
     dim3 g((nv + 127) / 128, nchunks);
-    k_sfac<<<g, 128, 0, c->stream>>>(B.d_kvec.as<double4_32a>(), nv, B.d_p64.as<double4_32a>(), B.d_molinfo.as<int4>(),
-                                     B.npacked_mols, dch.as<int>(), c->d_cos_mol.as<double>(),
-                                     c->d_sin_mol.as<double>(), c->cos_mol_stride, part.as<double2>());
+    auto kern = c->precision == CASS_PREC_MIXED ? k_sfac<true> : k_sfac<false>;
+    kern<<<g, 128, 0, c->stream>>>(B.d_kvec.as<double4_32a>(), nv, B.d_p64.as<double4_32a>(), B.d_molinfo.as<int4>(),
+                                   B.npacked_mols, dch.as<int>(), c->d_cos_mol.as<double>(),
+                                   c->d_sin_mol.as<double>(), c->cos_mol_stride, part.as<double2>());
     CASS_CUDA(cudaGetLastError());
   count_launch(c);
   } else {
@@ -1675,13 +1702,27 @@ int cass_system_total_energy(cass_ctx* c, int32_t ibox1, int32_t intra_flag, Cas
     const bool fast = c->precision == CASS_PREC_MIXED && B.desc.vdw_style == CASS_VDW_LJ &&
                       (B.desc.vdw_sum_style == CASS_VDW_SUM_CUT || B.desc.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) &&
                       (B.desc.charge_style == CASS_CHARGE_NONE || B.desc.charge_sum_style == CASS_QQ_EWALD);
+    // the largest cutoff cutoff_mask applies outside CBMC (none for the minimum-image styles)
+    double rmax2 = B.dev.rcut_lowsq;
+    bool bounded = true;
+    if (B.desc.vdw_style == CASS_VDW_LJ) {
+      if (B.desc.vdw_sum_style == CASS_VDW_SUM_MINIMUM || B.desc.vdw_sum_style == CASS_VDW_SUM_CHARMM) bounded = false;
+      else rmax2 = std::max(rmax2, B.desc.vdw_sum_style == CASS_VDW_SUM_CUT_SWITCH ? B.dev.roff_switch_sq : B.dev.rcut_vdwsq);
+    } else if (B.desc.vdw_style == CASS_VDW_MIE) {
+      rmax2 = std::max(rmax2, B.dev.rcut_vdwsq);
+    }
+    if (B.desc.charge_style == CASS_CHARGE_COUL) {
+      if (B.desc.charge_sum_style == CASS_QQ_MINIMUM) bounded = false;
+      else rmax2 = std::max(rmax2, B.dev.rcut_coulsq);
+    }
+    const float pre2 = bounded ? (float)(rmax2 * (1.0 + 1.0e-4) + 1.0e-3) : FLT_MAX;
     if (fast)
       k_pair_total<true><<<grid, kBlock, 0, c->stream>>>(B.dev, c->pt, B.d_p64.as<double4_32a>(), B.d_meta.as<int4>(), n,
-                                                        c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
+                                                        pre2, c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
                                                         c->d_result.as<double>(), c->d_query.as<int>());
     else
       k_pair_total<false><<<grid, kBlock, 0, c->stream>>>(B.dev, c->pt, B.d_p64.as<double4_32a>(), B.d_meta.as<int4>(), n,
-                                                         c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
+                                                         pre2, c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
                                                          c->d_result.as<double>(), c->d_query.as<int>());
     CASS_CUDA(cudaGetLastError());
   count_launch(c);

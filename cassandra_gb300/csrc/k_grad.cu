@@ -11,15 +11,22 @@
 // derivative of the computed energy (away from cutoff crossings, where the
 // truncated energy is discontinuous).  FP64 throughout.
 //
-//   k_grad_pairs  thread per atom i, all atoms j in shared-memory tiles:
-//                 the force on i, sum_j q_j dE/d(q_i q_j), and, for j > i, the
-//                 per-type-pair parameter derivatives (each pair counted once)
-//   k_grad_recip  thread per atom i, k-vectors in shared-memory tiles:
+//   k_grad_pairs  thread per atom i, a chunk of the atoms j per grid row in
+//                 shared-memory tiles: the force on i, sum_j q_j dE/d(q_i q_j),
+//                 and, for j > i, the per-type-pair parameter derivatives (each
+//                 pair counted once); one partial per (chunk, i)
+//   k_grad_recip  thread per atom i, a chunk of the k-vectors per grid row:
 //                 2 CF q_i sum_k Cn k (S_s cos - S_c sin) and
-//                 2 CF sum_k Cn (S_c cos + S_s sin)
-//   k_grad_types  fixed-order reduction of the per-atom parameter derivatives
+//                 2 CF sum_k Cn (S_c cos + S_s sin); one partial per (chunk, i)
+//   k_grad_reduce thread per atom: the chunks' partials added in chunk order
+//   k_grad_types  fixed-order tree reduction of the per-atom parameter
+//                 derivatives per type
+// The chunks spread the FP64 work of a box of a few thousand atoms over every
+// SM (a grid of atom blocks alone fills fewer SMs than GB300 has); the partial
+// buffers keep every sum in a fixed order, so repeated calls give equal bits.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -30,6 +37,7 @@
 namespace cassgpu {
 
 constexpr int kGradBlock = 128;
+constexpr int kGradPairVals = 4 + 2 * kMaxTypes;  // gx, gy, gz, dq, deps[t], dsig[t]
 
 // A&S 7.1.26: erfc(x) = t P(t) exp(-x^2), t = 1/(1+px); returns erfc and its
 // derivative with respect to x
@@ -51,16 +59,21 @@ struct GradAtom {
   int mol, type, species, atom;
 };
 
+// pre2: an FP32 bound on r^2 beyond every cutoff of the box (with a margin far
+// above FP32 rounding of the coordinates): pairs beyond it are skipped before
+// the FP64 arithmetic, which then decides every cutoff exactly
 __global__ void __launch_bounds__(kGradBlock) k_grad_pairs(BoxDev b, PairTable T, SpeciesPools P,
                                                            const double4_32a* __restrict__ p64,
-                                                           const int4* __restrict__ meta, int n, double* grad,
-                                                           double* dq, double* deps_atom, double* dsig_atom,
-                                                           int* ovflag) {
+                                                           const float4* __restrict__ p32,
+                                                           const int4* __restrict__ meta, int n, int jchunk,
+                                                           float pre2, double* part, int* ovflag) {
   __shared__ double4_32a sp[kGradBlock];
+  __shared__ float4 spf[kGradBlock];
   __shared__ int4 sm[kGradBlock];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = i < n;
   const double4_32a pi = live ? p64[i] : make_double4_32a(0, 0, 0, 0);
+  const float4 pif = live ? p32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   const int4 mi = live ? meta[i] : make_int4(-1, -1, -1, -1);
   const bool lj = b.vdw_style == CASS_VDW_LJ;
   const bool coul = b.charge_style == CASS_CHARGE_COUL;
@@ -70,18 +83,26 @@ __global__ void __launch_bounds__(kGradBlock) k_grad_pairs(BoxDev b, PairTable T
   for (int t = 0; t < kMaxTypes; ++t) de[t] = ds[t] = 0.0;
   bool ov = false;
   const SpeciesDevHdr* hi = live ? &P.hdr[mi.z] : nullptr;
-  for (int j0 = 0; j0 < n; j0 += kGradBlock) {
+  const int jbeg = blockIdx.y * jchunk, jend = min(n, jbeg + jchunk);
+  for (int j0 = jbeg; j0 < jend; j0 += kGradBlock) {
     __syncthreads();
-    if (j0 + threadIdx.x < n) {
+    if (j0 + threadIdx.x < jend) {
       sp[threadIdx.x] = p64[j0 + threadIdx.x];
+      spf[threadIdx.x] = p32[j0 + threadIdx.x];
       sm[threadIdx.x] = meta[j0 + threadIdx.x];
     }
     __syncthreads();
     if (!live) continue;
-    const int cnt = min(kGradBlock, n - j0);
+    const int cnt = min(kGradBlock, jend - j0);
     for (int k = 0; k < cnt; ++k) {
       const int j = j0 + k;
       if (j == i) continue;
+      {
+        const float4 q = spf[k];
+        const float ex = fold(pif.x - q.x, b.hLf[0], b.Lf[0]), ey = fold(pif.y - q.y, b.hLf[1], b.Lf[1]),
+                    ez = fold(pif.z - q.z, b.hLf[2], b.Lf[2]);
+        if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > pre2) continue;
+      }
       const double4_32a pj = sp[k];
       const int4 mj = sm[k];
       const bool intra = mj.x == mi.x;
@@ -134,40 +155,62 @@ __global__ void __launch_bounds__(kGradBlock) k_grad_pairs(BoxDev b, PairTable T
   }
   if (!live) return;
   if (ov) atomicOr(ovflag, 1);
-  grad[3 * i] = gx;
-  grad[3 * i + 1] = gy;
-  grad[3 * i + 2] = gz;
-  dq[i] = dqi;
+  // partial of (chunk, i): component-major so that the reduction reads coalesced
+  const size_t stride = (size_t)gridDim.y * n;
+  double* o = part + (size_t)blockIdx.y * n + i;
+  o[0] = gx;
+  o[stride] = gy;
+  o[2 * stride] = gz;
+  o[3 * stride] = dqi;
+#pragma unroll
   for (int t = 0; t < kMaxTypes; ++t) {
-    deps_atom[(size_t)i * kMaxTypes + t] = de[t];
-    dsig_atom[(size_t)i * kMaxTypes + t] = ds[t];
+    o[(4 + t) * stride] = de[t];
+    o[(4 + kMaxTypes + t) * stride] = ds[t];
   }
 }
 
+// The k-vectors come in rows of equal (ny, nz) with nx = n0, n0+1, ... (the
+// loop order of Ewald_Reciprocal_Lattice_Vector_Setup, energy_routines.f90:
+// 2260-2311), so along a row the phase advances by the factor e^{i 2 pi x / Lx}:
+// one complex product per k-vector, a sincos at the start of each row.
 __global__ void __launch_bounds__(kGradBlock) k_grad_recip(const double4_32a* __restrict__ kvec,
                                                            const double* __restrict__ cos_sum,
-                                                           const double* __restrict__ sin_sum, int nv,
-                                                           const double4_32a* __restrict__ p64, int n, double* grad,
-                                                           double* dq) {
+                                                           const double* __restrict__ sin_sum, int nv, int kchunk,
+                                                           double hx1, const double4_32a* __restrict__ p64, int n,
+                                                           double* part) {
   __shared__ double4_32a sk[kGradBlock];
   __shared__ double2 ss[kGradBlock];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = i < n;
   const double4_32a pi = live ? p64[i] : make_double4_32a(0, 0, 0, 0);
   double gx = 0, gy = 0, gz = 0, dqi = 0;
-  for (int k0 = 0; k0 < nv; k0 += kGradBlock) {
+  const int kbeg = blockIdx.y * kchunk, kend = min(nv, kbeg + kchunk);
+  double us, uc;  // e^{i hx1 x}
+  sincos(hx1 * pi.x, &us, &uc);
+  double c = 1.0, s = 0.0, py = 0.0, pz = 0.0, pxh = 0.0;
+  bool have = false;
+  for (int k0 = kbeg; k0 < kend; k0 += kGradBlock) {
     __syncthreads();
-    if (k0 + threadIdx.x < nv) {
+    if (k0 + threadIdx.x < kend) {
       sk[threadIdx.x] = kvec[k0 + threadIdx.x];
       ss[threadIdx.x] = make_double2(cos_sum[k0 + threadIdx.x], sin_sum[k0 + threadIdx.x]);
     }
     __syncthreads();
     if (!live) continue;
-    const int cnt = min(kGradBlock, nv - k0);
+    const int cnt = min(kGradBlock, kend - k0);
     for (int k = 0; k < cnt; ++k) {
       const double4_32a h = sk[k];
-      double s, c;
-      sincos(h.x * pi.x + h.y * pi.y + h.z * pi.z, &s, &c);
+      if (have && h.y == py && h.z == pz && fabs(h.x - (pxh + hx1)) <= 1e-9 * fabs(hx1)) {
+        const double c1 = c * uc - s * us;  // next nx of the row
+        s = s * uc + c * us;
+        c = c1;
+      } else {
+        sincos(h.x * pi.x + h.y * pi.y + h.z * pi.z, &s, &c);
+        py = h.y;
+        pz = h.z;
+        have = true;
+      }
+      pxh = h.x;
       const double w = h.w * (ss[k].y * c - ss[k].x * s);
       gx += w * h.x;
       gy += w * h.y;
@@ -176,26 +219,95 @@ __global__ void __launch_bounds__(kGradBlock) k_grad_recip(const double4_32a* __
     }
   }
   if (!live) return;
-  const double f = 2.0 * kCHARGE_FACTOR;
-  grad[3 * i] += f * pi.w * gx;
-  grad[3 * i + 1] += f * pi.w * gy;
-  grad[3 * i + 2] += f * pi.w * gz;
-  dq[i] += f * dqi;
+  const size_t stride = (size_t)gridDim.y * n;
+  double* o = part + (size_t)blockIdx.y * n + i;
+  o[0] = gx;
+  o[stride] = gy;
+  o[2 * stride] = gz;
+  o[3 * stride] = dqi;
 }
 
-// out[ti*kMaxTypes+tj] = sum over atoms of type ti of the per-atom values, in atom order
-__global__ void k_grad_types(const int4* __restrict__ meta, int n, const double* __restrict__ deps_atom,
-                             const double* __restrict__ dsig_atom, double* out_eps, double* out_sig) {
-  const int ti = blockIdx.x, tj = threadIdx.x;
-  if (tj >= kMaxTypes) return;
-  double e = 0.0, s = 0.0;
-  for (int i = 0; i < n; ++i) {
-    if (meta[i].y != ti) continue;
-    e += deps_atom[(size_t)i * kMaxTypes + tj];
-    s += dsig_atom[(size_t)i * kMaxTypes + tj];
+// the chunks' partials of atom i added in chunk order: the pair terms, then
+// 2 CF q_i times the reciprocal sums (no reciprocal part when nkc = 0)
+__global__ void k_grad_reduce(const double* __restrict__ ppart, int npc, const double* __restrict__ rpart, int nkc,
+                              const double4_32a* __restrict__ p64, int n, double* grad, double* dq,
+                              double* deps_atom, double* dsig_atom) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const size_t ps = (size_t)npc * n;
+  double v[kGradPairVals];
+#pragma unroll
+  for (int c = 0; c < kGradPairVals; ++c) {
+    double a = 0.0;
+    for (int k = 0; k < npc; ++k) a += ppart[c * ps + (size_t)k * n + i];
+    v[c] = a;
   }
-  out_eps[ti * kMaxTypes + tj] = e;
-  out_sig[ti * kMaxTypes + tj] = s;
+  if (nkc > 0) {
+    const size_t rs = (size_t)nkc * n;
+    double r[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      double a = 0.0;
+      for (int k = 0; k < nkc; ++k) a += rpart[c * rs + (size_t)k * n + i];
+      r[c] = a;
+    }
+    const double f = 2.0 * kCHARGE_FACTOR, qi = p64[i].w;
+    v[0] += f * qi * r[0];
+    v[1] += f * qi * r[1];
+    v[2] += f * qi * r[2];
+    v[3] += f * r[3];
+  }
+  grad[3 * i] = v[0];
+  grad[3 * i + 1] = v[1];
+  grad[3 * i + 2] = v[2];
+  dq[i] = v[3];
+#pragma unroll
+  for (int t = 0; t < kMaxTypes; ++t) {
+    deps_atom[(size_t)i * kMaxTypes + t] = v[4 + t];
+    dsig_atom[(size_t)i * kMaxTypes + t] = v[4 + kMaxTypes + t];
+  }
+}
+
+constexpr int kTypeBlock = 256;
+
+// out[ti*kMaxTypes+tj] = sum over atoms of type ti of the per-atom values: one
+// block per type, each thread a fixed stride of atoms, then a fixed tree
+__global__ void __launch_bounds__(kTypeBlock) k_grad_types(const int4* __restrict__ meta, int n,
+                                                           const double* __restrict__ deps_atom,
+                                                           const double* __restrict__ dsig_atom, double* out_eps,
+                                                           double* out_sig) {
+  __shared__ double se[kTypeBlock][kMaxTypes + 1], ssg[kTypeBlock][kMaxTypes + 1];
+  const int ti = blockIdx.x;
+  double e[kMaxTypes], s[kMaxTypes];
+#pragma unroll
+  for (int t = 0; t < kMaxTypes; ++t) e[t] = s[t] = 0.0;
+  for (int i = threadIdx.x; i < n; i += kTypeBlock) {
+    if (meta[i].y != ti) continue;
+#pragma unroll
+    for (int t = 0; t < kMaxTypes; ++t) {
+      e[t] += deps_atom[(size_t)i * kMaxTypes + t];
+      s[t] += dsig_atom[(size_t)i * kMaxTypes + t];
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < kMaxTypes; ++t) {
+    se[threadIdx.x][t] = e[t];
+    ssg[threadIdx.x][t] = s[t];
+  }
+  __syncthreads();
+  for (int h = kTypeBlock / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h)
+#pragma unroll
+      for (int t = 0; t < kMaxTypes; ++t) {
+        se[threadIdx.x][t] += se[threadIdx.x + h][t];
+        ssg[threadIdx.x][t] += ssg[threadIdx.x + h][t];
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x < kMaxTypes) {
+    out_eps[ti * kMaxTypes + threadIdx.x] = se[0][threadIdx.x];
+    out_sig[ti * kMaxTypes + threadIdx.x] = ssg[0][threadIdx.x];
+  }
 }
 
 int pack_box_ext(cass_ctx* c, int ibox);
@@ -239,7 +351,25 @@ extern "C" int cass_system_gradient(cass_ctx* c, int32_t ibox1, CassEnergy* ener
   if (energy) *energy = E;
   const int n = B.npacked;
   const int nt = c->ntypes;
-  const size_t bytes = (size_t)n * (3 + 1 + 2 * kMaxTypes) * sizeof(double) + 2 * kMaxTypes * kMaxTypes * sizeof(double) + 64;
+  // chunks of j atoms / k-vectors per grid row: about four CTAs per SM in all
+  int dev_sms = 0;
+  CASS_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
+  const int nb = std::max(1, (n + kGradBlock - 1) / kGradBlock);
+  const int want_rows = std::max(1, (4 * dev_sms + nb - 1) / nb);
+  auto chunking = [&](int total, int& rows) {  // chunk length, a multiple of the tile
+    rows = std::max(1, std::min(want_rows, (total + kGradBlock - 1) / kGradBlock));
+    int len = (total + rows - 1) / rows;
+    len = ((len + kGradBlock - 1) / kGradBlock) * kGradBlock;
+    rows = std::max(1, (total + len - 1) / len);
+    return len;
+  };
+  int npc = 1, nkc = 0;
+  const int jchunk = n > 0 ? chunking(n, npc) : 1;
+  const bool recip = d.charge_style == CASS_CHARGE_COUL && B.nvecs > 0;
+  int kchunk = 1;
+  if (recip) kchunk = chunking(B.nvecs, nkc);
+  const size_t bytes = (size_t)n * (3 + 1 + 2 * kMaxTypes) * sizeof(double) + 2 * kMaxTypes * kMaxTypes * sizeof(double) +
+                       (size_t)n * ((size_t)npc * kGradPairVals + (size_t)nkc * 4) * sizeof(double) + 64;
   if ((rc = c->d_grad.reserve(bytes))) return rc;
   double* d_g = c->d_grad.as<double>();
   double* d_dq = d_g + 3 * (size_t)n;
@@ -247,23 +377,34 @@ extern "C" int cass_system_gradient(cass_ctx* c, int32_t ibox1, CassEnergy* ener
   double* d_ds = d_de + (size_t)n * kMaxTypes;
   double* d_te = d_ds + (size_t)n * kMaxTypes;
   double* d_ts = d_te + kMaxTypes * kMaxTypes;
+  double* d_pp = d_ts + kMaxTypes * kMaxTypes;
+  double* d_rp = d_pp + (size_t)n * npc * kGradPairVals;
   if ((rc = c->d_query.reserve(16))) return rc;
   CASS_CUDA(cudaMemsetAsync(c->d_query.p, 0, sizeof(int), c->stream));
   if (n > 0) {
-    const int nb = (n + kGradBlock - 1) / kGradBlock;
-    k_grad_pairs<<<nb, kGradBlock, 0, c->stream>>>(B.dev, c->pt, c->pools, B.d_p64.as<double4_32a>(),
-                                                   B.d_meta.as<int4>(), n, d_g, d_dq, d_de, d_ds,
-                                                   c->d_query.as<int>());
+    // beyond every cutoff the kernel tests: pairs past it add nothing
+    double rmax2 = 0.0;
+    if (d.vdw_style == CASS_VDW_LJ) rmax2 = std::max(rmax2, B.dev.rcut_vdwsq);
+    if (d.charge_style == CASS_CHARGE_COUL) rmax2 = std::max(rmax2, B.dev.rcut_coulsq);
+    rmax2 = std::max(rmax2, B.dev.rcut_lowsq);
+    const float pre2 = (float)(rmax2 * (1.0 + 1.0e-4) + 1.0e-3);
+    k_grad_pairs<<<dim3(nb, npc), kGradBlock, 0, c->stream>>>(B.dev, c->pt, c->pools, B.d_p64.as<double4_32a>(),
+                                                              B.d_p32.as<float4>(), B.d_meta.as<int4>(), n, jchunk,
+                                                              pre2, d_pp, c->d_query.as<int>());
     CASS_CUDA(cudaGetLastError());
     count_launch(c);
-    if (d.charge_style == CASS_CHARGE_COUL && B.nvecs > 0) {
-      k_grad_recip<<<nb, kGradBlock, 0, c->stream>>>(B.d_kvec.as<double4_32a>(), B.d_cos_sum.as<double>(),
-                                                     B.d_sin_sum.as<double>(), B.nvecs, B.d_p64.as<double4_32a>(), n,
-                                                     d_g, d_dq);
+    if (recip) {
+      k_grad_recip<<<dim3(nb, nkc), kGradBlock, 0, c->stream>>>(B.d_kvec.as<double4_32a>(), B.d_cos_sum.as<double>(),
+                                                                B.d_sin_sum.as<double>(), B.nvecs, kchunk,
+                                                                kTWOPI / B.dev.L[0], B.d_p64.as<double4_32a>(), n, d_rp);
       CASS_CUDA(cudaGetLastError());
       count_launch(c);
     }
-    k_grad_types<<<kMaxTypes, 32, 0, c->stream>>>(B.d_meta.as<int4>(), n, d_de, d_ds, d_te, d_ts);
+    k_grad_reduce<<<nb, kGradBlock, 0, c->stream>>>(d_pp, npc, d_rp, recip ? nkc : 0, B.d_p64.as<double4_32a>(), n, d_g,
+                                                    d_dq, d_de, d_ds);
+    CASS_CUDA(cudaGetLastError());
+    count_launch(c);
+    k_grad_types<<<kMaxTypes, kTypeBlock, 0, c->stream>>>(B.d_meta.as<int4>(), n, d_de, d_ds, d_te, d_ts);
     CASS_CUDA(cudaGetLastError());
     count_launch(c);
   }
