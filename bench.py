@@ -270,6 +270,10 @@ def gcmc_leg(cg, abi, dev, with_cpu: bool, eq_steps: int = 150000, blocks: int =
     fp64, gf, _ = chains(abi.PREC_FP64, mu, eq_steps, blocks, block_steps, seed=911)
     gf.close()
     z = (mixed["mean_n"] - fp64["mean_n"]) / np.sqrt(np.maximum(mixed["se_n"] ** 2 + fp64["se_n"] ** 2, 1e-12))
+    dn = mixed["mean_n"] - fp64["mean_n"]
+    dse = float(dn.std(ddof=1) / np.sqrt(len(dn))) if len(dn) > 1 else float("nan")
+    pooled = {"mean_diff_n": float(dn.mean()), "se": dse, "z": float(dn.mean() / dse) if dse > 0 else None,
+              "mean_diff_rel": float(dn.mean() / fp64["mean_n"].mean())}
     per_box = [{"mu_kjmol": round(float(m), 4), "mean_n_mixed": float(a), "se_mixed": float(sa),
                 "mean_n_fp64": float(b), "se_fp64": float(sb), "density_g_cm3_mixed": density(a),
                 "density_g_cm3_fp64": density(b), "z": float(zz)}
@@ -280,11 +284,16 @@ def gcmc_leg(cg, abi, dev, with_cpu: bool, eq_steps: int = 150000, blocks: int =
                        "300 K, mu evenly spaced over [-30, -20] kJ/mol, 14 A cut_tail; insert/delete 40 %, "
                        "translate/rotate 40 %, regrow 20 %; one CTA per box, all boxes in one launch",
            "mixed": mixed, "fp64": fp64, "mixed_over_fp64": mixed["moves_per_s"] / fp64["moves_per_s"],
-           "density_check": {"max_abs_z": float(np.max(np.abs(z))), "mean_abs_rel_diff_n": float(
+           "density_check": {"max_abs_z": float(np.max(np.abs(z))), "rms_z": float(np.sqrt(np.mean(z ** 2))),
+               "mean_abs_rel_diff_n": float(
                np.mean([abs(p["mean_n_mixed"] / max(p["mean_n_fp64"], 1e-9) - 1) for p in per_box])),
+               "pooled": pooled,
                "note": f"z = (<N>_mixed - <N>_fp64) / combined block standard error ({blocks} blocks of "
-                       f"{block_steps} steps each); independent chains, so |z| ~ N(0,1) when both sample the "
-                       f"same ensemble"},
+                       f"{block_steps} steps each); successive blocks of a dense liquid box are correlated "
+                       f"(insertions are accepted about 1e-3 of the time), so the block errors are lower bounds "
+                       f"and rms_z above 1 measures that.  pooled: the mean of the 16 per-box differences "
+                       f"<N>_mixed - <N>_fp64 (independent chains, zero-mean when both sample the same ensembles) "
+                       f"with its standard error from their spread"},
            "per_box": per_box}
     # all SMs busy: 152 boxes (the 16 chemical potentials repeated), mixed precision
     wide, gw, _ = chains(abi.PREC_MIXED, [mu[k % nb] for k in range(152)], eq_steps // 4, 1, block_steps, seed=77)

@@ -432,6 +432,77 @@ __global__ void __launch_bounds__(128) k_sfac(const double4_32a* __restrict__ kv
   part[(size_t)blockIdx.y * nv + k] = make_double2(cs, sn);
 }
 
+// FP64 rebuild of the molecule rows along k-vector rows: thread per (row,
+// molecule); a sincos per atom at the row's start and for its step
+// e^{i 2 pi x / Lx}, then one complex product per k-vector and atom
+constexpr int kSfacRowAtoms = 4;  // molecules of up to this many atoms
+__global__ void __launch_bounds__(128) k_sfac_rows(const double4_32a* __restrict__ kvec, const int2* __restrict__ rows,
+                                                   int nrows, double hx1, const double4_32a* __restrict__ p64,
+                                                   const MolInfo* __restrict__ mols, int nm,
+                                                   const int* __restrict__ charged, double* cos_mol, double* sin_mol,
+                                                   int stride) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const int2 rw = rows[r];
+  const double4_32a h0 = kvec[rw.x];
+  for (int m = blockIdx.y; m < nm; m += gridDim.y) {
+    const MolInfo mi = mols[m];
+    if (!charged[mi.y]) continue;
+    double c[kSfacRowAtoms], s[kSfacRowAtoms], uc[kSfacRowAtoms], us[kSfacRowAtoms], q[kSfacRowAtoms];
+#pragma unroll
+    for (int a = 0; a < kSfacRowAtoms; ++a) {
+      c[a] = s[a] = us[a] = q[a] = 0.0;
+      uc[a] = 1.0;
+      if (a < mi.w) {
+        const double4_32a p = p64[mi.z + a];
+        sincos(h0.x * p.x + h0.y * p.y + h0.z * p.z, &s[a], &c[a]);
+        sincos(hx1 * p.x, &us[a], &uc[a]);
+        q[a] = p.w;
+      }
+    }
+    double* cm = cos_mol + (size_t)mi.x * stride + rw.x;
+    double* sm = sin_mol + (size_t)mi.x * stride + rw.x;
+    for (int j = 0; j < rw.y; ++j) {
+      double cs = 0.0, sn = 0.0;
+#pragma unroll
+      for (int a = 0; a < kSfacRowAtoms; ++a)
+        if (a < mi.w) {
+          cs = cs + q[a] * c[a];
+          sn = sn + q[a] * s[a];
+          const double c1 = c[a] * uc[a] - s[a] * us[a];
+          s[a] = s[a] * uc[a] + c[a] * us[a];
+          c[a] = c1;
+        }
+      cm[j] = cs;
+      sm[j] = sn;
+    }
+  }
+}
+
+// cos_sum / sin_sum from the molecule rows (charged species, packed order) and
+// the reciprocal energy, fixed order
+__global__ void __launch_bounds__(kBlock) k_sfac_sum(const double4_32a* __restrict__ kvec, int nv,
+                                                     const MolInfo* __restrict__ mols, int nm,
+                                                     const int* __restrict__ charged, const double* __restrict__ cos_mol,
+                                                     const double* __restrict__ sin_mol, int stride, double* cos_sum,
+                                                     double* sin_sum, double* partial, unsigned* counter, double* out) {
+  double e = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nv; k += gridDim.x * blockDim.x) {
+    double cs = 0.0, sn = 0.0;
+    for (int m = 0; m < nm; ++m) {
+      const MolInfo mi = mols[m];
+      if (!charged[mi.y]) continue;
+      cs += cos_mol[(size_t)mi.x * stride + k];
+      sn += sin_mol[(size_t)mi.x * stride + k];
+    }
+    cos_sum[k] = cs;
+    sin_sum[k] = sn;
+    e += kvec[k].w * (cs * cs + sn * sn);
+  }
+  double v[1] = {e};
+  reduce_partials<1>(v, partial, counter, out, nullptr, 0);
+}
+
 __global__ void __launch_bounds__(kBlock) k_sfac_reduce(const double4_32a* __restrict__ kvec, int nv, const double2* part,
                                                         int nchunks, double* cos_sum, double* sin_sum, double* partial,
                                                         unsigned* counter, double* out) {
@@ -1287,6 +1358,16 @@ int cass_set_box(cass_ctx* c, int32_t ibox, const CassBoxDesc* d) {
     if (!rc) rc = B.d_sin_old.reserve(nb);
     if (rc) return rc;
     CASS_CUDA(h2d(c, B.d_kvec.p, B.kvec.data(), B.kvec.size() * sizeof(double)));
+    B.krow.clear();
+    for (int k = 0; k < B.nvecs; ++k) {
+      const double* h = &B.kvec[4 * (size_t)k];
+      const bool cont = k > 0 && h[1] == h[-3] && h[2] == h[-2] &&
+                        std::fabs(h[0] - (h[-4] + kTWOPI / v.L[0])) <= 1e-9 * (kTWOPI / v.L[0]);
+      if (cont) ++B.krow.back().y;
+      else B.krow.push_back(make_int2(k, 1));
+    }
+    if ((rc = B.d_krow.reserve(std::max<size_t>(1, B.krow.size()) * sizeof(int2)))) return rc;
+    CASS_CUDA(h2d(c, B.d_krow.p, B.krow.data(), B.krow.size() * sizeof(int2)));
     CASS_CUDA(cudaMemsetAsync(B.d_cos_sum.p, 0, nb, c->stream));
     CASS_CUDA(cudaMemsetAsync(B.d_sin_sum.p, 0, nb, c->stream));
     CASS_CUDA(cudaStreamSynchronize(c->stream));
@@ -1633,6 +1714,33 @@ static int box_reciprocal(cass_ctx* c, int ibox, double* e_recip) {
   DevBuf& dch = c->d_cell_count;  // small reuse: species charged flags
   if ((rc = dch.reserve(std::max(c->nspecies, 1) * sizeof(int) + 256))) return rc;
   CASS_CUDA(h2d(c, dch.p, charged.data(), c->nspecies * sizeof(int)));
+  // FP64 contexts with small molecules: the row recurrence, then the sums
+  // from the molecule rows
+  int max_na = 0;
+  for (int is = 0; is < c->nspecies; ++is)
+    if (c->sp[is].defined && c->sp[is].has_charge) max_na = std::max(max_na, c->sp[is].natoms);
+  if (c->precision != CASS_PREC_MIXED && !B.krow.empty() && max_na <= kSfacRowAtoms && B.npacked_mols > 0) {
+    const int nrows = (int)B.krow.size();
+    dim3 g((nrows + 127) / 128, std::min(B.npacked_mols, 65535));
+    k_sfac_rows<<<g, 128, 0, c->stream>>>(B.d_kvec.as<double4_32a>(), B.d_krow.as<int2>(), nrows, kTWOPI / B.dev.L[0],
+                                          B.d_p64.as<double4_32a>(), B.d_molinfo.as<int4>(), B.npacked_mols,
+                                          dch.as<int>(), c->d_cos_mol.as<double>(), c->d_sin_mol.as<double>(),
+                                          c->cos_mol_stride);
+    CASS_CUDA(cudaGetLastError());
+    count_launch(c);
+    int nblk = std::max(1, std::min(296, (nv + kBlock - 1) / kBlock));
+    if ((rc = ensure_scratch(c, nblk, 1))) return rc;
+    k_sfac_sum<<<nblk, kBlock, 0, c->stream>>>(B.d_kvec.as<double4_32a>(), nv, B.d_molinfo.as<int4>(), B.npacked_mols,
+                                               dch.as<int>(), c->d_cos_mol.as<double>(), c->d_sin_mol.as<double>(),
+                                               c->cos_mol_stride, B.d_cos_sum.as<double>(), B.d_sin_sum.as<double>(),
+                                               c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
+                                               c->d_result.as<double>());
+    CASS_CUDA(cudaGetLastError());
+    count_launch(c);
+    if ((rc = sync_result(c, 1))) return rc;
+    *e_recip = c->h_result[0] * kCHARGE_FACTOR;
+    return CASS_OK;
+  }
   if (B.npacked_mols > 0) {
     dim3 g((nv + 127) / 128, nchunks);
     auto kern = c->precision == CASS_PREC_MIXED ? k_sfac<true> : k_sfac<false>;

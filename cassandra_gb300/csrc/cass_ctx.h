@@ -146,6 +146,10 @@ struct BoxH {
   std::vector<int> pk_mol_off;  // packed molecule -> first packed atom
   DevBuf d_p64, d_p32, d_meta, d_molinfo;
   DevBuf d_kvec, d_cos_sum, d_sin_sum, d_cos_old, d_sin_old;
+  // rows of the k-vector list: (first k, count) of runs of equal (ny, nz) with
+  // nx rising by one, for the phase recurrence of the FP64 rebuild
+  std::vector<int2> krow;
+  DevBuf d_krow;
   bool cell_dirty = true;
   // the state cass_volume_scale keeps for cass_volume_restore
   bool vol_saved = false;
