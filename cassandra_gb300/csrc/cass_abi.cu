@@ -479,28 +479,22 @@ __global__ void __launch_bounds__(128) k_sfac_rows(const double4_32a* __restrict
   }
 }
 
-// cos_sum / sin_sum from the molecule rows (charged species, packed order) and
-// the reciprocal energy, fixed order
-__global__ void __launch_bounds__(kBlock) k_sfac_sum(const double4_32a* __restrict__ kvec, int nv,
-                                                     const MolInfo* __restrict__ mols, int nm,
+// per (molecule chunk, k) sums of the molecule rows (charged species, packed
+// order), reduced over the chunks in order by k_sfac_reduce
+__global__ void __launch_bounds__(kBlock) k_sfac_sum(int nv, const MolInfo* __restrict__ mols, int nm,
                                                      const int* __restrict__ charged, const double* __restrict__ cos_mol,
-                                                     const double* __restrict__ sin_mol, int stride, double* cos_sum,
-                                                     double* sin_sum, double* partial, unsigned* counter, double* out) {
-  double e = 0.0;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nv; k += gridDim.x * blockDim.x) {
-    double cs = 0.0, sn = 0.0;
-    for (int m = 0; m < nm; ++m) {
-      const MolInfo mi = mols[m];
-      if (!charged[mi.y]) continue;
-      cs += cos_mol[(size_t)mi.x * stride + k];
-      sn += sin_mol[(size_t)mi.x * stride + k];
-    }
-    cos_sum[k] = cs;
-    sin_sum[k] = sn;
-    e += kvec[k].w * (cs * cs + sn * sn);
+                                                     const double* __restrict__ sin_mol, int stride, double2* part) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nv) return;
+  const int m0 = blockIdx.y * kSfacMolChunk, m1 = min(nm, m0 + kSfacMolChunk);
+  double cs = 0.0, sn = 0.0;
+  for (int m = m0; m < m1; ++m) {
+    const MolInfo mi = mols[m];
+    if (!charged[mi.y]) continue;
+    cs += cos_mol[(size_t)mi.x * stride + k];
+    sn += sin_mol[(size_t)mi.x * stride + k];
   }
-  double v[1] = {e};
-  reduce_partials<1>(v, partial, counter, out, nullptr, 0);
+  part[(size_t)blockIdx.y * nv + k] = make_double2(cs, sn);
 }
 
 __global__ void __launch_bounds__(kBlock) k_sfac_reduce(const double4_32a* __restrict__ kvec, int nv, const double2* part,
@@ -1728,20 +1722,12 @@ static int box_reciprocal(cass_ctx* c, int ibox, double* e_recip) {
                                           c->cos_mol_stride);
     CASS_CUDA(cudaGetLastError());
     count_launch(c);
-    int nblk = std::max(1, std::min(296, (nv + kBlock - 1) / kBlock));
-    if ((rc = ensure_scratch(c, nblk, 1))) return rc;
-    k_sfac_sum<<<nblk, kBlock, 0, c->stream>>>(B.d_kvec.as<double4_32a>(), nv, B.d_molinfo.as<int4>(), B.npacked_mols,
-                                               dch.as<int>(), c->d_cos_mol.as<double>(), c->d_sin_mol.as<double>(),
-                                               c->cos_mol_stride, B.d_cos_sum.as<double>(), B.d_sin_sum.as<double>(),
-                                               c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
-                                               c->d_result.as<double>());
+    k_sfac_sum<<<dim3((nv + kBlock - 1) / kBlock, nchunks), kBlock, 0, c->stream>>>(
+        nv, B.d_molinfo.as<int4>(), B.npacked_mols, dch.as<int>(), c->d_cos_mol.as<double>(),
+        c->d_sin_mol.as<double>(), c->cos_mol_stride, part.as<double2>());
     CASS_CUDA(cudaGetLastError());
     count_launch(c);
-    if ((rc = sync_result(c, 1))) return rc;
-    *e_recip = c->h_result[0] * kCHARGE_FACTOR;
-    return CASS_OK;
-  }
-  if (B.npacked_mols > 0) {
+  } else if (B.npacked_mols > 0) {
     dim3 g((nv + 127) / 128, nchunks);
     auto kern = c->precision == CASS_PREC_MIXED ? k_sfac<true> : k_sfac<false>;
     kern<<<g, 128, 0, c->stream>>>(B.d_kvec.as<double4_32a>(), nv, B.d_p64.as<double4_32a>(), B.d_molinfo.as<int4>(),
