@@ -170,6 +170,8 @@ SIGNATURES = {
     "system_gradient": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(CassEnergy), _f64p, _f64p, _f64p, _f64p]),
     "gcmc": (C.c_int, [C.c_void_p, C.c_int32, _i32p, C.POINTER(CassGCMCParams), _f64p, _f64p, _f64p, C.c_uint64,
                        C.POINTER(CassGCMCResult)]),
+    "atom_intra_energies": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _f64p, _i32p,
+                                      C.c_int32, _f64p, _i32p]),
     "cbmc_trial_energies": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _i32p, C.c_int32,
                                       _f64p, C.c_int32, _f64p, _i32p]),
     # allocation-free energy entry point and run-time extensions of the GPU
@@ -415,6 +417,18 @@ class Context:
             self._h, len(b), _p(b), C.byref(prm), md.ctypes.data_as(_f64p), mr.ctypes.data_as(_f64p),
             C.c_uint64(seed & (2**64 - 1)), res))
         return [r.as_dict() for r in res], md, mr
+
+    def atom_intra_energies(self, ibox: int, is_: int, ia: int, xyz, exist=None, cbmc: bool = True):
+        """Compute_Atom_Nonbond_Intra_Energy of atom ia (1-based) for trial configurations
+        xyz [ntrial][natoms][3]; returns (e [ntrial][3] = intra vdW, intra qq, inter qq, overlap [ntrial])."""
+        x = _f64(xyz)
+        ntrial = x.size // (3 * self.natoms[is_])
+        ex = _i32(exist) if exist is not None else None
+        e = np.zeros(3 * ntrial)
+        ov = np.zeros(ntrial, dtype=np.int32)
+        self._check("atom_intra_energies", self._f["atom_intra_energies"](
+            self._h, ibox, is_, ia, ntrial, _p(x), _p(ex), int(cbmc), _p(e), _p(ov)))
+        return e.reshape(ntrial, 3), ov.astype(bool)
 
     def cbmc_trial_energies(self, ibox: int, is_: int, atoms, xyz, cbmc: bool = True, skip_im: int = 0):
         """Energies of trial positions [ntrial, nat, 3] of atoms (1-based) of species is_."""

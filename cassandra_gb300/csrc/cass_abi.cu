@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "cass_cbmc.cuh"
 #include "cass_ctx.h"
 
 namespace cassgpu {
@@ -356,7 +357,7 @@ __global__ void __launch_bounds__(kBlock) k_pair_total(BoxDev b, PairTable t, co
 __global__ void __launch_bounds__(kBlock) k_intra_total(BoxDev b, PairTable t, SpeciesPools P,
                                                         const double4_32a* __restrict__ p64,
                                                         const MolInfo* __restrict__ mols, int nm, double* partial,
-                                                        unsigned* counter, double* out, int* ovflag) {
+                                                        unsigned* counter, double* out, int* ovflag, int cbmc = 0) {
   double v[7] = {0, 0, 0, 0, 0, 0, 0};
   double r[3 * 64];
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nm; m += gridDim.x * blockDim.x) {
@@ -368,7 +369,7 @@ __global__ void __launch_bounds__(kBlock) k_intra_total(BoxDev b, PairTable t, S
       r[3 * a + 1] = p.y;
       r[3 * a + 2] = p.z;
     }
-    IntraOut o = molecule_intra(P, mi.y, b, t, r);
+    IntraOut o = molecule_intra(P, mi.y, b, t, r, cbmc != 0);
     if (o.overlap) {
       atomicOr(ovflag, 1);
       continue;
@@ -580,6 +581,19 @@ __global__ void __launch_bounds__(kBlock) k_ewald_widom(const double4_32a* __res
   }
   e = block_sum(e, sh);
   if (threadIdx.x == 0) out[blockIdx.x] = e * kCHARGE_FACTOR;
+}
+
+// Compute_Atom_Nonbond_Intra_Energy for one trial configuration per thread
+__global__ void k_atom_intra(BoxDev b, PairTable t, SpeciesPools P, int is0, int ia, const double* __restrict__ xyz,
+                             int natoms, unsigned exist, int ntrial, int cbmc, double* e, int* ov) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ntrial) return;
+  double eiv, eiq, eoq;
+  const bool o = atom_intra(P.hdr[is0], P, b, t, ia, xyz + (size_t)k * natoms * 3, exist, eiv, eiq, eoq, cbmc != 0);
+  e[3 * k] = o ? 0.0 : eiv;
+  e[3 * k + 1] = o ? 0.0 : eiq;
+  e[3 * k + 2] = o ? 0.0 : eoq;
+  ov[k] = o ? 1 : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1609,6 +1623,41 @@ int cass_mol_inter_energy(cass_ctx* c, int32_t im, int32_t is, int32_t cbmc, dou
   return CASS_OK;
 }
 
+int cass_atom_intra_energies(cass_ctx* c, int32_t ibox1, int32_t is, int32_t ia, int32_t ntrial, const double* xyz,
+                             const int32_t* exist, int32_t cbmc, double* e, int32_t* overlap) {
+  if (!c || ibox1 < 1 || ibox1 > c->nboxes || is < 1 || is > c->nspecies || ntrial < 0 ||
+      (ntrial > 0 && (!xyz || !e || !overlap)))
+    return set_error(CASS_EINVAL, "bad atom intra arguments");
+  if (!c->pt_set) return set_error(CASS_ESTATE, "nonbond table not set");
+  const SpeciesH& s = c->sp[is - 1];
+  if (!s.defined) return set_error(CASS_ESTATE, "species not defined");
+  if (s.natoms > 32) return set_error(CASS_ECAPACITY, "at most 32 atoms per molecule");
+  if (ia < 1 || ia > s.natoms) return set_error(CASS_EINVAL, "atom index out of range");
+  if (ntrial == 0) return CASS_OK;
+  unsigned mask = 0u;
+  for (int a = 0; a < s.natoms; ++a)
+    if (!exist || exist[a]) mask |= 1u << a;
+  int rc;
+  if ((rc = set_device(c)) || (rc = ensure_pools(c))) return rc;
+  BoxH& B = c->box[ibox1 - 1];
+  if (!B.defined) return set_error(CASS_ESTATE, "box not defined");
+  const size_t nx = (size_t)ntrial * s.natoms * 3;
+  if ((rc = c->d_trial.reserve(nx * sizeof(double) + (size_t)ntrial * (3 * sizeof(double) + sizeof(int)) + 64)))
+    return rc;
+  double* d_x = c->d_trial.as<double>();
+  double* d_e = d_x + nx;
+  int* d_ov = reinterpret_cast<int*>(d_e + 3 * (size_t)ntrial);
+  CASS_CUDA(h2d(c, d_x, xyz, nx * sizeof(double)));
+  k_atom_intra<<<(ntrial + kBlock - 1) / kBlock, kBlock, 0, c->stream>>>(B.dev, c->pt, c->pools, is - 1, ia - 1, d_x,
+                                                                         s.natoms, mask, ntrial, cbmc, d_e, d_ov);
+  CASS_CUDA(cudaGetLastError());
+  count_launch(c);
+  CASS_CUDA(d2h(c, e, d_e, 3 * (size_t)ntrial * sizeof(double)));
+  CASS_CUDA(d2h(c, overlap, d_ov, (size_t)ntrial * sizeof(int)));
+  CASS_CUDA(cudaStreamSynchronize(c->stream));
+  return CASS_OK;
+}
+
 int cass_cbmc_trial_energies(cass_ctx* c, int32_t ibox1, int32_t is, int32_t skip_im, int32_t nat,
                              const int32_t* atoms, int32_t ntrial, const double* xyz, int32_t cbmc, double* e,
                              int32_t* overlap) {
@@ -1669,7 +1718,6 @@ int cass_mol_intra_energy(cass_ctx* c, int32_t im, int32_t is, int32_t cbmc, dou
   int slot = mol_slot(c, im, is);
   int ibox = c->mol_box[slot];
   if (ibox < 0) return set_error(CASS_ESTATE, "molecule not live");
-  if (cbmc) return set_error(CASS_EUNSUPPORTED, "intra energy with the CBMC cutoff is computed inside the Widom kernel");
   if ((rc = set_device(c)) || (rc = pack_box(c, ibox))) return rc;
   if ((rc = ensure_pools(c))) return rc;
   BoxH& B = c->box[ibox];
@@ -1679,7 +1727,7 @@ int cass_mol_intra_energy(cass_ctx* c, int32_t im, int32_t is, int32_t cbmc, dou
   CASS_CUDA(cudaMemsetAsync(c->d_query.p, 0, sizeof(int), c->stream));
   k_intra_total<<<1, kBlock, 0, c->stream>>>(B.dev, c->pt, c->pools, B.d_p64.as<double4_32a>(), B.d_molinfo.as<int4>() + q, 1,
                                              c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
-                                             c->d_result.as<double>(), c->d_query.as<int>());
+                                             c->d_result.as<double>(), c->d_query.as<int>(), cbmc ? 1 : 0);
   CASS_CUDA(cudaGetLastError());
   count_launch(c);
   int hov = 0;

@@ -86,7 +86,7 @@ __device__ inline double dihedral_masked(const SpeciesDevHdr& H, const SpeciesPo
 
 // Compute_Atom_Nonbond_Intra_Energy (energy_routines.f90:691-737), CBMC cutoffs
 __device__ inline bool atom_intra(const SpeciesDevHdr& H, const SpeciesPools& P, const BoxDev& b, const PairTable& T, int ia,
-                           const double* r, unsigned exist, double& eiv, double& eiq, double& eoq) {
+                           const double* r, unsigned exist, double& eiv, double& eiq, double& eoq, bool cbmc = true) {
   eiv = eiq = eoq = 0.0;
   int n = H.natoms;
   for (int ja = 0; ja < n; ++ja) {
@@ -97,7 +97,7 @@ __device__ inline bool atom_intra(const SpeciesDevHdr& H, const SpeciesPools& P,
     double dx = r[3 * ja] - r[3 * ia], dy = r[3 * ja + 1] - r[3 * ia + 1], dz = r[3 * ja + 2] - r[3 * ia + 2];
     double r2 = dx * dx + dy * dy + dz * dz;
     if (r2 < b.rcut_lowsq && nzv) return true;
-    int m = cutoff_mask(b, r2, true);
+    int m = cutoff_mask(b, r2, cbmc);
     if (!nzv) m &= ~1;
     if (!nzq) m &= ~2;
     if (m & 1) eiv += vdw_pair(T, b, P.ip[H.type_off + ja], P.ip[H.type_off + ia], r2, P.dp[H.vs_off + ja * n + ia]);

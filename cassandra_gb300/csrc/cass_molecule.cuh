@@ -43,8 +43,11 @@ struct IntraOut {
   bool overlap;
 };
 
+// cbmc: Check_AtomPair_Cutoff with rcut_cbmc, and no charge pairs when the
+// species' L_Coul_CBMC is set (energy_routines.f90:1062-1064; the opposite sense
+// of the intermolecular rule of :1684-1686, kept as the reference has it)
 __device__ inline IntraOut molecule_intra(const SpeciesPools& P, int is, const BoxDev& b, const PairTable& t,
-                                   const double* r) {
+                                   const double* r, bool cbmc = false) {
   const SpeciesDevHdr& h = P.hdr[is];
   IntraOut o{0, 0, 0, 0, 0, 0, 0, false};
   const int* ip = P.ip;
@@ -102,7 +105,8 @@ __device__ inline IntraOut molecule_intra(const SpeciesPools& P, int is, const B
         o.overlap = true;
         return o;
       }
-      int m = cutoff_mask(b, r2, false);
+      int m = cutoff_mask(b, r2, cbmc);
+      if (cbmc && h.l_coul_cbmc) m &= ~2;
       if (m & 1) o.ivdw += vdw_pair(t, b, ip[h.type_off + ia], ip[h.type_off + ja], r2, dp[h.vs_off + ia * n + ja]);
       if (m & 2)
         o.iqq += qq_pair_intra(b, dp[h.q_off + ia] * dp[h.q_off + ja], r2, dp[h.qs_off + ia * n + ja], &o.pqq);

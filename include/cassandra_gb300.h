@@ -199,7 +199,9 @@ int cass_get_molecule_boxes(cass_ctx* ctx, int32_t is, int32_t n, int32_t* which
  * cbmc_flag selects the rcut_cbmc cutoffs of Check_AtomPair_Cutoff. */
 int cass_mol_inter_energy(cass_ctx* ctx, int32_t im, int32_t is, int32_t cbmc_flag,
                           double* e_inter_vdw, double* e_inter_qq, int32_t* overlap);
-/* Compute_Molecule_Nonbond_Intra_Energy (energy_routines.f90:980-1085) */
+/* Compute_Molecule_Nonbond_Intra_Energy (energy_routines.f90:980-1085);
+ * cbmc_flag selects rcut_cbmc and drops the charge pairs of a species whose
+ * L_Coul_CBMC is set (:1062-1064), as the reference does. */
 int cass_mol_intra_energy(cass_ctx* ctx, int32_t im, int32_t is, int32_t cbmc_flag,
                           double* e_intra_vdw, double* e_intra_qq, double* e_inter_qq,
                           int32_t* overlap);
@@ -276,6 +278,19 @@ int cass_set_cbmc_options(cass_ctx* ctx, const CassCBMCOptions* opt);
  * deleted or regrown).  cbmc_flag selects rcut_cbmc and drops Coulomb unless
  * the species' L_Coul_CBMC is set.  e[k] = E_vdw + E_qq of trial k,
  * overlap[k] = 1 on a core overlap (e[k] = 0). */
+/* Compute_Atom_Nonbond_Intra_Energy (energy_routines.f90:691-737) for a batch
+ * of trial configurations of one molecule of species is, as Fragment_Placement
+ * calls it for each new atom of a dihedral trial (fragment_growth.f90:
+ * 1994-2000): atom ia (1-based) against the other existing atoms of the molecule
+ * (exist[natoms] flags, NULL = every atom) with no periodic image, pairs whose
+ * vdW and charge scale factors are both zero skipped, in the cutoffs of box
+ * ibox (rcut_cbmc when cbmc_flag, as Check_AtomPair_Cutoff).  xyz holds
+ * [ntrial][natoms][3]; e[3k..3k+2] = E_intra_vdw, E_intra_qq, E_inter_qq of trial
+ * k (E_inter_qq: the -erf part of an Ewald sum); overlap[k] = 1 when a pair with
+ * a nonzero vdW scale is closer than rcut_low (e = 0).  natoms <= 32. */
+int cass_atom_intra_energies(cass_ctx* ctx, int32_t ibox, int32_t is, int32_t ia, int32_t ntrial,
+                             const double* xyz, const int32_t* exist, int32_t cbmc_flag, double* e,
+                             int32_t* overlap);
 int cass_cbmc_trial_energies(cass_ctx* ctx, int32_t ibox, int32_t is, int32_t skip_im, int32_t nat,
                              const int32_t* atoms, int32_t ntrial, const double* xyz, int32_t cbmc_flag,
                              double* e, int32_t* overlap);

@@ -2940,6 +2940,30 @@ int orc_widom_insert(orc_ctx* c, int32_t is1, int32_t nboxes, const int32_t* ibo
 }
 
 // Compute_Molecule_Nonbond_Inter_Energy_Widom for each trial position
+int orc_atom_intra_energies(orc_ctx* c, int32_t ibox1, int32_t is1, int32_t ia, int32_t ntrial, const double* xyz,
+                            const int32_t* exist, int32_t cbmc, double* e, int32_t* overlap) {
+  if (check_ctx(c) || ibox1 < 1 || ibox1 > c->nboxes || is1 < 1 || is1 > c->nspecies || ntrial < 0 ||
+      (ntrial > 0 && (!xyz || !e || !overlap)))
+    return fail(CASS_EINVAL, "bad atom intra arguments");
+  const Species& s = c->sp[is1 - 1];
+  if (!s.defined) return fail(CASS_ESTATE, "species not defined");
+  if (s.natoms > 32) return fail(CASS_ECAPACITY, "at most 32 atoms per molecule");
+  if (ia < 1 || ia > s.natoms) return fail(CASS_EINVAL, "atom index out of range");
+  std::vector<char> ex(s.natoms, 1);
+  if (exist)
+    for (int a = 0; a < s.natoms; ++a) ex[a] = exist[a] ? 1 : 0;
+  for (int k = 0; k < ntrial; ++k) {
+    double eiv, eiq, eoq;
+    const bool ov = atom_intra_energy(c, c->box[ibox1 - 1], is1 - 1, ia - 1, xyz + (size_t)k * s.natoms * 3, ex.data(),
+                                      cbmc != 0, eiv, eiq, eoq);
+    overlap[k] = ov ? 1 : 0;
+    e[3 * k] = ov ? 0.0 : eiv;
+    e[3 * k + 1] = ov ? 0.0 : eiq;
+    e[3 * k + 2] = ov ? 0.0 : eoq;
+  }
+  return CASS_OK;
+}
+
 int orc_cbmc_trial_energies(orc_ctx* c, int32_t ibox1, int32_t is1, int32_t skip_im, int32_t nat, const int32_t* atoms,
                             int32_t ntrial, const double* xyz, int32_t cbmc, double* e, int32_t* overlap) {
   if (c) refresh_members(c);

@@ -127,11 +127,12 @@ def test_molecule_energies(prec):
                 if prec == abi.PREC_MIXED:
                     scale = max(scale, abs_pair_sum(s, int(im), cbmc))
                 assert abs(a[0] - b[0]) <= tol * scale and abs(a[1] - b[1]) <= tol * scale, (im, cbmc, a, b)
-            ia = o.mol_intra_energy(int(im), 1)
-            ib = g.mol_intra_energy(int(im), 1)
-            assert ia[3] == ib[3]
-            for x, y in zip(ia[:3], ib[:3]):
-                assert close(y, x, FP64_TOL, 1e-6)
+            for cbmc in (False, True):
+                ia = o.mol_intra_energy(int(im), 1, cbmc)
+                ib = g.mol_intra_energy(int(im), 1, cbmc)
+                assert ia[3] == ib[3]
+                for x, y in zip(ia[:3], ib[:3]):
+                    assert close(y, x, FP64_TOL, 1e-6)
 
 
 def test_molecule_overlap_flag():
@@ -323,3 +324,57 @@ def test_cbmc_trial_energies_match_oracle():
             eg, og = g.cbmc_trial_energies(2, 1, [1], sph[-1:], skip_im=m.im[k7])
             assert not og[0] and oo[0] == og[0]
             assert abs(eg[0] - eo[0]) <= FP64_TOL * abs(eo[0])
+
+
+@pytest.mark.parametrize("cbmc", [True, False])
+def test_atom_intra_energies_match_oracle(cbmc):
+    """Compute_Atom_Nonbond_Intra_Energy for batches of pentane conformations with
+    partial growth (exist flags): united atoms whose only scaled pair is 1-5,
+    and the same chain with charges in an Ewald box (the -erf part)."""
+    import dataclasses
+    rng = np.random.default_rng(17)
+    for charged in (False, True):
+        s = helpers.pregen_system("pentane", 1)
+        if charged:
+            sp = s.species[0]
+            sp.atoms = [dataclasses.replace(a, charge=q) for a, q in zip(sp.atoms, (0.3, -0.2, 0.1, -0.4, 0.2))]
+            bx = s.boxes[0]
+            bx.charge_style, bx.charge_sum_style = abi.CHARGE_COUL, abi.QQ_EWALD
+            bx.rcut_coul, bx.ewald_tol = 14.0, 1e-3
+        na = s.species[0].natoms
+        base = np.asarray(s.molecules.xyz[0])
+        xyz = np.stack([base + rng.normal(scale=0.4, size=base.shape) for _ in range(40)])
+        xyz[3, 0] = xyz[3, 4] + np.array([0.05, 0.0, 0.0])  # atoms 1 and 5 (the scaled 1-5 pair) overlap in trial 3
+        xyz[5, 1] = xyz[5, 3] + np.array([0.05, 0.0, 0.0])  # atoms 2 and 4 (1-3, zero scales): skipped, no overlap
+        with oracle.open_system(s) as o, cg.open_system(s, precision=abi.PREC_FP64) as g:
+            for ia in (1, 2, 3, 5):
+                for exist in (None, [1] * (na - 1) + [0], [1, 1, 1, 0, 0]):
+                    eo, oo = o.atom_intra_energies(1, 1, ia, xyz, exist, cbmc)
+                    eg, og = g.atom_intra_energies(1, 1, ia, xyz, exist, cbmc)
+                    assert np.array_equal(oo, og)
+                    assert np.allclose(eg, eo, rtol=1e-12, atol=1e-9), (charged, ia, exist)
+                    if exist is None and ia in (1, 5):  # the 1-5 pair is the chain's only scaled pair
+                        assert np.abs(eo).sum() > 0
+                        if charged:
+                            assert np.abs(eo[:, 2]).sum() > 0
+            assert g.atom_intra_energies(1, 1, 1, xyz)[1][3] and not g.atom_intra_energies(1, 1, 2, xyz)[1][5]
+
+
+def test_molecule_intra_cbmc_coulomb_rule():
+    """Compute_Molecule_Nonbond_Intra_Energy with cbmc_flag drops the charge pairs of a
+    species whose L_Coul_CBMC is set (energy_routines.f90:1062-1064)."""
+    for lcc in (False, True):
+        s = helpers.pregen_system("water_spce", 2)
+        s.species[0].l_coul_cbmc = lcc
+        with oracle.open_system(s) as o, cg.open_system(s, precision=abi.PREC_FP64) as g:
+            for im in (1, 7, 40):
+                for cbmc in (False, True):
+                    a = o.mol_intra_energy(im, 1, cbmc)
+                    b = g.mol_intra_energy(im, 1, cbmc)
+                    assert a[3] == b[3]
+                    for x, y in zip(a[:3], b[:3]):
+                        assert close(y, x, FP64_TOL, 1e-9), (lcc, im, cbmc, a, b)
+                    if cbmc and lcc:
+                        assert a[1] == 0.0 and a[2] == 0.0
+                    else:
+                        assert a[2] != 0.0  # the -erf part of the intramolecular Ewald pairs

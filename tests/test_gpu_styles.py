@@ -1,0 +1,88 @@
+"""Every vdW and charge style of Compute_AtomPair_Energy (energy_routines.f90:
+1831-2082) and Check_AtomPair_Cutoff (:3092-3195) through the FP64 GPU path
+against the oracle: LJ with cut, cut_tail, cut_shift, cut_switch, CHARMM,
+minimum image and cut_shift_force; Mie with cut, cut_shift and cut_tail; charges
+with the plain cut, minimum image, damped shifted force and Ewald.  Per style:
+the system energy (every component), molecule energies with and without the
+CBMC cutoffs, and Widom insertions record by record."""
+import numpy as np
+import pytest
+
+import cassandra_gb300 as cg
+import helpers
+from cassandra_gb300 import abi, workloads
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from cassandra_gb300 import build
+    build.build()
+    oracle.build()
+
+
+def _close(a, b, rel=TOL, abs_=1e-7):
+    return abs(a - b) <= rel * max(abs(a), abs(b)) + abs_
+
+
+def _lj_fluid(vdw_sum, vdw=("LJ", 120.0, 3.4), style=abi.VDW_LJ):
+    rng = np.random.default_rng(5)
+    xyz = workloads.lj_fluid_box(300, 25.0, 3.0, rng)
+    s = helpers.single_atom_system(xyz, 25.0, vdw=vdw, vdw_style=style, vdw_sum=vdw_sum, rcut=10.0, rcut_low=1.0,
+                                   extra_slots=2)
+    if vdw_sum == abi.VDW_SUM_CUT_SWITCH:
+        s.boxes[0].ron_switch, s.boxes[0].roff_switch = 8.0, 10.0
+    return s
+
+
+def _water(charge_sum, rcut=9.0):
+    s = helpers.pregen_system("water_spce", 4)
+    s.species[0].libraries = [workloads.water_species().libraries[0] * 1.0]
+    bx = s.boxes[0]
+    bx.charge_style, bx.charge_sum_style = abi.CHARGE_COUL, charge_sum
+    bx.rcut_coul = rcut
+    bx.rcut_vdw = rcut
+    return s
+
+
+CASES = [("lj_" + n, lambda v=v: _lj_fluid(v)) for n, v in (
+    ("cut", abi.VDW_SUM_CUT), ("cut_tail", abi.VDW_SUM_CUT_TAIL), ("cut_shift", abi.VDW_SUM_CUT_SHIFT),
+    ("cut_switch", abi.VDW_SUM_CUT_SWITCH), ("charmm", abi.VDW_SUM_CHARMM), ("minimum", abi.VDW_SUM_MINIMUM),
+    ("cut_shift_force", abi.VDW_SUM_CUT_SHIFT_FORCE))]
+CASES += [("mie_" + n, lambda v=v: _lj_fluid(v, vdw=("Mie", 120.0, 3.4, 14.0, 6.0), style=abi.VDW_MIE)) for n, v in (
+    ("cut", abi.VDW_SUM_CUT), ("cut_shift", abi.VDW_SUM_CUT_SHIFT), ("cut_tail", abi.VDW_SUM_CUT_TAIL))]
+CASES += [("water_" + n, lambda v=v: _water(v)) for n, v in (
+    ("qq_cut", abi.QQ_CUT), ("qq_minimum", abi.QQ_MINIMUM), ("qq_dsf", abi.QQ_DSF), ("qq_ewald", abi.QQ_EWALD))]
+
+
+@pytest.mark.parametrize("name,make", CASES, ids=[c[0] for c in CASES])
+def test_style_matches_oracle(name, make):
+    s = make()
+    water = name.startswith("water")
+    with oracle.open_system(s) as o, cg.open_system(s, precision=abi.PREC_FP64) as g:
+        eo, ovo = o.system_total_energy(1)
+        eg, ovg = g.system_total_energy(1)
+        assert ovo == ovg == False
+        for k in eo:
+            assert _close(eg[k], eo[k]), (name, k, eg[k], eo[k])
+        for im in (1, 17, 60):
+            for cbmc in (False, True):
+                a = o.mol_inter_energy(im, 1, cbmc)
+                b = g.mol_inter_energy(im, 1, cbmc)
+                assert a[2] == b[2]
+                assert _close(b[0], a[0]) and _close(b[1], a[1]), (name, im, cbmc, a, b)
+        n = 64
+        ro, to = o.widom_insert(1, [1], n, 8, 0, seed=3, trace=True)
+        rg, tg = g.widom_insert(1, [1], n, 8, 0, seed=3, trace=True)
+    assert np.array_equal(to["overlap"], tg["overlap"])
+    assert np.array_equal(to["selected_trial"], tg["selected_trial"])
+    ok = to["overlap"] == 0
+    assert ok.sum() > 0
+    assert np.allclose(tg["e_inter"][ok], to["e_inter"][ok], rtol=1e-9, atol=1e-6)
+    assert np.allclose(tg["widom_var"][ok], to["widom_var"][ok], rtol=1e-8, atol=0)
+    if not water:
+        assert ro[0]["n_insertions"] == rg[0]["n_insertions"] == n
