@@ -71,6 +71,16 @@ __global__ void k_patch_atoms(const PatchRec* rec, int n, const BoxPtrs* bp) {
 
 constexpr int kBlock = 256;
 
+// Check_MoleculePair_Cutoff (energy_routines.f90:3027-3088): the molecules
+// interact unless their COMs (minimum image) are farther apart than rmax
+// (rcut_max, or rcut_cbmc with the CBMC flag) plus both max_dcom
+__device__ __forceinline__ bool molpair_in(const BoxDev& b, double rmax, const double4_32a& ci, const double4_32a& cj) {
+  const double dx = fold(ci.x - cj.x, b.hL[0], b.L[0]), dy = fold(ci.y - cj.y, b.hL[1], b.L[1]),
+               dz = fold(ci.z - cj.z, b.hL[2], b.L[2]);
+  const double rcom = sqrt(dx * dx + dy * dy + dz * dz);
+  return !(rcom > rmax + ci.w + cj.w);
+}
+
 __device__ __forceinline__ double block_sum(double v, double* sh) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -121,6 +131,7 @@ template <bool MIXED>
 __global__ void __launch_bounds__(kBlock) k_mol_inter(BoxDev b, PairTable t, const double4_32a* __restrict__ p64,
                                                       const float4* __restrict__ p32, const int4* __restrict__ meta,
                                                       int n, int qslot, int qoff, int qn, int cbmc, int want_qq,
+                                                      const double4_32a* __restrict__ com, double rmax,
                                                       double* partial, unsigned* counter, double* out, int* ovflag) {
   __shared__ double4_32a qa[kMaxAtoms * 4];
   __shared__ int qt[kMaxAtoms * 4];
@@ -136,6 +147,7 @@ __global__ void __launch_bounds__(kBlock) k_mol_inter(BoxDev b, PairTable t, con
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
     int4 mj = meta[j];
     if (mj.x == qslot) continue;
+    if (com && !molpair_in(b, rmax, com[qoff], com[j])) continue;
     double4_32a pj = p64[j];
     for (int a = 0; a < qn; ++a) {
       double dx = fold(qa[a].x - pj.x, b.hL[0], b.L[0]);
@@ -259,9 +271,12 @@ template <bool FAST>
 // pre2 (FP64 kernel): an FP32 bound on r^2 beyond every cutoff of the box with
 // a margin far above FP32 rounding; pairs past it skip the FP64 arithmetic,
 // which decides every cutoff exactly (FLT_MAX where a style has no cutoff)
+// com (FP64 kernel, may be NULL): per-atom molecule COM records for
+// Check_MoleculePair_Cutoff with radius rmax
 __global__ void __launch_bounds__(kBlock) k_pair_total(BoxDev b, PairTable t, const double4_32a* __restrict__ p64,
-                                                       const int4* __restrict__ meta, int n, float pre2, double* partial,
-                                                       unsigned* counter, double* out, int* ovflag) {
+                                                       const int4* __restrict__ meta, int n, float pre2,
+                                                       const double4_32a* __restrict__ com, double rmax,
+                                                       double* partial, unsigned* counter, double* out, int* ovflag) {
   __shared__ double4_32a sj[FAST ? 1 : kBlock];
   __shared__ float4 sf[kBlock];
   __shared__ int2 sm[kBlock];  // molecule slot, type
@@ -333,6 +348,7 @@ __global__ void __launch_bounds__(kBlock) k_pair_total(BoxDev b, PairTable t, co
                         ez = fold(pif.z - q.z, b.hLf[2], b.Lf[2]);
             if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) > pre2) continue;
           }
+          if (com && !molpair_in(b, rmax, com[i], com[j])) continue;
           const double4_32a pj = sj[k];
           const double dx = fold(pi.x - pj.x, b.hL[0], b.L[0]);
           const double dy = fold(pi.y - pj.y, b.hL[1], b.L[1]);
@@ -770,6 +786,36 @@ int pack_box(cass_ctx* c, int ibox) {
   }
   B.npacked = (int)na;
   B.npacked_mols = (int)nm;
+  if (B.comcut && na > 0) {
+    // Get_COM and Compute_Max_Com_Distance (get_com.f90:45-105,220-295) per molecule
+    std::vector<double4_32a> com(na);
+    for (size_t q = 0; q < nm; ++q) {
+      const int4 mi = molinfo[q];
+      const SpeciesH& sp = c->sp[mi.y];
+      double tm = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
+      for (int a = 0; a < mi.w; ++a) {
+        const double4_32a& p = p64[mi.z + a];
+        tm = tm + sp.mass[a];
+        cx = cx + sp.mass[a] * p.x;
+        cy = cy + sp.mass[a] * p.y;
+        cz = cz + sp.mass[a] * p.z;
+      }
+      cx = cx / tm;
+      cy = cy / tm;
+      cz = cz / tm;
+      double dmax = 0.0;
+      for (int a = 0; a < mi.w; ++a) {
+        const double4_32a& p = p64[mi.z + a];
+        const double dx = p.x - cx, dy = p.y - cy, dz = p.z - cz;
+        dmax = std::max(dmax, dx * dx + dy * dy + dz * dz);
+      }
+      const double4_32a v = make_double4_32a(cx, cy, cz, std::sqrt(dmax));
+      for (int a = 0; a < mi.w; ++a) com[mi.z + a] = v;
+    }
+    if ((rc = B.d_com.reserve(na * sizeof(double4_32a)))) return rc;
+    CASS_CUDA(h2d(c, B.d_com.p, com.data(), na * sizeof(double4_32a)));
+    CASS_CUDA(cudaStreamSynchronize(c->stream));  // the host vector goes out of scope
+  }
   if (na > 0) {
     CASS_CUDA(h2d(c, B.d_p64.p, p64, na * sizeof(double4_32a)));
     CASS_CUDA(h2d(c, B.d_p32.p, p32, na * sizeof(float4)));
@@ -1330,6 +1376,9 @@ int cass_set_box(cass_ctx* c, int32_t ibox, const CassBoxDesc* d) {
   }
   v.beta = 1.0 / (kKBOLTZ * d->temperature);
   B.rcut_max = std::max(d->rcut_vdw, rcoul);  // precalculate.f90:79-83
+  B.comcut = d->vdw_sum_style != CASS_VDW_SUM_MINIMUM &&
+             ((d->vdw_style == CASS_VDW_LJ && d->vdw_sum_style == CASS_VDW_SUM_CHARMM) ||
+              (d->charge_style == CASS_CHARGE_COUL && d->charge_sum_style == CASS_QQ_MINIMUM));
   B.rcut3 = d->rcut_vdw * d->rcut_vdw * d->rcut_vdw;
   B.rcut9 = B.rcut3 * B.rcut3 * B.rcut3;
   B.kvec.clear();
@@ -1415,7 +1464,7 @@ int cass_set_molecules(cass_ctx* c, int32_t n, const int32_t* im, const int32_t*
     off += 3 * s.natoms;
     set_mol_box(c, slot, nb);
     if (old >= 0 && old != nb) invalidate(c, old);
-    if (old == nb && !c->box[nb].pack_dirty) patch_slots.push_back(slot);
+    if (old == nb && !c->box[nb].pack_dirty && !c->box[nb].comcut) patch_slots.push_back(slot);
     else invalidate(c, nb);
   }
   c->h_patch.clear();
@@ -1602,15 +1651,18 @@ int cass_mol_inter_energy(cass_ctx* c, int32_t im, int32_t is, int32_t cbmc, dou
   if (rc2) return rc2;
   CASS_CUDA(cudaMemsetAsync(c->d_query.p, 0, sizeof(int), c->stream));
   int want_qq = (cbmc && !s.l_coul_cbmc) ? 0 : 1;
+  // Check_MoleculePair_Cutoff where a style has no atom cutoff (rcut_cbmc with the CBMC flag)
+  const double4_32a* mcom = B.comcut ? B.d_com.as<double4_32a>() : nullptr;
+  const double mrad = cbmc ? B.desc.rcut_cbmc : B.rcut_max;
   if (c->precision == CASS_PREC_MIXED)
     k_mol_inter<true><<<nblk, kBlock, 0, c->stream>>>(B.dev, c->pt, B.d_p64.as<double4_32a>(), B.d_p32.as<float4>(),
                                                       B.d_meta.as<int4>(), B.npacked, slot, qoff, s.natoms, cbmc,
-                                                      want_qq, c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
+                                                      want_qq, mcom, mrad, c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
                                                       c->d_result.as<double>(), c->d_query.as<int>());
   else
     k_mol_inter<false><<<nblk, kBlock, 0, c->stream>>>(B.dev, c->pt, B.d_p64.as<double4_32a>(), B.d_p32.as<float4>(),
                                                        B.d_meta.as<int4>(), B.npacked, slot, qoff, s.natoms, cbmc,
-                                                       want_qq, c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
+                                                       want_qq, mcom, mrad, c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
                                                        c->d_result.as<double>(), c->d_query.as<int>());
   CASS_CUDA(cudaGetLastError());
   count_launch(c);
@@ -1673,6 +1725,7 @@ int cass_cbmc_trial_energies(cass_ctx* c, int32_t ibox1, int32_t is, int32_t ski
     if (atoms[a] < 1 || atoms[a] > s.natoms) return set_error(CASS_EINVAL, "trial atom index out of range");
   if (ntrial == 0) return CASS_OK;
   const int ib = ibox1 - 1;
+  if (c->box[ib].comcut) return set_error(CASS_EUNSUPPORTED, "molecule-pair COM cutoff (LJ CHARMM or minimum-image charges) is applied by the system and molecule energies only");
   int rc;
   if ((rc = set_device(c)) || (rc = pack_box(c, ib))) return rc;
   if (cbmc && (rc = ensure_cbmc(c))) return rc;
@@ -1860,12 +1913,15 @@ int cass_system_total_energy(cass_ctx* c, int32_t ibox1, int32_t intra_flag, Cas
     const float pre2 = bounded ? (float)(rmax2 * (1.0 + 1.0e-4) + 1.0e-3) : FLT_MAX;
     if (fast)
       k_pair_total<true><<<grid, kBlock, 0, c->stream>>>(B.dev, c->pt, B.d_p64.as<double4_32a>(), B.d_meta.as<int4>(), n,
-                                                        pre2, c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
-                                                        c->d_result.as<double>(), c->d_query.as<int>());
+                                                        pre2, nullptr, 0.0, c->d_partial.as<double>(),
+                                                        c->d_counter.as<unsigned>(), c->d_result.as<double>(),
+                                                        c->d_query.as<int>());
     else
       k_pair_total<false><<<grid, kBlock, 0, c->stream>>>(B.dev, c->pt, B.d_p64.as<double4_32a>(), B.d_meta.as<int4>(), n,
-                                                         pre2, c->d_partial.as<double>(), c->d_counter.as<unsigned>(),
-                                                         c->d_result.as<double>(), c->d_query.as<int>());
+                                                         pre2, B.comcut ? B.d_com.as<double4_32a>() : nullptr,
+                                                         B.rcut_max, c->d_partial.as<double>(),
+                                                         c->d_counter.as<unsigned>(), c->d_result.as<double>(),
+                                                         c->d_query.as<int>());
     CASS_CUDA(cudaGetLastError());
   count_launch(c);
     if ((rc = sync_result(c, 2))) return rc;

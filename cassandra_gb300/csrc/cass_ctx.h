@@ -151,6 +151,12 @@ struct BoxH {
   std::vector<int2> krow;
   DevBuf d_krow;
   bool cell_dirty = true;
+  // Check_MoleculePair_Cutoff decides which molecule pairs interact when a
+  // style has no atom cutoff (LJ CHARMM, minimum-image charges) and the vdW sum
+  // is not minimum image: then each packed atom carries its molecule's COM and
+  // max_dcom (x, y, z, max_dcom), rebuilt with the packed arrays
+  bool comcut = false;
+  DevBuf d_com;
   // the state cass_volume_scale keeps for cass_volume_restore
   bool vol_saved = false;
   CassBoxDesc vol_desc{};

@@ -148,6 +148,10 @@ extern "C" int cass_mol_box_energy_noalloc(const CassBoxDesc* box, int32_t ntype
     return set_error(CASS_EUNSUPPORTED, "cass_mol_box_energy_noalloc: vdw style must be LJ or NONE");
   for (int k = 0; k < 3; ++k)
     if (!(box->length[k] > 0.0)) return set_error(CASS_EINVAL, "cass_mol_box_energy_noalloc: box length");
+  if (box->vdw_sum_style != CASS_VDW_SUM_MINIMUM &&
+      ((box->vdw_style == CASS_VDW_LJ && box->vdw_sum_style == CASS_VDW_SUM_CHARMM) ||
+       (box->charge_style == CASS_CHARGE_COUL && box->charge_sum_style == CASS_QQ_MINIMUM)))
+    return set_error(CASS_EUNSUPPORTED, "cass_mol_box_energy_noalloc: styles with a molecule-pair COM cutoff");
   int dev = 0;
   CASS_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kNoAllocMaxDevices) return set_error(CASS_EINVAL, "cass_mol_box_energy_noalloc: device");

@@ -2193,6 +2193,7 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
       if (iboxes[j] == iboxes[k]) return set_error(CASS_EINVAL, "box listed twice");
     const BoxH& B = c->box[ib];
     if (!B.energy_valid) return set_error(CASS_ESTATE, "system energy of box not computed");
+    if (B.comcut) return set_error(CASS_EUNSUPPORTED, "molecule-pair COM cutoff (LJ CHARMM or minimum-image charges) is applied by the system and molecule energies only");
     if (B.desc.charge_style != CASS_CHARGE_NONE) return set_error(CASS_EUNSUPPORTED, "gcmc boxes hold no charges");
     if (B.desc.vdw_style != CASS_VDW_LJ) return set_error(CASS_EUNSUPPORTED, "gcmc needs LJ boxes");
     mixed = mixed && (B.desc.vdw_sum_style == CASS_VDW_SUM_CUT || B.desc.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL);

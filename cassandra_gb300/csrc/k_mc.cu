@@ -599,6 +599,7 @@ extern "C" int cass_mc_sweeps(cass_ctx* c, int32_t nboxes, const int32_t* iboxes
     for (int j = 0; j < k; ++j)
       if (iboxes[j] == iboxes[k]) return set_error(CASS_EINVAL, "box listed twice");
     if (!c->box[ib].energy_valid) return set_error(CASS_ESTATE, "system energy of box not computed");
+    if (c->box[ib].comcut) return set_error(CASS_EUNSUPPORTED, "molecule-pair COM cutoff (LJ CHARMM or minimum-image charges) is applied by the system and molecule energies only");
   }
   int rc;
   CASS_CUDA(cudaSetDevice(c->device));

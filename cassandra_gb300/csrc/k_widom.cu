@@ -1654,6 +1654,7 @@ extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const
     if (ib < 0 || ib >= c->nboxes) return set_error(CASS_EINVAL, "box index out of range");
     if (!c->box[ib].energy_valid && !c->box[ib].frame_ready)
       return set_error(CASS_ESTATE, "system energy of box not computed");
+    if (c->box[ib].comcut) return set_error(CASS_EUNSUPPORTED, "molecule-pair COM cutoff (LJ CHARMM or minimum-image charges) is applied by the system and molecule energies only");
   }
   int rc;
   CASS_CUDA(cudaSetDevice(c->device));

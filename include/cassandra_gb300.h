@@ -410,7 +410,8 @@ int cass_system_gradient(cass_ctx* ctx, int32_t ibox, CassEnergy* energy, double
  *   query_xyzq [nq][4], query_type [nq]; eps/sig: host [ntypes*ntypes] tables.
  *   out: device [3] = E_vdw, E_qq, overlap (1.0/0.0; energies 0 on overlap).
  * Limits: n <= 262144, 1 <= nq <= 64, LJ or no vdW.  Larger sizes return
- * CASS_ECAPACITY.  Runs on the current device, asynchronously on `stream`.
+ * CASS_ECAPACITY; LJ CHARMM or minimum-image charges with a vdW sum other than
+ * minimum image (where Check_MoleculePair_Cutoff decides) CASS_EUNSUPPORTED.  Runs on the current device, asynchronously on `stream`.
  * All calls on a device share the scratch: calls that overlap on the GPU race.
  * The first call on a device resolves the scratch address; make it before any
  * stream capture. */

@@ -4,7 +4,11 @@ against the oracle: LJ with cut, cut_tail, cut_shift, cut_switch, CHARMM,
 minimum image and cut_shift_force; Mie with cut, cut_shift and cut_tail; charges
 with the plain cut, minimum image, damped shifted force and Ewald.  Per style:
 the system energy (every component), molecule energies with and without the
-CBMC cutoffs, and Widom insertions record by record."""
+CBMC cutoffs, and Widom insertions record by record.  Where a style has no atom
+cutoff (LJ CHARMM, minimum-image charges) and the vdW sum is not minimum image,
+Check_MoleculePair_Cutoff (:3027-3088) selects the interacting molecules by their
+COM distance; the system and molecule energies apply it, the other paths refuse
+such boxes."""
 import numpy as np
 import pytest
 
@@ -59,6 +63,11 @@ CASES += [("water_" + n, lambda v=v: _water(v)) for n, v in (
     ("qq_cut", abi.QQ_CUT), ("qq_minimum", abi.QQ_MINIMUM), ("qq_dsf", abi.QQ_DSF), ("qq_ewald", abi.QQ_EWALD))]
 
 
+# styles without an atom cutoff whose vdW sum is not minimum image: the molecule
+# pairs are selected by their COM distance (energy_routines.f90:3027-3088)
+COMCUT = {"lj_charmm", "water_qq_minimum"}
+
+
 @pytest.mark.parametrize("name,make", CASES, ids=[c[0] for c in CASES])
 def test_style_matches_oracle(name, make):
     s = make()
@@ -76,6 +85,12 @@ def test_style_matches_oracle(name, make):
                 assert a[2] == b[2]
                 assert _close(b[0], a[0]) and _close(b[1], a[1]), (name, im, cbmc, a, b)
         n = 64
+        if name in COMCUT:  # Check_MoleculePair_Cutoff decides: refused where it is not applied
+            for call in (lambda: g.widom_insert(1, [1], n, 8, 0, seed=3),
+                         lambda: g.mc_sweeps([1], 1, [[0.1]], [[0.1]], seed=1)):
+                with pytest.raises(abi.CassError, match="COM cutoff"):
+                    call()
+            return
         ro, to = o.widom_insert(1, [1], n, 8, 0, seed=3, trace=True)
         rg, tg = g.widom_insert(1, [1], n, 8, 0, seed=3, trace=True)
     assert np.array_equal(to["overlap"], tg["overlap"])
