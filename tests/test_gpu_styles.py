@@ -101,3 +101,36 @@ def test_style_matches_oracle(name, make):
     assert np.allclose(tg["widom_var"][ok], to["widom_var"][ok], rtol=1e-8, atol=0)
     if not water:
         assert ro[0]["n_insertions"] == rg[0]["n_insertions"] == n
+
+
+@pytest.mark.parametrize("name,make", [c for c in CASES if c[0] not in COMCUT], ids=[c[0] for c in CASES if c[0] not in COMCUT])
+def test_style_mc_sweeps_match_oracle(name, make):
+    """NVT sweeps (translation, and rotation for water) in every style: the FP64 chain
+    equals the oracle's move by move (acceptances, adapted steps, energies)."""
+    s = make()
+    water = name.startswith("water")
+    pt = 0.5 if water else 1.0
+    with oracle.open_system(s) as o, cg.open_system(s, precision=abi.PREC_FP64) as g:
+        o.system_total_energy(1)
+        g.system_total_energy(1)
+        ro, mdo, mro = o.mc_sweeps([1], 2, [[0.5]], [[0.3]], seed=9, prob_translate=pt, nupdate=50)
+        rg, mdg, mrg = g.mc_sweeps([1], 2, [[0.5]], [[0.3]], seed=9, prob_translate=pt, nupdate=50)
+        for k in ("n_translate", "n_translate_accepted", "n_rotate", "n_rotate_accepted"):
+            assert ro[0][k] == rg[0][k], (name, k)
+        assert np.allclose(mdg, mdo, rtol=1e-12) and np.allclose(mrg, mro, rtol=1e-12)
+        for k in ro[0]["energy"]:
+            assert _close(rg[0]["energy"][k], ro[0]["energy"][k], 1e-9, 1e-6), (name, k)
+
+
+@pytest.mark.parametrize("name,make", CASES, ids=[c[0] for c in CASES])
+def test_style_mixed_system_energy(name, make):
+    """The mixed context's system energy in every style: FP32 pair terms where the
+    style has an FP32 kernel (LJ cut / cut_tail, Ewald), FP64 elsewhere; within 1e-5
+    of the sum of the magnitudes of the components."""
+    s = make()
+    with oracle.open_system(s) as o, cg.open_system(s, precision=abi.PREC_MIXED) as g:
+        eo, _ = o.system_total_energy(1)
+        eg, _ = g.system_total_energy(1)
+    scale = abs(eo["inter_vdw"]) + abs(eo["inter_q"]) + abs(eo["intra"]) + abs(eo["reciprocal"])
+    for k in ("total", "inter_vdw", "inter_q", "reciprocal", "lrc", "self"):
+        assert abs(eg[k] - eo[k]) <= 1e-5 * scale, (name, k, eg[k], eo[k])
