@@ -32,8 +32,18 @@ def _run(open_ctx, s, nsteps, seed, mu=(-22.0, -26.0)):
     return r, again, (where, xyz)
 
 
-def test_fp64_gcmc_matches_oracle():
-    s = workloads.gcmc_system(nboxes=2, length=25.0, max_per_box=300)
+STYLES = {"cut_tail": abi.VDW_SUM_CUT_TAIL, "cut": abi.VDW_SUM_CUT, "cut_shift": abi.VDW_SUM_CUT_SHIFT,
+          "cut_switch": abi.VDW_SUM_CUT_SWITCH, "cut_shift_force": abi.VDW_SUM_CUT_SHIFT_FORCE,
+          "minimum": abi.VDW_SUM_MINIMUM}
+
+
+@pytest.mark.parametrize("style", list(STYLES))
+def test_fp64_gcmc_matches_oracle(style):
+    s = workloads.gcmc_system(nboxes=2, length=25.0, max_per_box=300, rcut=12.0)
+    for bx in s.boxes:
+        bx.vdw_sum_style = STYLES[style]
+        if style == "cut_switch":
+            bx.ron_switch, bx.roff_switch = 10.0, 12.0
     ro, eo, so = _run(oracle.open_system, s, 600, seed=4)
     rg, eg, sg = _run(lambda x: cg.open_system(x, precision=abi.PREC_FP64), s, 600, seed=4)
     assert np.array_equal(so[0], sg[0])  # the same molecule slots live in the same boxes
