@@ -2060,13 +2060,21 @@ namespace cassgpu {
 // structure factors and reciprocal energy (Compute_System_Ewald_Reciprocal_Energy).
 // Enough for Widom insertions; the other energy components are left to
 // cass_system_total_energy.
-int frame_setup_ext(cass_ctx* c, int ibox) {
-  BoxH& B = c->box[ibox];
-  int rc;
-  if ((rc = pack_box(c, ibox))) return rc;
-  if (B.desc.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) B.energy.lrc = lr_correction(c, B, count_beads(c, ibox));
-  if (box_has_ewald(B) && B.nvecs > 0 && (rc = box_reciprocal(c, ibox, &B.energy.reciprocal))) return rc;
-  B.frame_ready = true;
+// Every box of the context; the molecule rows are sized for the largest k-vector
+// count first, so that no box's rebuild reallocates (and so invalidates) the
+// rows of a box set up before it.
+int frame_setup_ext(cass_ctx* c) {
+  int rc, nv = 0;
+  for (BoxH& B : c->box)
+    if (box_has_ewald(B)) nv = std::max(nv, B.nvecs);
+  if (nv > 0 && (rc = ensure_cos_mol(c, nv))) return rc;
+  for (int ibox = 0; ibox < c->nboxes; ++ibox) {
+    BoxH& B = c->box[ibox];
+    if ((rc = pack_box(c, ibox))) return rc;
+    if (B.desc.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) B.energy.lrc = lr_correction(c, B, count_beads(c, ibox));
+    if (box_has_ewald(B) && B.nvecs > 0 && (rc = box_reciprocal(c, ibox, &B.energy.reciprocal))) return rc;
+    B.frame_ready = true;
+  }
   return CASS_OK;
 }
 }  // namespace cassgpu

@@ -27,7 +27,7 @@
 namespace cassgpu {
 void invalidate_ext(cass_ctx* c, int ibox);
 void set_mol_box_ext(cass_ctx* c, int slot, int ibox);
-int frame_setup_ext(cass_ctx* c, int ibox);
+int frame_setup_ext(cass_ctx* c);
 }  // namespace cassgpu
 
 using namespace cassgpu;
@@ -398,8 +398,8 @@ int cass_load_next_frame(cass_ctx* c, int32_t nboxes, cass_traj* const* traj, in
   for (int b = 0; b < nboxes; ++b) {
     invalidate_ext(c, b);
     c->box[b].vol_saved = false;
-    if ((rc = frame_setup_ext(c, b))) return rc;
   }
+  if ((rc = frame_setup_ext(c))) return rc;
   return CASS_OK;
 }
 

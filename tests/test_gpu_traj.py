@@ -202,3 +202,47 @@ def test_widom_after_frame_load_needs_no_total_energy(tmp_path, name, prec):
             assert np.array_equal(ta["selected_trial"], tb["selected_trial"])
             assert np.array_equal(ta["widom_var"], tb["widom_var"])
             assert a[0]["widom_sum"] == b[0]["widom_sum"]
+
+
+def test_two_ewald_boxes_growing_kvectors(tmp_path):
+    """Two Ewald boxes loaded together, the second growing by 30 % in its second
+    frame (more k-vectors, so the molecule rows are resized): both boxes are ready
+    for Widom after each load and match the oracle's energies."""
+    import copy
+    from cassandra_gb300 import workloads
+    d = helpers.golden("pregen_water_spce.npz")
+    base = helpers.pregen_system("water_spce", 0)
+    base.species[0].libraries = [workloads.water_species().libraries[0] * 1.0]
+    nmol = len(d["frames"][0]) // 3
+    frames = {1: [d["frames"][0], d["frames"][1]], 2: [d["frames"][2], d["frames"][3] * 1.3]}
+    boxes = {1: [d["boxes"][0], d["boxes"][1]], 2: [d["boxes"][2], d["boxes"][3] * 1.3]}
+    trajs_paths = {}
+    for b in (1, 2):
+        xp, hp = os.path.join(tmp_path, f"b{b}.xyz"), os.path.join(tmp_path, f"b{b}.H")
+        with open(xp, "w") as fx, open(hp, "w") as fh:
+            for k in range(2):
+                io.write_xyz_frame(fx, frames[b][k], ["O", "H", "H"] * nmol, k)
+                io.write_H_frame(fh, boxes[b][k], [nmol])
+        trajs_paths[b] = (xp, hp)
+    s = copy.deepcopy(base)
+    s.boxes = [copy.deepcopy(base.boxes[0]), copy.deepcopy(base.boxes[0])]
+    s.max_molecules = [2 * nmol + 2]
+    with cg.open_system(s, precision=abi.PREC_FP64) as g:
+        t1 = cg.open_trajectory(*trajs_paths[1], [3])
+        t2 = cg.open_trajectory(*trajs_paths[2], [3])
+        for k in range(2):
+            assert not g.load_next_frame([t1, t2])
+            g.widom_insert(1, [1, 2], 50, 4, 0, seed=k)  # both boxes ready after the load
+            for b in (1, 2):
+                eg, _ = g.system_total_energy(b)
+                one = helpers.pregen_system("water_spce", 0)
+                one.boxes[0].length = tuple(boxes[b][k])
+                one.molecules = type(one.molecules)()
+                for m in range(nmol):
+                    one.molecules.add(m + 1, 1, 1, frames[b][k][3 * m:3 * m + 3])
+                with oracle.open_system(one) as o:
+                    eo, _ = o.system_total_energy(1)
+                for key in eo:
+                    assert _close(eg[key], eo[key], 1e-10), (k, b, key, eg[key], eo[key])
+        t1.close()
+        t2.close()
