@@ -681,6 +681,9 @@ def main():
                       "trial_energies_per_step": trials_step, "atoms_total": int(sum(natoms)),
                       "l2": "flushed (256 MB write) between timed steps", "precision": "mixed",
                       "parallelism": f"replicas x{world}"},
+           "widom_launch": {"ctas_per_box": st["widom_grid_x"], "threads": st["widom_block"],
+                            "smem_bytes": st["widom_smem_bytes"],
+                            "note": "shape chosen by the library's launch autotuner on its first call"},
            "gpu_launches": int(launches),
            "wall_s": t_wall,
            "fp64_gpu": fp64,

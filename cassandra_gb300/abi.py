@@ -187,9 +187,10 @@ SIGNATURES = {
     "get_stats": (C.c_int, [C.c_void_p, C.POINTER(CassStats)]),
     "set_count_pairs": (C.c_int, [C.c_void_p, C.c_int32]),
     "set_widom_cells": (C.c_int, [C.c_void_p, C.c_double]),
+    "set_widom_autotune": (C.c_int, [C.c_void_p, C.c_int32]),
     "set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
-OPTIONAL = {"get_stats", "set_count_pairs", "set_widom_cells", "set_stream", "mol_box_energy_noalloc", "system_gradient", "gcmc",
+OPTIONAL = {"get_stats", "set_count_pairs", "set_widom_cells", "set_widom_autotune", "set_stream", "mol_box_energy_noalloc", "system_gradient", "gcmc",
             "traj_open", "traj_next", "traj_stats", "traj_close", "load_next_frame"}
 
 
@@ -377,6 +378,10 @@ class Context:
         st = CassStats()
         self._check("get_stats", self._f["get_stats"](self._h, C.byref(st)))
         return st.as_dict()
+
+    def set_widom_autotune(self, on: bool) -> None:
+        """Launch-shape autotuning of cass_widom_insert (on by default)."""
+        self._check("set_widom_autotune", self._f["set_widom_autotune"](self._h, int(on)))
 
     def set_widom_cells(self, cells_per_cutoff: float) -> None:
         """Widom cell edge = rcut_cbmc / cells_per_cutoff (0: the precision's default)."""

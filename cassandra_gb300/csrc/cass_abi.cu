@@ -1184,6 +1184,12 @@ int cass_set_count_pairs(cass_ctx* c, int32_t on) {
   return CASS_OK;
 }
 
+int cass_set_widom_autotune(cass_ctx* c, int32_t on) {
+  if (!c) return set_error(CASS_EINVAL, "NULL context");
+  c->widom_autotune = on != 0;
+  return CASS_OK;
+}
+
 int cass_set_widom_cells(cass_ctx* c, double cells_per_cutoff) {
   if (!c || !(cells_per_cutoff >= 0.0 && cells_per_cutoff <= 8.0))
     return set_error(CASS_EINVAL, "cells_per_cutoff must be in [0, 8]");

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "cass_molecule.cuh"
@@ -177,6 +178,10 @@ struct cass_ctx_impl {
   CassStats stats{};
   int count_pairs = 0;
   double widom_cells = 0.0;  // cells per rcut_cbmc in the Widom cell lists (0: default)
+  int widom_waves = 0;       // CTAs per resident slot of the FP32 Widom launch (0: default)
+  // launch shapes the Widom autotuner chose, per batch signature: (cells per cutoff, waves)
+  bool widom_autotune = true;
+  std::vector<std::pair<std::vector<long long>, std::pair<double, int>>> widom_tuned;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   int nspecies = 0, ntypes = 0, nboxes = 0, max_kvec = 100000;
   std::vector<int> max_mol, mol_base;

@@ -1632,7 +1632,7 @@ int pack_box_ext(cass_ctx* c, int ibox);
 const std::vector<int>& members_ext(cass_ctx* c, int ibox);
 }  // namespace cassgpu
 
-extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const int32_t* iboxes, int64_t n_ins,
+static int widom_insert_impl(cass_ctx* c, int32_t is1, int32_t nboxes, const int32_t* iboxes, int64_t n_ins,
                                  int32_t kappa_ins, int32_t kappa_dih, uint64_t seed, CassWidomResult* out,
                                  CassWidomTrace* trace) {
   if (!c || is1 < 1 || is1 > c->nspecies || nboxes < 1 || !iboxes || !out || n_ins < 0)
@@ -1847,7 +1847,8 @@ extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const
     int per_sm = 1;
     CASS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kF32Threads, use_smem ? max_smem : 0));
     per_sm = std::max(per_sm, 1);
-    long long want = ((long long)dev_sms * per_sm * kF32Waves + nboxes - 1) / nboxes;
+    const int waves = c->widom_waves > 0 ? c->widom_waves : kF32Waves;
+    long long want = ((long long)dev_sms * per_sm * waves + nboxes - 1) / nboxes;
     long long need = (n_ins + kF32Threads - 1) / kF32Threads;
     int chunks = (int)std::max<long long>(1, std::min(want, need));
     dim3 g(chunks, nboxes);
@@ -1923,4 +1924,70 @@ extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const
     out[k].n_trials = n_ins * (int64_t)(kappa_ins + (s.nfrag - 1) * (s.nfrag > 1 ? kappa_dih : 0));
   }
   return CASS_OK;
+}
+
+// The launch-shape autotuner: the first call with a new batch signature
+// (species, boxes, precision, CBMC options, order of magnitude of the insertion
+// count) times the Widom kernel with each candidate cell edge on a sample of the
+// insertions with its own seed (the faster of two runs after a first that sizes
+// the buffers), keeps the fastest
+// for the context, and then runs the call.  A shape changes neither the
+// insertions' random streams nor the per-box sums (fixed order over
+// insertions); the cell edge changes only the order of each query's pair sum.
+extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const int32_t* iboxes, int64_t n_ins,
+                                 int32_t kappa_ins, int32_t kappa_dih, uint64_t seed, CassWidomResult* out,
+                                 CassWidomTrace* trace) {
+  if (!c || !iboxes || nboxes < 1 || !out || n_ins < 64 || !c->widom_autotune || c->widom_cells > 0.0 ||
+      c->widom_waves > 0)
+    return widom_insert_impl(c, is1, nboxes, iboxes, n_ins, kappa_ins, kappa_dih, seed, out, trace);
+  std::vector<long long> key = {is1, c->precision, kappa_ins, kappa_dih, c->cbmc_opt.energy_table_res,
+                                c->cbmc_opt.sector_overlap, (long long)std::log2((double)n_ins)};
+  for (int k = 0; k < nboxes; ++k) key.push_back(iboxes[k]);
+  for (const auto& e : c->widom_tuned)
+    if (e.first == key) {
+      c->widom_cells = e.second.first;
+      c->widom_waves = e.second.second;
+      const int rc = widom_insert_impl(c, is1, nboxes, iboxes, n_ins, kappa_ins, kappa_dih, seed, out, trace);
+      c->widom_cells = 0.0;
+      c->widom_waves = 0;
+      return rc;
+    }
+  const bool mixed = c->precision == CASS_PREC_MIXED;
+  const std::vector<double> cells = mixed ? std::vector<double>{1.0, 1.25} : std::vector<double>{3.0, 4.0};
+  const std::vector<int> waves = {kF32Waves};
+  // the CTAs per box follow the insertion count, so the mixed kernel is timed at
+  // the call's own count (up to 32,768 per box); the FP64 kernel on 4,096
+  const int64_t sample = std::min<int64_t>(n_ins, mixed ? 32768 : 4096);
+  std::vector<CassWidomResult> tmp(nboxes);
+  double best_c = 0.0;
+  int best_w = 0;
+  float best_ms = 0.0f;
+  for (double cc : cells)
+    for (int w : waves) {
+      c->widom_cells = cc;
+      c->widom_waves = w;
+      float ms = 0.0f;
+      for (int rep = 0; rep < 3; ++rep) {  // the first run of a shape also sizes its buffers
+        const int rc = widom_insert_impl(c, is1, nboxes, iboxes, sample, kappa_ins, kappa_dih, seed ^ 0x5bd1e995ULL,
+                                         tmp.data(), nullptr);
+        if (rc) {
+          c->widom_cells = 0.0;
+          c->widom_waves = 0;
+          return rc;
+        }
+        if (rep == 1 || (rep == 2 && c->stats.widom_kernel_ms < ms)) ms = c->stats.widom_kernel_ms;
+      }
+      if (best_w == 0 || ms < best_ms) {
+        best_ms = ms;
+        best_c = cc;
+        best_w = w;
+      }
+    }
+  c->widom_tuned.push_back({key, {best_c, best_w}});
+  c->widom_cells = best_c;
+  c->widom_waves = best_w;
+  const int rc = widom_insert_impl(c, is1, nboxes, iboxes, n_ins, kappa_ins, kappa_dih, seed, out, trace);
+  c->widom_cells = 0.0;
+  c->widom_waves = 0;
+  return rc;
 }

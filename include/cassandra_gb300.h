@@ -496,6 +496,12 @@ int cass_set_count_pairs(cass_ctx* ctx, int32_t count_pairs);
  * edge is rcut_cbmc / cells_per_cutoff (0 restores the default of the
  * context's precision).  Results do not depend on it beyond summation order. */
 int cass_set_widom_cells(cass_ctx* ctx, double cells_per_cutoff);
+/* on != 0 (the default): the first cass_widom_insert of each batch signature
+ * times a few launch shapes (cell edge, CTAs per resident slot) on a sample of
+ * insertions and the context keeps the fastest; a cell edge set with
+ * cass_set_widom_cells disables it.  Results do not depend on the shape beyond
+ * summation order. */
+int cass_set_widom_autotune(cass_ctx* ctx, int32_t on);
 /* Runs the context's work on a caller-owned cudaStream_t (NULL: its own). */
 int cass_set_stream(cass_ctx* ctx, void* stream);
 
