@@ -575,7 +575,7 @@ def main():
         for s in range(warmup):
             ctx.widom_insert(2, boxes, n_per_box, args.kappa, args.kappa, seed=seed0 + 1000 + s)
         st0 = ctx.stats()
-        per_step, kern = [], []
+        per_step, kern, allres = [], [], []
         barrier()
         torch.cuda.synchronize()
         for s in range(steps):
@@ -589,9 +589,20 @@ def main():
             torch.cuda.synchronize()
             per_step.append(e0.elapsed_time(e1))
             kern.append(ctx.stats()["widom_kernel_ms"])
+            allres.append(res)
         barrier()
         st1 = ctx.stats()
+        timed_steps.results = allres
         return per_step, kern, res, st1["kernel_launches"] - st0["kernel_launches"]
+
+    def mu_ex(allres):
+        """Excess chemical potential per box, -kT ln <widom_var>, in kJ/mol: the mean
+        over the timed steps and its standard error from their spread."""
+        kT = 0.8314472 * system.boxes[0].temperature * 0.01
+        per = np.array([[-kT * np.log(max(r["widom_sum"] / r["prefactor"] / r["n_insertions"], 1e-300))
+                         for r in step] for step in allres])  # [steps, boxes]
+        se = per.std(axis=0, ddof=1) / np.sqrt(len(per)) if len(per) > 1 else np.zeros(per.shape[1])
+        return per.mean(axis=0), se
 
     # headline: mixed precision
     gctx = cg.open_system(system, precision=abi.PREC_MIXED, device=dev)
@@ -608,6 +619,9 @@ def main():
         t = torch.tensor([total_ms], device=f"cuda:{dev}")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
+    mu_mixed, mu_mixed_se = mu_ex(timed_steps.results)
+    timed_steps_mixed_results = list(timed_steps.results)
+    mu_cmp = None
     trials_step = n_per_box * len(boxes) * trials_per_ins
     value = trials_step * args.steps * world / (total_ms / 1000.0)
     # work counts for the roofline (one extra, untimed pass)
@@ -624,9 +638,17 @@ def main():
         for b in boxes:
             fctx.system_total_energy(b)
         fms, fkms, _, _ = timed_steps(fctx, args.fp64_steps, 1, args.seed)
+        mu_fp64, _ = mu_ex(timed_steps.results)
+        nst = min(len(timed_steps.results), args.steps)
+        mu_mixed_same, _ = mu_ex(timed_steps_mixed_results[:nst])
         fp64_value = trials_step * len(fms) / (float(np.sum(fms)) / 1000.0)
         fp64 = {"value": fp64_value, "unit": UNIT, "ms_per_step": float(np.mean(fms)),
                 "kernel_ms": float(np.mean(fkms)), "mixed_over_fp64": value / world / fp64_value}
+        mu_cmp = {"max_abs_diff_kjmol": float(np.max(np.abs(mu_mixed_same - mu_fp64))),
+                  "mean_abs_diff_kjmol": float(np.mean(np.abs(mu_mixed_same - mu_fp64))),
+                  "steps_compared": nst,
+                  "note": "mixed and FP64 over the same timed steps (the same seeds, so the same insertion "
+                          "streams): the difference is the precision's, not sampling noise"}
         sub = boxes[:8]
         ra, ta = fctx.widom_insert(2, sub, 2000, args.kappa, args.kappa, seed=4242, trace=True)
         rb, tb = gctx.widom_insert(2, sub, 2000, args.kappa, args.kappa, seed=4242, trace=True)
@@ -686,6 +708,11 @@ def main():
                             "note": "shape chosen by the library's launch autotuner on its first call"},
            "gpu_launches": int(launches),
            "wall_s": t_wall,
+           "mu_ex_per_box": {"unit": "kJ/mol", "definition": "-kT ln <widom_var> (widom_insert.f90:445-447), "
+                                                         "T = 150 K", "mixed": [round(float(v), 5) for v in mu_mixed],
+                             "mixed_se": [round(float(v), 5) for v in mu_mixed_se],
+                             "n_atoms_per_box": [int(sum(1 for bi in system.molecules.ibox if bi == b)) for b in boxes],
+                             "mixed_vs_fp64": mu_cmp},
            "fp64_gpu": fp64,
            "accuracy_vs_fp64": accuracy,
            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
