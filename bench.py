@@ -390,7 +390,7 @@ def npt_leg(cg, abi, dev, nchains: int, eq_blocks: int, prod_blocks: int) -> dic
                               "formula": "-beta (<rho dU/deps> - <rho><dU/deps>)"},
             "adjoint_check_max_rel_diff": float(max(check)),
             "note": "configurations after short equilibration from the lattice start; the full 2000-configuration "
-                    "run is --npt-chains 64 --npt-blocks 32"}
+                    "run is --npt-chains 64 --npt-eq-blocks 300 --npt-blocks 32 (about 4.5 min)"}
 
 
 def pregen_leg(cg, abi, system, n_per_box: int, kappa: int, nframes: int, seed: int) -> dict:
