@@ -18,9 +18,10 @@
 //      move_rotate.f90:307-326)
 //   E  on acceptance: coordinates, COM and structure factors are committed.
 // FP64 kernel: the reference arithmetic.  Mixed kernel: FP32 positions for the
-// pair loop and FP32 phases for the structure factors; the master
-// coordinates, the running structure factors, the energy bookkeeping and the
-// acceptance exponent stay FP64.
+// pair loop, FP32 phases for the structure factors and the FP32 change of the
+// reciprocal energy, Cn [dc (2 S_c + dc) + ds (2 S_s + ds)] summed per thread
+// with compensation; the master coordinates, the running structure factors, the
+// energy bookkeeping and the acceptance exponent stay FP64.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -432,6 +433,7 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
       const double* cm = A.cos_mol + (size_t)mv.slot * A.stride;
       const double* smv = A.sin_mol + (size_t)mv.slot * A.stride;
       double part = 0.0;
+      KahanF partf;
       for (int k = threadIdx.x; k < G.nvecs; k += blockDim.x) {
         const double4_32a h = G.kvec[k];
         double cn = 0.0, sn = 0.0;
@@ -453,17 +455,26 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
             sn = sn + mv.q[a] * sin(hdotr);
           }
         }
-        const double c = G.cos_sum[k] + (cn - cm[k]);
-        const double s = G.sin_sum[k] + (sn - smv[k]);
-        part += h.w * (c * c + s * s);
+        if (MIXED) {
+          // the change of Cn (S_c^2 + S_s^2) in FP32: dc (2 S_c + dc) + ds (2 S_s + ds)
+          const float dc = (float)cn - (float)cm[k], ds = (float)sn - (float)smv[k];
+          const float sc = (float)G.cos_sum[k], ss = (float)G.sin_sum[k];
+          partf.add((float)h.w * (dc * (2.0f * sc + dc) + ds * (2.0f * ss + ds)));
+        } else {
+          const double c = G.cos_sum[k] + (cn - cm[k]);
+          const double s = G.sin_sum[k] + (sn - smv[k]);
+          part += h.w * (c * c + s * s);
+        }
         G.new_cos[k] = cn;
         G.new_sin[k] = sn;
       }
+      if (MIXED) part = partf.value();
       block_sum_mc(part, red, 4);
       __syncthreads();
       if (threadIdx.x == 0) {
         for (int w = 0; w < NW; ++w) e_recip += red[w * 8 + 4];
-        e_recip *= kCHARGE_FACTOR;
+        // mixed: the previous reciprocal energy plus the FP32 change (FP64 sum)
+        e_recip = MIXED ? E.reciprocal + e_recip * kCHARGE_FACTOR : e_recip * kCHARGE_FACTOR;
       }
     }
     // ---- D: acceptance
