@@ -744,11 +744,20 @@ void set_mol_box(cass_ctx* c, int slot, int ibox) {
   c->mol_box[slot] = ibox;
 }
 
-// Packs the live molecules of a box (species-major, locate order) into the
-// context's pinned staging buffer and uploads it.
-int pack_box(cass_ctx* c, int ibox) {
+// Bytes of pinned staging that packing box ibox needs.
+size_t pack_bytes(cass_ctx* c, int ibox) {
+  const std::vector<int>& mem = members(c, ibox);
+  size_t na = 0;
+  for (int slot : mem) na += (size_t)c->sp[c->slot_sp[slot]].natoms;
+  const size_t n = std::max<size_t>(1, na), m = std::max<size_t>(1, mem.size());
+  return (n * (sizeof(double4_32a) + sizeof(float4) + sizeof(int4)) + m * sizeof(int4) + 255) & ~(size_t)255;
+}
+
+// Packs the live molecules of a box (species-major, locate order) into pinned
+// staging at `stage` (pack_bytes long) and queues the uploads; the caller
+// synchronizes before the staging is reused.
+int pack_box_async(cass_ctx* c, int ibox, unsigned char* stage) {
   BoxH& B = c->box[ibox];
-  if (!B.pack_dirty) return CASS_OK;
   const std::vector<int>& mem = members(c, ibox);
   size_t na = 0;
   for (int slot : mem) na += (size_t)c->sp[c->slot_sp[slot]].natoms;
@@ -758,9 +767,8 @@ int pack_box(cass_ctx* c, int ibox) {
   if (!rc) rc = B.d_p32.reserve(n * sizeof(float4));
   if (!rc) rc = B.d_meta.reserve(n * sizeof(int4));
   if (!rc) rc = B.d_molinfo.reserve(m * sizeof(int4));
-  if (!rc) rc = c->h_pack.reserve(n * (sizeof(double4_32a) + sizeof(float4) + sizeof(int4)) + m * sizeof(int4));
   if (rc) return rc;
-  double4_32a* p64 = c->h_pack.as<double4_32a>();
+  double4_32a* p64 = reinterpret_cast<double4_32a*>(stage);
   float4* p32 = reinterpret_cast<float4*>(p64 + na);
   int4* meta = reinterpret_cast<int4*>(p32 + na);
   int4* molinfo = meta + na;
@@ -822,9 +830,18 @@ int pack_box(cass_ctx* c, int ibox) {
     CASS_CUDA(h2d(c, B.d_meta.p, meta, na * sizeof(int4)));
     CASS_CUDA(h2d(c, B.d_molinfo.p, molinfo, nm * sizeof(int4)));
   }
+  B.pack_dirty = false;
+  return CASS_OK;
+}
+
+// Packs one box through the context's pinned staging buffer.
+int pack_box(cass_ctx* c, int ibox) {
+  if (!c->box[ibox].pack_dirty) return CASS_OK;
+  int rc = c->h_pack.reserve(pack_bytes(c, ibox));
+  if (!rc) rc = pack_box_async(c, ibox, static_cast<unsigned char*>(c->h_pack.p));
+  if (rc) return rc;
   // the staging buffer is refilled by the next pack: wait for the copies
   CASS_CUDA(cudaStreamSynchronize(c->stream));
-  B.pack_dirty = false;
   return CASS_OK;
 }
 
@@ -2074,9 +2091,18 @@ int frame_setup_ext(cass_ctx* c) {
   for (BoxH& B : c->box)
     if (box_has_ewald(B)) nv = std::max(nv, B.nvecs);
   if (nv > 0 && (rc = ensure_cos_mol(c, nv))) return rc;
+  // every dirty box packed into one pinned staging area, one synchronization
+  std::vector<size_t> off(c->nboxes + 1, 0);
+  for (int ibox = 0; ibox < c->nboxes; ++ibox)
+    off[ibox + 1] = off[ibox] + (c->box[ibox].pack_dirty ? pack_bytes(c, ibox) : 0);
+  if ((rc = c->h_pack.reserve(std::max<size_t>(off[c->nboxes], 256)))) return rc;
+  for (int ibox = 0; ibox < c->nboxes; ++ibox)
+    if (c->box[ibox].pack_dirty &&
+        (rc = pack_box_async(c, ibox, static_cast<unsigned char*>(c->h_pack.p) + off[ibox])))
+      return rc;
+  CASS_CUDA(cudaStreamSynchronize(c->stream));
   for (int ibox = 0; ibox < c->nboxes; ++ibox) {
     BoxH& B = c->box[ibox];
-    if ((rc = pack_box(c, ibox))) return rc;
     if (B.desc.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) B.energy.lrc = lr_correction(c, B, count_beads(c, ibox));
     if (box_has_ewald(B) && B.nvecs > 0 && (rc = box_reciprocal(c, ibox, &B.energy.reciprocal))) return rc;
     B.frame_ready = true;
