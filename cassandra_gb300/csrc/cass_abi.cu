@@ -164,9 +164,7 @@ __global__ void __launch_bounds__(kBlock) k_mol_inter(BoxDev b, PairTable t, con
       }
       int m = cutoff_mask(b, r2, cbmc != 0);
       if (!want_qq) m &= 1;
-      if (MIXED && b.vdw_style == CASS_VDW_LJ &&
-          (b.vdw_sum_style == CASS_VDW_SUM_CUT || b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL ||
-           b.vdw_sum_style == CASS_VDW_SUM_MINIMUM || cbmc)) {
+      if (MIXED && lj_plain_style(b)) {
         if ((m & 1) && qt[a] >= 0 && mj.y >= 0) {
           int k = pidx(qt[a], mj.y, t.ntypes);
           fv.add(lj_pair_f(t.epsf[k], t.sig2f[k], (float)r2));
@@ -234,7 +232,7 @@ __global__ void __launch_bounds__(kBlock) k_trial_energy(BoxDev b, PairTable t, 
       }
       int m = cutoff_mask(b, r2, cbmc != 0);
       if (!want_qq) m &= 1;
-      if (MIXED && b.vdw_style == CASS_VDW_LJ) {
+      if (MIXED && lj_plain_style(b)) {
         if ((m & 1) && qt[a] >= 0 && mj.y >= 0) {
           const int k = pidx(qt[a], mj.y, t.ntypes);
           fv.add(lj_pair_f(t.epsf[k], t.sig2f[k], (float)r2));

@@ -306,8 +306,18 @@ __device__ __forceinline__ double rmin2_pair(const BoxDev& b, int nt, int ti, in
   return (ti >= 0 && tj >= 0) ? b.rminsq[ti * nt + tj] : b.rcut_lowsq;
 }
 
-// FP32 LJ (cut / cut_tail / minimum_image) used by the mixed path; other vdw
-// styles fall back to the FP64 function.
+// True where the mixed kernels may take the FP32 form lj_pair_f: LJ with the
+// cut, cut_tail or minimum-image sum, whose pair energy is the plain
+// 4 eps (s^12 - s^6).  The shift, switch, shifted-force and CHARMM forms
+// (energy_routines.f90:1927-1970) apply whatever the CBMC flag is, so those
+// styles keep the FP64 vdw_pair in every precision.
+__host__ __device__ inline bool lj_plain_style(const BoxDev& b) {
+  return b.vdw_style == CASS_VDW_LJ &&
+         (b.vdw_sum_style == CASS_VDW_SUM_CUT || b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL ||
+          b.vdw_sum_style == CASS_VDW_SUM_MINIMUM);
+}
+
+// FP32 LJ without shift or switch terms, for the styles of lj_plain_style
 __device__ __forceinline__ float lj_pair_f(float eps, float sig2, float r2) {
   float s2 = sig2 * __frcp_rn(r2);
   float s6 = s2 * s2 * s2;

@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(kNoAllocThreads)
       int m = cutoff_mask(b, r2, cbmc != 0);
       if (!want_qq) m &= 1;
       if (m & 1) {
-        if (MIXED && qt[a] >= 0 && tj >= 0) {
+        if (MIXED && lj_plain_style(b) && qt[a] >= 0 && tj >= 0) {
           int k = pidx(qt[a], tj, t.ntypes);
           fv.add(lj_pair_f(t.epsf[k], t.sig2f[k], (float)r2));
         } else {

@@ -414,7 +414,10 @@ int cass_system_gradient(cass_ctx* ctx, int32_t ibox, CassEnergy* energy, double
  * minimum image (where Check_MoleculePair_Cutoff decides) CASS_EUNSUPPORTED.  Runs on the current device, asynchronously on `stream`.
  * All calls on a device share the scratch: calls that overlap on the GPU race.
  * The first call on a device resolves the scratch address; make it before any
- * stream capture. */
+ * stream capture.  The address is kept for the life of the process: after a
+ * cudaDeviceReset (or any teardown of the device's primary context) the module
+ * is loaded anew and the kept address is stale, so do not call this function
+ * again in a process that has reset its device. */
 int cass_mol_box_energy_noalloc(const CassBoxDesc* box, int32_t ntypes, const double* eps, const double* sig,
                                 const double* box_xyzq, const int32_t* box_type, const int32_t* box_mol,
                                 int32_t n, const double* query_xyzq, const int32_t* query_type, int32_t nq,

@@ -1,8 +1,8 @@
 """Extract golden vectors from the reference's own test suite into small fixtures.
 
-Run in a checkout that has the Cassandra reference tree (default path below);
-the fixtures it writes travel with the repository so that the tests can run
-where the reference is absent.  Everything is read as text or data: no
+Usage: python tests/golden/make_golden.py <path of the Cassandra source tree>
+(or set CASSANDRA_REFERENCE to that path).  The fixtures it writes travel with
+the repository so that the tests can run where the reference is absent.  Everything is read as text or data: no
 reference code is executed.
 
 Sources (paths inside the Cassandra tree):
@@ -24,7 +24,9 @@ import sys
 
 import numpy as np
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CASSANDRA_REFERENCE", "")
+if not REF or not os.path.isdir(REF):
+    sys.exit("usage: make_golden.py <Cassandra source tree>  (or set CASSANDRA_REFERENCE)")
 TS = os.path.join(REF, "Scripts", "testSuite")
 OUT = os.path.dirname(os.path.abspath(__file__))
 

@@ -117,3 +117,43 @@ def de_broglie(system: System, is_: int = 1, ibox: int = 1) -> float:
     beta = 1.0 / (0.8314472 * T)
     mw = sum(a.mass for a in system.species[is_ - 1].atoms)
     return 39.9031268605 * math.sqrt(beta / (2.0 * math.pi * mw))
+
+
+def pair_magnitude_scale(s, q_xyz, q_types, q_charges, skip_im, rc):
+    """Sum of |plain LJ| + |bare Coulomb| over the box-1 pairs of the query atoms within rc
+    (minimum image; rc None: every pair): the magnitude scale of a mixed-precision energy."""
+    bx = s.boxes[0]
+    L = np.asarray(bx.length, dtype=np.float64)
+    m = s.molecules
+    tot = 0.0
+    for k in range(len(m.im)):
+        if m.ibox[k] != 1 or (m.is_[k] == 1 and m.im[k] == skip_im):
+            continue
+        sp = s.species[m.is_[k] - 1]
+        for ja, pj in enumerate(m.xyz[k]):
+            tj = sp.type_index[ja]
+            qj = sp.atoms[ja].charge
+            for pa, ta, qa in zip(q_xyz, q_types, q_charges):
+                d = pa - pj
+                d -= L * np.round(d / L)
+                r2 = float(d @ d)
+                if rc is not None and r2 > rc * rc:
+                    continue
+                if ta > 0 and tj > 0:
+                    eps, sig = s.ff.eps[ta - 1][tj - 1], s.ff.sig[ta - 1][tj - 1]
+                    s6 = (sig * sig / r2) ** 3
+                    tot += abs(4.0 * eps * (s6 * s6 - s6))
+                tot += abs(138935.4558 * qa * qj / np.sqrt(r2))
+    return tot
+
+
+def lj_fluid_system(vdw_sum, vdw=("LJ", 120.0, 3.4), style=abi.VDW_LJ):
+    """300 single-site LJ (or Mie) atoms in a 25 A box, cutoff 10 A (switch 8-10 A)."""
+    from cassandra_gb300 import workloads
+    rng = np.random.default_rng(5)
+    xyz = workloads.lj_fluid_box(300, 25.0, 3.0, rng)
+    s = single_atom_system(xyz, 25.0, vdw=vdw, vdw_style=style, vdw_sum=vdw_sum, rcut=10.0, rcut_low=1.0,
+                           extra_slots=2)
+    if vdw_sum == abi.VDW_SUM_CUT_SWITCH:
+        s.boxes[0].ron_switch, s.boxes[0].roff_switch = 8.0, 10.0
+    return s

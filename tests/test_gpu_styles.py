@@ -34,13 +34,7 @@ def _close(a, b, rel=TOL, abs_=1e-7):
 
 
 def _lj_fluid(vdw_sum, vdw=("LJ", 120.0, 3.4), style=abi.VDW_LJ):
-    rng = np.random.default_rng(5)
-    xyz = workloads.lj_fluid_box(300, 25.0, 3.0, rng)
-    s = helpers.single_atom_system(xyz, 25.0, vdw=vdw, vdw_style=style, vdw_sum=vdw_sum, rcut=10.0, rcut_low=1.0,
-                                   extra_slots=2)
-    if vdw_sum == abi.VDW_SUM_CUT_SWITCH:
-        s.boxes[0].ron_switch, s.boxes[0].roff_switch = 8.0, 10.0
-    return s
+    return helpers.lj_fluid_system(vdw_sum, vdw, style)
 
 
 def _water(charge_sum, rcut=9.0):
@@ -134,3 +128,51 @@ def test_style_mixed_system_energy(name, make):
     scale = abs(eo["inter_vdw"]) + abs(eo["inter_q"]) + abs(eo["intra"]) + abs(eo["reciprocal"])
     for k in ("total", "inter_vdw", "inter_q", "reciprocal", "lrc", "self"):
         assert abs(eg[k] - eo[k]) <= 1e-5 * scale, (name, k, eg[k], eo[k])
+
+
+@pytest.mark.parametrize("name,make", CASES, ids=[c[0] for c in CASES])
+def test_style_mixed_molecule_and_trial_energies(name, make):
+    """The mixed context's molecule energies (cbmc_flag off and on) and CBMC trial
+    energies against the oracle in every style.  Compute_AtomPair_Energy applies the
+    shift, switch, shifted-force and CHARMM forms whatever the CBMC flag is
+    (energy_routines.f90:1927-1970), so the mixed kernels must too: the FP32 pair form
+    serves LJ cut, cut_tail and minimum image only.  Bound: 1e-5 of the summed pair
+    magnitudes (a missing shift term is several per cent of it)."""
+    s = make()
+    bx = s.boxes[0]
+    water = name.startswith("water")
+    sp = s.species[0]
+    types = list(sp.type_index)
+    charges = [a.charge for a in sp.atoms]
+    rmax = max(bx.rcut_vdw, bx.rcut_coul if bx.charge_style == abi.CHARGE_COUL else 0.0)
+    all_pairs = name in ("lj_minimum", "lj_charmm", "water_qq_minimum")
+    m = s.molecules
+    with oracle.open_system(s) as o, cg.open_system(s, precision=abi.PREC_MIXED) as g:
+        o.system_total_energy(1)
+        g.system_total_energy(1)
+        for im in (1, 17, 60):
+            k = m.im.index(im)
+            for cbmc in (False, True):
+                a = o.mol_inter_energy(im, 1, cbmc)
+                b = g.mol_inter_energy(im, 1, cbmc)
+                assert a[2] == b[2]
+                rc = bx.rcut_cbmc if cbmc else (None if all_pairs else rmax)
+                scale = helpers.pair_magnitude_scale(s, m.xyz[k], types, charges, im, rc)
+                err = abs(b[0] + b[1] - a[0] - a[1])
+                assert err <= 1e-5 * scale, (name, im, cbmc, a, b, err / scale)
+        if name in COMCUT:
+            return
+        rng = np.random.default_rng(11)
+        L = bx.length[0]
+        shape = np.asarray(m.xyz[0]) - np.asarray(m.xyz[0]).mean(axis=0)
+        xyz = np.array([shape + (rng.random(3) - 0.5) * L for _ in range(24)])
+        atoms = list(range(1, sp.natoms + 1))
+        for cbmc in (True, False):
+            eo, oo = o.cbmc_trial_energies(1, 1, atoms, xyz, cbmc=cbmc)
+            eg, og = g.cbmc_trial_energies(1, 1, atoms, xyz, cbmc=cbmc)
+            assert np.array_equal(oo, og)
+            assert (~oo).sum() > 10
+            rc = bx.rcut_cbmc if cbmc else (None if all_pairs else rmax)
+            for t in np.nonzero(~oo)[0]:
+                scale = helpers.pair_magnitude_scale(s, xyz[t], types, charges, 0, rc)
+                assert abs(eg[t] - eo[t]) <= 1e-5 * scale, (name, cbmc, t, eg[t], eo[t])

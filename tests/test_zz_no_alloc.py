@@ -91,3 +91,53 @@ def test_noalloc_rejects_oversize():
                                        0, abi.PREC_FP64, ctypes.c_void_p(8), None)
     assert rc == abi.CASS_ECAPACITY
     assert b"262144" in fns["last_error"]()
+
+
+@pytest.mark.parametrize("vdw_sum", [abi.VDW_SUM_CUT_SHIFT, abi.VDW_SUM_CUT_SWITCH, abi.VDW_SUM_CUT_TAIL],
+                         ids=["cut_shift", "cut_switch", "cut_tail"])
+def test_noalloc_mixed_matches_oracle(vdw_sum):
+    """Mixed precision through the allocation-free call, in LJ styles with and without a
+    shift or switch term, against the oracle's molecule energy: the shift and switch
+    terms apply in every precision and with or without the CBMC flag
+    (energy_routines.f90:1927-1970).  Two calls in a row per style."""
+    import torch
+
+    from cassandra_gb300 import build
+    from oracle import oracle
+    build.build()
+    fns = cg.functions()
+    noalloc = fns["mol_box_energy_noalloc"]
+    s = helpers.lj_fluid_system(vdw_sum)
+    sp = s.species[0]
+    xyz = np.concatenate([x for x in s.molecules.xyz])
+    box_xyzq = np.concatenate([xyz, np.zeros((len(xyz), 1))], axis=1)
+    dev = torch.device("cuda:0")
+    d_box = torch.tensor(box_xyzq, dtype=torch.float64, device=dev).contiguous()
+    d_type = torch.ones(len(xyz), dtype=torch.int32, device=dev)
+    d_mol = torch.arange(1, len(xyz) + 1, dtype=torch.int32, device=dev)
+    d_out = torch.zeros(3, dtype=torch.float64, device=dev)
+    d_qt = torch.ones(1, dtype=torch.int32, device=dev)
+    desc = _box_desc(s.boxes[0])
+    eps = np.ascontiguousarray(s.ff.eps, dtype=np.float64).ravel()
+    sig = np.ascontiguousarray(s.ff.sig, dtype=np.float64).ravel()
+    pe = eps.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    ps = sig.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    with oracle.open_system(s) as o:
+        o.system_total_energy(1)
+        for im, cbmc in ((17, 0), (42, 1)):
+            want = o.mol_inter_energy(im, 1, bool(cbmc))
+            d_q = torch.tensor(box_xyzq[im - 1:im], dtype=torch.float64, device=dev).contiguous()
+            d_out.fill_(-7.0)
+            torch.cuda.synchronize()
+            rc = noalloc(ctypes.byref(desc), s.ff.ntypes, pe, ps, ctypes.c_void_p(d_box.data_ptr()),
+                         ctypes.c_void_p(d_type.data_ptr()), ctypes.c_void_p(d_mol.data_ptr()), d_type.numel(),
+                         ctypes.c_void_p(d_q.data_ptr()), ctypes.c_void_p(d_qt.data_ptr()), 1, im, cbmc, 0,
+                         abi.PREC_MIXED, ctypes.c_void_p(d_out.data_ptr()), None)
+            assert rc == abi.CASS_OK, fns["last_error"]()
+            torch.cuda.synchronize()
+            got = d_out.cpu().numpy()
+            assert bool(got[2]) == want[2]
+            k = s.molecules.im.index(im)
+            scale = helpers.pair_magnitude_scale(s, s.molecules.xyz[k], sp.type_index, [0.0], im,
+                                                 s.boxes[0].rcut_cbmc if cbmc else s.boxes[0].rcut_vdw)
+            assert abs(got[0] - want[0]) <= 1e-5 * scale, (vdw_sum, im, cbmc, got, want)
