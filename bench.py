@@ -128,32 +128,40 @@ class ClockSampler:
 
 
 def build_workload(args, rank):
+    """Rank r's shard of the job: its own `args.boxes` boxes (seed offset by the rank),
+    so that the per-rank work stays fixed as ranks are added (weak scaling)."""
     from cassandra_gb300 import workloads
-    return workloads.widom_batch_system(nboxes=args.boxes, seed=args.seed, nconfig=1000)
+    return workloads.widom_batch_system(nboxes=args.boxes, seed=args.seed + 1000 * rank, nconfig=1000)
 
 
-def cpu_baseline(system, args, per_box_cap=None):
-    """CPU FP64 oracle (restatement of the reference's Widom loop), OpenMP over insertions."""
+def cpu_baseline(system, args, per_box_cap=None, threads=0, seconds=None):
+    """CPU FP64 oracle (restatement of the reference's Widom loop), OpenMP over
+    insertions on `threads` host threads (0: all)."""
     from oracle import oracle
     boxes = list(range(1, len(system.boxes) + 1))
-    with oracle.open_system(system) as o:
-        for b in boxes:
-            o.system_total_energy(b)
-        # calibrate on a small sample, then size the run to ~cpu_seconds
-        t0 = time.perf_counter()
-        o.widom_insert(2, boxes, 8, args.kappa, args.kappa, seed=1)
-        dt = max(time.perf_counter() - t0, 1e-3)
-        per = dt / (8 * len(boxes))
-        n = max(8, int(args.cpu_seconds / (per * len(boxes))))
-        if per_box_cap:
-            n = min(n, per_box_cap)
-        t0 = time.perf_counter()
-        res = o.widom_insert(2, boxes, n, args.kappa, args.kappa, seed=99)
-        dt = time.perf_counter() - t0
+    secs = args.cpu_seconds if seconds is None else seconds
+    nthr = oracle.set_num_threads(threads)
+    try:
+        with oracle.open_system(system) as o:
+            for b in boxes:
+                o.system_total_energy(b)
+            # calibrate on a small sample, then size the run to ~secs
+            t0 = time.perf_counter()
+            o.widom_insert(2, boxes, 8 if nthr > 1 else 1, args.kappa, args.kappa, seed=1)
+            dt = max(time.perf_counter() - t0, 1e-3)
+            per = dt / ((8 if nthr > 1 else 1) * len(boxes))
+            n = max(1, int(secs / (per * len(boxes))))
+            if per_box_cap:
+                n = min(n, per_box_cap)
+            t0 = time.perf_counter()
+            res = o.widom_insert(2, boxes, n, args.kappa, args.kappa, seed=99)
+            dt = time.perf_counter() - t0
+    finally:
+        oracle.set_num_threads(0)
     trials = sum(r["n_trials"] for r in res)
-    return {"value": trials / dt, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+    return {"value": trials / dt, "unit": UNIT, "cores": nthr, "kind": "port",
             "sample": f"{len(boxes)} boxes x {n} insertions ({trials} trial energies) in {dt:.2f} s, "
-                      f"FP64 C++ oracle, OpenMP over insertions"}
+                      f"FP64 C++ oracle, OpenMP over insertions, {nthr} thread(s)"}
 
 
 def mc_leg(cg, abi, dev, with_cpu: bool) -> dict:
@@ -619,8 +627,14 @@ def main():
         t = torch.tensor([total_ms], device=f"cuda:{dev}")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
-    mu_mixed, mu_mixed_se = mu_ex(timed_steps.results)
     timed_steps_mixed_results = list(timed_steps.results)
+    # per-box accumulators of every rank's boxes, merged with one small all-reduce per
+    # step (each box has one owner): the job's mu_ex over all world x boxes boxes
+    from cassandra_gb300 import shard
+    gboxes = list(range(1, world * len(boxes) + 1))
+    mine_g = [rank * len(boxes) + b for b in boxes]
+    merged_steps = [shard.merge_box_results(gboxes, mine_g, r) for r in timed_steps_mixed_results]
+    mu_mixed, mu_mixed_se = mu_ex(merged_steps)
     mu_cmp = None
     trials_step = n_per_box * len(boxes) * trials_per_ins
     value = trials_step * args.steps * world / (total_ms / 1000.0)
@@ -640,7 +654,7 @@ def main():
         fms, fkms, _, _ = timed_steps(fctx, args.fp64_steps, 1, args.seed)
         mu_fp64, _ = mu_ex(timed_steps.results)
         nst = min(len(timed_steps.results), args.steps)
-        mu_mixed_same, _ = mu_ex(timed_steps_mixed_results[:nst])
+        mu_mixed_same, _ = mu_ex(timed_steps_mixed_results[:nst])  # rank 0's boxes, as mu_fp64
         fp64_value = trials_step * len(fms) / (float(np.sum(fms)) / 1000.0)
         fp64 = {"value": fp64_value, "unit": UNIT, "ms_per_step": float(np.mean(fms)),
                 "kernel_ms": float(np.mean(fkms)), "mixed_over_fp64": value / world / fp64_value}
@@ -702,7 +716,9 @@ def main():
                       "boxes": len(boxes), "insertions_per_step": n_per_box * len(boxes),
                       "trial_energies_per_step": trials_step, "atoms_total": int(sum(natoms)),
                       "l2": "flushed (256 MB write) between timed steps", "precision": "mixed",
-                      "parallelism": f"replicas x{world}"},
+                      "parallelism": f"box shards x{world}",
+                      "sharding": "each rank owns its own boxes (rank r: boxes seeded by r), per-rank work fixed; "
+                                  "per-box Widom accumulators merged by one all-reduce after the timed steps"},
            "widom_launch": {"ctas_per_box": st["widom_grid_x"], "threads": st["widom_block"],
                             "smem_bytes": st["widom_smem_bytes"],
                             "note": "shape chosen by the library's launch autotuner on its first call"},
@@ -711,7 +727,9 @@ def main():
            "mu_ex_per_box": {"unit": "kJ/mol", "definition": "-kT ln <widom_var> (widom_insert.f90:445-447), "
                                                          "T = 150 K", "mixed": [round(float(v), 5) for v in mu_mixed],
                              "mixed_se": [round(float(v), 5) for v in mu_mixed_se],
-                             "n_atoms_per_box": [int(sum(1 for bi in system.molecules.ibox if bi == b)) for b in boxes],
+                             "boxes": len(gboxes),
+                             "n_atoms_per_box_rank0": [int(sum(1 for bi in system.molecules.ibox if bi == b))
+                                                       for b in boxes],
                              "mixed_vs_fp64": mu_cmp},
            "fp64_gpu": fp64,
            "accuracy_vs_fp64": accuracy,
@@ -773,6 +791,8 @@ def main():
         out["npt_fluctuation"] = npt_leg(cg, abi, dev, args.npt_chains, args.npt_eq_blocks, args.npt_blocks)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(system, args)
+        one = cpu_baseline(system, args, threads=1, seconds=min(args.cpu_seconds, 10.0))
+        out["cpu_baseline"]["one_thread"] = {"value": one["value"], "cores": one["cores"], "sample": one["sample"]}
     if rank == 0:
         print(json.dumps(out))
     if dist is not None:

@@ -3180,4 +3180,15 @@ int orc_num_threads(void) {
 #endif
 }
 
+// threads of the OpenMP regions that follow (n < 1: all the host's processors)
+int orc_set_num_threads(int n) {
+#ifdef _OPENMP
+  omp_set_num_threads(n >= 1 ? n : omp_get_num_procs());
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
+
 }  // extern "C"

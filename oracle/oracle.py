@@ -37,6 +37,8 @@ def lib() -> C.CDLL:
         _lib.orc_rng_stream.argtypes = [C.c_uint64, C.c_int64, C.c_int64, C.c_int32, C.POINTER(C.c_double)]
         _lib.orc_rng_reference.argtypes = [C.c_int64, C.c_int64, C.c_int32, C.POINTER(C.c_double)]
         _lib.orc_num_threads.restype = C.c_int
+        _lib.orc_set_num_threads.restype = C.c_int
+        _lib.orc_set_num_threads.argtypes = [C.c_int]
     return _lib
 
 
@@ -64,3 +66,8 @@ def rng_reference(i1: int, i3: int, n: int) -> np.ndarray:
 
 def num_threads() -> int:
     return int(lib().orc_num_threads())
+
+
+def set_num_threads(n: int) -> int:
+    """OpenMP threads of the oracle's parallel loops (n < 1: every host processor)."""
+    return int(lib().orc_set_num_threads(int(n)))
