@@ -23,11 +23,14 @@ struct SpeciesF {
   float bond_k[kMaxBonded], bond_l0[kMaxBonded], angle_k[kMaxBonded], angle_t0[kMaxBonded];
   float rb[kMaxBonded][6], imp_k[kMaxBonded], imp_p0[kMaxBonded];
   float cum_prob_ins[kMaxFrags];
+  // floor(cum_prob_ins * 2^32): the fragment choice decided on the top 32 bits of a draw
+  unsigned long long cumthr[kMaxFrags];
 };
 
 // FP32 constants of the CTA's box
 struct BoxF {
   float L[3], hL[3], cinv[3];
+  float Llo[3];  // L - (float)L: the box edge as a two-term FP32 value (Widom centres of mass)
   float ch[3];  // cell edge L / nc (Widom stencils)
   int nc[3];
   float rcb2, rv2, rq2, low2, rc_cbmc, rc_full, beta, kmaxE, alpha;
@@ -65,6 +68,36 @@ __device__ __forceinline__ float draw_f(Lfsr& g) {
   g.next_bits();
   unsigned v = (unsigned)(((g.s1 ^ g.s2 ^ g.s3 ^ g.s4 ^ g.s5) ^ 0x8000000000000000ull) >> 41);
   return (__int_as_float(0x4B000000 | v) - 8388608.0f) * 1.1920928955078125e-7f;
+}
+
+// The Widom kernel's draws keep the top 32 bits v of the reference's uniform
+// u = x 2^-64 + 0.5 (v = (x ^ 2^63) >> 32), so that
+//   * uniforms that enter the geometry carry 24 significant bits (rounded toward zero);
+//   * int(u * n) (library conformations) is exact in integer arithmetic unless
+//     u * n lies within n 2^-32 of an integer (a 2^-32 n chance per draw);
+//   * a centre-of-mass coordinate (0.5 - u) L is formed in two-term FP32 and
+//     rounded once, so it carries only the FP32 rounding of its own value.
+__device__ __forceinline__ unsigned draw_u32(Lfsr& g) {
+  g.next_bits();
+  return (unsigned)(((g.s1 ^ g.s2 ^ g.s3 ^ g.s4 ^ g.s5) ^ 0x8000000000000000ull) >> 32);
+}
+
+__device__ __forceinline__ float unit_of(unsigned v) { return __uint2float_rz(v) * 2.3283064365386963e-10f; }
+
+__device__ __forceinline__ int index_of(unsigned v, int n) {
+  const int k = (int)(((unsigned long long)v * (unsigned)n) >> 32);
+  return k < n ? k : n - 1;
+}
+
+// (0.5 - u) L = (2^31 - v) L 2^-32 with L = Lh + Ll
+__device__ __forceinline__ float centre_of(unsigned v, float Lh, float Ll) {
+  const long long m = 2147483648LL - (long long)v;
+  const long long mhi = m & ~0xFFLL;
+  const float mh = (float)mhi, ml = (float)(m - mhi);
+  const float p = mh * Lh;
+  const float e = fmaf(mh, Lh, -p);
+  const float rest = fmaf(mh, Ll, fmaf(ml, Lh, e));
+  return (p + rest) * 2.3283064365386963e-10f;
 }
 
 __device__ __forceinline__ void get_com_f(const SpeciesF& S, const float* r, unsigned exist, float com[3]) {

