@@ -185,12 +185,15 @@ SIGNATURES = {
     "traj_close": (C.c_int, [C.c_void_p]),
     "load_next_frame": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), _i32p]),
     "get_stats": (C.c_int, [C.c_void_p, C.POINTER(CassStats)]),
+    "build_molecule": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                 C.POINTER(C.c_uint64), _i32p, _f64p, _f64p, _f64p, _i32p]),
     "set_count_pairs": (C.c_int, [C.c_void_p, C.c_int32]),
+    "set_mc_cluster": (C.c_int, [C.c_void_p, C.c_int32]),
     "set_widom_cells": (C.c_int, [C.c_void_p, C.c_double]),
     "set_widom_autotune": (C.c_int, [C.c_void_p, C.c_int32]),
     "set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
-OPTIONAL = {"get_stats", "set_count_pairs", "set_widom_cells", "set_widom_autotune", "set_stream", "mol_box_energy_noalloc", "system_gradient", "gcmc",
+OPTIONAL = {"get_stats", "set_count_pairs", "set_mc_cluster", "set_widom_cells", "set_widom_autotune", "set_stream", "mol_box_energy_noalloc", "system_gradient", "gcmc",
             "traj_open", "traj_next", "traj_stats", "traj_close", "load_next_frame"}
 
 
@@ -245,6 +248,7 @@ class Context:
         self.max_molecules = list(max_molecules)
         self.precision = precision
         self.natoms: dict[int, int] = {}
+        self.nfrag: dict[int, int] = {}
 
     # -- plumbing --------------------------------------------------------
     def _check(self, fn: str, rc: int) -> None:
@@ -288,6 +292,7 @@ class Context:
                 setattr(d, k, v)
         self._check("set_species", self._f["set_species"](self._h, is_, C.byref(d)))
         self.natoms[is_] = sp.natoms
+        self.nfrag[is_] = len(sp.fragments)
 
     def set_box(self, ibox: int, bx) -> None:
         d = CassBoxDesc()
@@ -387,6 +392,10 @@ class Context:
         """Widom cell edge = rcut_cbmc / cells_per_cutoff (0: the precision's default)."""
         self._check("set_widom_cells", self._f["set_widom_cells"](self._h, float(cells_per_cutoff)))
 
+    def set_mc_cluster(self, ctas: int) -> None:
+        """CTAs per chain of mc_sweeps (0: chosen per call)."""
+        self._check("set_mc_cluster", self._f["set_mc_cluster"](self._h, int(ctas)))
+
     def set_count_pairs(self, on: bool) -> None:
         self._check("set_count_pairs", self._f["set_count_pairs"](self._h, int(on)))
 
@@ -445,6 +454,25 @@ class Context:
             self._h, ibox, is_, skip_im, len(at), _p(at), x.shape[0], x.ctypes.data_as(_f64p), int(cbmc),
             e.ctypes.data_as(_f64p), ov.ctypes.data_as(_i32p)))
         return e, ov.astype(bool)
+
+    def build_molecule(self, im: int, is_: int, ibox: int, del_flag: bool, kappa_ins: int, kappa_dih: int,
+                       rng_state):
+        """Build_Molecule for molecule im of species is_ in box ibox from the lfsr258
+        state rng_state (5 words).  Returns a dict with frag_order (1-based), ln_pseq,
+        ln_pbias, xyz [natoms, 3], cbmc_overlap and the advanced rng_state."""
+        st = np.array(rng_state, dtype=np.uint64).reshape(-1)
+        if st.shape != (5,):
+            raise ValueError("rng_state must hold 5 words")
+        order = np.zeros(8, dtype=np.int32)
+        lp, lb = C.c_double(0.0), C.c_double(0.0)
+        xyz = np.zeros(3 * self.natoms[is_])
+        ov = C.c_int32(0)
+        self._check("build_molecule", self._f["build_molecule"](
+            self._h, im, is_, ibox, int(bool(del_flag)), kappa_ins, kappa_dih,
+            st.ctypes.data_as(C.POINTER(C.c_uint64)), order.ctypes.data_as(_i32p), C.byref(lp), C.byref(lb),
+            xyz.ctypes.data_as(_f64p), C.byref(ov)))
+        return {"frag_order": order[:self.nfrag.get(is_, 8)], "ln_pseq": lp.value, "ln_pbias": lb.value,
+                "xyz": xyz.reshape(-1, 3), "cbmc_overlap": bool(ov.value), "rng_state": st}
 
     def system_gradient(self, ibox: int, n_atoms_box: int):
         """(energy dict, dU/dr [n_atoms_box, 3], dU/deps [nt, nt], dU/dsig [nt, nt], dU/dq [sum natoms])."""

@@ -1212,6 +1212,12 @@ int cass_set_widom_cells(cass_ctx* c, double cells_per_cutoff) {
   return CASS_OK;
 }
 
+int cass_set_mc_cluster(cass_ctx* c, int32_t ctas) {
+  if (!c || ctas < 0 || ctas > 8) return set_error(CASS_EINVAL, "ctas must be in [0, 8]");
+  c->mc_cluster = ctas;
+  return CASS_OK;
+}
+
 int cass_set_stream(cass_ctx* c, void* stream) {
   if (!c) return set_error(CASS_EINVAL, "NULL context");
   CASS_CUDA(cudaStreamSynchronize(c->stream));

@@ -179,6 +179,7 @@ struct cass_ctx_impl {
   int count_pairs = 0;
   double widom_cells = 0.0;  // cells per rcut_cbmc in the Widom cell lists (0: default)
   int widom_waves = 0;       // CTAs per resident slot of the FP32 Widom launch (0: default)
+  int mc_cluster = 0;        // CTAs per chain of cass_mc_sweeps (0: chosen per call)
   // launch shapes the Widom autotuner chose, per batch signature: (cells per cutoff, waves)
   bool widom_autotune = true;
   std::vector<std::pair<std::vector<long long>, std::pair<double, int>>> widom_tuned;

@@ -1240,28 +1240,15 @@ __device__ __forceinline__ void gc_skip_draw(Lfsr& rng) {
   else (void)rng.next();
 }
 
+// The box view of a grand-canonical kernel (one box per CTA, or per cluster):
+// the box constants, the pair table and the FP32 tables in shared memory, the
+// records' atoms and COMs, the live-atom list and the sorted live records in
+// dynamic shared memory `smem` (gc_smem_bytes).  All threads; ends with a barrier.
 template <bool MIXED>
-__global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, PairTable T, int csize) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ BoxDev b;
-  __shared__ GrowState gs;
-  __shared__ double em[10];
-  __shared__ int eov[2];
-  __shared__ int mv_kind, mv_rec, mv_is, mv_skip, mv_acc, mv_stop, s_nlv;
-  __shared__ int rs0[kGcMaxSpecies];
-  __shared__ double old_r[3 * kMaxAtoms], old_com[3];
-  __shared__ int ttype[kMaxAtoms];
-  __shared__ float s_epsf[kMaxTypes * kMaxTypes], s_sig2f[kMaxTypes * kMaxTypes];
-  __shared__ double rg_new[3 * kMaxAtoms], rg_new_com[3], rg_en[8], rg_e_prev, rg_ln_pfor;
-  __shared__ GrowF gf;
-  __shared__ BoxF bf;
-  __shared__ float2 s_ljp[kMaxTypes * kMaxTypes];
-  __shared__ PairTable sT;  // the pair table in shared memory (its address is passed to device functions)
-  __shared__ float rgf_new[3 * kMaxAtoms], rgf_new_com[3], rgf_e_prev, rgf_ln_pfor;
-  const int crank = (int)(blockIdx.x % (unsigned)csize);
-  GcBox& G = boxes[blockIdx.x / csize];
+__device__ void gc_setup(const GcArgs& A, const GcBox& G, const PairTable& T, int csize, int crank,
+                         unsigned char* smem, BoxDev& b, BoxF& bf, PairTable& sT, float2* s_ljp, float* s_epsf,
+                         float* s_sig2f, int* rs0, int& s_nlv, int* ttype, GcView& V) {
   if (threadIdx.x == 0) {
-    gs.cbuf = 0;
     b = G.b;
     if (MIXED) {  // FP32 box constants
       for (int d = 0; d < 3; ++d) {
@@ -1368,7 +1355,6 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
     scom[3 * r + 2] = z / tm;
   }
   if (threadIdx.x < kMaxAtoms) ttype[threadIdx.x] = threadIdx.x < A.S.natoms ? A.S.type[threadIdx.x] : -1;
-  GcView V;
   V.b = &b;
   V.T = &sT;
   V.epsf = s_epsf;
@@ -1392,6 +1378,45 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
   V.nrec = R;
   V.crank = crank;
   V.csize = csize;
+  __syncthreads();
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, PairTable T, int csize) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ BoxDev b;
+  __shared__ GrowState gs;
+  __shared__ double em[10];
+  __shared__ int eov[2];
+  __shared__ int mv_kind, mv_rec, mv_is, mv_skip, mv_acc, mv_stop, s_nlv;
+  __shared__ int rs0[kGcMaxSpecies];
+  __shared__ double old_r[3 * kMaxAtoms], old_com[3];
+  __shared__ int ttype[kMaxAtoms];
+  __shared__ float s_epsf[kMaxTypes * kMaxTypes], s_sig2f[kMaxTypes * kMaxTypes];
+  __shared__ double rg_new[3 * kMaxAtoms], rg_new_com[3], rg_en[8], rg_e_prev, rg_ln_pfor;
+  __shared__ GrowF gf;
+  __shared__ BoxF bf;
+  __shared__ float2 s_ljp[kMaxTypes * kMaxTypes];
+  __shared__ PairTable sT;  // the pair table in shared memory (its address is passed to device functions)
+  __shared__ float rgf_new[3 * kMaxAtoms], rgf_new_com[3], rgf_e_prev, rgf_ln_pfor;
+  const int crank = (int)(blockIdx.x % (unsigned)csize);
+  GcBox& G = boxes[blockIdx.x / csize];
+  if (threadIdx.x == 0) gs.cbuf = 0;
+  GcView V;
+  gc_setup<MIXED>(A, G, T, csize, crank, smem, b, bf, sT, s_ljp, s_epsf, s_sig2f, rs0, s_nlv, ttype, V);
+  const int N = G.natoms, R = G.nrec;
+  double* sx = V.sx;
+  double* sy = V.sy;
+  double* sz = V.sz;
+  double* scom = V.com;
+  int* lv = V.lv;
+  int* apos = V.apos;
+  int* rlive = V.rlive;
+  int* rsp = V.rsp;
+  int* roff = V.roff;
+  int* pool = V.roff + R;
+  int* lrec = V.lrec;
+  float4* lv32 = V.lv32;
   // thread-0 state
   Lfsr rng;
   CassEnergy E;
@@ -2157,6 +2182,73 @@ void set_mol_box_ext(cass_ctx* c, int slot, int ibox);
 
 // the dynamic shared memory layout of k_gcmc: sx, sy, sz, scom, lv, apos,
 // [lvt], rlive, rsp, roff, pool, lrec, [lv32]
+// Build_Molecule (fragment_growth.f90:72-707) of one molecule, record `rec` of
+// the box view, as a host's own insertion or deletion move calls it: the
+// whole CTA grows it (gc_build in FP64, gc_build_f in the mixed kernel) from
+// the caller's lfsr258 state.  Outputs: iout = cbmc overlap, number of
+// fragments placed, the growth order; out = ln_pseq, ln_pbias, coordinates.
+template <bool MIXED>
+__global__ void __launch_bounds__(kGcThreads, 1)
+    k_build_mol(GcArgs A, const GcBox* box, PairTable T, int rec, int del, unsigned long long* state, double* out,
+                int* iout) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ BoxDev b;
+  __shared__ GrowState gs;
+  __shared__ GrowF gf;
+  __shared__ BoxF bf;
+  __shared__ PairTable sT;
+  __shared__ float2 s_ljp[kMaxTypes * kMaxTypes];
+  __shared__ float s_epsf[kMaxTypes * kMaxTypes], s_sig2f[kMaxTypes * kMaxTypes];
+  __shared__ int rs0[kGcMaxSpecies];
+  __shared__ int ttype[kMaxAtoms];
+  __shared__ int s_nlv;
+  if (threadIdx.x == 0) gs.cbuf = 0;
+  GcView V;
+  gc_setup<MIXED>(A, *box, T, 1, 0, smem, b, bf, sT, s_ljp, s_epsf, s_sig2f, rs0, s_nlv, ttype, V);
+  Lfsr rng;
+  if (threadIdx.x == 0) {
+    rng.s1 = state[0];
+    rng.s2 = state[1];
+    rng.s3 = state[2];
+    rng.s4 = state[3];
+    rng.s5 = state[4];
+    gs.rec = rec;
+    gs.is = A.is_ex;
+    gs.na = A.sp[A.is_ex].natoms;
+    for (int a = 0; a < gs.na; ++a) {
+      gs.r[3 * a] = V.sx[V.roff[rec] + a];
+      gs.r[3 * a + 1] = V.sy[V.roff[rec] + a];
+      gs.r[3 * a + 2] = V.sz[V.roff[rec] + a];
+    }
+    for (int d = 0; d < 3; ++d) gs.com[d] = V.com[3 * rec + d];
+    if (MIXED) {
+      for (int i = 0; i < 3 * gs.na; ++i) gf.r[i] = (float)gs.r[i];
+      for (int d = 0; d < 3; ++d) gf.com[d] = (float)gs.com[d];
+    }
+  }
+  __syncthreads();
+  bool ov;
+  if constexpr (MIXED) ov = gc_build_f(A, V, gs, gf, del != 0, rng);
+  else ov = gc_build<false>(A, V, gs, del != 0, rng);
+  if (threadIdx.x == 0) {
+    state[0] = rng.s1;
+    state[1] = rng.s2;
+    state[2] = rng.s3;
+    state[3] = rng.s4;
+    state[4] = rng.s5;
+    iout[0] = ov ? 1 : 0;
+    iout[1] = gs.norder;
+    for (int k = 0; k < gs.norder && k < kMaxFrags; ++k) iout[2 + k] = gs.order[k];
+    out[0] = MIXED ? (double)gf.ln_pseq : gs.ln_pseq;
+    out[1] = MIXED ? (double)gf.ln_pbias : gs.ln_pbias;
+    for (int a = 0; a < gs.na; ++a)
+      for (int d = 0; d < 3; ++d) {
+        const double v = d == 0 ? V.sx[V.roff[rec] + a] : (d == 1 ? V.sy[V.roff[rec] + a] : V.sz[V.roff[rec] + a]);
+        out[2 + 3 * a + d] = del ? v : (MIXED ? (double)gf.r[3 * a + d] : gs.r[3 * a + d]);
+      }
+  }
+}
+
 size_t gc_smem_bytes(int natoms, int nrec, bool mixed) {
   size_t s = (size_t)natoms * (3 * sizeof(double) + (mixed ? 2 : 3) * sizeof(int)) +
              (size_t)nrec * (3 * sizeof(double) + 5 * sizeof(int));
@@ -2167,6 +2259,113 @@ size_t gc_smem_bytes(int natoms, int nrec, bool mixed) {
 }  // namespace cassgpu
 
 using namespace cassgpu;
+
+// A box as a grand-canonical kernel holds it: records of its live molecules and
+// of the free slots `free_slots`, in slot order, with their atoms (free slots at
+// the origin), the free records' indices, and the box constants of g (mu and
+// the de Broglie term are the caller's).
+struct HostBox {
+  std::vector<int> slots;
+  std::vector<int4> rec;
+  std::vector<double4_32a> xyzq;
+  std::vector<int> atype, pool;
+};
+
+static void gc_host_box(cass_ctx* c, int ib, const std::vector<int>& free_slots, HostBox& h, GcBox& g) {
+  BoxH& B = c->box[ib];
+  const std::vector<int>& mem = members_ext(c, ib);
+  h.slots.assign(mem.begin(), mem.end());
+  h.slots.insert(h.slots.end(), free_slots.begin(), free_slots.end());
+  std::sort(h.slots.begin(), h.slots.end());
+  int off = 0;
+  double nb0[kMaxTypes] = {0};
+  for (size_t r = 0; r < h.slots.size(); ++r) {
+    const int slot = h.slots[r], sp = c->slot_sp[slot];
+    const SpeciesH& t = c->sp[sp];
+    const bool live = c->mol_box[slot] == ib;
+    h.rec.push_back(make_int4(slot, sp, off, live ? 1 : 0));
+    const double* x = &t.pos[(size_t)(slot - c->mol_base[sp]) * 3 * t.natoms];
+    for (int a = 0; a < t.natoms; ++a) {
+      h.xyzq.push_back(make_double4_32a(live ? x[3 * a] : 0.0, live ? x[3 * a + 1] : 0.0, live ? x[3 * a + 2] : 0.0, t.q[a]));
+      h.atype.push_back(t.type[a]);
+      if (live && t.type[a] >= 0) nb0[t.type[a]] += 1.0;
+    }
+    off += t.natoms;
+  }
+  for (int slot : free_slots) h.pool.push_back((int)(std::lower_bound(h.slots.begin(), h.slots.end(), slot) - h.slots.begin()));
+  memset(&g, 0, sizeof(g));
+  g.b = B.dev;
+  g.natoms = off;
+  g.nrec = (int)h.slots.size();
+  g.npool = (int)h.pool.size();
+  g.ibox1 = ib + 1;
+  g.rcut3 = B.rcut3;
+  g.rcut9 = B.rcut9;
+  const int nt = c->pt.ntypes;
+  for (int ia = 0; ia < nt; ++ia)
+    for (int ja = 0; ja < nt; ++ja) {
+      const double eps = c->pt.eps[ia * nt + ja], s2 = c->pt.sig2[ia * nt + ja];
+      const double s6 = s2 * s2 * s2, s12 = s6 * s6;
+      g.lrc_c[ia * nt + ja] = 4.0 * eps * (s12 / (9.0 * B.rcut9) - (s6 / (3.0 * B.rcut3)));
+    }
+  g.lrc_pref = 2.0 * kPI / B.dev.volume;
+  g.log_vol = std::log(B.dev.volume);
+  for (int t = 0; t < kMaxTypes; ++t) g.nb0[t] = nb0[t];
+}
+
+// The growth tables and species tables of a grand-canonical kernel for the
+// exchanged species is (0-based); mixed is cleared when the species does not fit
+// the FP32 tables.  Move probabilities, steps and seed are the caller's.
+static void gc_fill_args(cass_ctx* c, int is, int kappa_ins, int kappa_dih, bool& mixed, GcArgs& A) {
+  const SpeciesH& s = c->sp[is];
+  memset(&A, 0, sizeof(A));
+  fill_growth_species(s, is, kappa_ins, kappa_dih, A.S);
+  A.is_ex = is;
+  A.nspecies = c->nspecies;
+  for (int k = 0; k < c->nspecies; ++k) {
+    const SpeciesH& t = c->sp[k];
+    A.sp[k].natoms = t.natoms;
+    bool lin = true;
+    for (size_t q = 0; q < t.angle_kind.size(); ++q)
+      if (t.angle_kind[q] != CASS_BONDED_FIXED || t.angle_param[2 * q] != 180.0) lin = false;
+    A.sp[k].linear = lin ? 1 : 0;
+    for (int a = 0; a < kMaxAtoms; ++a) A.sp[k].type[a] = -1;
+    for (int a = 0; a < t.natoms && a < kMaxAtoms; ++a) {
+      A.sp[k].mass[a] = t.mass[a];
+      A.sp[k].type[a] = t.type[a];
+    }
+  }
+  A.lib = s.d_library.as<double>();
+  A.P = c->pools;
+  // the mixed kernel grows molecules in FP32 from FP32 copies of the species and library
+  mixed = mixed && species_f(s, A.SF) && s.d_library_f.p != nullptr;
+  A.libf = s.d_library_f.as<float>();
+  // fragment bonds (f, g), f < g, and the probability of deleting f when the bond is cut
+  // (input_routines.f90:3035-3120): atoms beyond the bond on g's side over both sides
+  for (int f = 0; f < s.nfrag; ++f)
+    for (int g : s.frag_connect[f]) {
+      if (g <= f || A.nfbond >= kMaxFrags) continue;
+      int ndel[2];
+      for (int side = 0; side < 2; ++side) {
+        const int f1 = side ? g : f, f2 = side ? f : g;
+        std::vector<int> live(s.nfrag, 0), order{f1};
+        live[f1] = live[f2] = 1;
+        for (size_t q = 0; q < order.size(); ++q)
+          for (int h : s.frag_connect[order[q]])
+            if (!live[h]) {
+              live[h] = 1;
+              order.push_back(h);
+            }
+        ndel[side] = 0;
+        for (int h : order) ndel[side] += (int)s.frag_atoms[h].size() - 2;
+      }
+      A.fb_a[A.nfbond] = f;
+      A.fb_b[A.nfbond] = g;
+      A.prob_del1[A.nfbond] = (double)ndel[1] / (double)(ndel[0] + ndel[1]);
+      A.prob_del1f[A.nfbond] = (float)A.prob_del1[A.nfbond];
+      ++A.nfbond;
+    }
+}
 
 extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, const CassGCMCParams* p,
                          const double* mu, const double* max_disp, const double* max_rot, uint64_t seed,
@@ -2203,23 +2402,7 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
   if ((rc = ensure_pools(c))) return rc;
   if ((rc = ensure_cbmc(c))) return rc;
   GcArgs A;
-  memset(&A, 0, sizeof(A));
-  fill_growth_species(s, is, p->kappa_ins, p->kappa_dih, A.S);
-  A.is_ex = is;
-  A.nspecies = c->nspecies;
-  for (int k = 0; k < c->nspecies; ++k) {
-    const SpeciesH& t = c->sp[k];
-    A.sp[k].natoms = t.natoms;
-    bool lin = true;
-    for (size_t q = 0; q < t.angle_kind.size(); ++q)
-      if (t.angle_kind[q] != CASS_BONDED_FIXED || t.angle_param[2 * q] != 180.0) lin = false;
-    A.sp[k].linear = lin ? 1 : 0;
-    for (int a = 0; a < kMaxAtoms; ++a) A.sp[k].type[a] = -1;
-    for (int a = 0; a < t.natoms && a < kMaxAtoms; ++a) {
-      A.sp[k].mass[a] = t.mass[a];
-      A.sp[k].type[a] = t.type[a];
-    }
-  }
+  gc_fill_args(c, is, p->kappa_ins, p->kappa_dih, mixed, A);
   A.nsteps = p->nsteps;
   A.cut_t = p->cut_translate;
   A.cut_r = p->cut_rotate;
@@ -2227,41 +2410,11 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
   A.cut_d = p->cut_delete;
   A.cut_g = p->cut_regrow;
   A.seed = seed;
-  A.lib = s.d_library.as<double>();
-  A.P = c->pools;
   A.cutf[0] = (float)p->cut_translate;
   A.cutf[1] = (float)p->cut_rotate;
   A.cutf[2] = (float)p->cut_insert;
   A.cutf[3] = (float)p->cut_delete;
   A.cutf[4] = (float)p->cut_regrow;
-  // the mixed kernel grows molecules in FP32 from FP32 copies of the species and library
-  mixed = mixed && species_f(s, A.SF) && s.d_library_f.p != nullptr;
-  A.libf = s.d_library_f.as<float>();
-  // fragment bonds (f, g), f < g, and the probability of deleting f when the bond is cut
-  // (input_routines.f90:3035-3120): atoms beyond the bond on g's side over both sides
-  for (int f = 0; f < s.nfrag; ++f)
-    for (int g : s.frag_connect[f]) {
-      if (g <= f || A.nfbond >= kMaxFrags) continue;
-      int ndel[2];
-      for (int side = 0; side < 2; ++side) {
-        const int f1 = side ? g : f, f2 = side ? f : g;
-        std::vector<int> live(s.nfrag, 0), order{f1};
-        live[f1] = live[f2] = 1;
-        for (size_t q = 0; q < order.size(); ++q)
-          for (int h : s.frag_connect[order[q]])
-            if (!live[h]) {
-              live[h] = 1;
-              order.push_back(h);
-            }
-        ndel[side] = 0;
-        for (int h : order) ndel[side] += (int)s.frag_atoms[h].size() - 2;
-      }
-      A.fb_a[A.nfbond] = f;
-      A.fb_b[A.nfbond] = g;
-      A.prob_del1[A.nfbond] = (double)ndel[1] / (double)(ndel[0] + ndel[1]);
-      A.prob_del1f[A.nfbond] = (float)A.prob_del1[A.nfbond];
-      ++A.nfbond;
-    }
   double mw = 0.0;
   for (double m : s.mass) mw += m;
   // free slots of the exchanged species, in ascending order, each to the box
@@ -2282,13 +2435,6 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
       load[kmin] += s.natoms;
     }
   }
-  // per-box records: the live molecules and the box's free slots, in slot order
-  struct HostBox {
-    std::vector<int> slots;
-    std::vector<int4> rec;
-    std::vector<double4_32a> xyzq;
-    std::vector<int> atype, pool;
-  };
   std::vector<HostBox> hb(nboxes);
   std::vector<GcBox> gb(nboxes);
   size_t smem = 0, tot_atoms = 0, tot_rec = 0;
@@ -2296,51 +2442,12 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
     const int ib = iboxes[k] - 1;
     BoxH& B = c->box[ib];
     HostBox& h = hb[k];
-    const std::vector<int>& mem = members_ext(c, ib);
-    h.slots.assign(mem.begin(), mem.end());
-    h.slots.insert(h.slots.end(), pools[k].begin(), pools[k].end());
-    std::sort(h.slots.begin(), h.slots.end());
-    int off = 0;
-    double nb0[kMaxTypes] = {0};
-    for (size_t r = 0; r < h.slots.size(); ++r) {
-      const int slot = h.slots[r], sp = c->slot_sp[slot];
-      const SpeciesH& t = c->sp[sp];
-      const bool live = c->mol_box[slot] == ib;
-      h.rec.push_back(make_int4(slot, sp, off, live ? 1 : 0));
-      const double* x = &t.pos[(size_t)(slot - c->mol_base[sp]) * 3 * t.natoms];
-      for (int a = 0; a < t.natoms; ++a) {
-        h.xyzq.push_back(make_double4_32a(live ? x[3 * a] : 0.0, live ? x[3 * a + 1] : 0.0, live ? x[3 * a + 2] : 0.0, t.q[a]));
-        h.atype.push_back(t.type[a]);
-        if (live && t.type[a] >= 0) nb0[t.type[a]] += 1.0;
-      }
-      off += t.natoms;
-    }
-    for (int slot : pools[k]) h.pool.push_back((int)(std::lower_bound(h.slots.begin(), h.slots.end(), slot) - h.slots.begin()));
     GcBox& g = gb[k];
-    memset(&g, 0, sizeof(g));
-    g.b = B.dev;
-    g.natoms = off;
-    g.nrec = (int)h.slots.size();
-    g.npool = (int)h.pool.size();
-    g.ibox1 = iboxes[k];
+    gc_host_box(c, ib, pools[k], h, g);
     g.mu = mu[k] / 0.01;  // kJ/mol to internal units (atomic_to_kJmol)
     g.log_lambda3 = 3.0 * std::log(39.9031268605 * std::sqrt(B.dev.beta / (kTWOPI * mw)));  // de Broglie
-    g.rcut3 = B.rcut3;
-    g.rcut9 = B.rcut9;
-    {
-      const int nt = c->pt.ntypes;
-      for (int ia = 0; ia < nt; ++ia)
-        for (int ja = 0; ja < nt; ++ja) {
-          const double eps = c->pt.eps[ia * nt + ja], s2 = c->pt.sig2[ia * nt + ja];
-          const double s6 = s2 * s2 * s2, s12 = s6 * s6;
-          g.lrc_c[ia * nt + ja] = 4.0 * eps * (s12 / (9.0 * B.rcut9) - (s6 / (3.0 * B.rcut3)));
-        }
-      g.lrc_pref = 2.0 * kPI / B.dev.volume;
-      g.log_vol = std::log(B.dev.volume);
-    }
-    for (int t = 0; t < kMaxTypes; ++t) g.nb0[t] = nb0[t];
     smem = std::max(smem, gc_smem_bytes(g.natoms, g.nrec, mixed));
-    tot_atoms += (size_t)off;
+    tot_atoms += (size_t)g.natoms;
     tot_rec += h.slots.size();
   }
   if (smem > kGcSmemLimit)
@@ -2488,5 +2595,99 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
     if (hs[k] == 1) return set_error(CASS_ESTATE, "a molecule overlapped another before its move (energy too high)");
     if (hs[k] == 2) return set_error(CASS_ECAPACITY, "no free molecule slot left for an insertion");
   }
+  return CASS_OK;
+}
+
+// Build_Molecule for one molecule (the per-call growth a host's own CBMC moves
+// use): the box view of cass_gcmc with the molecule's slot as a record (live
+// for del_flag, else a free record), one CTA, the caller's lfsr258 state
+extern "C" int cass_build_molecule(cass_ctx* c, int32_t im, int32_t is1, int32_t ibox, int32_t del_flag,
+                                   int32_t kappa_ins, int32_t kappa_dih, uint64_t* rng_state, int32_t* frag_order,
+                                   double* ln_pseq, double* ln_pbias, double* xyz, int32_t* cbmc_overlap) {
+  if (!c || is1 < 1 || is1 > c->nspecies || ibox < 1 || ibox > c->nboxes || !rng_state || !ln_pseq || !ln_pbias ||
+      !cbmc_overlap || kappa_ins < 1 || kappa_ins > kMaxKappa)
+    return set_error(CASS_EINVAL, "bad build_molecule arguments");
+  if (c->nspecies > kGcMaxSpecies) return set_error(CASS_ECAPACITY, "build_molecule supports at most 8 species");
+  if (!c->pt_set) return set_error(CASS_ESTATE, "nonbond table not set");
+  const int is = is1 - 1, ib = ibox - 1;
+  const SpeciesH& s = c->sp[is];
+  if (!s.defined || s.nfrag < 1) return set_error(CASS_ESTATE, "species not defined or without fragments");
+  if (im < 1 || im > c->max_mol[is]) return set_error(CASS_EINVAL, "molecule index out of range");
+  if (s.nfrag > 1 && (kappa_dih < 1 || kappa_dih > kMaxKappa)) return set_error(CASS_EINVAL, "kappa_dih must be in 1..32");
+  if (s.nfrag > kMaxFrags) return set_error(CASS_ECAPACITY, "species has more than 8 fragments");
+  for (int k = 0; k < c->nspecies; ++k)
+    if (c->sp[k].defined && c->sp[k].natoms > kMaxAtoms) return set_error(CASS_ECAPACITY, "molecules of at most 16 atoms");
+  for (int f = 0; f < s.nfrag; ++f)
+    if (s.frag_nconfig[f] < 1) return set_error(CASS_EINVAL, "fragment library is empty");
+  const BoxH& B = c->box[ib];
+  if (!B.defined) return set_error(CASS_ESTATE, "box not defined");
+  if (B.comcut) return set_error(CASS_EUNSUPPORTED, "molecule-pair COM cutoff (LJ CHARMM or minimum-image charges) is applied by the system and molecule energies only");
+  if (B.desc.charge_style != CASS_CHARGE_NONE) return set_error(CASS_EUNSUPPORTED, "build_molecule boxes hold no charges");
+  if (B.desc.vdw_style != CASS_VDW_LJ) return set_error(CASS_EUNSUPPORTED, "build_molecule needs LJ boxes");
+  const int slot = c->mol_base[is] + im - 1;
+  if (del_flag && c->mol_box[slot] != ib) return set_error(CASS_ESTATE, "del_flag: the molecule is not live in the box");
+  if (!del_flag && c->mol_box[slot] >= 0) return set_error(CASS_ESTATE, "the molecule to grow is live");
+  bool mixed = c->precision == CASS_PREC_MIXED &&
+               (B.desc.vdw_sum_style == CASS_VDW_SUM_CUT || B.desc.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL);
+  int rc;
+  CASS_CUDA(cudaSetDevice(c->device));
+  if ((rc = ensure_pools(c))) return rc;
+  if ((rc = ensure_cbmc(c))) return rc;
+  GcArgs A;
+  gc_fill_args(c, is, kappa_ins, kappa_dih, mixed, A);
+  HostBox h;
+  GcBox g;
+  gc_host_box(c, ib, del_flag ? std::vector<int>() : std::vector<int>{slot}, h, g);
+  const int rec = (int)(std::lower_bound(h.slots.begin(), h.slots.end(), slot) - h.slots.begin());
+  const size_t smem = gc_smem_bytes(g.natoms, g.nrec, mixed);
+  if (smem > kGcSmemLimit)
+    return set_error(CASS_ECAPACITY, "build_molecule holds the box in shared memory: too many atoms");
+  const size_t nout = 2 + 3 * (size_t)s.natoms, niout = 2 + kMaxFrags;
+  const size_t bytes = sizeof(GcBox) + h.xyzq.size() * sizeof(double4_32a) + h.atype.size() * sizeof(int) +
+                       h.rec.size() * sizeof(int4) + 8 * sizeof(double) + nout * sizeof(double) +
+                       niout * sizeof(int) + 256;
+  if ((rc = c->d_gc.reserve(bytes))) return rc;
+  char* base = static_cast<char*>(c->d_gc.p);
+  auto carve = [&](size_t n, size_t align) {
+    size_t o = ((size_t)(base - static_cast<char*>(c->d_gc.p)) + align - 1) & ~(align - 1);
+    char* q = static_cast<char*>(c->d_gc.p) + o;
+    base = q + n;
+    return q;
+  };
+  GcBox* d_box = reinterpret_cast<GcBox*>(carve(sizeof(GcBox), 64));
+  double4_32a* d_xyz = reinterpret_cast<double4_32a*>(carve(std::max<size_t>(1, h.xyzq.size()) * sizeof(double4_32a), 32));
+  int* d_at = reinterpret_cast<int*>(carve(std::max<size_t>(1, h.atype.size()) * sizeof(int), 16));
+  int4* d_rec = reinterpret_cast<int4*>(carve(std::max<size_t>(1, h.rec.size()) * sizeof(int4), 16));
+  unsigned long long* d_state = reinterpret_cast<unsigned long long*>(carve(8 * sizeof(double), 16));
+  double* d_out = reinterpret_cast<double*>(carve(nout * sizeof(double), 16));
+  int* d_iout = reinterpret_cast<int*>(carve(niout * sizeof(int), 16));
+  CASS_CUDA(h2d(c, d_xyz, h.xyzq.data(), h.xyzq.size() * sizeof(double4_32a)));
+  CASS_CUDA(h2d(c, d_at, h.atype.data(), h.atype.size() * sizeof(int)));
+  CASS_CUDA(h2d(c, d_rec, h.rec.data(), h.rec.size() * sizeof(int4)));
+  CASS_CUDA(h2d(c, d_state, rng_state, 5 * sizeof(uint64_t)));
+  g.xyzq = d_xyz;
+  g.atype = d_at;
+  g.rec = d_rec;
+  g.pool = nullptr;
+  g.npool = 0;
+  CASS_CUDA(h2d(c, d_box, &g, sizeof(GcBox)));
+  auto kern = mixed ? k_build_mol<true> : k_build_mol<false>;
+  CASS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<1, kGcThreads, smem, c->stream>>>(A, d_box, c->pt, rec, del_flag ? 1 : 0, d_state, d_out, d_iout);
+  CASS_CUDA(cudaGetLastError());
+  count_launch(c);
+  std::vector<double> hout(nout);
+  int hiout[2 + kMaxFrags];
+  CASS_CUDA(d2h(c, rng_state, d_state, 5 * sizeof(uint64_t)));
+  CASS_CUDA(d2h(c, hout.data(), d_out, nout * sizeof(double)));
+  CASS_CUDA(d2h(c, hiout, d_iout, niout * sizeof(int)));
+  CASS_CUDA(cudaStreamSynchronize(c->stream));
+  *cbmc_overlap = hiout[0];
+  *ln_pseq = hout[0];
+  *ln_pbias = hout[1];
+  if (frag_order)
+    for (int k = 0; k < s.nfrag; ++k) frag_order[k] = k < hiout[1] ? hiout[2 + k] + 1 : 0;
+  if (xyz)
+    for (int k = 0; k < 3 * s.natoms; ++k) xyz[k] = hout[2 + k];
   return CASS_OK;
 }

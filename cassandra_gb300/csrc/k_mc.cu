@@ -22,6 +22,7 @@
 // reciprocal energy, Cn [dc (2 S_c + dc) + ds (2 S_s + ds)] summed per thread
 // with compensation; the master coordinates, the running structure factors, the
 // energy bookkeeping and the acceptance exponent stay FP64.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -130,10 +131,41 @@ __device__ __forceinline__ V block_sum_mc(V v, V* red, int slot) {
   return v;
 }
 
+// Sums over the CTAs of a box's cluster, in rank order, of the nd doubles and
+// ni ints that thread 0 of every CTA placed in cd[buf] / ci[buf]; the results
+// land in the same arrays of every CTA's thread 0 view.  Two buffers alternate,
+// so a buffer is written again only after every CTA passed the barrier that
+// followed its last read.  Thread 0 only reads; all threads take the barrier.
+__device__ __forceinline__ void cluster_sum(int csize, double (*cd)[4], int (*ci)[2], int buf, int nd, int ni,
+                                            double* od, int* oi) {
+  namespace cgr = cooperative_groups;
+  cgr::cluster_group cl = cgr::this_cluster();
+  cl.sync();
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < nd; ++k) {
+      double v = 0.0;
+      for (int r = 0; r < csize; ++r) v += *cl.map_shared_rank(&cd[buf][k], r);
+      od[k] = v;
+    }
+    for (int k = 0; k < ni; ++k) {
+      int v = 0;
+      for (int r = 0; r < csize; ++r) v |= *cl.map_shared_rank(&ci[buf][k], r);
+      oi[k] = v;
+    }
+  }
+}
+
 // GMEM: the box layout lives in a per-box global buffer (L2-resident) instead
-// of shared memory, for boxes above the shared-memory limit; same code
+// of shared memory, for boxes above the shared-memory limit; same code.
+// csize > 1 (shared-memory boxes only): a thread-block cluster of csize CTAs
+// runs one box's chain.  Every CTA holds the whole box and makes the same
+// serial decisions from the same lfsr258 stream; the pair loop over the box
+// atoms and the k-vector loop are split over the CTAs, whose partial sums are
+// added in rank order through distributed shared memory, and each CTA commits
+// the structure factors of its own k-vectors.
 template <bool MIXED, bool GMEM>
-__global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(McArgs A, McBox* boxes, PairTable T) {
+__global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(McArgs A, McBox* boxes, PairTable T,
+                                                                           int csize) {
   constexpr int NW = (GMEM ? kMcThreadsG : kMcThreads) / 32;
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ BoxDev b;
@@ -141,7 +173,11 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
   __shared__ double red[NW * 8];
   __shared__ int redi[NW * 2];
   __shared__ float2 ljp[kMaxTypes * kMaxTypes];
-  McBox& G = boxes[blockIdx.x];
+  __shared__ double cd[2][4];  // this CTA's partial sums for the cluster (alternating buffers)
+  __shared__ int ci[2][2];
+  const int crank = (int)(blockIdx.x % (unsigned)csize);
+  int cbuf = 0;
+  McBox& G = boxes[blockIdx.x / csize];
   if (threadIdx.x == 0) b = G.b;
   for (int i = threadIdx.x; i < kMaxTypes * kMaxTypes; i += blockDim.x) {
     const int a = i / kMaxTypes, c = i % kMaxTypes;
@@ -335,12 +371,13 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
     const int pm = mv.pm, na = mv.na;
     double pdv = 0, pdq = 0;  // this thread's share of E_new - E_old
     int po = 0, pn = 0;
+    const int j0 = threadIdx.x + crank * blockDim.x, jstep = blockDim.x * csize;
     if (MIXED) {
       KahanF kv, kq;
       const float rv2 = (float)b.rcut_vdwsq, rq2 = (float)b.rcut_coulsq, low2 = (float)b.rcut_lowsq;
       const float alpha = (float)b.alpha;
       const bool qq_on = b.charge_style == CASS_CHARGE_COUL;
-      for (int j = threadIdx.x; j < N; j += blockDim.x) {
+      for (int j = j0; j < N; j += jstep) {
         if (smol[j] == pm) continue;
         const float4 pj = s32[j];
         const int tj = __float_as_int(pj.w);
@@ -372,7 +409,7 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
       pdv = kv.value();
       pdq = kq.value();
     } else {
-      for (int j = threadIdx.x; j < N; j += blockDim.x) {
+      for (int j = j0; j < N; j += jstep) {
         if (smol[j] == pm) continue;
         const double xj = sx[j], yj = sy[j], zj = sz[j], qj = sq[j];
         const int tj = stype[j];
@@ -407,15 +444,35 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
       }
     }
     __syncthreads();
+    int o = 0, n = 0;
     if (threadIdx.x == 0) {
       dv = dq = 0.0;
-      int o = 0, n = 0;
       for (int w = 0; w < NW; ++w) {
         dv += red[w * 8];
         dq += red[w * 8 + 1];
         o |= redi[2 * w];
         n |= redi[2 * w + 1];
       }
+      if (csize > 1) {
+        cd[cbuf][0] = dv;
+        cd[cbuf][1] = dq;
+        ci[cbuf][0] = o;
+        ci[cbuf][1] = n;
+      }
+    }
+    if (csize > 1) {
+      double sums[2];
+      int flags[2];
+      cluster_sum(csize, cd, ci, cbuf, 2, 2, sums, flags);
+      cbuf ^= 1;
+      if (threadIdx.x == 0) {
+        dv = sums[0];
+        dq = sums[1];
+        o = flags[0];
+        n = flags[1];
+      }
+    }
+    if (threadIdx.x == 0) {
       if (o) {
         mv.stop = 1;
         status = 1;
@@ -434,7 +491,7 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
       const double* smv = A.sin_mol + (size_t)mv.slot * A.stride;
       double part = 0.0;
       KahanF partf;
-      for (int k = threadIdx.x; k < G.nvecs; k += blockDim.x) {
+      for (int k = threadIdx.x + crank * blockDim.x; k < G.nvecs; k += blockDim.x * csize) {
         const double4_32a h = G.kvec[k];
         double cn = 0.0, sn = 0.0;
         if (MIXED) {
@@ -473,9 +530,16 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
       __syncthreads();
       if (threadIdx.x == 0) {
         for (int w = 0; w < NW; ++w) e_recip += red[w * 8 + 4];
-        // mixed: the previous reciprocal energy plus the FP32 change (FP64 sum)
-        e_recip = MIXED ? E.reciprocal + e_recip * kCHARGE_FACTOR : e_recip * kCHARGE_FACTOR;
+        if (csize > 1) cd[cbuf][0] = e_recip;
       }
+      if (csize > 1) {
+        double sums[1];
+        cluster_sum(csize, cd, ci, cbuf, 1, 0, sums, nullptr);
+        cbuf ^= 1;
+        if (threadIdx.x == 0) e_recip = sums[0];
+      }
+      if (threadIdx.x == 0)  // mixed: the previous reciprocal energy plus the FP32 change (FP64 sum)
+        e_recip = MIXED ? E.reciprocal + e_recip * kCHARGE_FACTOR : e_recip * kCHARGE_FACTOR;
     }
     // ---- D: acceptance
     if (threadIdx.x == 0) {
@@ -553,7 +617,7 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
     if (mv.accept && mv.ewald) {
       double* cm = A.cos_mol + (size_t)mv.slot * A.stride;
       double* smv = A.sin_mol + (size_t)mv.slot * A.stride;
-      for (int k = threadIdx.x; k < G.nvecs; k += blockDim.x) {
+      for (int k = threadIdx.x + crank * blockDim.x; k < G.nvecs; k += blockDim.x * csize) {
         const double cn = G.new_cos[k], sn = G.new_sin[k];
         G.cos_sum[k] = G.cos_sum[k] + (cn - cm[k]);
         G.sin_sum[k] = G.sin_sum[k] + (sn - smv[k]);
@@ -565,6 +629,8 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
     __syncthreads();
   }
   __syncthreads();
+  if (csize > 1) cooperative_groups::this_cluster().sync();  // no CTA leaves while its shared memory may be read
+  if (crank != 0) return;  // every CTA of the cluster holds the same state
   for (int j = threadIdx.x; j < N; j += blockDim.x) {
     G.p64[j] = make_double4_32a(sx[j], sy[j], sz[j], sq[j]);
     float4 f = G.p32[j];
@@ -731,8 +797,51 @@ extern "C" int cass_mc_sweeps(cass_ctx* c, int32_t nboxes, const int32_t* iboxes
                    : (mixed ? k_mc_sweeps<true, false> : k_mc_sweeps<false, false>);
   if (gmem) dyn = 0;
   CASS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  const int threads = gmem ? kMcThreadsG : kMcThreads;
+  // CTAs per chain: a cluster splits the pair and k-vector loops of a move when
+  // SMs would otherwise stay idle (few chains); every cluster must be resident
+  int csize = 1;
+  if (!gmem) {
+    int sms = 0, nmax = 1;
+    CASS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+    for (const McBox& g : hb) nmax = std::max(nmax, g.natoms);
+    int want = c->mc_cluster > 0 ? c->mc_cluster : std::min(8, std::max(1, sms / nboxes));
+    if (c->mc_cluster <= 0) want = std::min(want, std::max(1, (nmax + 63) / 64));
+    for (int cs = std::min(8, want); cs >= 2; --cs) {
+      cudaLaunchConfig_t q = {};
+      cudaLaunchAttribute qa[1];
+      qa[0].id = cudaLaunchAttributeClusterDimension;
+      qa[0].val.clusterDim.x = cs;
+      qa[0].val.clusterDim.y = 1;
+      qa[0].val.clusterDim.z = 1;
+      q.gridDim = dim3(nboxes * cs);
+      q.blockDim = dim3(threads);
+      q.dynamicSmemBytes = dyn;
+      q.attrs = qa;
+      q.numAttrs = 1;
+      int nclusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &q) == cudaSuccess && nclusters >= nboxes) {
+        csize = cs;
+        break;
+      }
+      (void)cudaGetLastError();
+    }
+  }
+  c->stats.gcmc_cluster = csize;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = csize;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(nboxes * csize);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = dyn;
+  cfg.stream = c->stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
   CASS_CUDA(cudaEventRecord(c->ev[0], c->stream));
-  kern<<<nboxes, gmem ? kMcThreadsG : kMcThreads, dyn, c->stream>>>(A, d_box, c->pt);
+  CASS_CUDA(cudaLaunchKernelEx(&cfg, kern, A, d_box, c->pt, csize));
   CASS_CUDA(cudaGetLastError());
   CASS_CUDA(cudaEventRecord(c->ev[1], c->stream));
   count_launch(c);

@@ -376,6 +376,34 @@ int cass_gcmc(cass_ctx* ctx, int32_t nboxes, const int32_t* ibox, const CassGCMC
               const double* mu, const double* max_disp, const double* max_rot, uint64_t seed,
               CassGCMCResult* out);
 
+/* ---- CBMC growth of one molecule ---------------------------------------- */
+/* Build_Molecule (fragment_growth.f90:72-707) for molecule im (1-based locate)
+ * of species is in box ibox, for a host that keeps its own insertion,
+ * deletion and regrowth moves (Build_Molecule's callers move_insert.f90:166,
+ * move_delete.f90:175, widom_insert.f90:345): the first fragment, its library
+ * conformation, Euler rotation and kappa_ins trial positions, then kappa_dih
+ * dihedral trials per further fragment, every trial's energy against the
+ * box's live molecules evaluated on the device.
+ *   del_flag 0: the molecule is grown anew; it must not be live.  xyz [natoms][3]
+ *     receives the grown coordinates, not folded into the box (the caller folds,
+ *     as move_insert.f90 does); the molecule stays not live until the caller
+ *     stores it with cass_set_molecules.
+ *   del_flag 1: the molecule is live in ibox; trial 1 of every stage is its
+ *     present configuration (the old-weight pass of a deletion or regrowth),
+ *     and xyz receives that configuration.
+ *   rng_state [5] in / out: the lfsr258 state the draws come from
+ *     (random_generators.f90:95-122), advanced exactly as rranf would be.
+ *   frag_order [nfrag] out: the fragments (1-based) in growth order.
+ *   ln_pseq, ln_pbias out: as Build_Molecule returns them, before the kappa
+ *     terms that the calling move adds.
+ *   cbmc_overlap out: 1 when every trial of a stage overlapped (ln_pbias and xyz
+ *     are then undefined).
+ * Boxes as cass_gcmc takes them (LJ, no charges).  FP64 contexts grow in FP64
+ * and reproduce the reference's arithmetic; mixed contexts grow in FP32. */
+int cass_build_molecule(cass_ctx* ctx, int32_t im, int32_t is, int32_t ibox, int32_t del_flag, int32_t kappa_ins,
+                        int32_t kappa_dih, uint64_t* rng_state, int32_t* frag_order, double* ln_pseq,
+                        double* ln_pbias, double* xyz, int32_t* cbmc_overlap);
+
 /* ---- configuration gradient (adjoint) ---------------------------------- */
 /* The derivatives of the total energy of box ibox, as cass_system_total_energy
  * computes it (and returns it in *energy), for LJ cut / cut_tail boxes with no
@@ -489,7 +517,7 @@ typedef struct CassStats {
   int32_t widom_smem_bytes;
   double mc_ms;             /* the most recent cass_mc_sweeps or cass_gcmc: its kernel */
   int64_t mc_moves;         /* moves it ran, all boxes */
-  int32_t gcmc_cluster;     /* CTAs per box of the most recent cass_gcmc (a thread-block cluster) */
+  int32_t gcmc_cluster;     /* CTAs per box (a thread-block cluster) of the most recent cass_gcmc or cass_mc_sweeps */
   int32_t reserved;
 } CassStats;
 int cass_get_stats(cass_ctx* ctx, CassStats* out);
@@ -505,6 +533,13 @@ int cass_set_widom_cells(cass_ctx* ctx, double cells_per_cutoff);
  * cass_set_widom_cells disables it.  Results do not depend on the shape beyond
  * summation order. */
 int cass_set_widom_autotune(cass_ctx* ctx, int32_t on);
+/* CTAs (a thread-block cluster) that run each chain of cass_mc_sweeps: 0 (the
+ * default) chooses per call -- several when few chains leave SMs idle, so a
+ * single chain's pair and k-vector loops spread over up to 8 multiprocessors;
+ * 1..8 fixes it (boxes kept in global memory always run on one CTA).  Results
+ * do not depend on it beyond summation order.  cass_get_stats reports the
+ * choice in gcmc_cluster. */
+int cass_set_mc_cluster(cass_ctx* ctx, int32_t ctas);
 /* Runs the context's work on a caller-owned cudaStream_t (NULL: its own). */
 int cass_set_stream(cass_ctx* ctx, void* stream);
 

@@ -1894,7 +1894,7 @@ bool place_fragments(orc_ctx* c, int ibox, Mol& m, int slot, const std::vector<i
 // Build_Molecule (fragment_growth.f90:72-707) for molecule m (slot) of box
 // ibox.  Returns cbmc_overlap; sets ln_pseq and ln_pbias.
 bool build_molecule(orc_ctx* c, int ibox, Mol& m, int slot, bool del, int kappa_ins, int kappa_dih, double& ln_pseq,
-                    double& ln_pbias, Rng& rng) {
+                    double& ln_pbias, Rng& rng, std::vector<int>* order_out = nullptr) {
   const Species& s = c->sp[m.is];
   const Box& b = c->box[ibox];
   const double beta = b.beta;
@@ -1908,6 +1908,7 @@ bool build_molecule(orc_ctx* c, int ibox, Mol& m, int slot, bool del, int kappa_
   std::vector<int> order{fstart}, live(s.nfrag, 0);
   live[fstart] = 1;
   if (s.nfrag > 1) fragment_order(s, fstart, order, live, ln_pseq, rng);
+  if (order_out) *order_out = order;
   const std::vector<int>& fa = s.frag_atoms[fstart];
   const int nfa = (int)fa.size();
   if (!del) {
@@ -3041,6 +3042,52 @@ int orc_mc_sweeps(orc_ctx* c, int32_t nboxes, const int32_t* iboxes, const CassM
 }
 
 // Grand-canonical Monte Carlo, one chain per box (boxes in parallel)
+// Build_Molecule for one molecule (the cass_build_molecule entry point): a
+// not-live molecule grown anew in a scratch record, or the old-weight pass of
+// a live one, whose stored coordinates are left as they were
+int orc_build_molecule(orc_ctx* c, int32_t im, int32_t is1, int32_t ibox1, int32_t del_flag, int32_t kappa_ins,
+                       int32_t kappa_dih, uint64_t* rng_state, int32_t* frag_order, double* ln_pseq, double* ln_pbias,
+                       double* xyz, int32_t* cbmc_overlap) {
+  if (c) refresh_members(c);
+  if (check_ctx(c) || is1 < 1 || is1 > c->nspecies || ibox1 < 1 || ibox1 > c->nboxes || kappa_ins < 1 || !rng_state ||
+      !ln_pseq || !ln_pbias || !cbmc_overlap)
+    return fail(CASS_EINVAL, "bad build_molecule arguments");
+  const int is = is1 - 1, ib = ibox1 - 1;
+  const Species& s = c->sp[is];
+  if (!s.defined || s.nfrag < 1) return fail(CASS_ESTATE, "species not defined or without fragments");
+  if (im < 1 || im > c->max_mol[is]) return fail(CASS_EINVAL, "molecule index out of range");
+  if (s.nfrag > 1 && kappa_dih < 1) return fail(CASS_EINVAL, "kappa_dih must be >= 1");
+  if (c->box[ib].charge_style != CASS_CHARGE_NONE) return fail(CASS_EUNSUPPORTED, "build_molecule boxes hold no charges");
+  if (int rc = cbmc_ready(c)) return rc;
+  const int slot = c->mol_base[is] + im - 1;
+  const Mol& live = c->mol[slot];
+  if (del_flag && !(live.live && live.ibox == ib)) return fail(CASS_ESTATE, "del_flag: the molecule is not live in the box");
+  if (!del_flag && live.live) return fail(CASS_ESTATE, "the molecule to grow is live");
+  Mol m;
+  if (del_flag) {
+    m = live;
+  } else {
+    m.is = is;
+    m.ibox = ib;
+    m.r.assign(3 * s.natoms, 0.0);
+    m.exist.assign(s.natoms, 0);
+  }
+  Rng rng;
+  for (int k = 0; k < 5; ++k) rng.s[k] = (int64_t)rng_state[k];
+  std::vector<int> order;
+  double lp = 0.0, lb = 0.0;
+  const bool ov = build_molecule(c, ib, m, slot, del_flag != 0, kappa_ins, kappa_dih, lp, lb, rng, &order);
+  for (int k = 0; k < 5; ++k) rng_state[k] = (uint64_t)rng.s[k];
+  *ln_pseq = lp;
+  *ln_pbias = lb;
+  *cbmc_overlap = ov ? 1 : 0;
+  if (frag_order)
+    for (int k = 0; k < s.nfrag; ++k) frag_order[k] = k < (int)order.size() ? order[k] + 1 : 0;
+  if (xyz)
+    for (int k = 0; k < 3 * s.natoms; ++k) xyz[k] = del_flag ? live.r[k] : m.r[k];
+  return CASS_OK;
+}
+
 int orc_gcmc(orc_ctx* c, int32_t nboxes, const int32_t* iboxes, const CassGCMCParams* p, const double* mu,
              const double* max_disp, const double* max_rot, uint64_t seed, CassGCMCResult* out) {
   if (c) refresh_members(c);
