@@ -66,6 +66,9 @@ def parse():
     p.add_argument("--npt-chains", type=int, default=64)
     p.add_argument("--npt-eq-blocks", type=int, default=6)
     p.add_argument("--npt-blocks", type=int, default=4, help="production blocks (configurations per chain)")
+    p.add_argument("--profile-case", choices=["mixed", "fp64"], default=None,
+                   help="only the small Widom case the kernel profiles use: 16 of the benchmark boxes, 16,000 "
+                        "(mixed) or 4,096 (FP64) insertions per box, fixed cell edge, three launches")
     return p.parse_args()
 
 
@@ -297,14 +300,17 @@ def gcmc_leg(cg, abi, dev, with_cpu: bool, eq_steps: int = 150000, blocks: int =
     fp64, gf, _ = chains(abi.PREC_FP64, mu, eq_steps, nsub, sub_steps, seed=911)
     gf.close()
     z = (mixed["mean_n"] - fp64["mean_n"]) / np.sqrt(np.maximum(mixed["se_n"] ** 2 + fp64["se_n"] ** 2, 1e-12))
+    from scipy import stats as _st
+    pvals = 2.0 * _st.t.sf(np.abs(z), 3)
     dn = mixed["mean_n"] - fp64["mean_n"]
     dse = float(dn.std(ddof=1) / np.sqrt(len(dn))) if len(dn) > 1 else float("nan")
     pooled = {"mean_diff_n": float(dn.mean()), "se": dse, "z": float(dn.mean() / dse) if dse > 0 else None,
               "mean_diff_rel": float(dn.mean() / fp64["mean_n"].mean())}
     per_box = [{"mu_kjmol": round(float(m), 4), "mean_n_mixed": float(a), "se_mixed": float(sa),
                 "mean_n_fp64": float(b), "se_fp64": float(sb), "density_g_cm3_mixed": density(a),
-                "density_g_cm3_fp64": density(b), "z": float(zz)}
-               for m, a, sa, b, sb, zz in zip(mu, mixed["mean_n"], mixed["se_n"], fp64["mean_n"], fp64["se_n"], z)]
+                "density_g_cm3_fp64": density(b), "z": float(zz), "p": float(pp)}
+               for m, a, sa, b, sb, zz, pp in zip(mu, mixed["mean_n"], mixed["se_n"], fp64["mean_n"], fp64["se_n"], z,
+                                                  pvals)]
     for d in (mixed, fp64):
         del d["mean_n"], d["se_n"]
     out = {"workload": "GCMC of united-atom n-butane (CBMC kappa_ins 12, kappa_dih 12) in 16 boxes of 40 A at "
@@ -312,6 +318,9 @@ def gcmc_leg(cg, abi, dev, with_cpu: bool, eq_steps: int = 150000, blocks: int =
                        "translate/rotate 40 %, regrow 20 %; one CTA per box, all boxes in one launch",
            "mixed": mixed, "fp64": fp64, "mixed_over_fp64": mixed["moves_per_s"] / fp64["moves_per_s"],
            "density_check": {"max_abs_z": float(np.max(np.abs(z))), "rms_z": float(np.sqrt(np.mean(z ** 2))),
+               "boxes_p_below_0.01": int(np.sum(pvals < 0.01)), "min_p": float(np.min(pvals)),
+               "p_note": "two-sided p of each box's z under a Student t with 3 degrees of freedom (the top "
+                         "blocking level keeps 4 blocks, so each standard error is itself uncertain)",
                "mean_abs_rel_diff_n": float(
                np.mean([abs(p["mean_n_mixed"] / max(p["mean_n_fp64"], 1e-9) - 1) for p in per_box])),
                "pooled": pooled,
@@ -569,9 +578,35 @@ def run_reference(args, rank, world):
     print(json.dumps(out))
 
 
+def profile_case(args):
+    """The small Widom case of the ncu captures in profiles/: three launches of the
+    mixed (cells of rcut_cbmc) or FP64 (cells of rcut_cbmc / 4) kernel on 16 boxes."""
+    import cassandra_gb300 as cg
+    from cassandra_gb300 import abi, build, workloads
+    build.build()
+    nb = 16
+    s = workloads.widom_batch_system(nboxes=nb, seed=args.seed, nconfig=1000)
+    boxes = list(range(1, nb + 1))
+    mixed = args.profile_case == "mixed"
+    n = 16000 if mixed else 4096
+    with cg.open_system(s, precision=abi.PREC_MIXED if mixed else abi.PREC_FP64) as g:
+        for b in boxes:
+            g.system_total_energy(b)
+        g.set_widom_autotune(False)
+        g.set_widom_cells(1.0 if mixed else 4.0)
+        for r in range(3):
+            g.widom_insert(2, boxes, n, args.kappa, args.kappa, seed=1 + r)
+            st = g.stats()
+            print(json.dumps({"case": args.profile_case, "insertions": nb * n, "kernel_ms": st["widom_kernel_ms"],
+                              "grid": st["widom_grid_x"], "block": st["widom_block"]}))
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
+    if args.profile_case:
+        profile_case(args)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
         return

@@ -190,11 +190,15 @@ __global__ void __launch_bounds__(kBlock) k_mol_inter(BoxDev b, PairTable t, con
 // atoms, the trial's atoms in shared memory; block sum in a fixed order.
 constexpr int kTrialMaxAtoms = 64;
 
+// tcom (may be NULL): per trial its atoms' COM and max_dcom, with com the box
+// atoms' COM records, for Check_MoleculePair_Cutoff with radius rmax
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlock) k_trial_energy(BoxDev b, PairTable t, const double4_32a* __restrict__ p64,
                                                          const int4* __restrict__ meta, int n, int skip_slot,
                                                          const double4_32a* __restrict__ trial, const int* ttype,
-                                                         int nat, int cbmc, int want_qq, double* e, int* overlap) {
+                                                         int nat, int cbmc, int want_qq, const double4_32a* __restrict__ tcom,
+                                                         const double4_32a* __restrict__ com, double rmax, double* e,
+                                                         int* overlap) {
   __shared__ double4_32a qa[kTrialMaxAtoms];
   __shared__ int qt[kTrialMaxAtoms];
   __shared__ double sh[32];
@@ -213,6 +217,7 @@ __global__ void __launch_bounds__(kBlock) k_trial_energy(BoxDev b, PairTable t, 
   for (int j = threadIdx.x; j < n && !ov; j += blockDim.x) {
     const int4 mj = meta[j];
     if (mj.x == skip_slot) continue;
+    if (tcom && !molpair_in(b, rmax, tcom[blockIdx.x], com[j])) continue;
     const double4_32a pj = p64[j];
     for (int a = 0; a < nat; ++a) {
       const double dx = fold(qa[a].x - pj.x, b.hL[0], b.L[0]);
@@ -1752,7 +1757,6 @@ int cass_cbmc_trial_energies(cass_ctx* c, int32_t ibox1, int32_t is, int32_t ski
     if (atoms[a] < 1 || atoms[a] > s.natoms) return set_error(CASS_EINVAL, "trial atom index out of range");
   if (ntrial == 0) return CASS_OK;
   const int ib = ibox1 - 1;
-  if (c->box[ib].comcut) return set_error(CASS_EUNSUPPORTED, "molecule-pair COM cutoff (LJ CHARMM or minimum-image charges) is applied by the system and molecule energies only");
   int rc;
   if ((rc = set_device(c)) || (rc = pack_box(c, ib))) return rc;
   if (cbmc && (rc = ensure_cbmc(c))) return rc;
@@ -1765,23 +1769,55 @@ int cass_cbmc_trial_energies(cass_ctx* c, int32_t ibox1, int32_t is, int32_t ski
       const double* x = xyz + ((size_t)k * nat + a) * 3;
       tr[(size_t)k * nat + a] = make_double4_32a(x[0], x[1], x[2], s.q[atoms[a] - 1]);
     }
+  // Check_MoleculePair_Cutoff where a style has no atom cutoff: the COM and
+  // max_dcom of each trial's atoms (get_com.f90:45-105, 220-295)
+  std::vector<double4_32a> tcom;
+  if (B.comcut)
+    for (int k = 0; k < ntrial; ++k) {
+      double tm = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
+      for (int a = 0; a < nat; ++a) {
+        const double m = s.mass[atoms[a] - 1];
+        const double4_32a& p = tr[(size_t)k * nat + a];
+        tm = tm + m;
+        cx = cx + m * p.x;
+        cy = cy + m * p.y;
+        cz = cz + m * p.z;
+      }
+      cx = cx / tm;
+      cy = cy / tm;
+      cz = cz / tm;
+      double dmax = 0.0;
+      for (int a = 0; a < nat; ++a) {
+        const double4_32a& p = tr[(size_t)k * nat + a];
+        const double dx = p.x - cx, dy = p.y - cy, dz = p.z - cz;
+        dmax = std::max(dmax, dx * dx + dy * dy + dz * dz);
+      }
+      tcom.push_back(make_double4_32a(cx, cy, cz, std::sqrt(dmax)));
+    }
   const size_t tb = tr.size() * sizeof(double4_32a);
-  if ((rc = c->d_trial.reserve(tb + (size_t)nat * sizeof(int) + (size_t)ntrial * (sizeof(double) + sizeof(int)) + 64)))
+  const size_t cb = tcom.size() * sizeof(double4_32a);
+  if ((rc = c->d_trial.reserve(tb + cb + (size_t)nat * sizeof(int) + (size_t)ntrial * (sizeof(double) + sizeof(int)) + 64)))
     return rc;
   double4_32a* d_tr = c->d_trial.as<double4_32a>();
-  int* d_tt = reinterpret_cast<int*>(d_tr + tr.size());
+  double4_32a* d_tcom = B.comcut ? d_tr + tr.size() : nullptr;
+  int* d_tt = reinterpret_cast<int*>(d_tr + tr.size() + tcom.size());
   double* d_e = reinterpret_cast<double*>(reinterpret_cast<char*>(d_tt) + (((size_t)nat * sizeof(int) + 7) & ~(size_t)7));
   int* d_ov = reinterpret_cast<int*>(d_e + ntrial);
   CASS_CUDA(h2d(c, d_tr, tr.data(), tb));
+  if (B.comcut) CASS_CUDA(h2d(c, d_tcom, tcom.data(), cb));
   CASS_CUDA(h2d(c, d_tt, tt.data(), (size_t)nat * sizeof(int)));
+  const double4_32a* d_com = B.comcut ? B.d_com.as<double4_32a>() : nullptr;
+  const double rmax = cbmc ? B.desc.rcut_cbmc : B.rcut_max;
   const int skip_slot = skip_im > 0 ? mol_slot(c, skip_im, is) : -1;
   const int want_qq = (cbmc && !s.l_coul_cbmc) ? 0 : 1;  // Compute_MoleculePair_Energy, energy_routines.f90:1684-1686
   if (c->precision == CASS_PREC_MIXED)
     k_trial_energy<true><<<ntrial, kBlock, 0, c->stream>>>(B.dev, c->pt, B.d_p64.as<double4_32a>(), B.d_meta.as<int4>(),
-                                                           B.npacked, skip_slot, d_tr, d_tt, nat, cbmc, want_qq, d_e, d_ov);
+                                                           B.npacked, skip_slot, d_tr, d_tt, nat, cbmc, want_qq, d_tcom,
+                                                           d_com, rmax, d_e, d_ov);
   else
     k_trial_energy<false><<<ntrial, kBlock, 0, c->stream>>>(B.dev, c->pt, B.d_p64.as<double4_32a>(), B.d_meta.as<int4>(),
-                                                            B.npacked, skip_slot, d_tr, d_tt, nat, cbmc, want_qq, d_e, d_ov);
+                                                            B.npacked, skip_slot, d_tr, d_tt, nat, cbmc, want_qq, d_tcom,
+                                                            d_com, rmax, d_e, d_ov);
   CASS_CUDA(cudaGetLastError());
   count_launch(c);
   CASS_CUDA(d2h(c, e, d_e, (size_t)ntrial * sizeof(double)));

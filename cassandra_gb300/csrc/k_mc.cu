@@ -73,12 +73,17 @@ struct McBox {
   double* new_cos;  // scratch [nvecs]
   double* new_sin;
   int nvecs, ewald;
+  // Check_MoleculePair_Cutoff decides which molecule pairs interact (LJ CHARMM,
+  // minimum-image charges): COM distance against rmax + both max_dcom
+  int comcut;
+  double rmax;
   double* max_disp;   // [nspecies] in/out
   double* max_rot;
   CassEnergy* energy;  // in/out
   CassMCResult* res;   // out
   int* status;         // out: 0 ok, 1 overlapping molecule before a move
-  unsigned char* gbox; // the box layout in global memory (boxes too large for shared memory)
+  unsigned char* gbox; // the box layout in global memory (boxes too large for shared memory),
+  size_t gbox_stride;  // one copy per CTA of the box's cluster, this many bytes apart
 };
 
 // the move thread 0 prepared for the block
@@ -157,8 +162,8 @@ __device__ __forceinline__ void cluster_sum(int csize, double (*cd)[4], int (*ci
 
 // GMEM: the box layout lives in a per-box global buffer (L2-resident) instead
 // of shared memory, for boxes above the shared-memory limit; same code.
-// csize > 1 (shared-memory boxes only): a thread-block cluster of csize CTAs
-// runs one box's chain.  Every CTA holds the whole box and makes the same
+// csize > 1: a thread-block cluster of csize CTAs runs one box's chain (a box
+// in global memory has one layout copy per CTA).  Every CTA holds the whole box and makes the same
 // serial decisions from the same lfsr258 stream; the pair loop over the box
 // atoms and the k-vector loop are split over the CTAs, whose partial sums are
 // added in rank order through distributed shared memory, and each CTA commits
@@ -175,29 +180,35 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
   __shared__ float2 ljp[kMaxTypes * kMaxTypes];
   __shared__ double cd[2][4];  // this CTA's partial sums for the cluster (alternating buffers)
   __shared__ int ci[2][2];
+  __shared__ McBox G;  // the box descriptor, read by the serial steps of every move
   const int crank = (int)(blockIdx.x % (unsigned)csize);
   int cbuf = 0;
-  McBox& G = boxes[blockIdx.x / csize];
-  if (threadIdx.x == 0) b = G.b;
+  if (threadIdx.x == 0) {
+    G = boxes[blockIdx.x / csize];
+    b = G.b;
+  }
+  __syncthreads();
   for (int i = threadIdx.x; i < kMaxTypes * kMaxTypes; i += blockDim.x) {
     const int a = i / kMaxTypes, c = i % kMaxTypes;
     const bool ok = a < T.ntypes && c < T.ntypes;
     ljp[i] = ok ? make_float2(T.epsf[a * T.ntypes + c], T.sig2f[a * T.ntypes + c]) : make_float2(0.f, 0.f);
   }
   const int N = G.natoms, M = G.nmols;
-  unsigned char* smem = GMEM ? G.gbox : dsmem;
+  unsigned char* smem = GMEM ? G.gbox + (size_t)crank * G.gbox_stride : dsmem;
   // shared layout: x y z q (double), type, mol (int), [x y z type (float4), q (float)], COM (double x3), first, nat
   double* sx = reinterpret_cast<double*>(smem);
   double* sy = sx + N;
   double* sz = sy + N;
   double* sq = sz + N;
   double* com = sq + N;  // [M][3]
-  int* stype = reinterpret_cast<int*>(com + 3 * M);
+  double* dcom = com + 3 * M;  // [M] max_dcom (Compute_Max_Com_Distance, get_com.f90:220-295)
+  int* stype = reinterpret_cast<int*>(dcom + M);
   int* smol = stype + N;
   int* mfirst = smol + N;
   int* mnat = mfirst + M;
+  int* mslot = mnat + M;  // molecule slot (the cos_mol / sin_mol row)
   float4* s32 = reinterpret_cast<float4*>(reinterpret_cast<unsigned char*>(smem) +
-                                          ((((size_t)(mnat + M) - (size_t)smem) + 15) & ~(size_t)15));
+                                          ((((size_t)(mslot + M) - (size_t)smem) + 15) & ~(size_t)15));
   float* sq32 = reinterpret_cast<float*>(s32 + (MIXED ? N : 0));
   for (int j = threadIdx.x; j < N; j += blockDim.x) {
     const double4_32a p = G.p64[j];
@@ -215,6 +226,7 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
     const int4 mi = G.molinfo[m];
     mfirst[m] = mi.z;
     mnat[m] = mi.w;
+    mslot[m] = mi.x;
     for (int a = 0; a < mi.w; ++a) smol[mi.z + a] = m;
   }
   __syncthreads();
@@ -232,6 +244,13 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
     com[3 * m] = x / tm;
     com[3 * m + 1] = y / tm;
     com[3 * m + 2] = z / tm;
+    double dmax = 0.0;  // rigid moves keep it
+    for (int a = 0; a < mnat[m]; ++a) {
+      const int j = mfirst[m] + a;
+      const double dx = sx[j] - com[3 * m], dy = sy[j] - com[3 * m + 1], dz = sz[j] - com[3 * m + 2];
+      dmax = fmax(dmax, dx * dx + dy * dy + dz * dz);
+    }
+    dcom[m] = sqrt(dmax);
   }
   // thread 0 state
   Lfsr rng;
@@ -277,7 +296,7 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
         mv.pm = pm;
         mv.na = mnat[pm];
         mv.first = mfirst[pm];
-        mv.slot = G.molinfo[pm].x;
+        mv.slot = mslot[pm];
         mv.ewald = G.ewald && s.has_charge;
         for (int a = 0; a < mv.na; ++a) {
           const int j = mv.first + a;
@@ -410,12 +429,24 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
       pdq = kq.value();
     } else {
       for (int j = j0; j < N; j += jstep) {
-        if (smol[j] == pm) continue;
+        const int mj = smol[j];
+        if (mj == pm) continue;
         const double xj = sx[j], yj = sy[j], zj = sz[j], qj = sq[j];
         const int tj = stype[j];
+        bool in[2] = {true, true};
+        if (G.comcut)  // Check_MoleculePair_Cutoff (energy_routines.f90:3027-3088), old and trial COM
+#pragma unroll
+          for (int w = 0; w < 2; ++w) {
+            const double* cw = w ? mv.com_new : com + 3 * pm;
+            const double dx = fold(cw[0] - com[3 * mj], b.hL[0], b.L[0]);
+            const double dy = fold(cw[1] - com[3 * mj + 1], b.hL[1], b.L[1]);
+            const double dz = fold(cw[2] - com[3 * mj + 2], b.hL[2], b.L[2]);
+            in[w] = !(sqrt(dx * dx + dy * dy + dz * dz) > G.rmax + dcom[pm] + dcom[mj]);
+          }
         for (int a = 0; a < na; ++a) {
 #pragma unroll
           for (int w = 0; w < 2; ++w) {
+            if (!in[w]) continue;
             const double* r = w ? mv.trial : mv.old_r;
             const double dx = fold(r[3 * a] - xj, b.hL[0], b.L[0]);
             const double dy = fold(r[3 * a + 1] - yj, b.hL[1], b.L[1]);
@@ -649,7 +680,7 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
 }
 
 size_t mc_smem_bytes(int natoms, int nmols, bool mixed) {
-  size_t s = (size_t)natoms * (4 * sizeof(double) + 2 * sizeof(int)) + (size_t)nmols * (3 * sizeof(double) + 2 * sizeof(int));
+  size_t s = (size_t)natoms * (4 * sizeof(double) + 2 * sizeof(int)) + (size_t)nmols * (4 * sizeof(double) + 3 * sizeof(int));
   s = (s + 15) & ~(size_t)15;
   if (mixed) s += (size_t)natoms * (sizeof(float4) + sizeof(float));
   return s;
@@ -676,7 +707,6 @@ extern "C" int cass_mc_sweeps(cass_ctx* c, int32_t nboxes, const int32_t* iboxes
     for (int j = 0; j < k; ++j)
       if (iboxes[j] == iboxes[k]) return set_error(CASS_EINVAL, "box listed twice");
     if (!c->box[ib].energy_valid) return set_error(CASS_ESTATE, "system energy of box not computed");
-    if (c->box[ib].comcut) return set_error(CASS_EUNSUPPORTED, "molecule-pair COM cutoff (LJ CHARMM or minimum-image charges) is applied by the system and molecule energies only");
   }
   int rc;
   CASS_CUDA(cudaSetDevice(c->device));
@@ -763,6 +793,8 @@ extern "C" int cass_mc_sweeps(cass_ctx* c, int32_t nboxes, const int32_t* iboxes
       g.first_sp[is] = first;
       first += n;
     }
+    g.comcut = B.comcut ? 1 : 0;
+    g.rmax = B.rcut_max;
     g.ewald = B.desc.charge_style == CASS_CHARGE_COUL && B.desc.charge_sum_style == CASS_QQ_EWALD && B.nvecs > 0;
     g.nvecs = g.ewald ? B.nvecs : 0;
     g.kvec = B.d_kvec.as<double4_32a>();
@@ -777,17 +809,7 @@ extern "C" int cass_mc_sweeps(cass_ctx* c, int32_t nboxes, const int32_t* iboxes
     g.status = d_status + k;
     hE[k] = B.energy;
   }
-  if (gmem) {
-    std::vector<size_t> off(nboxes);
-    size_t tot = 0;
-    for (int k = 0; k < nboxes; ++k) {
-      off[k] = tot;
-      tot += (mc_smem_bytes(hb[k].natoms, hb[k].nmols, mixed) + 255) & ~(size_t)255;
-    }
-    if ((rc = c->d_mc_box.reserve(std::max<size_t>(tot, 256)))) return rc;
-    for (int k = 0; k < nboxes; ++k) hb[k].gbox = static_cast<unsigned char*>(c->d_mc_box.p) + off[k];
-  }
-  CASS_CUDA(h2d(c, d_box, hb.data(), nboxes * sizeof(McBox)));
+
   CASS_CUDA(h2d(c, d_E, hE.data(), nboxes * sizeof(CassEnergy)));
   CASS_CUDA(h2d(c, d_md, max_disp, nboxes * nsp * sizeof(double)));
   CASS_CUDA(h2d(c, d_mr, max_rot, nboxes * nsp * sizeof(double)));
@@ -799,14 +821,18 @@ extern "C" int cass_mc_sweeps(cass_ctx* c, int32_t nboxes, const int32_t* iboxes
   CASS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
   const int threads = gmem ? kMcThreadsG : kMcThreads;
   // CTAs per chain: a cluster splits the pair and k-vector loops of a move when
-  // SMs would otherwise stay idle (few chains); every cluster must be resident
+  // SMs would otherwise stay idle (few chains); every cluster must be resident.
+  // Measured on single chains (sweeps/s, 1 -> best cluster): FP64 LJ-500
+  // 117 -> 218 at 4 CTAs, FP64 water-256 with Ewald 20 -> 100 at 8, mixed
+  // water-256 143 -> 288 at 8, while mixed LJ-500 (FP32 pairs, no k-space) is
+  // bound by the serial steps of a move and loses a little (307 -> 278-292).
   int csize = 1;
-  if (!gmem) {
+  {
     int sms = 0, nmax = 1;
     CASS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
     for (const McBox& g : hb) nmax = std::max(nmax, g.natoms);
     int want = c->mc_cluster > 0 ? c->mc_cluster : std::min(8, std::max(1, sms / nboxes));
-    if (c->mc_cluster <= 0) want = std::min(want, std::max(1, (nmax + 63) / 64));
+    if (c->mc_cluster <= 0) want = std::min(want, any_ewald ? 8 : (mixed ? 1 : std::max(1, (nmax + 127) / 128)));
     for (int cs = std::min(8, want); cs >= 2; --cs) {
       cudaLaunchConfig_t q = {};
       cudaLaunchAttribute qa[1];
@@ -828,6 +854,21 @@ extern "C" int cass_mc_sweeps(cass_ctx* c, int32_t nboxes, const int32_t* iboxes
     }
   }
   c->stats.gcmc_cluster = csize;
+  if (gmem) {  // one layout per CTA of each box's cluster
+    std::vector<size_t> off(nboxes), stride(nboxes);
+    size_t tot = 0;
+    for (int k = 0; k < nboxes; ++k) {
+      off[k] = tot;
+      stride[k] = (mc_smem_bytes(hb[k].natoms, hb[k].nmols, mixed) + 255) & ~(size_t)255;
+      tot += stride[k] * csize;
+    }
+    if ((rc = c->d_mc_box.reserve(std::max<size_t>(tot, 256)))) return rc;
+    for (int k = 0; k < nboxes; ++k) {
+      hb[k].gbox = static_cast<unsigned char*>(c->d_mc_box.p) + off[k];
+      hb[k].gbox_stride = stride[k];
+    }
+  }
+  CASS_CUDA(h2d(c, d_box, hb.data(), nboxes * sizeof(McBox)));
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
