@@ -736,7 +736,11 @@ def main():
                     "frac_within_1e-5": float((rel <= 1e-5).mean()) if rel.size else None,
                     "e_inter_max_rel_err_of_abs_E": float(rel_e.max()) if rel_e.size else None,
                     "e_inter_median_rel_err_of_abs_E": float(np.median(rel_e)) if rel_e.size else None,
-                    "insertions_compared": int(same.size)}
+                    "insertions_compared": int(same.size),
+                    "fp64_fixups": int(gctx.stats()["widom_fixups"]),
+                    "note": "pairs whose FP32 r^2 lies within rounding of a cutoff are decided again in FP64 "
+                            "(k_widom_fix, fp64_fixups insertions here), so every cutoff and overlap decision "
+                            "is the FP64 one; the error left is the FP32 rounding of coordinates"}
         fctx.close()
 
     # roofline of the Widom kernel
@@ -787,7 +791,8 @@ def main():
                       "sharding": "each rank owns its own boxes (rank r: boxes seeded by r), per-rank work fixed; "
                                   "per-box Widom accumulators merged by one all-reduce after the timed steps"},
            "widom_launch": {"ctas_per_box": st["widom_grid_x"], "threads": st["widom_block"],
-                            "smem_bytes": st["widom_smem_bytes"],
+                            "smem_bytes": st["widom_smem_bytes"], "fp64_fixups": int(st["widom_fixups"]),
+                            "fp64_fixup_fraction": st["widom_fixups"] / float(n_per_box * len(boxes)),
                             "note": "shape chosen by the library's launch autotuner on its first call"},
            "gpu_launches": int(launches),
            "wall_s": t_wall,
@@ -804,7 +809,8 @@ def main():
                         "frac": achieved_tf / fp32_peak, "traffic": traffic,
                         "pairs_visited": st["widom_pairs_visited"], "pairs_in_cutoff": st["widom_pairs_in_cutoff"],
                         "in_cutoff_only": {"achieved": achieved_alg_tf, "frac": achieved_alg_tf / fp32_peak},
-                        "note": "the Widom kernel (one warp per insertion); 15 FP32 ops per visited candidate pair "
+                        "note": "the Widom kernels (k_widom_f32, one thread per insertion, then k_widom_fix for the "
+                                "insertions it queues; kernel_ms spans both); 15 FP32 ops per visited candidate pair "
                                 "+ 8 per in-cutoff LJ pair, pairs counted by the kernel in an extra untimed pass; "
                                 "peak is nominal (SMs x 128 FP32 lanes x 2 x max SM clock): the measured-peak file "
                                 "has no FP32 figure; traffic = DRAM bytes per launch scaled from the ncu capture "

@@ -124,7 +124,7 @@ class CassStats(C.Structure):
                 ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("widom_pairs_visited", C.c_int64),
                 ("widom_pairs_in_cutoff", C.c_int64), ("widom_grid_x", C.c_int32), ("widom_grid_y", C.c_int32),
                 ("widom_block", C.c_int32), ("widom_smem_bytes", C.c_int32), ("mc_ms", C.c_double),
-                ("mc_moves", C.c_int64), ("gcmc_cluster", C.c_int32), ("reserved", C.c_int32)]
+                ("mc_moves", C.c_int64), ("gcmc_cluster", C.c_int32), ("widom_fixups", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -189,11 +189,12 @@ SIGNATURES = {
                                  C.POINTER(C.c_uint64), _i32p, _f64p, _f64p, _f64p, _i32p]),
     "set_count_pairs": (C.c_int, [C.c_void_p, C.c_int32]),
     "set_mc_cluster": (C.c_int, [C.c_void_p, C.c_int32]),
+    "set_widom_band": (C.c_int, [C.c_void_p, C.c_double]),
     "set_widom_cells": (C.c_int, [C.c_void_p, C.c_double]),
     "set_widom_autotune": (C.c_int, [C.c_void_p, C.c_int32]),
     "set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
-OPTIONAL = {"get_stats", "set_count_pairs", "set_mc_cluster", "set_widom_cells", "set_widom_autotune", "set_stream", "mol_box_energy_noalloc", "system_gradient", "gcmc",
+OPTIONAL = {"get_stats", "set_count_pairs", "set_mc_cluster", "set_widom_band", "set_widom_cells", "set_widom_autotune", "set_stream", "mol_box_energy_noalloc", "system_gradient", "gcmc",
             "traj_open", "traj_next", "traj_stats", "traj_close", "load_next_frame"}
 
 
@@ -391,6 +392,10 @@ class Context:
     def set_widom_cells(self, cells_per_cutoff: float) -> None:
         """Widom cell edge = rcut_cbmc / cells_per_cutoff (0: the precision's default)."""
         self._check("set_widom_cells", self._f["set_widom_cells"](self._h, float(cells_per_cutoff)))
+
+    def set_widom_band(self, scale: float) -> None:
+        """Scale (>= 1) of the FP32 cutoff bands whose pairs the mixed Widom pass decides in FP64."""
+        self._check("set_widom_band", self._f["set_widom_band"](self._h, float(scale)))
 
     def set_mc_cluster(self, ctas: int) -> None:
         """CTAs per chain of mc_sweeps (0: chosen per call)."""

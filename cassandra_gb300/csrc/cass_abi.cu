@@ -1217,6 +1217,12 @@ int cass_set_widom_cells(cass_ctx* c, double cells_per_cutoff) {
   return CASS_OK;
 }
 
+int cass_set_widom_band(cass_ctx* c, double scale) {
+  if (!c || !(scale >= 1.0 && scale <= 1.0e4)) return set_error(CASS_EINVAL, "scale must be in [1, 1e4]");
+  c->widom_band = scale;
+  return CASS_OK;
+}
+
 int cass_set_mc_cluster(cass_ctx* c, int32_t ctas) {
   if (!c || ctas < 0 || ctas > 8) return set_error(CASS_EINVAL, "ctas must be in [0, 8]");
   c->mc_cluster = ctas;

@@ -41,6 +41,12 @@ struct BoxF {
   const float* tab_v;
   const float* tab_f2;
   float rmin2[kMaxTypes * kMaxTypes];  // row stride kMaxTypes
+  // Widom full-cutoff pass: FP64 box edges and squared cutoffs, and the half
+  // widths (A^2) of the bands about rv2, rq2 and low2 inside which an FP32 r^2
+  // can fall on the other side of a cutoff than the FP64 r^2
+  double L64[3], hL64[3];
+  double rv2d, rq2d, low2d;
+  float band_v, band_q, band_low;
 };
 
 // the CBMC-option fields of f from the box's BoxDev; thread 0 then all threads

@@ -179,6 +179,7 @@ struct cass_ctx_impl {
   int count_pairs = 0;
   double widom_cells = 0.0;  // cells per rcut_cbmc in the Widom cell lists (0: default)
   int widom_waves = 0;       // CTAs per resident slot of the FP32 Widom launch (0: default)
+  double widom_band = 1.0;   // scale of the FP32 cutoff bands of the mixed Widom full-cutoff pass
   int mc_cluster = 0;        // CTAs per chain of cass_mc_sweeps (0: chosen per call)
   // launch shapes the Widom autotuner chose, per batch signature: (cells per cutoff, waves)
   bool widom_autotune = true;
@@ -219,7 +220,7 @@ struct cass_ctx_impl {
   std::vector<double> h_result;
   // cell-sorted arrays of the boxes of the last Widom batch
   DevBuf d_c64, d_c32, d_cq32, d_cell_start, d_cell_count, d_cell_of, d_boxdev, d_widom_out, d_widom_xyz,
-      d_trace, d_box_sums;
+      d_trace, d_box_sums, d_widom_fix;
   std::vector<int> widom_boxes;
   // CBMC options and the tables they derive (energy table per box, r_min^2)
   CassCBMCOptions cbmc_opt{};

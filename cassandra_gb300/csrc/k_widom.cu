@@ -705,16 +705,41 @@ __device__ void run_insertion(const WidomSpecies& S, const SpeciesPools& P, cons
 struct BoxViewF {
   const BoxF* f;
   const float4* p32;   // cell-sorted atoms (x, y, z, type bits), smem or global
+  const double4_32a* p64;  // the same atoms in FP64 (global): cutoff decisions near a cutoff
   const float* q32;    // their charges (global)
   const int* cstart;   // cell starts, local atom indices, smem or global
   const float2* ljp;   // (eps, sigma^2) [kMaxTypes][kMaxTypes], smem
 };
 
+// A pair of the full-cutoff pass whose FP32 r^2 lies within the band of a
+// cutoff (kind 0: rcut_vdw^2 or rcut_coul^2; kind 1: rcut_low^2) where the
+// FP32 and the FP64 decisions can differ: box atom j, test atom `atom`
+struct BandPair {
+  int j;
+  float r2;
+  unsigned char atom, kind, pad0, pad1;
+};
+constexpr int kMaxBand = 4;
+
 struct QueryAcc {
   KahanF e;
   float eabs = 0.0f;
   unsigned long long visited = 0, in_cut = 0;
+  int nband = 0, atom = 0;      // kQDetect: band pairs met, the current test atom
+  BandPair* band = nullptr;     // kQDetect: the first kMaxBand of them
 };
+
+// Query modes.  kQPlain: FP32 decisions.  kQDetect (the full-cutoff pass of
+// the FP32 growth): FP32 decisions, every pair within a band noted in A (a
+// pair in the band of rcut_low^2 counts as no overlap and adds its energy;
+// only an FP32 r^2 below the band is a certain overlap).  kQExact: decisions
+// inside a band made in FP64 from the FP64 coordinates p64.
+constexpr int kQPlain = 0, kQDetect = 1, kQExact = 2;
+
+__device__ __forceinline__ void band_note(QueryAcc& A, int j, float r2, int kind) {
+  if (A.nband < kMaxBand) A.band[A.nband] = BandPair{j, r2, (unsigned char)A.atom, (unsigned char)kind, 0, 0};
+  ++A.nband;
+}
 
 // r^2 to a stored atom, through the row's image shift (folded in full dimensions)
 __device__ __forceinline__ float pair_r2(const BoxF& f, const bool (&full)[3], bool fold_any, float qx, float qy,
@@ -761,20 +786,54 @@ __device__ __forceinline__ void row_x_cells_f(const BoxF& f, float px, float rem
   hi = fullx ? f.nc[0] - 1 : h;
 }
 
-// LJ and real-space Ewald energy of one pair inside the selection radius
-template <bool COUNT>
+// FP64 minimum-image r^2 between p and cell-sorted atom j, as the FP64 query
+// forms it (Minimum_Image_Separation, orthorhombic branch)
+__device__ __noinline__ double exact_r2(const BoxF& f, const double4_32a* p64, int j, const double* p) {
+  const double4_32a a = p64[j];
+  const double dx = fold(p[0] - a.x, f.hL64[0], f.L64[0]);
+  const double dy = fold(p[1] - a.y, f.hL64[1], f.L64[1]);
+  const double dz = fold(p[2] - a.z, f.hL64[2], f.L64[2]);
+  return dx * dx + dy * dy + dz * dz;
+}
+
+// Core overlap of the full-cutoff pass: an FP32 r^2 within band_low of
+// rcut_low^2 is decided from the FP64 coordinates
+__device__ __forceinline__ bool overlap_exact(const BoxViewF& V, float r2, int j, const double* p64) {
+  const BoxF& f = *V.f;
+  if (r2 < f.low2 - f.band_low) return true;
+  if (r2 >= f.low2 + f.band_low) return false;
+  return exact_r2(f, V.p64, j, p64) < f.low2d;
+}
+
+// LJ and real-space Ewald energy of one pair inside the selection radius.
+// kQDetect flags a pair at or above the lower edge rlo of the cutoff bands;
+// kQExact compares an FP32 r^2 within a band of the vdW or Coulomb cutoff with
+// the cutoff in FP64, from the FP64 coordinates, so that the pair counts
+// exactly when the FP64 energy counts it.
+template <bool COUNT, int MODE = kQPlain>
 __device__ __forceinline__ void pair_energy(const BoxViewF& V, QueryAcc& A, const float4& a, int j, float r2,
                                             const float2* lrow, bool vdw_on, bool qq_on, float rv2, float rq2,
-                                            float qa) {
+                                            float qa, float rlo = 0.0f, const double* p64 = nullptr) {
+  bool in_v = r2 <= rv2, in_q = r2 <= rq2;
+  if (MODE == kQDetect && r2 >= rlo) band_note(A, j, r2, 0);
+  if (MODE == kQExact) {
+    const BoxF& f = *V.f;
+    if (fabsf(r2 - rv2) <= f.band_v || fabsf(r2 - rq2) <= f.band_q) {
+      const double d2 = exact_r2(f, V.p64, j, p64);
+      in_v = d2 <= f.rv2d;
+      in_q = d2 <= f.rq2d;
+    }
+    if (!in_v && !in_q) return;
+  }
   if (COUNT) ++A.in_cut;
   const int tj = __float_as_int(a.w);
-  if (vdw_on && tj >= 0 && r2 <= rv2) {
+  if (vdw_on && tj >= 0 && in_v) {
     const float2 es = lrow[tj];
     const float ev = lj_pair_f(es.x, es.y, r2);
     A.e.add(ev);
     A.eabs += fabsf(ev);
   }
-  if (qq_on && r2 <= rq2) {
+  if (qq_on && in_q) {
     const float eq = qq_ewald_inter_f(V.f->alpha, qa * V.q32[j], r2);
     A.e.add(eq);
     A.eabs += fabsf(eq);
@@ -861,9 +920,11 @@ __device__ bool query_f_opt(const BoxViewF& V, QueryAcc& A, float px, float py, 
   return false;
 }
 
-template <bool COUNT, bool OPT = false>
+// MODE: kQPlain, kQDetect or kQExact (then p64 holds the FP64 coordinates of
+// the query atom).
+template <bool COUNT, bool OPT = false, int MODE = kQPlain>
 __device__ bool query_f(const BoxViewF& V, QueryAcc& A, float px, float py, float pz, int ta, float qa, bool cbmc,
-                        bool want_qq) {
+                        bool want_qq, const double* p64 = nullptr) {
   if (OPT && cbmc) return query_f_opt(V, A, px, py, pz, ta, qa);
   const BoxF& f = *V.f;
   const float rc = cbmc ? f.rc_cbmc : f.rc_full;
@@ -885,7 +946,12 @@ __device__ bool query_f(const BoxViewF& V, QueryAcc& A, float px, float py, floa
   const float low2 = f.low2;
   const bool vdw_on = ta >= 0;
   const bool qq_on = want_qq && f.charge_on && qa != 0.0f;
-  const float rsel2 = fmaxf(vdw_on ? rv2 : -1.0f, qq_on ? rq2 : -1.0f);
+  // the selection and overlap radii, widened by the FP32 bands in the
+  // kQDetect and kQExact modes; rlo: the lower edge of the cutoff bands
+  const float band = MODE != kQPlain ? fmaxf(vdw_on ? f.band_v : 0.0f, qq_on ? f.band_q : 0.0f) : 0.0f;
+  const float rsel2 = fmaxf(vdw_on ? rv2 : -1.0f, qq_on ? rq2 : -1.0f) + band;
+  const float low2q = MODE != kQPlain ? low2 + f.band_low : low2;
+  const float rlo = fminf(vdw_on ? rv2 : 3.0e38f, qq_on ? rq2 : 3.0e38f) - band;
   const float rc2 = rc * rc;
   const float2* lrow = V.ljp + (vdw_on ? ta : 0) * kMaxTypes;
   const int nc0 = f.nc[0], nc1 = f.nc[1], nc2 = f.nc[2];
@@ -927,15 +993,32 @@ __device__ bool query_f(const BoxViewF& V, QueryAcc& A, float px, float py, floa
             r20 = pair_r2(f, fl, fold_any, qx, qy, qz, a0);
             r21 = pair_r2(f, fl, fold_any, qx, qy, qz, a1);
           }
-          if (fminf(r20, r21) < low2) return true;
-          if (r20 <= rsel2) pair_energy<COUNT>(V, A, a0, j, r20, lrow, vdw_on, qq_on, rv2, rq2, qa);
-          if (r21 <= rsel2) pair_energy<COUNT>(V, A, a1, j + 1, r21, lrow, vdw_on, qq_on, rv2, rq2, qa);
+          if (fminf(r20, r21) < low2q) {
+            if (MODE == kQPlain) return true;
+            if (MODE == kQDetect) {
+              if (fminf(r20, r21) < low2 - f.band_low) return true;  // a certain overlap
+              if (r20 < low2q) band_note(A, j, r20, 1);
+              if (r21 < low2q) band_note(A, j + 1, r21, 1);
+            } else if (overlap_exact(V, r20, j, p64) || overlap_exact(V, r21, j + 1, p64)) {
+              return true;
+            }
+          }
+          if (r20 <= rsel2) pair_energy<COUNT, MODE>(V, A, a0, j, r20, lrow, vdw_on, qq_on, rv2, rq2, qa, rlo, p64);
+          if (r21 <= rsel2) pair_energy<COUNT, MODE>(V, A, a1, j + 1, r21, lrow, vdw_on, qq_on, rv2, rq2, qa, rlo, p64);
         }
         if (j < j1) {
           const float4 a0 = V.p32[j];
           const float r20 = pair_r2(f, fl, fold_any, qx, qy, qz, a0);
-          if (r20 < low2) return true;
-          if (r20 <= rsel2) pair_energy<COUNT>(V, A, a0, j, r20, lrow, vdw_on, qq_on, rv2, rq2, qa);
+          if (r20 < low2q) {
+            if (MODE == kQPlain) return true;
+            if (MODE == kQDetect) {
+              if (r20 < low2 - f.band_low) return true;
+              band_note(A, j, r20, 1);
+            } else if (overlap_exact(V, r20, j, p64)) {
+              return true;
+            }
+          }
+          if (r20 <= rsel2) pair_energy<COUNT, MODE>(V, A, a0, j, r20, lrow, vdw_on, qq_on, rv2, rq2, qa, rlo, p64);
         }
         cx += run;
       }
@@ -944,11 +1027,188 @@ __device__ bool query_f(const BoxViewF& V, QueryAcc& A, float px, float py, floa
   return false;
 }
 
-// Record of one insertion (FP32 parts)
+// Record of one insertion (FP32 parts; the full-cutoff energy as a two-term sum)
 struct RecF {
-  float dE_intra, e_inter, dE_frag, ln_pbias, e_abs, first_sum;
+  float dE_intra, dE_frag, ln_pbias, e_abs, first_sum;
+  double e_inter;
   int status, selected;
+  bool fix;  // the full-cutoff pass met a band: k_widom_fix redoes it
 };
+
+// An insertion queued for k_widom_fix: its index in the box and the choices of
+// its FP32 growth (growth order, first-fragment trial, dihedral trials)
+struct FixEntry {
+  int ins;
+  unsigned char sel, norder, pad0, pad1;
+  unsigned char order[kMaxFrags];
+  unsigned char trl[kMaxFrags];
+  int nband;                   // band pairs met (more than kMaxBand: the pass is redone)
+  BandPair band[kMaxBand];
+};
+
+// Get_Aligner_Hanger with reciprocal square roots (row-major): the frame of
+// aligner_hanger to a few ulps
+__device__ inline void aligner_hanger_rs(double v1[3], double v2[3], double al[9], double hg[9]) {
+  const double n1 = rsqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+  for (int i = 0; i < 3; ++i) v1[i] = v1[i] * n1;
+  const double n2 = rsqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
+  for (int i = 0; i < 3; ++i) v2[i] = v2[i] * n2;
+  double p1[3] = {v1[1] * v2[2] - v1[2] * v2[1], -v1[0] * v2[2] + v1[2] * v2[0], v1[0] * v2[1] - v1[1] * v2[0]};
+  const double np1 = rsqrt(p1[0] * p1[0] + p1[1] * p1[1] + p1[2] * p1[2]);
+  for (int i = 0; i < 3; ++i) p1[i] = p1[i] * np1;
+  double p2[3] = {v1[1] * p1[2] - v1[2] * p1[1], -v1[0] * p1[2] + v1[2] * p1[0], v1[0] * p1[1] - v1[1] * p1[0]};
+  const double np2 = rsqrt(p2[0] * p2[0] + p2[1] * p2[1] + p2[2] * p2[2]);
+  for (int i = 0; i < 3; ++i) p2[i] = p2[i] * np2;
+  for (int i = 0; i < 3; ++i) {
+    al[i] = v1[i];
+    al[3 + i] = p2[i];
+    al[6 + i] = p1[i];
+    hg[i * 3 + 0] = v1[i];
+    hg[i * 3 + 1] = p2[i];
+    hg[i * 3 + 2] = p1[i];
+  }
+}
+
+// The grown molecule again in FP64 (the arithmetic of run_insertion): the
+// same lfsr258 stream from the insertion's first draw, the choices the FP32
+// growth made (first fragment and order, selected first-fragment trial, the
+// selected dihedral trial of each later fragment) and the FP64 fragment
+// library.  Library conformations are taken with the same 32-bit rule as the
+// FP32 growth; every geometry uniform is the full FP64 draw, and the angles'
+// sines and cosines and the frames' normalisations agree with the FP64 path's
+// to a few ulps, so the coordinates are those of the FP64 path for the same
+// choices to about 1e-15 A.  Ends with
+// Fold_Molecule (orthorhombic branch) as Widom_Insert does before the
+// full-cutoff energy.
+__device__ inline void replay_molecule_f64(const WidomSpecies& S, const BoxF& f, const double* __restrict__ lib,
+                                           Lfsr g, const int* order, int norder, int sel, const int* trls,
+                                           double* r) {
+  const int n = S.natoms;
+  for (int k = 0; k < norder; ++k) g.next_bits();  // first fragment, growth order
+  const int f0 = order[0];
+  const int nfa = S.frag_natoms[f0];
+  unsigned exist = 0u;
+  {
+    const int conf = index_of(draw_u32(g), S.nconfig[f0]);
+    const double* L0 = lib + S.lib_off[f0] + (size_t)conf * nfa * 3;
+    for (int i = 0; i < nfa; ++i) {
+      const int a = S.frag_atoms[f0][i];
+      r[3 * a] = L0[3 * i];
+      r[3 * a + 1] = L0[3 * i + 1];
+      r[3 * a + 2] = L0[3 * i + 2];
+      exist |= 1u << a;
+    }
+  }
+  double com[3];
+  get_com(S, r, exist, com);
+  {
+    // theta = acos(1 - 2u): cos theta = 1 - 2u, sin theta = 2 sqrt(u (1 - u));
+    // phi, psi = (1 - 2u) pi through sincospi (the same angles to a few ulps)
+    const double ut = g.next();
+    const double ct = 1.0 - 2.0 * ut, st = 2.0 * sqrt(ut * (1.0 - ut));
+    double sp, cp, ss, cs;
+    sincospi(1.0 - 2.0 * g.next(), &sp, &cp);
+    sincospi(1.0 - 2.0 * g.next(), &ss, &cs);
+    const double r11 = cs * cp - ct * sp * ss, r12 = cs * sp + ct * cp * ss, r13 = ss * st;
+    const double r21 = -ss * cp - ct * sp * cs, r22 = -ss * sp + ct * cp * cs, r23 = cs * st;
+    const double r31 = st * sp, r32 = -st * cp, r33 = ct;
+    for (int i = 0; i < nfa; ++i) {
+      const int a = S.frag_atoms[f0][i];
+      const double x = r[3 * a] - com[0], y = r[3 * a + 1] - com[1], z = r[3 * a + 2] - com[2];
+      r[3 * a] = (r11 * x + r12 * y + r13 * z) + com[0];
+      r[3 * a + 1] = (r21 * x + r22 * y + r23 * z) + com[1];
+      r[3 * a + 2] = (r31 * x + r32 * y + r33 * z) + com[2];
+    }
+  }
+  for (int k = 0; k < 3 * sel; ++k) g.next_bits();
+  const double ax = (0.5 - g.next()) * f.L64[0];
+  const double ay = (0.5 - g.next()) * f.L64[1];
+  const double az = (0.5 - g.next()) * f.L64[2];
+  for (int i = 0; i < nfa; ++i) {
+    const int a = S.frag_atoms[f0][i];
+    r[3 * a] = r[3 * a] - com[0] + ax;
+    r[3 * a + 1] = r[3 * a + 1] - com[1] + ay;
+    r[3 * a + 2] = r[3 * a + 2] - com[2] + az;
+  }
+  for (int k = 0; k < 3 * (S.kappa_ins - sel - 1) + 1; ++k) g.next_bits();  // later trials, selection
+  unsigned placed = 1u << f0;
+  const int kd = S.kappa_dih;
+  for (int oi = 1; oi < norder; ++oi) {
+    const int fr = order[oi];
+    const int nf = S.frag_natoms[fr];
+    g.next_bits();  // the duplicated draw of fragment_growth.f90:1578,1584
+    const int cf = index_of(draw_u32(g), S.nconfig[fr]);
+    double cfg[3 * kMaxAtoms];
+    const double* Lf = lib + S.lib_off[fr] + (size_t)cf * nf * 3;
+    for (int j = 0; j < nf; ++j) {
+      const int a = S.frag_atoms[fr][j];
+      exist |= 1u << a;
+      cfg[3 * a] = Lf[3 * j];
+      cfg[3 * a + 1] = Lf[3 * j + 1];
+      cfg[3 * a + 2] = Lf[3 * j + 2];
+    }
+    int fc = 0;
+    for (int q = 0; q < S.frag_nconnect[fr]; ++q) {
+      const int gg = S.frag_connect[fr][q];
+      if ((placed >> gg) & 1u) {
+        fc = gg;
+        break;
+      }
+    }
+    const int anc_i = S.frag_atoms[fr][0], anc_c = S.frag_atoms[fc][0];
+    int ids[kMaxAtoms], nid = 0;
+    for (int j = 0; j < nf; ++j) {
+      const int a = S.frag_atoms[fr][j];
+      if (a != anc_i && a != anc_c) ids[nid++] = a;
+    }
+    const int atom_ifrag = nid > 0 ? ids[0] : S.frag_atoms[fr][nf - 1];
+    int atom_fc = S.frag_atoms[fc][S.frag_natoms[fc] - 1];
+    for (int j = 0; j < S.frag_natoms[fc]; ++j) {
+      const int a = S.frag_atoms[fc][j];
+      if (a != anc_i && a != anc_c) {
+        atom_fc = a;
+        break;
+      }
+    }
+    double v1[3], v2[3], al_i[9], hg_i[9], al_c[9], hg_c[9];
+    for (int d = 0; d < 3; ++d) {
+      v1[d] = cfg[3 * anc_i + d] - cfg[3 * anc_c + d];
+      v2[d] = cfg[3 * atom_ifrag + d] - cfg[3 * anc_c + d];
+    }
+    aligner_hanger_rs(v1, v2, al_i, hg_i);
+    for (int d = 0; d < 3; ++d) {
+      v1[d] = r[3 * anc_i + d] - r[3 * anc_c + d];
+      v2[d] = r[3 * atom_fc + d] - r[3 * anc_c + d];
+    }
+    aligner_hanger_rs(v1, v2, al_c, hg_c);
+    const double tx = cfg[3 * anc_c], ty = cfg[3 * anc_c + 1], tz = cfg[3 * anc_c + 2];
+    // theta0 + trl (2 pi / kappa_dih), theta0 = 2 pi u, in units of pi
+    const double t = 2.0 * g.next() + (double)trls[oi] * (2.0 / (double)kd);
+    double sth, cth;
+    sincospi(t, &sth, &cth);
+    for (int j = 0; j < nid; ++j) {
+      const int a = ids[j];
+      const double x0 = cfg[3 * a] - tx, y0 = cfg[3 * a + 1] - ty, z0 = cfg[3 * a + 2] - tz;
+      const double x = x0 * al_i[0] + y0 * al_i[1] + z0 * al_i[2];
+      const double y = x0 * al_i[3] + y0 * al_i[4] + z0 * al_i[5];
+      const double z = x0 * al_i[6] + y0 * al_i[7] + z0 * al_i[8];
+      const double yr = cth * y + sth * z, zr = -sth * y + cth * z;
+      r[3 * a] = (x * hg_c[0] + yr * hg_c[1] + zr * hg_c[2]) + r[3 * anc_c];
+      r[3 * a + 1] = (x * hg_c[3] + yr * hg_c[4] + zr * hg_c[5]) + r[3 * anc_c + 1];
+      r[3 * a + 2] = (x * hg_c[6] + yr * hg_c[7] + zr * hg_c[8]) + r[3 * anc_c + 2];
+    }
+    g.next_bits();  // trial selection
+    placed |= 1u << fr;
+  }
+  if (S.nfrag > 1) {
+    get_com(S, r, exist, com);
+    for (int d = 0; d < 3; ++d) {
+      const double sh = com[d] > f.hL64[d] ? -f.L64[d] : (com[d] < -f.hL64[d] ? f.L64[d] : 0.0);
+      if (sh != 0.0)
+        for (int a = 0; a < n; ++a) r[3 * a + d] += sh;
+    }
+  }
+}
 
 // Energy of atoms `ids` against the box: sum into e, true on overlap
 template <bool COUNT, bool OPT>
@@ -968,10 +1228,13 @@ __device__ __forceinline__ bool query_atoms_f(const BoxViewF& V, QueryAcc& A, co
 // Fragment_Placement (:1449-2132), in FP32
 template <bool COUNT, bool OPT>
 __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const BoxViewF& V,
-                                const float* __restrict__ lib, Lfsr rng, double* xyz_out, QueryAcc& cnt) {
+                                const float* __restrict__ lib, Lfsr rng, double* xyz_out, QueryAcc& cnt,
+                                FixEntry& fe) {
   const BoxF& f = *V.f;
   const int n = S.natoms;
-  RecF out{0, 0, 0, 0, 0, 0, 0, 0};
+  RecF out{0, 0, 0, 0, 0, 0.0, 0, 0, false};
+  int sel_first = 0;
+  int trls[kMaxFrags];
   float r[3 * kMaxAtoms];
   unsigned exist = 0u;
   float ln_pbias = 0.0f;
@@ -1100,6 +1363,7 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
       com[1] = ay;
       com[2] = az;
       out.selected = sel + 1;
+      sel_first = sel;
     }
   }
   // Step 5: Fragment_Placement, kappa_dih dihedral trials per fragment
@@ -1239,6 +1503,7 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
         r[3 * a + 2] = (x * hg_c[6] + yr * hg_c[7] + zr * hg_c[8]) + r[3 * anc_c + 2];
       }
       e_prev = dd[trl];
+      trls[oi] = trl;
       placed |= 1u << fr;
     }
     if (!cbmc_overlap) get_com_f(SF, r, exist, com);
@@ -1258,11 +1523,25 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
     }
   }
   QueryAcc A;
+  A.band = fe.band;
   bool ov = false;
-  for (int a = 0; a < n && !ov; ++a)
-    ov = query_f<COUNT>(V, A, r[3 * a], r[3 * a + 1], r[3 * a + 2], SF.type[a], SF.q[a], false, true);
+  for (int a = 0; a < n && !ov; ++a) {
+    A.atom = a;
+    ov = query_f<COUNT, false, kQDetect>(V, A, r[3 * a], r[3 * a + 1], r[3 * a + 2], SF.type[a], SF.q[a], false,
+                                         true);
+  }
   cnt.visited += A.visited;
   cnt.in_cut += A.in_cut;
+  if (!ov && A.nband > 0) {  // pairs within FP32 rounding of a cutoff: k_widom_fix decides them in FP64
+    out.fix = true;
+    fe.nband = A.nband;
+    fe.sel = (unsigned char)sel_first;
+    fe.norder = (unsigned char)norder;
+    for (int k = 0; k < norder; ++k) {
+      fe.order[k] = (unsigned char)order[k];
+      fe.trl[k] = (unsigned char)(k > 0 ? trls[k] : 0);
+    }
+  }
   if (ov) {
     out.status = 2;
     return out;
@@ -1272,7 +1551,7 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
     out.status = 3;
     return out;
   }
-  out.e_inter = (A.e.s + A.e.c) + io.pqq;
+  out.e_inter = (A.e.value() + (double)io.pqq);
   out.e_abs = A.eabs;
   out.dE_intra = (io.ivdw + io.iqq) + io.bond + io.angle + io.dih + io.imp;
   out.dE_frag = io.angle;
@@ -1288,12 +1567,62 @@ constexpr int kF32Threads = 512;
 constexpr int kF32MinBlocks = 2;
 constexpr int kF32Waves = 8;  // CTAs per resident slot: many short waves even out uneven boxes
 
+// FP32 constants of box b (thread 0), the FP64 edges and squared cutoffs
+// and the FP32 error bands of the full-cutoff pass
+__device__ inline void widom_boxf(BoxF& sf, const BoxDev& b, double band_scale) {
+  double lmax = 0.0;
+  for (int d = 0; d < 3; ++d) {
+    sf.L[d] = (float)b.L[d];
+    sf.Llo[d] = (float)(b.L[d] - (double)sf.L[d]);
+    sf.hL[d] = (float)b.hL[d];
+    sf.cinv[d] = (float)b.cell_inv[d];
+    sf.ch[d] = (float)(b.L[d] / (double)b.nc[d]);
+    sf.nc[d] = b.nc[d];
+    sf.L64[d] = b.L[d];
+    sf.hL64[d] = b.hL[d];
+    lmax = fmax(lmax, b.L[d]);
+  }
+  sf.rcb2 = (float)b.rcut_cbmcsq;
+  sf.rv2 = (float)b.rcut_vdwsq;
+  sf.rq2 = (float)b.rcut_coulsq;
+  sf.low2 = (float)b.rcut_lowsq;
+  sf.rc_cbmc = (float)sqrt(b.rcut_cbmcsq);
+  sf.rc_full = (float)sqrt(fmax(b.rcut_vdwsq, b.rcut_coulsq));
+  sf.beta = (float)b.beta;
+  sf.kmaxE = (float)(kMAX_KBT / b.beta);
+  sf.alpha = (float)b.alpha;
+  sf.charge_on = b.charge_style == CASS_CHARGE_COUL;
+  // |r2_32 - r2_64| <= 2 sqrt(3) r delta + the rounding of r^2, where delta
+  // bounds the FP32 error of a coordinate difference: the FP32 growth of the
+  // test molecule (its centre of mass rounded once, rotations of a few A), the
+  // rounding of the stored box atom, of a row's image shift and of the
+  // difference -- about 12 half-ulps of the largest coordinate, up to
+  // L / 2 + rcut; delta = 5e-7 (L + 20 A) exceeds it by a factor of 2 or more
+  const double delta = 5.0e-7 * (lmax + 20.0) * band_scale;
+  auto band = [&](double rc2) { return (float)(3.5 * sqrt(rc2) * delta + 1.0e-6 * rc2); };
+  sf.rv2d = b.rcut_vdwsq;
+  sf.rq2d = b.rcut_coulsq;
+  sf.low2d = b.rcut_lowsq;
+  sf.band_v = band(b.rcut_vdwsq);
+  sf.band_q = band(b.rcut_coulsq);
+  sf.band_low = band(b.rcut_lowsq);
+}
+
+__device__ inline void widom_ljp(float2* s_ljp, const PairTable& T) {
+  for (int i = threadIdx.x; i < kMaxTypes * kMaxTypes; i += blockDim.x) {
+    const int a = i / kMaxTypes, c = i % kMaxTypes;
+    const bool ok = a < T.ntypes && c < T.ntypes;
+    s_ljp[i] = ok ? make_float2(T.epsf[a * T.ntypes + c], T.sig2f[a * T.ntypes + c]) : make_float2(0.f, 0.f);
+  }
+}
+
 template <bool SMEM, bool COUNT, bool OPT>
 __global__ void __launch_bounds__(kF32Threads, kF32MinBlocks) k_widom_f32(WidomSpecies S, SpeciesF SF, PairTable T, const BoxDev* boxes,
                                                    const int* box_ids, const float4* c32, const float* cq32,
                                                    const int* cstart, const float* __restrict__ libf, long long n_ins,
                                                    uint64_t seed, WRec* rec, signed char* status, double* xyz,
-                                                   int want_xyz, CassWidomTrace* trace,
+                                                   int want_xyz, CassWidomTrace* trace, FixEntry* fix_q,
+                                                   int* fix_n, double band_scale,
                                                    unsigned long long* pair_counts) {
   extern __shared__ __align__(32) unsigned char smem[];
   __shared__ BoxF sf;
@@ -1303,40 +1632,20 @@ __global__ void __launch_bounds__(kF32Threads, kF32MinBlocks) k_widom_f32(WidomS
   const int k = blockIdx.y;
   if (threadIdx.x == 0) {
     const BoxDev& b = boxes[k];
-    for (int d = 0; d < 3; ++d) {
-      sf.L[d] = (float)b.L[d];
-      sf.Llo[d] = (float)(b.L[d] - (double)sf.L[d]);
-      sf.hL[d] = (float)b.hL[d];
-      sf.cinv[d] = (float)b.cell_inv[d];
-      sf.ch[d] = (float)(b.L[d] / (double)b.nc[d]);
-      sf.nc[d] = b.nc[d];
-    }
-    sf.rcb2 = (float)b.rcut_cbmcsq;
-    sf.rv2 = (float)b.rcut_vdwsq;
-    sf.rq2 = (float)b.rcut_coulsq;
-    sf.low2 = (float)b.rcut_lowsq;
-    sf.rc_cbmc = (float)sqrt(b.rcut_cbmcsq);
-    sf.rc_full = (float)sqrt(fmax(b.rcut_vdwsq, b.rcut_coulsq));
-    sf.beta = (float)b.beta;
-    sf.kmaxE = (float)(kMAX_KBT / b.beta);
-    sf.alpha = (float)b.alpha;
-    sf.charge_on = b.charge_style == CASS_CHARGE_COUL;
+    widom_boxf(sf, b, band_scale);
     s_atom_off = b.atom_off;
     s_cell_off = b.cell_off;
     s_natoms = b.natoms;
     s_ec = b.e_inter_constant;
   }
   if (OPT) boxf_options(sf, boxes[k], T.ntypes);
-  for (int i = threadIdx.x; i < kMaxTypes * kMaxTypes; i += blockDim.x) {
-    const int a = i / kMaxTypes, c = i % kMaxTypes;
-    const bool ok = a < T.ntypes && c < T.ntypes;
-    s_ljp[i] = ok ? make_float2(T.epsf[a * T.ntypes + c], T.sig2f[a * T.ntypes + c]) : make_float2(0.f, 0.f);
-  }
+  widom_ljp(s_ljp, T);
   __syncthreads();
   const int ncell = sf.nc[0] * sf.nc[1] * sf.nc[2];
   BoxViewF V;
   V.f = &sf;
   V.q32 = cq32 + s_atom_off;
+  V.p64 = nullptr;
   V.ljp = s_ljp;
   if (SMEM) {
     int* cs = reinterpret_cast<int*>(smem);
@@ -1356,8 +1665,10 @@ __global__ void __launch_bounds__(kF32Threads, kF32MinBlocks) k_widom_f32(WidomS
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n_ins; i += stride) {
     const size_t g = (size_t)k * n_ins + i;
     const Lfsr rng = seed_stream(seed, box_ids[k], i);
-    const RecF o = run_insertion_f<COUNT, OPT>(S, SF, V, libf, rng, want_xyz ? xyz + g * 3 * S.natoms : nullptr, cnt);
-    const double e_int = (double)o.e_inter;
+    FixEntry fe;
+    const RecF o = run_insertion_f<COUNT, OPT>(S, SF, V, libf, rng, want_xyz ? xyz + g * 3 * S.natoms : nullptr,
+                                               cnt, fe);
+    const double e_int = o.e_inter;
     rec[g] = make_double4_32a((double)o.dE_intra, e_int + s_ec, (double)o.dE_frag, (double)o.ln_pbias);
     status[g] = (signed char)o.status;
     if (trace) {
@@ -1369,10 +1680,141 @@ __global__ void __launch_bounds__(kF32Threads, kF32MinBlocks) k_widom_f32(WidomS
       t.e_inter_abs = o.status == 0 ? (double)o.e_abs : 0.0;
       t.overlap = o.status;
     }
+    if (o.fix) {
+      fe.ins = (int)i;
+      const int slot = atomicAdd(&fix_n[k], 1);  // < n_ins: one entry per insertion at most
+      fix_q[(size_t)k * n_ins + slot] = fe;
+    }
   }
   if (pair_counts) {
     atomicAdd(&pair_counts[0], cnt.visited);
     atomicAdd(&pair_counts[1], cnt.in_cut);
+  }
+}
+
+// The insertions whose full-cutoff pass met pairs within a band of FP32
+// rounding about a cutoff, one thread each: the selected molecule again in
+// FP64 (replay_molecule_f64, the same choices), each band pair's r^2 in FP64
+// from it (the FP64 path's r^2 to about 1e-15 A^2), and the FP64 decision:
+// an overlap makes the insertion an overlap (status 2); a vdW or Coulomb term
+// on the other side of its cutoff than in FP32 is added or removed (its FP32
+// pair energy).  An insertion with more than kMaxBand band pairs has its whole
+// full-cutoff pass redone from the FP64 coordinates (kQExact).  Record, status
+// and trace are corrected in place; the box stays in global memory.
+__global__ void __launch_bounds__(128) k_widom_fix(WidomSpecies S, SpeciesF SF, PairTable T, const BoxDev* boxes,
+                                                   const int* box_ids, const float4* c32, const float* cq32,
+                                                   const double4_32a* c64, const int* cstart,
+                                                   const double* __restrict__ lib64, long long n_ins, uint64_t seed,
+                                                   const FixEntry* fix_q, const int* fix_n, WRec* rec,
+                                                   signed char* status, double* xyz, int want_xyz,
+                                                   CassWidomTrace* trace, double band_scale) {
+  __shared__ BoxF sf;
+  __shared__ float2 s_ljp[kMaxTypes * kMaxTypes];
+  __shared__ int s_atom_off, s_cell_off;
+  __shared__ double s_ec;
+  const int k = blockIdx.y;
+  const int nq = fix_n[k];
+  if ((long long)blockIdx.x * blockDim.x >= nq) return;  // nothing queued for this block
+  if (threadIdx.x == 0) {
+    const BoxDev& b = boxes[k];
+    widom_boxf(sf, b, band_scale);
+    s_atom_off = b.atom_off;
+    s_cell_off = b.cell_off;
+    s_ec = b.e_inter_constant;
+  }
+  widom_ljp(s_ljp, T);
+  __syncthreads();
+  BoxViewF V;
+  V.f = &sf;
+  V.p32 = c32 + s_atom_off;
+  V.p64 = c64 + s_atom_off;
+  V.q32 = cq32 + s_atom_off;
+  V.cstart = cstart + s_cell_off + k;
+  V.ljp = s_ljp;
+  const int n = S.natoms;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nq; e += gridDim.x * blockDim.x) {
+    const FixEntry& fe = fix_q[(size_t)k * n_ins + e];
+    const size_t g = (size_t)k * n_ins + fe.ins;
+    int order[kMaxFrags], trls[kMaxFrags];
+    const int norder = fe.norder;
+    for (int q = 0; q < norder; ++q) {
+      order[q] = fe.order[q];
+      trls[q] = fe.trl[q];
+    }
+    double r64[3 * kMaxAtoms];
+    replay_molecule_f64(S, sf, lib64, seed_stream(seed, box_ids[k], fe.ins), order, norder, fe.sel, trls, r64);
+    const double lnp = rec[g].w;
+    if (fe.nband > kMaxBand) {  // redo the pass from the FP64 coordinates
+      float r[3 * kMaxAtoms];
+      for (int i = 0; i < 3 * n; ++i) r[i] = (float)r64[i];
+      QueryAcc A;
+      bool ov = false;
+      for (int a = 0; a < n && !ov; ++a)
+        ov = query_f<false, false, kQExact>(V, A, r[3 * a], r[3 * a + 1], r[3 * a + 2], SF.type[a], SF.q[a], false,
+                                            true, r64 + 3 * a);
+      int st = 2;
+      double e_int = 0.0, e_abs = 0.0, dE_intra = 0.0, dE_frag = 0.0;
+      if (!ov) {
+        const IntraF io = molecule_intra_f(SF, sf, V.ljp, r);
+        st = io.overlap ? 3 : 0;
+        if (st == 0) {
+          e_int = A.e.value() + (double)io.pqq;
+          e_abs = (double)A.eabs;
+          dE_intra = (double)((io.ivdw + io.iqq) + io.bond + io.angle + io.dih + io.imp);
+          dE_frag = (double)io.angle;
+        }
+      }
+      rec[g] = make_double4_32a(dE_intra, e_int + s_ec, dE_frag, lnp);
+      status[g] = (signed char)st;
+      if (trace) {
+        trace[g].e_inter = e_int;
+        trace[g].e_inter_abs = e_abs;
+        trace[g].overlap = st;
+      }
+      if (want_xyz && st == 0)
+        for (int i = 0; i < 3 * n; ++i) xyz[g * 3 * n + i] = r64[i];
+      continue;
+    }
+    bool ov = false;
+    double de = 0.0, dab = 0.0;
+    for (int q = 0; q < fe.nband; ++q) {
+      const BandPair bp = fe.band[q];
+      const int a = bp.atom;
+      const double d2 = exact_r2(sf, V.p64, bp.j, r64 + 3 * a);
+      if (bp.kind == 1) {
+        ov = ov || d2 < sf.low2d;
+        continue;
+      }
+      const float4 at = V.p32[bp.j];
+      const int ta = SF.type[a], tj = __float_as_int(at.w);
+      if (ta >= 0 && tj >= 0 && (bp.r2 <= sf.rv2) != (d2 <= sf.rv2d)) {
+        const float2 es = s_ljp[ta * kMaxTypes + tj];
+        const double ev = (double)lj_pair_f(es.x, es.y, bp.r2);
+        de += d2 <= sf.rv2d ? ev : -ev;
+        dab += d2 <= sf.rv2d ? fabs(ev) : -fabs(ev);
+      }
+      const float qa = SF.q[a];
+      if (sf.charge_on && qa != 0.0f && (bp.r2 <= sf.rq2) != (d2 <= sf.rq2d)) {
+        const double eq = (double)qq_ewald_inter_f(sf.alpha, qa * V.q32[bp.j], bp.r2);
+        de += d2 <= sf.rq2d ? eq : -eq;
+        dab += d2 <= sf.rq2d ? fabs(eq) : -fabs(eq);
+      }
+    }
+    if (ov) {
+      rec[g] = make_double4_32a(0.0, s_ec, 0.0, lnp);
+      status[g] = 2;
+      if (trace) {
+        trace[g].e_inter = 0.0;
+        trace[g].e_inter_abs = 0.0;
+        trace[g].overlap = 2;
+      }
+    } else if (status[g] == 0 && (de != 0.0 || dab != 0.0)) {
+      rec[g].y += de;
+      if (trace) {
+        trace[g].e_inter += de;
+        trace[g].e_inter_abs += dab;
+      }
+    }
   }
 }
 
@@ -1864,8 +2306,17 @@ static int widom_insert_impl(cass_ctx* c, int32_t is1, int32_t nboxes, const int
     count_launch(c);
     return CASS_OK;
   };
-  // FP32 kernel of the mixed path
+  // FP32 kernel of the mixed path, then the FP64 fix-up of the insertions it
+  // queued (both inside the kernel timing)
+  int* d_fixn = nullptr;
+  FixEntry* d_fixq = nullptr;
   auto launch_f32 = [&](auto kern, const SpeciesF& SF) -> int {
+    int rc2 = c->d_widom_fix.reserve((size_t)nboxes * sizeof(int) + 64 + nrec * sizeof(FixEntry));
+    if (rc2) return rc2;
+    d_fixn = c->d_widom_fix.as<int>();
+    d_fixq = reinterpret_cast<FixEntry*>(c->d_widom_fix.as<unsigned char>() +
+                                         (((size_t)nboxes * sizeof(int) + 63) & ~(size_t)63));
+    CASS_CUDA(cudaMemsetAsync(d_fixn, 0, (size_t)nboxes * sizeof(int), c->stream));
     if (use_smem) CASS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem));
     int per_sm = 1;
     CASS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kF32Threads, use_smem ? max_smem : 0));
@@ -1882,10 +2333,19 @@ static int widom_insert_impl(cass_ctx* c, int32_t is1, int32_t nboxes, const int
     CASS_CUDA(cudaEventRecord(c->ev[1], c->stream));
     kern<<<g, kF32Threads, use_smem ? max_smem : 0, c->stream>>>(
         S, SF, c->pt, d_bd, d_ids, d_c32, c->d_cq32.as<float>(), c->d_cell_start.as<int>(), s.d_library_f.as<float>(),
-        (long long)n_ins, seed, d_rec, d_status, d_xyz, any_recip ? 1 : 0, d_trace, d_pairs);
+        (long long)n_ins, seed, d_rec, d_status, d_xyz, any_recip ? 1 : 0, d_trace, d_fixq, d_fixn, c->widom_band,
+        d_pairs);
+    CASS_CUDA(cudaGetLastError());
+    // one thread per queued insertion, the grid sized for 3 % of the
+    // insertions (one to two per cent are queued; a longer queue is strided)
+    const int fix_chunks = (int)std::max<long long>(1, std::min<long long>(64, (n_ins * 3 / 100 + 127) / 128));
+    k_widom_fix<<<dim3(fix_chunks, nboxes), 128, 0, c->stream>>>(
+        S, SF, c->pt, d_bd, d_ids, d_c32, c->d_cq32.as<float>(), c->d_c64.as<double4_32a>(), c->d_cell_start.as<int>(),
+        s.d_library.as<double>(), (long long)n_ins, seed, d_fixq, d_fixn, d_rec, d_status, d_xyz, any_recip ? 1 : 0,
+        d_trace, c->widom_band);
     CASS_CUDA(cudaGetLastError());
     CASS_CUDA(cudaEventRecord(c->ev[2], c->stream));
-    count_launch(c);
+    count_launch(c, 2);
     return CASS_OK;
   };
   if (n_ins > 0) {
@@ -1925,6 +2385,8 @@ static int widom_insert_impl(cass_ctx* c, int32_t is1, int32_t nboxes, const int
   CASS_CUDA(cudaEventRecord(c->ev[3], c->stream));
   unsigned long long hpairs[2] = {0, 0};
   if (d_pairs) CASS_CUDA(d2h(c, hpairs, d_pairs, sizeof(hpairs)));
+  std::vector<int> hfix(d_fixn ? nboxes : 0);
+  if (d_fixn) CASS_CUDA(d2h(c, hfix.data(), d_fixn, nboxes * sizeof(int)));
   std::vector<double> hs(nboxes);
   std::vector<long long> ho(nboxes);
   CASS_CUDA(d2h(c, hs.data(), d_bsum, nboxes * sizeof(double)));
@@ -1939,6 +2401,8 @@ static int widom_insert_impl(cass_ctx* c, int32_t is1, int32_t nboxes, const int
   c->stats.widom_kernel_ms = ms_k;
   c->stats.widom_pairs_visited = (int64_t)hpairs[0];
   c->stats.widom_pairs_in_cutoff = (int64_t)hpairs[1];
+  c->stats.widom_fixups = 0;
+  for (int v : hfix) c->stats.widom_fixups += v;
   for (int k = 0; k < nboxes; ++k) {
     out[k].widom_sum = hs[k] * bd[k].prefactor;
     out[k].prefactor = bd[k].prefactor;

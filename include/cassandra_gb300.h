@@ -518,7 +518,8 @@ typedef struct CassStats {
   double mc_ms;             /* the most recent cass_mc_sweeps or cass_gcmc: its kernel */
   int64_t mc_moves;         /* moves it ran, all boxes */
   int32_t gcmc_cluster;     /* CTAs per box (a thread-block cluster) of the most recent cass_gcmc or cass_mc_sweeps */
-  int32_t reserved;
+  int32_t widom_fixups;     /* mixed precision: insertions of the last Widom call whose full-cutoff pass met a
+                               pair within FP32 rounding of a cutoff and was redone from FP64 coordinates */
 } CassStats;
 int cass_get_stats(cass_ctx* ctx, CassStats* out);
 /* count_pairs != 0 makes the Widom kernel count visited / in-cutoff pairs. */
@@ -540,6 +541,15 @@ int cass_set_widom_autotune(cass_ctx* ctx, int32_t on);
  * do not depend on it beyond summation order.  cass_get_stats reports the
  * choice in gcmc_cluster. */
 int cass_set_mc_cluster(cass_ctx* ctx, int32_t ctas);
+/* Mixed precision: the full-cutoff pass of each Widom insertion notes the pairs
+ * whose FP32 r^2 lies within a band about rcut_low^2, the vdW or the Coulomb
+ * cutoff^2 (the bound of the FP32 rounding of the test and box coordinates),
+ * and those pairs are decided again in FP64 from the molecule regrown in FP64,
+ * so that every cutoff and overlap decision is the FP64 one.  scale (>= 1,
+ * default 1) widens the bands: more pairs are decided in FP64, the results do
+ * not change beyond rounding.  cass_get_stats reports the insertions
+ * corrected in widom_fixups. */
+int cass_set_widom_band(cass_ctx* ctx, double scale);
 /* Runs the context's work on a caller-owned cudaStream_t (NULL: its own). */
 int cass_set_stream(cass_ctx* ctx, void* stream);
 
