@@ -97,7 +97,18 @@ struct McMove {
 
 __device__ __forceinline__ bool accept_or_reject_d(double ln_pacc, Lfsr& rng) {
   if (ln_pacc <= 0.0) return true;
-  if (ln_pacc < kMAX_KBT) return rng.next() <= exp(-ln_pacc);
+  if (ln_pacc < kMAX_KBT) {
+    const double u = rng.next();
+    // exp(-ln_pacc) in FP32 first (FP64 issues at 1/64 of the FP32 rate): with
+    // ln_pacc < 80 rounded to FP32 the value is within 6e-6 relative, so a
+    // draw outside a band of 2e-5 about it is decided as in FP64
+    if (ln_pacc < 80.0) {
+      const float e = expf(-(float)ln_pacc), uf = (float)u;
+      if (uf < e * 0.99998f) return true;
+      if (uf > e * 1.00002f) return false;
+    }
+    return u <= exp(-ln_pacc);
+  }
   return false;
 }
 
@@ -172,6 +183,7 @@ template <bool MIXED, bool GMEM>
 __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(McArgs A, McBox* boxes, PairTable T,
                                                                            int csize) {
   constexpr int NW = (GMEM ? kMcThreadsG : kMcThreads) / 32;
+  const int nwarps = blockDim.x >> 5;  // <= NW
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ BoxDev b;
   __shared__ McMove mv;
@@ -478,7 +490,7 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
     int o = 0, n = 0;
     if (threadIdx.x == 0) {
       dv = dq = 0.0;
-      for (int w = 0; w < NW; ++w) {
+      for (int w = 0; w < nwarps; ++w) {
         dv += red[w * 8];
         dq += red[w * 8 + 1];
         o |= redi[2 * w];
@@ -560,7 +572,7 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
       block_sum_mc(part, red, 4);
       __syncthreads();
       if (threadIdx.x == 0) {
-        for (int w = 0; w < NW; ++w) e_recip += red[w * 8 + 4];
+        for (int w = 0; w < nwarps; ++w) e_recip += red[w * 8 + 4];
         if (csize > 1) cd[cbuf][0] = e_recip;
       }
       if (csize > 1) {
