@@ -64,8 +64,8 @@ def parse():
     p.add_argument("--gcmc-block-steps", type=int, default=15000)
     p.add_argument("--pregen-frames", type=int, default=4)
     p.add_argument("--npt-chains", type=int, default=64)
-    p.add_argument("--npt-eq-blocks", type=int, default=6)
-    p.add_argument("--npt-blocks", type=int, default=4, help="production blocks (configurations per chain)")
+    p.add_argument("--npt-eq-blocks", type=int, default=300)
+    p.add_argument("--npt-blocks", type=int, default=32, help="production blocks (configurations per chain)")
     p.add_argument("--profile-case", choices=["mixed", "fp64"], default=None,
                    help="only the small Widom case the kernel profiles use: 16 of the benchmark boxes, 16,000 "
                         "(mixed) or 4,096 (FP64) insertions per box, fixed cell edge, three launches")
@@ -425,8 +425,9 @@ def npt_leg(cg, abi, dev, nchains: int, eq_blocks: int, prod_blocks: int) -> dic
             "d_rho_d_eps_O": {"value": sens, "jackknife_err": err, "unit": "g/cm^3 per K of eps_O/k",
                               "formula": "-beta (<rho dU/deps> - <rho><dU/deps>)"},
             "adjoint_check_max_rel_diff": float(max(check)),
-            "note": "configurations after short equilibration from the lattice start; the full 2000-configuration "
-                    "run is --npt-chains 64 --npt-eq-blocks 300 --npt-blocks 32 (about 4.5 min)"}
+            "note": f"{nchains} independent chains from the lattice start, {eq_blocks} equilibration blocks, then one "
+                    f"configuration per chain after each of {prod_blocks} production blocks; the error is the "
+                    f"jackknife over chains"}
 
 
 def pregen_leg(cg, abi, system, n_per_box: int, kappa: int, nframes: int, seed: int) -> dict:
@@ -856,14 +857,17 @@ def main():
                               "(frame) cass_load_next_frame of all 64 boxes (text parsed by reader threads into "
                               "pinned buffers, pinned upload) and one cass_widom_insert, results read back; "
                               "host wall clock"}
-    if not args.no_mc:
-        out["mc_sweeps"] = mc_leg(cg, abi, dev, rank == 0 and world == 1 and not args.no_cpu_baseline)
-    if not args.no_gcmc:
-        out["gcmc"] = gcmc_leg(cg, abi, dev, rank == 0 and world == 1 and not args.no_cpu_baseline,
+    # the other configurations run on one GPU only: a multi-GPU run measures the
+    # sharded Widom headline and holds its GPUs no longer than that
+    solo = world == 1
+    if solo and not args.no_mc:
+        out["mc_sweeps"] = mc_leg(cg, abi, dev, not args.no_cpu_baseline)
+    if solo and not args.no_gcmc:
+        out["gcmc"] = gcmc_leg(cg, abi, dev, not args.no_cpu_baseline,
                                eq_steps=args.gcmc_eq_steps, blocks=args.gcmc_blocks, block_steps=args.gcmc_block_steps)
-    if not args.no_grad:
+    if solo and not args.no_grad:
         out["gradient"] = gradient_leg(cg, abi, dev)
-    if not args.no_npt:
+    if solo and not args.no_npt:
         out["npt_fluctuation"] = npt_leg(cg, abi, dev, args.npt_chains, args.npt_eq_blocks, args.npt_blocks)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(system, args)
