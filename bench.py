@@ -66,9 +66,11 @@ def parse():
     p.add_argument("--npt-chains", type=int, default=64)
     p.add_argument("--npt-eq-blocks", type=int, default=300)
     p.add_argument("--npt-blocks", type=int, default=32, help="production blocks (configurations per chain)")
-    p.add_argument("--profile-case", choices=["mixed", "fp64"], default=None,
-                   help="only the small Widom case the kernel profiles use: 16 of the benchmark boxes, 16,000 "
-                        "(mixed) or 4,096 (FP64) insertions per box, fixed cell edge, three launches")
+    p.add_argument("--profile-case", choices=["mixed", "fp64", "mc"], default=None,
+                   help="only the small case a kernel profile uses: the Widom kernel on 16 of the benchmark boxes, "
+                        "16,000 (mixed) or 4,096 (FP64) insertions per box, fixed cell edge, three launches; or (mc) "
+                        "single MC chains: FP64 water-256 (warm-up and 2 sweeps), then mixed LJ-500 (warm-up and 20 "
+                        "sweeps)")
     return p.parse_args()
 
 
@@ -580,11 +582,24 @@ def run_reference(args, rank, world):
 
 
 def profile_case(args):
-    """The small Widom case of the ncu captures in profiles/: three launches of the
-    mixed (cells of rcut_cbmc) or FP64 (cells of rcut_cbmc / 4) kernel on 16 boxes."""
+    """The small cases of the ncu captures in profiles/: three launches of the
+    mixed (cells of rcut_cbmc) or FP64 (cells of rcut_cbmc / 4) Widom kernel on 16
+    boxes, or four launches of the MC kernel on single chains."""
     import cassandra_gb300 as cg
     from cassandra_gb300 import abi, build, workloads
     build.build()
+    if args.profile_case == "mc":
+        for sysm, prec, pt, nsw in ((workloads.water_nvt_system(nboxes=1), abi.PREC_FP64, 0.5, 2),
+                                    (workloads.lj_nvt_system(nboxes=1), abi.PREC_MIXED, 1.0, 20)):
+            ns = len(sysm.species)
+            with cg.open_system(sysm, precision=prec) as g:
+                g.system_total_energy(1)
+                g.mc_sweeps([1], 1, [[0.8] * ns], [[0.4] * ns], seed=1, prob_translate=pt)
+                g.mc_sweeps([1], nsw, [[0.8] * ns], [[0.4] * ns], seed=2, prob_translate=pt)
+                st = g.stats()
+                print(json.dumps({"case": "mc", "precision": prec, "sweeps": nsw, "kernel_ms": st["mc_ms"],
+                                  "sweeps_per_s": nsw / (st["mc_ms"] / 1e3), "ctas_per_chain": st["gcmc_cluster"]}))
+        return
     nb = 16
     s = workloads.widom_batch_system(nboxes=nb, seed=args.seed, nconfig=1000)
     boxes = list(range(1, nb + 1))

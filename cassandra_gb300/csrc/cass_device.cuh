@@ -70,6 +70,10 @@ struct BoxDev {
   const float* tab_f2f;
   const double* rminsq;  // [ntypes][ntypes]
   const float* rminsqf;
+  // Check_MoleculePair_Cutoff boxes (LJ CHARMM, minimum-image charges; Widom
+  // path): per packed atom its molecule's COM and max_dcom, and rcut_max
+  const double4_32a* mcom;
+  double rcut_max;
 };
 
 __host__ __device__ inline int pidx(int i, int j, int nt) { return i * nt + j; }

@@ -2392,7 +2392,7 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
       if (iboxes[j] == iboxes[k]) return set_error(CASS_EINVAL, "box listed twice");
     const BoxH& B = c->box[ib];
     if (!B.energy_valid) return set_error(CASS_ESTATE, "system energy of box not computed");
-    if (B.comcut) return set_error(CASS_EUNSUPPORTED, "molecule-pair COM cutoff (LJ CHARMM or minimum-image charges) is applied by the system and molecule energies only");
+    if (B.comcut) return set_error(CASS_EUNSUPPORTED, "molecule-pair COM cutoff (LJ CHARMM or minimum-image charges) is not applied by the grand-canonical kernel");
     if (B.desc.charge_style != CASS_CHARGE_NONE) return set_error(CASS_EUNSUPPORTED, "gcmc boxes hold no charges");
     if (B.desc.vdw_style != CASS_VDW_LJ) return set_error(CASS_EUNSUPPORTED, "gcmc needs LJ boxes");
     mixed = mixed && (B.desc.vdw_sum_style == CASS_VDW_SUM_CUT || B.desc.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL);
@@ -2621,7 +2621,7 @@ extern "C" int cass_build_molecule(cass_ctx* c, int32_t im, int32_t is1, int32_t
     if (s.frag_nconfig[f] < 1) return set_error(CASS_EINVAL, "fragment library is empty");
   const BoxH& B = c->box[ib];
   if (!B.defined) return set_error(CASS_ESTATE, "box not defined");
-  if (B.comcut) return set_error(CASS_EUNSUPPORTED, "molecule-pair COM cutoff (LJ CHARMM or minimum-image charges) is applied by the system and molecule energies only");
+  if (B.comcut) return set_error(CASS_EUNSUPPORTED, "molecule-pair COM cutoff (LJ CHARMM or minimum-image charges) is not applied by the grand-canonical kernel");
   if (B.desc.charge_style != CASS_CHARGE_NONE) return set_error(CASS_EUNSUPPORTED, "build_molecule boxes hold no charges");
   if (B.desc.vdw_style != CASS_VDW_LJ) return set_error(CASS_EUNSUPPORTED, "build_molecule needs LJ boxes");
   const int slot = c->mol_base[is] + im - 1;

@@ -190,7 +190,15 @@ struct BoxView {
   const double4_32a* p64;   // cell-sorted FP64 atoms (x, y, z, q) of this box (smem or global)
   const int* ptype;         // their types (smem or global)
   const int* cstart;        // cell starts, local atom indices (smem or global)
+  const int* corig;         // packed index of each cell-sorted atom (global; molecule-pair boxes)
   double rc_cbmc, rc_full;
+};
+
+// The test molecule of one energy call as Check_MoleculePair_Cutoff sees it
+// (energy_routines.f90:3027-3088): the COM and max_dcom of its existing atoms
+struct QueryMol {
+  double com[3];
+  double dcom;
 };
 
 // Energy of one test atom at p against every box atom within the cutoff.
@@ -201,10 +209,20 @@ struct PairCount {
   double eabs = 0.0;  // sum of |pair energy| of the current query
 };
 
+// With qm (a box with a molecule-pair cutoff) a candidate atom counts only when
+// its molecule passes Check_MoleculePair_Cutoff against the test molecule:
+// |COM - COM_j| <= (rcut_cbmc or rcut_max) + max_dcom + max_dcom_j, as the
+// molecule loop of Compute_Molecule_Nonbond_Inter_Energy_Widom applies it
+// (energy_routines.f90:1266-1297) -- the overlap test included.
 __device__ bool query_box(const BoxView& V, const PairTable& T, const double p[3], int qt, double qch, bool cbmc,
-                          bool want_qq, double& eout, PairCount& pc) {
+                          bool want_qq, double& eout, PairCount& pc, const QueryMol* qm = nullptr) {
   const BoxDev& b = *V.b;
   double rc = cbmc ? V.rc_cbmc : V.rc_full;
+  // minimum-image charges count every pair of a molecule within the
+  // molecule-pair cutoff, in CBMC calls too: the whole box is searched
+  if (qm && cbmc && want_qq && b.charge_style == CASS_CHARGE_COUL && b.charge_sum_style == CASS_QQ_MINIMUM)
+    rc = 1e30;
+  const double rint0 = cbmc ? V.rc_cbmc : b.rcut_max;
   int lo[3], hi[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
@@ -258,6 +276,13 @@ __device__ bool query_box(const BoxView& V, const PairTable& T, const double p[3
         int j1 = V.cstart[row + wx + run];
         pc.visited += (unsigned long long)(j1 - V.cstart[row + wx]);
         for (int j = V.cstart[row + wx]; j < j1; ++j) {
+          if (qm) {  // Check_MoleculePair_Cutoff
+            const double4_32a mc = b.mcom[V.corig[j]];
+            const double cx = fold(qm->com[0] - mc.x, b.hL[0], b.L[0]);
+            const double cy = fold(qm->com[1] - mc.y, b.hL[1], b.L[1]);
+            const double cz = fold(qm->com[2] - mc.z, b.hL[2], b.L[2]);
+            if (sqrt(cx * cx + cy * cy + cz * cz) > rint0 + qm->dcom + mc.w) continue;
+          }
           double4_32a a = P[j];
           double dx = fold(p[0] - a.x, b.hL[0], b.L[0]);
           double dy = fold(p[1] - a.y, b.hL[1], b.L[1]);
@@ -297,6 +322,17 @@ __device__ bool query_box(const BoxView& V, const PairTable& T, const double p[3
   eout = acc;
   pc.eabs = eabs;
   return false;
+}
+
+// Compute_Max_COM_Distance (get_com.f90:220-295) over the atoms of `mask`
+__device__ inline double max_dcom_of(const double* r, unsigned mask, const double com[3], int n) {
+  double dmax = 0.0;
+  for (int k = 0; k < n; ++k) {
+    if (!((mask >> k) & 1u)) continue;
+    const double dx = r[3 * k] - com[0], dy = r[3 * k + 1] - com[1], dz = r[3 * k + 2] - com[2];
+    dmax = fmax(dmax, dx * dx + dy * dy + dz * dz);
+  }
+  return sqrt(dmax);
 }
 
 // ---------------------------------------------------------------------------
@@ -407,18 +443,27 @@ __device__ void run_insertion(const WidomSpecies& S, const SpeciesPools& P, cons
   double r0[3 * kMaxAtoms];
   for (int i = 0; i < 3 * n; ++i) r0[i] = r[i];
   const double com_old[3] = {com[0], com[1], com[2]};
+  // molecule-pair cutoff boxes: the fragment at a trial centre has that COM
+  // and the max_dcom of its atoms about it
+  const bool mp = b.mcom != nullptr;
+  QueryMol qm;
+  qm.dcom = 0.0;
+  if (mp) qm.dcom = max_dcom_of(r0, exist, com_old, n);
   Lfsr replay = rng;
   for (int it = 0; it < ki; ++it) {
     double ax = (0.5 - rng.next()) * b.L[0];
     double ay = (0.5 - rng.next()) * b.L[1];
     double az = (0.5 - rng.next()) * b.L[2];
+    qm.com[0] = ax;
+    qm.com[1] = ay;
+    qm.com[2] = az;
     double e = 0.0;
     bool ov = false;
     for (int i = 0; i < nfa && !ov; ++i) {
       int a = S.frag_atoms[fstart][i];
       double p[3] = {r0[3 * a] - com_old[0] + ax, r0[3 * a + 1] - com_old[1] + ay, r0[3 * a + 2] - com_old[2] + az};
       double ea;
-      ov = query_box(V, T, p, S.type[a], S.q[a], true, S.want_qq_cbmc != 0, ea, pc);
+      ov = query_box(V, T, p, S.type[a], S.q[a], true, S.want_qq_cbmc != 0, ea, pc, mp ? &qm : nullptr);
       e += ea;
     }
     nrg[it] = e;
@@ -575,11 +620,15 @@ __device__ void run_insertion(const WidomSpecies& S, const SpeciesPools& P, cons
           continue;
         }
         double einter = 0.0;
+        if (mp) {  // the new atoms of the trial (fragment_growth.f90 Fragment_Placement energy call)
+          get_com(S, r, newex, qm.com);
+          qm.dcom = max_dcom_of(r, newex, qm.com, n);
+        }
         for (int a = 0; a < n && !ov; ++a) {
           if (!((newex >> a) & 1u)) continue;
           double p[3] = {r[3 * a], r[3 * a + 1], r[3 * a + 2]};
           double ea;
-          ov = query_box(V, T, p, S.type[a], S.q[a], true, S.want_qq_cbmc != 0, ea, pc);
+          ov = query_box(V, T, p, S.type[a], S.q[a], true, S.want_qq_cbmc != 0, ea, pc, mp ? &qm : nullptr);
           einter += ea;
         }
         exist = combined;
@@ -660,10 +709,14 @@ __device__ void run_insertion(const WidomSpecies& S, const SpeciesPools& P, cons
     }
   }
   double e_inter = 0.0, e_abs = 0.0;
+  if (mp) {  // the whole molecule, folded
+    get_com(S, r, exist, qm.com);
+    qm.dcom = max_dcom_of(r, exist, qm.com, n);
+  }
   for (int a = 0; a < n; ++a) {
     double p[3] = {r[3 * a], r[3 * a + 1], r[3 * a + 2]};
     double ea;
-    if (query_box(V, T, p, S.type[a], S.q[a], false, true, ea, pc)) {
+    if (query_box(V, T, p, S.type[a], S.q[a], false, true, ea, pc, mp ? &qm : nullptr)) {
       status = 2;
       return;
     }
@@ -1822,7 +1875,8 @@ __global__ void __launch_bounds__(128) k_widom_fix(WidomSpecies S, SpeciesF SF, 
 template <bool SMEM>
 __global__ void __launch_bounds__(128) k_widom(WidomSpecies S, PairTable T, SpeciesPools P, const BoxDev* boxes,
                                                const int* box_ids, const double4_32a* c64, const int* ctype,
-                                               const int* cstart, const double* __restrict__ lib, long long n_ins,
+                                               const int* corig, const int* cstart,
+                                               const double* __restrict__ lib, long long n_ins,
                                                uint64_t seed, WRec* rec, signed char* status, double* xyz,
                                                int want_xyz, CassWidomTrace* trace, unsigned long long* pair_counts) {
   extern __shared__ __align__(32) unsigned char smem[];
@@ -1841,6 +1895,7 @@ __global__ void __launch_bounds__(128) k_widom(WidomSpecies S, PairTable T, Spec
     rfull = 1e30;
   if (sb.vdw_sum_style == CASS_VDW_SUM_CUT_SWITCH) rfull = fmax(rfull, sqrt(sb.roff_switch_sq));
   V.rc_full = rfull;
+  V.corig = corig + sb.atom_off;
   if (SMEM) {
     int* cs = reinterpret_cast<int*>(smem);
     for (int c = threadIdx.x; c <= ncell; c += blockDim.x) cs[c] = cstart[sb.cell_off + k + c];
@@ -2119,7 +2174,6 @@ static int widom_insert_impl(cass_ctx* c, int32_t is1, int32_t nboxes, const int
     if (ib < 0 || ib >= c->nboxes) return set_error(CASS_EINVAL, "box index out of range");
     if (!c->box[ib].energy_valid && !c->box[ib].frame_ready)
       return set_error(CASS_ESTATE, "system energy of box not computed");
-    if (c->box[ib].comcut) return set_error(CASS_EUNSUPPORTED, "molecule-pair COM cutoff (LJ CHARMM or minimum-image charges) is applied by the system and molecule energies only");
   }
   int rc;
   CASS_CUDA(cudaSetDevice(c->device));
@@ -2160,6 +2214,8 @@ static int widom_insert_impl(cass_ctx* c, int32_t is1, int32_t nboxes, const int
     v.atom_off = atom_off;
     v.natoms = B.npacked;
     v.cell_off = cell_off;
+    v.mcom = B.comcut ? B.d_com.as<double4_32a>() : nullptr;  // built with the packed arrays
+    v.rcut_max = B.rcut_max;
     // Widom_Insert set-up (widom_insert.f90:201-245)
     const std::vector<int>& mem = members_ext(c, ib);
     int nmols = 1;
@@ -2299,7 +2355,7 @@ static int widom_insert_impl(cass_ctx* c, int32_t is1, int32_t nboxes, const int
     c->stats.widom_smem_bytes = use_smem ? (int)max_smem : 0;
     CASS_CUDA(cudaEventRecord(c->ev[1], c->stream));
     kern<<<g, threads, use_smem ? max_smem : 0, c->stream>>>(
-        S, c->pt, c->pools, d_bd, d_ids, c->d_c64.as<double4_32a>(), d_ctype, c->d_cell_start.as<int>(),
+        S, c->pt, c->pools, d_bd, d_ids, c->d_c64.as<double4_32a>(), d_ctype, d_corig, c->d_cell_start.as<int>(),
         s.d_library.as<double>(), (long long)n_ins, seed, d_rec, d_status, d_xyz, any_recip ? 1 : 0, d_trace, d_pairs);
     CASS_CUDA(cudaGetLastError());
     CASS_CUDA(cudaEventRecord(c->ev[2], c->stream));

@@ -7,8 +7,9 @@ the system energy (every component), molecule energies with and without the
 CBMC cutoffs, and Widom insertions record by record.  Where a style has no atom
 cutoff (LJ CHARMM, minimum-image charges) and the vdW sum is not minimum image,
 Check_MoleculePair_Cutoff (:3027-3088) selects the interacting molecules by their
-COM distance; the system and molecule energies and the MC sweeps apply it, the
-batched CBMC paths refuse such boxes."""
+COM distance; the system and molecule energies, the MC sweeps, the CBMC trial
+energies and the Widom insertions apply it (grand-canonical moves and the
+allocation-free call refuse such boxes)."""
 import numpy as np
 import pytest
 
@@ -79,10 +80,6 @@ def test_style_matches_oracle(name, make):
                 assert a[2] == b[2]
                 assert _close(b[0], a[0]) and _close(b[1], a[1]), (name, im, cbmc, a, b)
         n = 64
-        if name in COMCUT:  # Check_MoleculePair_Cutoff decides: refused where it is not applied
-            with pytest.raises(abi.CassError, match="COM cutoff"):
-                g.widom_insert(1, [1], n, 8, 0, seed=3)
-            return
         ro, to = o.widom_insert(1, [1], n, 8, 0, seed=3, trace=True)
         rg, tg = g.widom_insert(1, [1], n, 8, 0, seed=3, trace=True)
     assert np.array_equal(to["overlap"], tg["overlap"])
@@ -93,6 +90,32 @@ def test_style_matches_oracle(name, make):
     assert np.allclose(tg["widom_var"][ok], to["widom_var"][ok], rtol=1e-8, atol=0)
     if not water:
         assert ro[0]["n_insertions"] == rg[0]["n_insertions"] == n
+
+
+@pytest.mark.parametrize("prec", [abi.PREC_FP64, abi.PREC_MIXED])
+def test_widom_butane_molecule_pair_cutoff(prec):
+    """Butane Widom insertions into an LJ CHARMM box (no atom cutoff: every energy
+    call of the growth selects molecule pairs by Check_MoleculePair_Cutoff,
+    energy_routines.f90:3027-3088): the first fragment at its trial centre, the new
+    atoms of each dihedral trial, then the whole folded molecule, each with the COM
+    and max_dcom of its atoms -- against the oracle insertion by insertion.  A
+    mixed context runs the FP64 kernel for this style."""
+    s = workloads.widom_batch_system(nboxes=1, sizes=[300], seed=5, nconfig=200)
+    s.boxes[0].vdw_sum_style = abi.VDW_SUM_CHARMM
+    n = 256
+    with oracle.open_system(s) as o, cg.open_system(s, precision=prec) as g:
+        o.system_total_energy(1)
+        g.system_total_energy(1)
+        ro, to = o.widom_insert(2, [1], n, 12, 12, seed=5, trace=True)
+        rg, tg = g.widom_insert(2, [1], n, 12, 12, seed=5, trace=True)
+    assert np.array_equal(to["overlap"], tg["overlap"])
+    assert np.array_equal(to["selected_trial"], tg["selected_trial"])
+    assert np.allclose(tg["ln_pbias"], to["ln_pbias"], rtol=1e-10, atol=1e-10)
+    ok = to["overlap"] == 0
+    assert ok.sum() > 0.3 * n
+    assert np.allclose(tg["e_inter"][ok], to["e_inter"][ok], rtol=1e-9, atol=1e-6)
+    assert np.allclose(tg["widom_var"][ok], to["widom_var"][ok], rtol=1e-8, atol=0)
+    assert ro[0]["n_overlaps"] == rg[0]["n_overlaps"]
 
 
 @pytest.mark.parametrize("name,make", CASES, ids=[c[0] for c in CASES])
