@@ -84,6 +84,8 @@ struct GcBox {
   CassEnergy* energy;
   CassGCMCResult* res;
   int* status;  // 0 ok, 1 overlapping molecule before a move, 2 no free slot
+  int comcut;    // LJ CHARMM: molecule pairs selected by Check_MoleculePair_Cutoff (FP64 kernel)
+  double rmax;   // rcut_max of that test
 };
 
 // the molecule being built / moved and one stage of trials (shared memory)
@@ -99,6 +101,7 @@ struct GrowState {
   double e[kMaxKappa];
   float ef[kMaxKappa];
   int ov[kMaxKappa];
+  double tcom[kMaxKappa][4];  // COM and max_dcom of each trial's atoms (molecule-pair cutoff boxes)
   double cpart[2][kMaxKappa];  // per-CTA trial sums read by the cluster (alternating buffers)
   float cpartf[2][kMaxKappa];
   int covl[2][kMaxKappa];
@@ -154,6 +157,10 @@ struct GcView {
   int *rlive, *rsp, *roff, *lrec;
   const int* nlv;
   double* com;
+  double* rdcom;  // per record max_dcom (molecule-pair cutoff boxes)
+  int* arec;      // record of each atom
+  int comcut;
+  double rmax;
   int natoms, nrec;
   int crank, csize;  // rank of this CTA in the box's cluster, cluster size
 };
@@ -194,12 +201,43 @@ __device__ __forceinline__ R warp_multi_sum(R (&v)[TG], int lane, int& which) {
 // of GB300 issues at 1/64 of the FP32 rate); CBMC trial batches (TG > 2) stay
 // FP32 to the end and fill gs.ef only, molecule energies (TG = 2) add the
 // per-warp sums in FP64 and fill both gs.e and gs.ef.
+// In a molecule-pair cutoff box (FP64 kernel) a box atom counts for trial t
+// only when its molecule passes Check_MoleculePair_Cutoff (energy_routines.f90:
+// 3027-3088) against the trial's atoms gs.tids (their COM and max_dcom, masses
+// tmass), overlap test included, as in the reference's molecule loops.
 template <bool MIXED, int TG>
 __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip_rec, bool cbmc,
-                               const int* ttype, bool convert = true) {
+                               const int* ttype, bool convert = true, const double* tmass = nullptr) {
   const BoxDev& b = *V.b;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntid = gs.ntid;
+  const bool mp = !MIXED && V.comcut && tmass != nullptr;
+  if (mp) {
+    for (int t = threadIdx.x; t < ntr; t += blockDim.x) {  // Get_COM, Compute_Max_COM_Distance
+      double tm = 0.0, x = 0.0, y = 0.0, z = 0.0;
+      for (int k = 0; k < ntid; ++k) {
+        const int a = gs.tids[k];
+        const double* tr = gs.trial[t] + 3 * a;
+        tm += tmass[a];
+        x += tmass[a] * tr[0];
+        y += tmass[a] * tr[1];
+        z += tmass[a] * tr[2];
+      }
+      const double cx = x / tm, cy = y / tm, cz = z / tm;
+      double dmax = 0.0;
+      for (int k = 0; k < ntid; ++k) {
+        const double* tr = gs.trial[t] + 3 * gs.tids[k];
+        const double dx = tr[0] - cx, dy = tr[1] - cy, dz = tr[2] - cz;
+        dmax = fmax(dmax, dx * dx + dy * dy + dz * dz);
+      }
+      gs.tcom[t][0] = cx;
+      gs.tcom[t][1] = cy;
+      gs.tcom[t][2] = cz;
+      gs.tcom[t][3] = sqrt(dmax);
+    }
+    __syncthreads();
+  }
+  const double rint0 = cbmc ? sqrt(b.rcut_cbmcsq) : V.rmax;
   if (MIXED && convert) {  // else the caller wrote gs.trialf
     for (int q = threadIdx.x; q < ntr * ntid * 3; q += blockDim.x) {
       const int t = q / (3 * ntid), r = q % (3 * ntid), a = gs.tids[r / 3];
@@ -263,11 +301,26 @@ __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip
       } else {
         const double xj = V.sx[j], yj = V.sy[j], zj = V.sz[j];
         const int tj = V.lvt[i];
+        unsigned inm = 0xffffffffu;  // trials whose molecule pair with j's molecule interacts
+        if (mp) {
+          const int rj = V.arec[j];
+          const double mx = V.com[3 * rj], my = V.com[3 * rj + 1], mz = V.com[3 * rj + 2], md = V.rdcom[rj];
+#pragma unroll
+          for (int u = 0; u < TG; ++u) {
+            if (t0 + u < ntr) {
+              const double* c = gs.tcom[t0 + u];
+              const double dx = fold(c[0] - mx, b.hL[0], b.L[0]);
+              const double dy = fold(c[1] - my, b.hL[1], b.L[1]);
+              const double dz = fold(c[2] - mz, b.hL[2], b.L[2]);
+              if (sqrt(dx * dx + dy * dy + dz * dz) > rint0 + c[3] + md) inm &= ~(1u << u);
+            }
+          }
+        }
         for (int k = 0; k < ntid; ++k) {
           const int a = gs.tids[k], ta = ttype[a];
 #pragma unroll
           for (int u = 0; u < TG; ++u) {
-            if (t0 + u < ntr) {
+            if (t0 + u < ntr && ((inm >> u) & 1u)) {
               const double* tr = gs.trial[t0 + u] + 3 * a;
               const double dx = fold(tr[0] - xj, b.hL[0], b.L[0]);
               const double dy = fold(tr[1] - yj, b.hL[1], b.L[1]);
@@ -610,7 +663,7 @@ __device__ bool gc_place_fragments(const GcArgs& A, const GcView& V, GrowState& 
         if ((gs.newex >> a) & 1u) gs.tids[gs.ntid++] = a;
     }
     __syncthreads();
-    batch_energies<MIXED, 16>(V, gs, kd, gs.rec, true, S.type);
+    batch_energies<MIXED, 16>(V, gs, kd, gs.rec, true, S.type, true, S.mass);
     if (threadIdx.x == 0) {
       const double beta = b.beta;
       double w[kMaxKappa];
@@ -732,7 +785,7 @@ __device__ bool gc_build(const GcArgs& A, const GcView& V, GrowState& gs, bool d
       for (int d = 0; d < 3; ++d) gs.trial[it][3 * a + d] = gs.r[3 * a + d] - gs.com[d] + gs.draws[3 * it + d];
     }
   __syncthreads();
-  batch_energies<MIXED, 16>(V, gs, ki, gs.rec, true, S.type);
+  batch_energies<MIXED, 16>(V, gs, ki, gs.rec, true, S.type, true, S.mass);
   if (threadIdx.x == 0) {
     const double beta = b.beta;
     double w[kMaxKappa];
@@ -790,7 +843,7 @@ __device__ void gc_mol_energies(const GcArgs& A, const GcView& V, GrowState& gs,
     }
   }
   __syncthreads();
-  batch_energies<MIXED, 2>(V, gs, 1, gs.rec, false, ttype);
+  batch_energies<MIXED, 2>(V, gs, 1, gs.rec, false, ttype, true, A.sp[gs.is].mass);
   if (threadIdx.x == 0) {
     IntraOut io{0, 0, 0, 0, 0, 0, 0, false};
     if (with_intra) io = molecule_intra(A.P, gs.is, *V.b, *V.T, gs.r);
@@ -1285,7 +1338,8 @@ __device__ void gc_setup(const GcArgs& A, const GcBox& G, const PairTable& T, in
   double* sy = sx + N;
   double* sz = sy + N;
   double* scom = sz + N;  // [R][3]
-  int* lv = reinterpret_cast<int*>(scom + 3 * R);
+  double* rdcom = scom + 3 * R;  // [R]
+  int* lv = reinterpret_cast<int*>(rdcom + R);
   int* apos = lv + N;
   int* lvt = apos + N;  // FP64 kernel only
   int* rlive = lvt + (MIXED ? 0 : N);
@@ -1293,8 +1347,9 @@ __device__ void gc_setup(const GcArgs& A, const GcBox& G, const PairTable& T, in
   int* roff = rsp + R;
   int* pool = roff + R;
   int* lrec = pool + R;
+  int* arec = lrec + R;  // [N]
   float4* lv32 = reinterpret_cast<float4*>(reinterpret_cast<unsigned char*>(smem) +
-                                           ((((size_t)(lrec + R) - (size_t)smem) + 15) & ~(size_t)15));
+                                           ((((size_t)(arec + N) - (size_t)smem) + 15) & ~(size_t)15));
   for (int j = threadIdx.x; j < N; j += blockDim.x) {
     const double4_32a p = G.xyzq[j];
     sx[j] = p.x;
@@ -1353,6 +1408,14 @@ __device__ void gc_setup(const GcArgs& A, const GcBox& G, const PairTable& T, in
     scom[3 * r] = x / tm;
     scom[3 * r + 1] = y / tm;
     scom[3 * r + 2] = z / tm;
+    double dmax = 0.0;  // Compute_Max_COM_Distance
+    for (int a = 0; a < s.natoms; ++a) {
+      const int j = roff[r] + a;
+      arec[j] = r;
+      const double dx = sx[j] - scom[3 * r], dy = sy[j] - scom[3 * r + 1], dz = sz[j] - scom[3 * r + 2];
+      dmax = fmax(dmax, dx * dx + dy * dy + dz * dz);
+    }
+    rdcom[r] = sqrt(dmax);
   }
   if (threadIdx.x < kMaxAtoms) ttype[threadIdx.x] = threadIdx.x < A.S.natoms ? A.S.type[threadIdx.x] : -1;
   V.b = &b;
@@ -1374,6 +1437,10 @@ __device__ void gc_setup(const GcArgs& A, const GcBox& G, const PairTable& T, in
   V.lrec = lrec;
   V.nlv = &s_nlv;
   V.com = scom;
+  V.rdcom = rdcom;
+  V.arec = arec;
+  V.comcut = G.comcut;
+  V.rmax = G.rmax;
   V.natoms = N;
   V.nrec = R;
   V.crank = crank;
@@ -1409,6 +1476,7 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
   double* sy = V.sy;
   double* sz = V.sz;
   double* scom = V.com;
+  double* rdcom = V.rdcom;
   int* lv = V.lv;
   int* apos = V.apos;
   int* rlive = V.rlive;
@@ -1609,7 +1677,7 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
           }
         }
         __syncthreads();
-        batch_energies<MIXED, 2>(V, gs, 2, gs.rec, false, A.sp[is].type);
+        batch_energies<MIXED, 2>(V, gs, 2, gs.rec, false, A.sp[is].type, true, A.sp[is].mass);
         if (threadIdx.x == 0) {
           mv_acc = 0;
           if (gs.ov[0]) {  // the molecule overlapped before the move
@@ -2143,6 +2211,15 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
             if (MIXED && i >= 0) lv32[i] = make_float4((float)gs.r[3 * a], (float)gs.r[3 * a + 1], (float)gs.r[3 * a + 2], lv32[i].w);
           }
           for (int d = 0; d < 3; ++d) scom[3 * gs.rec + d] = gs.com[d];
+          if (!MIXED) {  // max_dcom of the molecule as placed (insertion, regrowth; rigid moves keep it)
+            double dmax = 0.0;
+            for (int a = 0; a < gs.na; ++a) {
+              const double dx = gs.r[3 * a] - gs.com[0], dy = gs.r[3 * a + 1] - gs.com[1],
+                           dz = gs.r[3 * a + 2] - gs.com[2];
+              dmax = fmax(dmax, dx * dx + dy * dy + dz * dz);
+            }
+            rdcom[gs.rec] = sqrt(dmax);
+          }
         }
       }
     }
@@ -2250,8 +2327,8 @@ __global__ void __launch_bounds__(kGcThreads, 1)
 }
 
 size_t gc_smem_bytes(int natoms, int nrec, bool mixed) {
-  size_t s = (size_t)natoms * (3 * sizeof(double) + (mixed ? 2 : 3) * sizeof(int)) +
-             (size_t)nrec * (3 * sizeof(double) + 5 * sizeof(int));
+  size_t s = (size_t)natoms * (3 * sizeof(double) + (mixed ? 3 : 4) * sizeof(int)) +
+             (size_t)nrec * (4 * sizeof(double) + 5 * sizeof(int));
   s = (s + 15) & ~(size_t)15;
   if (mixed) s += (size_t)natoms * sizeof(float4);
   return s;
@@ -2301,6 +2378,8 @@ static void gc_host_box(cass_ctx* c, int ib, const std::vector<int>& free_slots,
   g.ibox1 = ib + 1;
   g.rcut3 = B.rcut3;
   g.rcut9 = B.rcut9;
+  g.comcut = B.comcut ? 1 : 0;
+  g.rmax = B.rcut_max;
   const int nt = c->pt.ntypes;
   for (int ia = 0; ia < nt; ++ia)
     for (int ja = 0; ja < nt; ++ja) {
@@ -2392,7 +2471,6 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
       if (iboxes[j] == iboxes[k]) return set_error(CASS_EINVAL, "box listed twice");
     const BoxH& B = c->box[ib];
     if (!B.energy_valid) return set_error(CASS_ESTATE, "system energy of box not computed");
-    if (B.comcut) return set_error(CASS_EUNSUPPORTED, "molecule-pair COM cutoff (LJ CHARMM or minimum-image charges) is not applied by the grand-canonical kernel");
     if (B.desc.charge_style != CASS_CHARGE_NONE) return set_error(CASS_EUNSUPPORTED, "gcmc boxes hold no charges");
     if (B.desc.vdw_style != CASS_VDW_LJ) return set_error(CASS_EUNSUPPORTED, "gcmc needs LJ boxes");
     mixed = mixed && (B.desc.vdw_sum_style == CASS_VDW_SUM_CUT || B.desc.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL);
@@ -2621,7 +2699,6 @@ extern "C" int cass_build_molecule(cass_ctx* c, int32_t im, int32_t is1, int32_t
     if (s.frag_nconfig[f] < 1) return set_error(CASS_EINVAL, "fragment library is empty");
   const BoxH& B = c->box[ib];
   if (!B.defined) return set_error(CASS_ESTATE, "box not defined");
-  if (B.comcut) return set_error(CASS_EUNSUPPORTED, "molecule-pair COM cutoff (LJ CHARMM or minimum-image charges) is not applied by the grand-canonical kernel");
   if (B.desc.charge_style != CASS_CHARGE_NONE) return set_error(CASS_EUNSUPPORTED, "build_molecule boxes hold no charges");
   if (B.desc.vdw_style != CASS_VDW_LJ) return set_error(CASS_EUNSUPPORTED, "build_molecule needs LJ boxes");
   const int slot = c->mol_base[is] + im - 1;

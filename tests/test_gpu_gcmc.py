@@ -34,7 +34,10 @@ def _run(open_ctx, s, nsteps, seed, mu=(-22.0, -26.0)):
 
 STYLES = {"cut_tail": abi.VDW_SUM_CUT_TAIL, "cut": abi.VDW_SUM_CUT, "cut_shift": abi.VDW_SUM_CUT_SHIFT,
           "cut_switch": abi.VDW_SUM_CUT_SWITCH, "cut_shift_force": abi.VDW_SUM_CUT_SHIFT_FORCE,
-          "minimum": abi.VDW_SUM_MINIMUM}
+          "minimum": abi.VDW_SUM_MINIMUM,
+          # no atom cutoff: molecule pairs selected by Check_MoleculePair_Cutoff
+          # (energy_routines.f90:3027-3088) in every energy of every move
+          "charmm": abi.VDW_SUM_CHARMM}
 
 
 @pytest.mark.parametrize("style", list(STYLES))

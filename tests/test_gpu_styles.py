@@ -8,8 +8,8 @@ CBMC cutoffs, and Widom insertions record by record.  Where a style has no atom
 cutoff (LJ CHARMM, minimum-image charges) and the vdW sum is not minimum image,
 Check_MoleculePair_Cutoff (:3027-3088) selects the interacting molecules by their
 COM distance; the system and molecule energies, the MC sweeps, the CBMC trial
-energies and the Widom insertions apply it (grand-canonical moves and the
-allocation-free call refuse such boxes)."""
+energies, the Widom insertions and the grand-canonical moves apply it (the
+allocation-free call refuses such boxes)."""
 import numpy as np
 import pytest
 
