@@ -704,6 +704,26 @@ int ensure_pools(cass_ctx* c) {
 
 using namespace cassgpu;
 
+namespace cassgpu {
+// One upload of a frame load: `bytes` (a multiple of 16) from offset `src` of
+// the staged frame to the device array `dst`
+struct StageCopy {
+  long long src, bytes;
+  void* dst;
+  long long pad;
+};
+
+// Copies of a frame load out of the device copy of the staging area, one CTA
+// per copy, 16-byte words
+__global__ void k_stage_scatter(const unsigned char* stage, const StageCopy* cp) {
+  const StageCopy d = cp[blockIdx.x];
+  const uint4* s = reinterpret_cast<const uint4*>(stage + d.src);
+  uint4* t = reinterpret_cast<uint4*>(d.dst);
+  for (long long i = threadIdx.x; i < d.bytes / 16; i += blockDim.x) t[i] = s[i];
+}
+
+}  // namespace cassgpu
+
 namespace {
 
 int set_device(cass_ctx* c) {
@@ -757,9 +777,11 @@ size_t pack_bytes(cass_ctx* c, int ibox) {
 }
 
 // Packs the live molecules of a box (species-major, locate order) into pinned
-// staging at `stage` (pack_bytes long) and queues the uploads; the caller
+// staging at `stage` (pack_bytes long) and queues the uploads (or, with
+// `defer`, lists them for one upload of the whole staging area); the caller
 // synchronizes before the staging is reused.
-int pack_box_async(cass_ctx* c, int ibox, unsigned char* stage) {
+int pack_box_async(cass_ctx* c, int ibox, unsigned char* stage, std::vector<cassgpu::StageCopy>* defer = nullptr,
+                   const unsigned char* base = nullptr) {
   BoxH& B = c->box[ibox];
   const std::vector<int>& mem = members(c, ibox);
   size_t na = 0;
@@ -827,7 +849,15 @@ int pack_box_async(cass_ctx* c, int ibox, unsigned char* stage) {
     CASS_CUDA(h2d(c, B.d_com.p, com.data(), na * sizeof(double4_32a)));
     CASS_CUDA(cudaStreamSynchronize(c->stream));  // the host vector goes out of scope
   }
-  if (na > 0) {
+  if (na > 0 && defer) {
+    auto add = [&](const void* src, void* dst, size_t bytes) {
+      defer->push_back(cassgpu::StageCopy{(long long)(static_cast<const unsigned char*>(src) - base), (long long)bytes, dst, 0});
+    };
+    add(p64, B.d_p64.p, na * sizeof(double4_32a));
+    add(p32, B.d_p32.p, na * sizeof(float4));
+    add(meta, B.d_meta.p, na * sizeof(int4));
+    add(molinfo, B.d_molinfo.p, nm * sizeof(int4));
+  } else if (na > 0) {
     CASS_CUDA(h2d(c, B.d_p64.p, p64, na * sizeof(double4_32a)));
     CASS_CUDA(h2d(c, B.d_p32.p, p32, na * sizeof(float4)));
     CASS_CUDA(h2d(c, B.d_meta.p, meta, na * sizeof(int4)));
@@ -2137,15 +2167,29 @@ int frame_setup_ext(cass_ctx* c) {
   for (BoxH& B : c->box)
     if (box_has_ewald(B)) nv = std::max(nv, B.nvecs);
   if (nv > 0 && (rc = ensure_cos_mol(c, nv))) return rc;
-  // every dirty box packed into one pinned staging area, one synchronization
+  // every dirty box packed into one pinned staging area, uploaded in one copy
+  // with the list of its per-box arrays and scattered by one kernel (four
+  // copies per box cost more in API calls than in bytes), one synchronization
   std::vector<size_t> off(c->nboxes + 1, 0);
   for (int ibox = 0; ibox < c->nboxes; ++ibox)
     off[ibox + 1] = off[ibox] + (c->box[ibox].pack_dirty ? pack_bytes(c, ibox) : 0);
-  if ((rc = c->h_pack.reserve(std::max<size_t>(off[c->nboxes], 256)))) return rc;
+  const size_t list_off = (off[c->nboxes] + 255) & ~(size_t)255;
+  const size_t total = list_off + (size_t)4 * c->nboxes * sizeof(StageCopy);
+  if ((rc = c->h_pack.reserve(std::max<size_t>(total, 256)))) return rc;
+  unsigned char* hs = static_cast<unsigned char*>(c->h_pack.p);
+  std::vector<StageCopy> cps;
   for (int ibox = 0; ibox < c->nboxes; ++ibox)
-    if (c->box[ibox].pack_dirty &&
-        (rc = pack_box_async(c, ibox, static_cast<unsigned char*>(c->h_pack.p) + off[ibox])))
-      return rc;
+    if (c->box[ibox].pack_dirty && (rc = pack_box_async(c, ibox, hs + off[ibox], &cps, hs))) return rc;
+  if (!cps.empty()) {
+    memcpy(hs + list_off, cps.data(), cps.size() * sizeof(StageCopy));
+    const size_t up = list_off + cps.size() * sizeof(StageCopy);
+    if ((rc = c->d_stage.reserve(up))) return rc;
+    CASS_CUDA(h2d(c, c->d_stage.p, hs, up));
+    k_stage_scatter<<<(unsigned)cps.size(), 256, 0, c->stream>>>(
+        c->d_stage.as<unsigned char>(), reinterpret_cast<const StageCopy*>(c->d_stage.as<unsigned char>() + list_off));
+    CASS_CUDA(cudaGetLastError());
+    count_launch(c);
+  }
   CASS_CUDA(cudaStreamSynchronize(c->stream));
   for (int ibox = 0; ibox < c->nboxes; ++ibox) {
     BoxH& B = c->box[ibox];

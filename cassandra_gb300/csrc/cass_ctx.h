@@ -228,6 +228,7 @@ struct cass_ctx_impl {
   DevBuf d_cbmc_tab;
   // pinned staging of the packed-box uploads
   PinnedBuf h_pack;
+  DevBuf d_stage;  // device copy of a frame load's staging area
 };
 
 // builds the CBMC-option tables if needed and points each box's BoxDev at them

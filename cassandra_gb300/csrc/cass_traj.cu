@@ -11,6 +11,7 @@
 // atoms are uploaded from pinned staging.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -118,6 +119,31 @@ struct Frame {
 
 }  // namespace
 
+// Readers parse at most (hardware threads - 1) frames at a time, so that the
+// thread loading a frame (folding and packing its molecules) keeps a core:
+// with one reader per box and all of them busy it ran 2-4x slower.
+struct ParseSlots {
+  std::mutex mu;
+  std::condition_variable cv;
+  int free_slots = std::max(1, (int)std::thread::hardware_concurrency() - 1);
+  void acquire() {
+    std::unique_lock<std::mutex> lk(mu);
+    cv.wait(lk, [&] { return free_slots > 0; });
+    --free_slots;
+  }
+  void release() {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      ++free_slots;
+    }
+    cv.notify_one();
+  }
+};
+ParseSlots& parse_slots() {
+  static ParseSlots p;
+  return p;
+}
+
 struct cass_traj {
   RecordFile fx, fh;
   bool has_h = false;
@@ -208,11 +234,13 @@ struct cass_traj {
         if (stop) return;
         k = fill;
       }
+      parse_slots().acquire();
       auto t0 = std::chrono::steady_clock::now();
       Frame& F = slot[k];
       read_frame(F);
       F.index = frames;
       auto t1 = std::chrono::steady_clock::now();
+      parse_slots().release();
       {
         std::lock_guard<std::mutex> lk(mu);
         parse_s += std::chrono::duration<double>(t1 - t0).count();
@@ -223,6 +251,16 @@ struct cass_traj {
       }
       cv.notify_all();
       if (F.status != 0) return;  // the end or an error: nothing more to read
+    }
+  }
+
+  // the frame taken last goes back to the reader (its data is no longer read)
+  void release_taken() {
+    std::lock_guard<std::mutex> lk(mu);
+    const int prev = take ^ 1;
+    if (state[prev] == 2) {
+      state[prev] = 0;
+      cv.notify_all();
     }
   }
 
@@ -393,6 +431,9 @@ int cass_load_next_frame(cass_ctx* c, int32_t nboxes, cass_traj* const* traj, in
       base[is] += fr[b].nmols[is];
     }
   }
+  // the frames are copied: the readers parse the next ones while the boxes
+  // are packed and the device works on this frame
+  for (int b = 0; b < nboxes; ++b) traj[b]->release_taken();
   CASS_CUDA(cudaSetDevice(c->device));
   int rc;
   for (int b = 0; b < nboxes; ++b) {
