@@ -59,6 +59,66 @@ struct GradAtom {
   int mol, type, species, atom;
 };
 
+// The vdW pair energy of Compute_AtomPair_Energy (energy_routines.f90:1907-2000)
+// in the box's style, differentiated: dE/d(r^2), dE/d(eps) and dE/d(sigma) of
+// a pair within its cutoff (scale: vdw_intra_scale or 1).  LJ: cut, cut_tail,
+// cut_shift, cut_switch, cut_shift_force and minimum image; Mie: cut and
+// cut_shift.  The forms follow vdw_pair term by term.
+__device__ __forceinline__ void vdw_pair_grad(const PairTable& T, const BoxDev& b, int k, double r2, double vs,
+                                              double& dEdr2, double& dEde, double& dEds) {
+  const double eps = T.eps[k], sig2 = T.sig2[k], sig = sqrt(sig2);
+  if (b.vdw_style == CASS_VDW_MIE) {
+    const double r = sqrt(r2), n = T.mie_n[k], m = T.mie_m[k], cm = T.mie_c[k];
+    const double sn = pow(sig / r, n), sm = pow(sig / r, m);
+    double e = sn - sm, de_sig = n * sn - m * sm;
+    if (b.vdw_sum_style == CASS_VDW_SUM_CUT_SHIFT) {
+      const double cn = pow(sig / b.rcut_vdw, n), cmm = pow(sig / b.rcut_vdw, m);
+      e -= cn - cmm;
+      de_sig -= n * cn - m * cmm;
+    }
+    dEdr2 = cm * eps * vs * (-n * sn + m * sm) / (2.0 * r2);
+    dEde = cm * vs * e;
+    dEds = cm * eps * vs * de_sig / sig;
+    return;
+  }
+  const double s2 = sig2 / r2, s6 = s2 * s2 * s2, s12 = s6 * s6;
+  const double elj = 4.0 * (s12 - s6);                  // E / eps
+  const double dlj_dr2 = 4.0 * (-6.0 * s12 + 3.0 * s6) / r2;  // d(E / eps) / d(r^2)
+  const double dlj_ds = 4.0 * (12.0 * s12 - 6.0 * s6) / sig;  // d(E / eps) / d(sigma)
+  double fe = elj, fr = dlj_dr2, fs = dlj_ds;  // the style's E / eps and its derivatives
+  switch (b.vdw_sum_style) {
+    case CASS_VDW_SUM_CUT_SHIFT: {
+      const double c2 = sig2 / b.rcut_vdwsq, c6 = c2 * c2 * c2, c12 = c6 * c6;
+      fe -= 4.0 * (c12 - c6);
+      fs -= 4.0 * (12.0 * c12 - 6.0 * c6) / sig;
+      break;
+    }
+    case CASS_VDW_SUM_CUT_SWITCH:
+      if (r2 >= b.ron_switch_sq) {  // E = S(r^2) E_LJ, S = d^2 (f2 + 2 r^2) f1, d = roff^2 - r^2
+        const double d = b.roff_switch_sq - r2;
+        const double S = d * d * (b.switch_factor2 + 2.0 * r2) * b.switch_factor1;
+        const double dS = 2.0 * b.switch_factor1 * d * (d - (b.switch_factor2 + 2.0 * r2));
+        fr = dS * elj + S * dlj_dr2;
+        fe = S * elj;
+        fs = S * dlj_ds;
+      }
+      break;
+    case CASS_VDW_SUM_CUT_SHIFT_FORCE: {  // E - E(rc) - (r - rc) dE/dr(rc)
+      const double c2 = sig2 / b.rcut_vdwsq, c6 = c2 * c2 * c2, c12 = c6 * c6, rc = b.rcut_vdw, r = sqrt(r2);
+      const double g = -24.0 * (2.0 * c12 / rc - c6 / rc);  // dE/dr(rc) / eps
+      fe = elj - 4.0 * (c12 - c6) - (r - rc) * g;
+      fr = dlj_dr2 - g / (2.0 * r);
+      fs = dlj_ds - 4.0 * (12.0 * c12 - 6.0 * c6) / sig + (r - rc) * 24.0 * (24.0 * c12 - 6.0 * c6) / (rc * sig);
+      break;
+    }
+    default:
+      break;
+  }
+  dEdr2 = eps * vs * fr;
+  dEde = vs * fe;
+  dEds = eps * vs * fs;
+}
+
 // pre2: an FP32 bound on r^2 beyond every cutoff of the box (with a margin far
 // above FP32 rounding of the coordinates): pairs beyond it are skipped before
 // the FP64 arithmetic, which then decides every cutoff exactly
@@ -75,7 +135,7 @@ __global__ void __launch_bounds__(kGradBlock) k_grad_pairs(BoxDev b, PairTable T
   const double4_32a pi = live ? p64[i] : make_double4_32a(0, 0, 0, 0);
   const float4 pif = live ? p32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   const int4 mi = live ? meta[i] : make_int4(-1, -1, -1, -1);
-  const bool lj = b.vdw_style == CASS_VDW_LJ;
+  const bool vdw = b.vdw_style == CASS_VDW_LJ || b.vdw_style == CASS_VDW_MIE;
   const bool coul = b.charge_style == CASS_CHARGE_COUL;
   double gx = 0, gy = 0, gz = 0, dqi = 0;
   double de[kMaxTypes], ds[kMaxTypes];
@@ -124,16 +184,15 @@ __global__ void __launch_bounds__(kGradBlock) k_grad_pairs(BoxDev b, PairTable T
         ov = true;
       }
       double dEdr2 = 0.0;  // dE/d(r^2) of this pair
-      // LJ: E = 4 eps s (s12 - s6), s6 = (sigma^2/r^2)^3
-      if (lj && r2 <= b.rcut_vdwsq && mi.y >= 0 && mj.y >= 0) {
+      if (vdw && (cutoff_mask(b, r2, false) & 1) && mi.y >= 0 && mj.y >= 0) {
         const int kk = pidx(mi.y, mj.y, T.ntypes);
-        const double eps = T.eps[kk], sig2 = T.sig2[kk];
-        if (eps != 0.0 && vs != 0.0) {
-          const double s2 = sig2 / r2, s6 = s2 * s2 * s2, s12 = s6 * s6;
-          dEdr2 += 4.0 * eps * vs * (-6.0 * s12 + 3.0 * s6) / r2;
+        if (T.eps[kk] != 0.0 && vs != 0.0) {
+          double er, ee, es;
+          vdw_pair_grad(T, b, kk, r2, vs, er, ee, es);
+          dEdr2 += er;
           if (j > i) {
-            de[mj.y] += 4.0 * vs * (s12 - s6);
-            ds[mj.y] += 4.0 * eps * vs * (12.0 * s12 - 6.0 * s6) / sqrt(sig2);
+            de[mj.y] += ee;
+            ds[mj.y] += es;
           }
         }
       }
@@ -328,10 +387,10 @@ extern "C" int cass_system_gradient(cass_ctx* c, int32_t ibox1, CassEnergy* ener
   BoxH& B = c->box[ib];
   if (!B.defined) return set_error(CASS_ESTATE, "box not defined");
   const CassBoxDesc& d = B.desc;
-  if (d.vdw_style != CASS_VDW_LJ && d.vdw_style != CASS_VDW_NONE)
-    return set_error(CASS_EUNSUPPORTED, "gradient: LJ or no vdW only");
-  if (d.vdw_style == CASS_VDW_LJ && d.vdw_sum_style != CASS_VDW_SUM_CUT && d.vdw_sum_style != CASS_VDW_SUM_CUT_TAIL)
-    return set_error(CASS_EUNSUPPORTED, "gradient: vdw sum style cut or cut_tail only");
+  if (d.vdw_style == CASS_VDW_LJ && d.vdw_sum_style == CASS_VDW_SUM_CHARMM)
+    return set_error(CASS_EUNSUPPORTED, "gradient: LJ CHARMM (molecule-pair cutoff) is not differentiated");
+  if (d.vdw_style == CASS_VDW_MIE && d.vdw_sum_style != CASS_VDW_SUM_CUT && d.vdw_sum_style != CASS_VDW_SUM_CUT_SHIFT)
+    return set_error(CASS_EUNSUPPORTED, "gradient: Mie with cut or cut_shift only");
   if (d.charge_style == CASS_CHARGE_COUL && d.charge_sum_style != CASS_QQ_EWALD)
     return set_error(CASS_EUNSUPPORTED, "gradient: charges need the Ewald sum");
   for (int is = 0; is < c->nspecies; ++is) {
@@ -384,7 +443,11 @@ extern "C" int cass_system_gradient(cass_ctx* c, int32_t ibox1, CassEnergy* ener
   if (n > 0) {
     // beyond every cutoff the kernel tests: pairs past it add nothing
     double rmax2 = 0.0;
-    if (d.vdw_style == CASS_VDW_LJ) rmax2 = std::max(rmax2, B.dev.rcut_vdwsq);
+    if (d.vdw_style != CASS_VDW_NONE) {
+      if (d.vdw_sum_style == CASS_VDW_SUM_MINIMUM) rmax2 = 1.0e30;  // every pair within the minimum image
+      else if (d.vdw_sum_style == CASS_VDW_SUM_CUT_SWITCH) rmax2 = std::max(rmax2, B.dev.roff_switch_sq);
+      else rmax2 = std::max(rmax2, B.dev.rcut_vdwsq);
+    }
     if (d.charge_style == CASS_CHARGE_COUL) rmax2 = std::max(rmax2, B.dev.rcut_coulsq);
     rmax2 = std::max(rmax2, B.dev.rcut_lowsq);
     const float pre2 = (float)(rmax2 * (1.0 + 1.0e-4) + 1.0e-3);

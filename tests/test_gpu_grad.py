@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 import cassandra_gb300 as cg
+import helpers
 import mc_helpers
 from cassandra_gb300 import abi
 from oracle import oracle
@@ -29,8 +30,7 @@ def _oracle_energy(system, xyz_by_mol, eps=None, sig=None, species=None):
         s.species = species
     with s.open(oracle.fns()) as o:
         if eps is not None:
-            nt = eps.shape[0]
-            o.set_nonbond_table(eps, sig, np.zeros((nt, nt)), np.zeros((nt, nt)))
+            o.set_nonbond_table(eps, sig, system.ff.mie_n, system.ff.mie_m)
         m = s.molecules
         o.set_molecules(m.im, m.is_, m.ibox, np.concatenate([x.ravel() for x in xyz_by_mol]))
         return o.system_total_energy(1)[0]["total"]
@@ -88,6 +88,46 @@ def test_lj_gradient_matches_numpy_and_fd():
         em = _oracle_energy(s, m.xyz, eps, sig)
         fd = (ep - em) / (2 * h)
         assert abs(fd - dref) <= 1e-6 * abs(fd), (tab, fd, dref)
+
+
+STYLES = {"lj_cut_shift": (abi.VDW_LJ, abi.VDW_SUM_CUT_SHIFT), "lj_cut_switch": (abi.VDW_LJ, abi.VDW_SUM_CUT_SWITCH),
+          "lj_cut_shift_force": (abi.VDW_LJ, abi.VDW_SUM_CUT_SHIFT_FORCE),
+          "lj_minimum": (abi.VDW_LJ, abi.VDW_SUM_MINIMUM),
+          "mie_cut": (abi.VDW_MIE, abi.VDW_SUM_CUT), "mie_cut_shift": (abi.VDW_MIE, abi.VDW_SUM_CUT_SHIFT)}
+
+
+@pytest.mark.parametrize("name", list(STYLES))
+def test_vdw_style_gradients_match_fd(name):
+    """dU/dr, dU/d(eps) and dU/d(sigma) in the shifted, switched, shifted-force and
+    minimum-image LJ sums and the Mie cut and cut_shift forms, against central
+    differences of the oracle's energy (300 atoms, 10 A cutoff, switch 8-10 A)."""
+    style, vsum = STYLES[name]
+    vdw = ("Mie", 120.0, 3.4, 14.0, 6.0) if style == abi.VDW_MIE else ("LJ", 120.0, 3.4)
+    s = helpers.lj_fluid_system(vsum, vdw, style)
+    e, g, de, ds, dq = _gpu_gradient(s)
+    m = s.molecules
+    order = _box_order(s)
+    scale = np.max(np.abs(g))
+    rng = np.random.default_rng(7)
+    for k in rng.choice(len(order), 4, replace=False):
+        for d in range(3):
+            xyz = [x.copy() for x in m.xyz]
+            h = H_REL * max(1.0, abs(xyz[order[k]][0, d]))
+            xyz[order[k]][0, d] += h
+            ep = _oracle_energy(s, xyz)
+            xyz[order[k]][0, d] -= 2 * h
+            em = _oracle_energy(s, xyz)
+            assert abs((ep - em) / (2 * h) - g[k, d]) <= FD_TOL * scale, (name, k, d)
+    for tab, dref in (("eps", de[0, 0]), ("sig", ds[0, 0])):
+        eps, sig = s.ff.eps.copy(), s.ff.sig.copy()
+        t = eps if tab == "eps" else sig
+        h = H_REL * t[0, 0]
+        t[0, 0] += h
+        ep = _oracle_energy(s, m.xyz, eps, sig)
+        t[0, 0] -= 2 * h
+        em = _oracle_energy(s, m.xyz, eps, sig)
+        fd = (ep - em) / (2 * h)
+        assert abs(fd - dref) <= 1e-6 * abs(fd), (name, tab, fd, dref)
 
 
 def test_water_ewald_gradient_matches_fd():
