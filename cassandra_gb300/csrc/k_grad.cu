@@ -38,6 +38,7 @@ namespace cassgpu {
 
 constexpr int kGradBlock = 128;
 constexpr int kGradPairVals = 4 + 2 * kMaxTypes;  // gx, gy, gz, dq, deps[t], dsig[t]
+constexpr int kMaxAtomsGrad = 64;  // atoms of a molecule with bonded terms (k_grad_bonded's arrays)
 
 // A&S 7.1.26: erfc(x) = t P(t) exp(-x^2), t = 1/(1+px); returns erfc and its
 // derivative with respect to x
@@ -117,6 +118,143 @@ __device__ __forceinline__ void vdw_pair_grad(const PairTable& T, const BoxDev& 
   dEdr2 = eps * vs * fr;
   dEde = vs * fe;
   dEds = eps * vs * fs;
+}
+
+// d cos(phi) / d r of the dihedral angle of dihedral_cos_d (atoms a[0..3]):
+// cos phi = m.n / (|m||n|), m = r12 x r32, n = r32 x r34 (r12 = r1 - r2,
+// r32 = r3 - r2, r34 = r3 - r4); returns cos phi, adds scale * d cos / d r_k
+// to g[3 a[k] ...]
+__device__ inline double dihedral_cos_grad(const double* r, const int* a, double scale, double* g, bool add) {
+  double r12[3], r32[3], r34[3];
+  for (int d = 0; d < 3; ++d) {
+    r12[d] = r[3 * a[0] + d] - r[3 * a[1] + d];
+    r32[d] = r[3 * a[2] + d] - r[3 * a[1] + d];
+    r34[d] = r[3 * a[2] + d] - r[3 * a[3] + d];
+  }
+  const double m[3] = {r12[1] * r32[2] - r32[1] * r12[2], -r12[0] * r32[2] + r12[2] * r32[0],
+                       r12[0] * r32[1] - r12[1] * r32[0]};
+  const double nv[3] = {r32[1] * r34[2] - r32[2] * r34[1], -r32[0] * r34[2] + r32[2] * r34[0],
+                        r32[0] * r34[1] - r32[1] * r34[0]};
+  const double mm = m[0] * m[0] + m[1] * m[1] + m[2] * m[2], nn = nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2];
+  const double inv = 1.0 / sqrt(mm * nn);
+  const double cphi = (m[0] * nv[0] + m[1] * nv[1] + m[2] * nv[2]) * inv;
+  if (!add) return cphi;
+  double gm[3], gn[3];  // d cos / d m, d cos / d n
+  for (int d = 0; d < 3; ++d) {
+    gm[d] = nv[d] * inv - cphi * m[d] / mm;
+    gn[d] = m[d] * inv - cphi * nv[d] / nn;
+  }
+  // m = r12 x r32: d/d r12 = r32 x gm, d/d r32 = gm x r12; n = r32 x r34: d/d r32 = r34 x gn, d/d r34 = gn x r32
+  const double d12[3] = {r32[1] * gm[2] - r32[2] * gm[1], r32[2] * gm[0] - r32[0] * gm[2], r32[0] * gm[1] - r32[1] * gm[0]};
+  const double d32[3] = {gm[1] * r12[2] - gm[2] * r12[1] + r34[1] * gn[2] - r34[2] * gn[1],
+                         gm[2] * r12[0] - gm[0] * r12[2] + r34[2] * gn[0] - r34[0] * gn[2],
+                         gm[0] * r12[1] - gm[1] * r12[0] + r34[0] * gn[1] - r34[1] * gn[0]};
+  const double d34[3] = {gn[1] * r32[2] - gn[2] * r32[1], gn[2] * r32[0] - gn[0] * r32[2], gn[0] * r32[1] - gn[1] * r32[0]};
+  for (int d = 0; d < 3; ++d) {
+    g[3 * a[0] + d] += scale * d12[d];
+    g[3 * a[1] + d] += scale * (-d12[d] - d32[d]);
+    g[3 * a[2] + d] += scale * (d32[d] + d34[d]);
+    g[3 * a[3] + d] -= scale * d34[d];
+  }
+  return cphi;
+}
+
+// dU/dr of the bonded terms of Compute_Molecule_{Bond,Angle,Dihedral,Improper}_
+// Energy (energy_routines.f90:197-496), as molecule_intra forms them: harmonic
+// bonds k (l - l0)^2, harmonic angles k (theta - theta0)^2 with cos theta held
+// within +-0.999999 (flat beyond), Ryckaert-Bellemans dihedrals sum c_j cos^j
+// phi and harmonic impropers k (phi - phi0)^2.  One thread per molecule, added
+// to the molecule's atoms of grad (packed order).
+__global__ void k_grad_bonded(SpeciesPools P, const int4* __restrict__ molinfo, int nm,
+                              const double4_32a* __restrict__ p64, double* grad) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nm) return;
+  const int4 mi = molinfo[q];  // slot, species, first atom, atoms
+  const SpeciesDevHdr& h = P.hdr[mi.y];
+  if (h.nbonds + h.nangles + h.ndih + h.nimp == 0) return;
+  const int* ip = P.ip;
+  const double* dp = P.dp;
+  const int n = mi.w;
+  double r[3 * kMaxAtomsGrad], g[3 * kMaxAtomsGrad];
+  for (int a = 0; a < n; ++a) {
+    const double4_32a p = p64[mi.z + a];
+    r[3 * a] = p.x;
+    r[3 * a + 1] = p.y;
+    r[3 * a + 2] = p.z;
+    g[3 * a] = g[3 * a + 1] = g[3 * a + 2] = 0.0;
+  }
+  for (int k = 0; k < h.nbonds; ++k) {
+    if (ip[h.bond_kind_off + k] != CASS_BONDED_HARMONIC) continue;
+    const int a = ip[h.bond_atoms_off + 2 * k], c = ip[h.bond_atoms_off + 2 * k + 1];
+    const double dx = r[3 * a] - r[3 * c], dy = r[3 * a + 1] - r[3 * c + 1], dz = r[3 * a + 2] - r[3 * c + 2];
+    const double l = sqrt(dx * dx + dy * dy + dz * dz), l0 = dp[h.bond_param_off + 2 * k + 1];
+    const double f = 2.0 * dp[h.bond_param_off + 2 * k] * (l - l0) / l;
+    g[3 * a] += f * dx;
+    g[3 * a + 1] += f * dy;
+    g[3 * a + 2] += f * dz;
+    g[3 * c] -= f * dx;
+    g[3 * c + 1] -= f * dy;
+    g[3 * c + 2] -= f * dz;
+  }
+  for (int k = 0; k < h.nangles; ++k) {
+    if (ip[h.angle_kind_off + k] != CASS_BONDED_HARMONIC) continue;
+    const int a1 = ip[h.angle_atoms_off + 3 * k], a2 = ip[h.angle_atoms_off + 3 * k + 1],
+              a3 = ip[h.angle_atoms_off + 3 * k + 2];
+    double v21[3], v32[3];
+    for (int d = 0; d < 3; ++d) {
+      v21[d] = r[3 * a2 + d] - r[3 * a1 + d];
+      v32[d] = r[3 * a3 + d] - r[3 * a2 + d];
+    }
+    const double C23 = v21[0] * v32[0] + v21[1] * v32[1] + v21[2] * v32[2];
+    const double C22 = v21[0] * v21[0] + v21[1] * v21[1] + v21[2] * v21[2];
+    const double C33 = v32[0] * v32[0] + v32[1] * v32[1] + v32[2] * v32[2];
+    const double ct = C23 * (1.0 / sqrt(C33 * C22));
+    if (ct >= 0.999999 || ct <= -0.999999) continue;  // the clamp: theta is constant there
+    const double th = kPI - acos(ct), t0 = dp[h.angle_param_off + 2 * k + 1];
+    // dE/dcos = 2 k (theta - theta0) dtheta/dcos, dtheta/dcos = 1 / sqrt(1 - cos^2)
+    const double f = 2.0 * dp[h.angle_param_off + 2 * k] * (th - t0) / sqrt(1.0 - ct * ct);
+    const double inv = 1.0 / sqrt(C22 * C33);
+    for (int d = 0; d < 3; ++d) {
+      const double d21 = v32[d] * inv - ct * v21[d] / C22;  // dcos / d v21
+      const double d32 = v21[d] * inv - ct * v32[d] / C33;  // dcos / d v32
+      g[3 * a1 + d] -= f * d21;
+      g[3 * a2 + d] += f * (d21 - d32);
+      g[3 * a3 + d] += f * d32;
+    }
+  }
+  for (int k = 0; k < h.ndih; ++k) {
+    const int* a = ip + h.dih_atoms_off + 4 * k;
+    const double* c = dp + h.dih_rb_off + 6 * k;
+    const double cp = dihedral_cos_grad(r, a, 0.0, g, false);
+    double dEdc = 0.0, pw = 1.0;  // sum_j j c_j cos^(j-1)
+    for (int j = 1; j < 6; ++j) {
+      dEdc += j * c[j] * pw;
+      pw *= cp;
+    }
+    dihedral_cos_grad(r, a, dEdc, g, true);
+  }
+  for (int k = 0; k < h.nimp; ++k) {
+    const int* a = ip + h.imp_atoms_off + 4 * k;
+    const double cp = dihedral_cos_grad(r, a, 0.0, g, false);
+    if (cp >= 1.0 || cp <= -1.0) continue;
+    double n34[3];
+    double r12[3], r32[3], r34[3];
+    for (int d = 0; d < 3; ++d) {
+      r12[d] = r[3 * a[0] + d] - r[3 * a[1] + d];
+      r32[d] = r[3 * a[2] + d] - r[3 * a[1] + d];
+      r34[d] = r[3 * a[2] + d] - r[3 * a[3] + d];
+    }
+    n34[0] = r32[1] * r34[2] - r32[2] * r34[1];
+    n34[1] = -r32[0] * r34[2] + r32[2] * r34[0];
+    n34[2] = r32[0] * r34[1] - r32[1] * r34[0];
+    const double sgn = (r12[0] * n34[0] + r12[1] * n34[1] + r12[2] * n34[2]) < 0.0 ? -1.0 : 1.0;
+    const double phi = sgn * acos(cp), p0 = dp[h.imp_param_off + 2 * k + 1];
+    // dE/dcos = 2 k (phi - phi0) dphi/dcos, dphi/dcos = -sgn / sqrt(1 - cos^2)
+    const double dEdc = 2.0 * dp[h.imp_param_off + 2 * k] * (phi - p0) * (-sgn / sqrt(1.0 - cp * cp));
+    dihedral_cos_grad(r, a, dEdc, g, true);
+  }
+  for (int a = 0; a < n; ++a)
+    for (int d = 0; d < 3; ++d) grad[3 * (size_t)(mi.z + a) + d] += g[3 * a + d];
 }
 
 // pre2: an FP32 bound on r^2 beyond every cutoff of the box (with a margin far
@@ -393,13 +531,16 @@ extern "C" int cass_system_gradient(cass_ctx* c, int32_t ibox1, CassEnergy* ener
     return set_error(CASS_EUNSUPPORTED, "gradient: Mie with cut or cut_shift only");
   if (d.charge_style == CASS_CHARGE_COUL && d.charge_sum_style != CASS_QQ_EWALD)
     return set_error(CASS_EUNSUPPORTED, "gradient: charges need the Ewald sum");
+  bool flexible = false;  // harmonic or torsional terms: their gradient runs too
   for (int is = 0; is < c->nspecies; ++is) {
     const SpeciesH& s = c->sp[is];
     if (!s.defined) continue;
-    bool flexible = !s.dih_atoms.empty() || !s.imp_atoms.empty();
-    for (int k : s.bond_kind) flexible = flexible || k == CASS_BONDED_HARMONIC;
-    for (int k : s.angle_kind) flexible = flexible || k == CASS_BONDED_HARMONIC;
-    if (flexible) return set_error(CASS_EUNSUPPORTED, "gradient: species with harmonic or torsional terms");
+    bool flex = !s.dih_atoms.empty() || !s.imp_atoms.empty();
+    for (int k : s.bond_kind) flex = flex || k == CASS_BONDED_HARMONIC;
+    for (int k : s.angle_kind) flex = flex || k == CASS_BONDED_HARMONIC;
+    if (flex && s.natoms > kMaxAtomsGrad)
+      return set_error(CASS_ECAPACITY, "gradient: a species with bonded terms has more than 64 atoms");
+    flexible = flexible || flex;
   }
   // energy, packed atoms and structure factors of the current configuration
   CassEnergy E;
@@ -470,6 +611,12 @@ extern "C" int cass_system_gradient(cass_ctx* c, int32_t ibox1, CassEnergy* ener
     k_grad_types<<<kMaxTypes, kTypeBlock, 0, c->stream>>>(B.d_meta.as<int4>(), n, d_de, d_ds, d_te, d_ts);
     CASS_CUDA(cudaGetLastError());
     count_launch(c);
+    if (flexible && B.npacked_mols > 0) {
+      k_grad_bonded<<<(B.npacked_mols + 127) / 128, 128, 0, c->stream>>>(c->pools, B.d_molinfo.as<int4>(),
+                                                                          B.npacked_mols, B.d_p64.as<double4_32a>(), d_g);
+      CASS_CUDA(cudaGetLastError());
+      count_launch(c);
+    }
   }
   std::vector<double> g(3 * (size_t)n), q(n), te(kMaxTypes * kMaxTypes, 0.0), ts(kMaxTypes * kMaxTypes, 0.0);
   int hov = 0;

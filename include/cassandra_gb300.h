@@ -408,10 +408,11 @@ int cass_build_molecule(cass_ctx* ctx, int32_t im, int32_t is, int32_t ibox, int
 /* The derivatives of the total energy of box ibox, as cass_system_total_energy
  * computes it (and returns it in *energy), for boxes with LJ (cut, cut_tail,
  * cut_shift, cut_switch, cut_shift_force or minimum image), Mie (cut or
- * cut_shift) or no vdW, no charges or an Ewald sum, and rigid species (fixed
- * bonds and angles, no dihedrals or impropers): intramolecular nonbond pairs
- * with their scale factors, intermolecular vdW and real-space Ewald pairs, the
- * long-range correction, the reciprocal sum and the self energy.  The real-space term is
+ * cut_shift) or no vdW, and no charges or an Ewald sum: the bonded terms
+ * (harmonic bonds and angles, Ryckaert-Bellemans dihedrals, harmonic
+ * impropers; molecules with such terms up to 64 atoms), intramolecular nonbond
+ * pairs with their scale factors, intermolecular vdW and real-space Ewald
+ * pairs, the long-range correction, the reciprocal sum and the self energy.  The real-space term is
  * differentiated through the same A&S erfc.  No counterpart in the reference,
  * which has no derivatives; computed in FP64.
  *   dU_dr    [n][natoms(is)][3]: the live molecules of the box in species-major,

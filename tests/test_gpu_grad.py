@@ -198,10 +198,36 @@ def test_autograd_function_chain_rule():
         model.close()
 
 
-def test_gradient_rejects_flexible_species():
-    from cassandra_gb300 import workloads
-    s = workloads.widom_batch_system(nboxes=1, sizes=[200])
+def test_flexible_pentane_gradient_matches_fd():
+    """Pentane (60 molecules from the reference's pregen example) with its
+    harmonic angles and Ryckaert-Bellemans dihedrals, plus harmonic bonds (k 450
+    K/A^2) and a harmonic improper per molecule added for the test: dU/dr against
+    central differences of the oracle's energy, every atom of three molecules."""
+    s = helpers.pregen_system("pentane", 0)
+    sp = copy.deepcopy(s.species[0])
+    sp.bonds = [(a, b, "harmonic", 450.0, 0.97 * l0) for (a, b, _, l0, _t) in sp.bonds]  # strained
+    sp.impropers = [(1, 2, 3, 4, "harmonic", 25.0, 170.0)]
+    s.species = [sp]
+    e, g, de, ds, dq = _gpu_gradient(s)
+    m = s.molecules
+    order = _box_order(s)
+    scale = np.max(np.abs(g))
+    rng = np.random.default_rng(4)
+    for k in rng.choice(len(order), 3, replace=False):
+        for a in range(sp.natoms):
+            for d in range(3):
+                xyz = [x.copy() for x in m.xyz]
+                h = H_REL * max(1.0, abs(xyz[order[k]][a, d]))
+                xyz[order[k]][a, d] += h
+                ep = _oracle_energy(s, xyz)
+                xyz[order[k]][a, d] -= 2 * h
+                em = _oracle_energy(s, xyz)
+                assert abs((ep - em) / (2 * h) - g[sp.natoms * k + a, d]) <= FD_TOL * scale, (k, a, d)
+
+
+def test_gradient_rejects_charmm():
+    s = helpers.lj_fluid_system(abi.VDW_SUM_CHARMM)
     with cg.open_system(s, precision=abi.PREC_FP64) as g:
         with pytest.raises(abi.CassError) as e:
-            g.system_gradient(1, 200)
+            g.system_gradient(1, 300)
         assert e.value.code == abi.CASS_EUNSUPPORTED
