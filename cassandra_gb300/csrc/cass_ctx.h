@@ -179,11 +179,16 @@ struct cass_ctx_impl {
   int count_pairs = 0;
   double widom_cells = 0.0;  // cells per rcut_cbmc in the Widom cell lists (0: default)
   int widom_waves = 0;       // CTAs per resident slot of the FP32 Widom launch (0: default)
+  int widom_threads = 0;     // threads per CTA of the FP32 Widom launch, 512 or 256 (0: 512)
   double widom_band = 1.0;   // scale of the FP32 cutoff bands of the mixed Widom full-cutoff pass
   int mc_cluster = 0;        // CTAs per chain of cass_mc_sweeps (0: chosen per call)
   // launch shapes the Widom autotuner chose, per batch signature: (cells per cutoff, waves)
   bool widom_autotune = true;
-  std::vector<std::pair<std::vector<long long>, std::pair<double, int>>> widom_tuned;
+  struct WidomShape {
+    double cells;
+    int waves, threads;
+  };
+  std::vector<std::pair<std::vector<long long>, WidomShape>> widom_tuned;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   int nspecies = 0, ntypes = 0, nboxes = 0, max_kvec = 100000;
   std::vector<int> max_mol, mol_base;

@@ -1615,9 +1615,10 @@ __device__ RecF run_insertion_f(const WidomSpecies& S, const SpeciesF& SF, const
 }
 
 // 16 warps per staged box and two CTAs per SM (64 registers): the kernel is
-// latency-bound, and warps per scheduler matter more than the few spills
+// latency-bound, and warps per scheduler matter more than the few spills.  The
+// launch autotuner may choose 256-thread CTAs instead (four per SM by
+// registers, fewer by shared memory for large boxes; more CTAs per box).
 constexpr int kF32Threads = 512;
-constexpr int kF32MinBlocks = 2;
 constexpr int kF32Waves = 8;  // CTAs per resident slot: many short waves even out uneven boxes
 
 // FP32 constants of box b (thread 0), the FP64 edges and squared cutoffs
@@ -1669,8 +1670,8 @@ __device__ inline void widom_ljp(float2* s_ljp, const PairTable& T) {
   }
 }
 
-template <bool SMEM, bool COUNT, bool OPT>
-__global__ void __launch_bounds__(kF32Threads, kF32MinBlocks) k_widom_f32(WidomSpecies S, SpeciesF SF, PairTable T, const BoxDev* boxes,
+template <bool SMEM, bool COUNT, bool OPT, int NT = kF32Threads>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_widom_f32(WidomSpecies S, SpeciesF SF, PairTable T, const BoxDev* boxes,
                                                    const int* box_ids, const float4* c32, const float* cq32,
                                                    const int* cstart, const float* __restrict__ libf, long long n_ins,
                                                    uint64_t seed, WRec* rec, signed char* status, double* xyz,
@@ -2366,7 +2367,7 @@ static int widom_insert_impl(cass_ctx* c, int32_t is1, int32_t nboxes, const int
   // queued (both inside the kernel timing)
   int* d_fixn = nullptr;
   FixEntry* d_fixq = nullptr;
-  auto launch_f32 = [&](auto kern, const SpeciesF& SF) -> int {
+  auto launch_f32 = [&](auto kern, const SpeciesF& SF, int nthreads) -> int {
     int rc2 = c->d_widom_fix.reserve((size_t)nboxes * sizeof(int) + 64 + nrec * sizeof(FixEntry));
     if (rc2) return rc2;
     d_fixn = c->d_widom_fix.as<int>();
@@ -2375,19 +2376,19 @@ static int widom_insert_impl(cass_ctx* c, int32_t is1, int32_t nboxes, const int
     CASS_CUDA(cudaMemsetAsync(d_fixn, 0, (size_t)nboxes * sizeof(int), c->stream));
     if (use_smem) CASS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem));
     int per_sm = 1;
-    CASS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kF32Threads, use_smem ? max_smem : 0));
+    CASS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nthreads, use_smem ? max_smem : 0));
     per_sm = std::max(per_sm, 1);
     const int waves = c->widom_waves > 0 ? c->widom_waves : kF32Waves;
     long long want = ((long long)dev_sms * per_sm * waves + nboxes - 1) / nboxes;
-    long long need = (n_ins + kF32Threads - 1) / kF32Threads;
+    long long need = (n_ins + nthreads - 1) / nthreads;
     int chunks = (int)std::max<long long>(1, std::min(want, need));
     dim3 g(chunks, nboxes);
     c->stats.widom_grid_x = chunks;
     c->stats.widom_grid_y = nboxes;
-    c->stats.widom_block = kF32Threads;
+    c->stats.widom_block = nthreads;
     c->stats.widom_smem_bytes = use_smem ? (int)max_smem : 0;
     CASS_CUDA(cudaEventRecord(c->ev[1], c->stream));
-    kern<<<g, kF32Threads, use_smem ? max_smem : 0, c->stream>>>(
+    kern<<<g, nthreads, use_smem ? max_smem : 0, c->stream>>>(
         S, SF, c->pt, d_bd, d_ids, d_c32, c->d_cq32.as<float>(), c->d_cell_start.as<int>(), s.d_library_f.as<float>(),
         (long long)n_ins, seed, d_rec, d_status, d_xyz, any_recip ? 1 : 0, d_trace, d_fixq, d_fixn, c->widom_band,
         d_pairs);
@@ -2406,9 +2407,12 @@ static int widom_insert_impl(cass_ctx* c, int32_t is1, int32_t nboxes, const int
   };
   if (n_ins > 0) {
     const bool opt = c->cbmc_opt.energy_table_res > 0 || c->cbmc_opt.sector_overlap;  // no pair counts with options
-    if (f32 && opt) rc = use_smem ? launch_f32(k_widom_f32<true, false, true>, SF) : launch_f32(k_widom_f32<false, false, true>, SF);
-    else if (f32 && d_pairs) rc = use_smem ? launch_f32(k_widom_f32<true, true, false>, SF) : launch_f32(k_widom_f32<false, true, false>, SF);
-    else if (f32) rc = use_smem ? launch_f32(k_widom_f32<true, false, false>, SF) : launch_f32(k_widom_f32<false, false, false>, SF);
+    const int nt = opt || d_pairs ? kF32Threads : (c->widom_threads == 256 ? 256 : kF32Threads);
+    if (f32 && opt) rc = use_smem ? launch_f32(k_widom_f32<true, false, true>, SF, nt) : launch_f32(k_widom_f32<false, false, true>, SF, nt);
+    else if (f32 && d_pairs) rc = use_smem ? launch_f32(k_widom_f32<true, true, false>, SF, nt) : launch_f32(k_widom_f32<false, true, false>, SF, nt);
+    else if (f32 && nt == 256)
+      rc = use_smem ? launch_f32(k_widom_f32<true, false, false, 256>, SF, nt) : launch_f32(k_widom_f32<false, false, false, 256>, SF, nt);
+    else if (f32) rc = use_smem ? launch_f32(k_widom_f32<true, false, false>, SF, nt) : launch_f32(k_widom_f32<false, false, false>, SF, nt);
     else rc = use_smem ? launch(k_widom<true>) : launch(k_widom<false>);
     if (rc) return rc;
     if (any_recip) {
@@ -2481,56 +2485,51 @@ extern "C" int cass_widom_insert(cass_ctx* c, int32_t is1, int32_t nboxes, const
                                  int32_t kappa_ins, int32_t kappa_dih, uint64_t seed, CassWidomResult* out,
                                  CassWidomTrace* trace) {
   if (!c || !iboxes || nboxes < 1 || !out || n_ins < 64 || !c->widom_autotune || c->widom_cells > 0.0 ||
-      c->widom_waves > 0)
+      c->widom_waves > 0 || c->widom_threads > 0)
     return widom_insert_impl(c, is1, nboxes, iboxes, n_ins, kappa_ins, kappa_dih, seed, out, trace);
   std::vector<long long> key = {is1, c->precision, kappa_ins, kappa_dih, c->cbmc_opt.energy_table_res,
                                 c->cbmc_opt.sector_overlap, (long long)std::log2((double)n_ins)};
   for (int k = 0; k < nboxes; ++k) key.push_back(iboxes[k]);
+  auto run_with = [&](const cass_ctx_impl::WidomShape& sh, int64_t n, uint64_t sd, CassWidomResult* o,
+                      CassWidomTrace* tr) {
+    c->widom_cells = sh.cells;
+    c->widom_waves = sh.waves;
+    c->widom_threads = sh.threads;
+    const int rc = widom_insert_impl(c, is1, nboxes, iboxes, n, kappa_ins, kappa_dih, seed ^ sd, o, tr);
+    c->widom_cells = 0.0;
+    c->widom_waves = 0;
+    c->widom_threads = 0;
+    return rc;
+  };
   for (const auto& e : c->widom_tuned)
-    if (e.first == key) {
-      c->widom_cells = e.second.first;
-      c->widom_waves = e.second.second;
-      const int rc = widom_insert_impl(c, is1, nboxes, iboxes, n_ins, kappa_ins, kappa_dih, seed, out, trace);
-      c->widom_cells = 0.0;
-      c->widom_waves = 0;
-      return rc;
-    }
+    if (e.first == key) return run_with(e.second, n_ins, 0, out, trace);
   const bool mixed = c->precision == CASS_PREC_MIXED;
-  const std::vector<double> cells = mixed ? std::vector<double>{1.0, 1.25} : std::vector<double>{3.0, 4.0};
-  const std::vector<int> waves = {kF32Waves};
+  // candidate shapes: the cell edge (cells per rcut_cbmc) and, for the FP32
+  // kernel, the CTA size (512 threads two per SM, or 256 threads)
+  std::vector<cass_ctx_impl::WidomShape> shapes;
+  if (mixed)
+    for (int nt : {512, 256})
+      for (double cc : {1.0, 1.25}) shapes.push_back({cc, kF32Waves, nt});
+  else
+    for (double cc : {3.0, 4.0}) shapes.push_back({cc, kF32Waves, 512});
   // the CTAs per box follow the insertion count, so the mixed kernel is timed at
   // the call's own count (up to 32,768 per box); the FP64 kernel on 4,096
   const int64_t sample = std::min<int64_t>(n_ins, mixed ? 32768 : 4096);
   std::vector<CassWidomResult> tmp(nboxes);
-  double best_c = 0.0;
-  int best_w = 0;
-  float best_ms = 0.0f;
-  for (double cc : cells)
-    for (int w : waves) {
-      c->widom_cells = cc;
-      c->widom_waves = w;
-      float ms = 0.0f;
-      for (int rep = 0; rep < 3; ++rep) {  // the first run of a shape also sizes its buffers
-        const int rc = widom_insert_impl(c, is1, nboxes, iboxes, sample, kappa_ins, kappa_dih, seed ^ 0x5bd1e995ULL,
-                                         tmp.data(), nullptr);
-        if (rc) {
-          c->widom_cells = 0.0;
-          c->widom_waves = 0;
-          return rc;
-        }
-        if (rep == 1 || (rep == 2 && c->stats.widom_kernel_ms < ms)) ms = c->stats.widom_kernel_ms;
-      }
-      if (best_w == 0 || ms < best_ms) {
-        best_ms = ms;
-        best_c = cc;
-        best_w = w;
-      }
+  cass_ctx_impl::WidomShape best = shapes[0];
+  float best_ms = -1.0f;
+  for (const auto& sh : shapes) {
+    float ms = 0.0f;
+    for (int rep = 0; rep < 3; ++rep) {  // the first run of a shape also sizes its buffers
+      const int rc = run_with(sh, sample, 0x5bd1e995ULL, tmp.data(), nullptr);
+      if (rc) return rc;
+      if (rep == 1 || (rep == 2 && c->stats.widom_kernel_ms < ms)) ms = c->stats.widom_kernel_ms;
     }
-  c->widom_tuned.push_back({key, {best_c, best_w}});
-  c->widom_cells = best_c;
-  c->widom_waves = best_w;
-  const int rc = widom_insert_impl(c, is1, nboxes, iboxes, n_ins, kappa_ins, kappa_dih, seed, out, trace);
-  c->widom_cells = 0.0;
-  c->widom_waves = 0;
-  return rc;
+    if (best_ms < 0.0f || ms < best_ms) {
+      best_ms = ms;
+      best = sh;
+    }
+  }
+  c->widom_tuned.push_back({key, best});
+  return run_with(best, n_ins, 0, out, trace);
 }
