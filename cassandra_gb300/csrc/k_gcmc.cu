@@ -1338,8 +1338,7 @@ __device__ void gc_setup(const GcArgs& A, const GcBox& G, const PairTable& T, in
   double* sy = sx + N;
   double* sz = sy + N;
   double* scom = sz + N;  // [R][3]
-  double* rdcom = scom + 3 * R;  // [R]
-  int* lv = reinterpret_cast<int*>(rdcom + R);
+  int* lv = reinterpret_cast<int*>(scom + 3 * R);
   int* apos = lv + N;
   int* lvt = apos + N;  // FP64 kernel only
   int* rlive = lvt + (MIXED ? 0 : N);
@@ -1347,9 +1346,15 @@ __device__ void gc_setup(const GcArgs& A, const GcBox& G, const PairTable& T, in
   int* roff = rsp + R;
   int* pool = roff + R;
   int* lrec = pool + R;
-  int* arec = lrec + R;  // [N]
   float4* lv32 = reinterpret_cast<float4*>(reinterpret_cast<unsigned char*>(smem) +
-                                           ((((size_t)(arec + N) - (size_t)smem) + 15) & ~(size_t)15));
+                                           ((((size_t)(lrec + R) - (size_t)smem) + 15) & ~(size_t)15));
+  // molecule-pair cutoff boxes only: per record max_dcom, the record of each atom
+  double* rdcom = nullptr;
+  int* arec = nullptr;
+  if (G.comcut) {
+    rdcom = reinterpret_cast<double*>(lv32 + (MIXED ? N : 0));
+    arec = reinterpret_cast<int*>(rdcom + R);
+  }
   for (int j = threadIdx.x; j < N; j += blockDim.x) {
     const double4_32a p = G.xyzq[j];
     sx[j] = p.x;
@@ -1408,14 +1413,16 @@ __device__ void gc_setup(const GcArgs& A, const GcBox& G, const PairTable& T, in
     scom[3 * r] = x / tm;
     scom[3 * r + 1] = y / tm;
     scom[3 * r + 2] = z / tm;
-    double dmax = 0.0;  // Compute_Max_COM_Distance
-    for (int a = 0; a < s.natoms; ++a) {
-      const int j = roff[r] + a;
-      arec[j] = r;
-      const double dx = sx[j] - scom[3 * r], dy = sy[j] - scom[3 * r + 1], dz = sz[j] - scom[3 * r + 2];
-      dmax = fmax(dmax, dx * dx + dy * dy + dz * dz);
+    if (G.comcut) {
+      double dmax = 0.0;  // Compute_Max_COM_Distance
+      for (int a = 0; a < s.natoms; ++a) {
+        const int j = roff[r] + a;
+        arec[j] = r;
+        const double dx = sx[j] - scom[3 * r], dy = sy[j] - scom[3 * r + 1], dz = sz[j] - scom[3 * r + 2];
+        dmax = fmax(dmax, dx * dx + dy * dy + dz * dz);
+      }
+      rdcom[r] = sqrt(dmax);
     }
-    rdcom[r] = sqrt(dmax);
   }
   if (threadIdx.x < kMaxAtoms) ttype[threadIdx.x] = threadIdx.x < A.S.natoms ? A.S.type[threadIdx.x] : -1;
   V.b = &b;
@@ -2211,7 +2218,7 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
             if (MIXED && i >= 0) lv32[i] = make_float4((float)gs.r[3 * a], (float)gs.r[3 * a + 1], (float)gs.r[3 * a + 2], lv32[i].w);
           }
           for (int d = 0; d < 3; ++d) scom[3 * gs.rec + d] = gs.com[d];
-          if (!MIXED) {  // max_dcom of the molecule as placed (insertion, regrowth; rigid moves keep it)
+          if (!MIXED && V.comcut) {  // max_dcom of the molecule as placed (insertion, regrowth; rigid moves keep it)
             double dmax = 0.0;
             for (int a = 0; a < gs.na; ++a) {
               const double dx = gs.r[3 * a] - gs.com[0], dy = gs.r[3 * a + 1] - gs.com[1],
@@ -2326,11 +2333,12 @@ __global__ void __launch_bounds__(kGcThreads, 1)
   }
 }
 
-size_t gc_smem_bytes(int natoms, int nrec, bool mixed) {
-  size_t s = (size_t)natoms * (3 * sizeof(double) + (mixed ? 3 : 4) * sizeof(int)) +
-             (size_t)nrec * (4 * sizeof(double) + 5 * sizeof(int));
+size_t gc_smem_bytes(int natoms, int nrec, bool mixed, bool comcut) {
+  size_t s = (size_t)natoms * (3 * sizeof(double) + (mixed ? 2 : 3) * sizeof(int)) +
+             (size_t)nrec * (3 * sizeof(double) + 5 * sizeof(int));
   s = (s + 15) & ~(size_t)15;
   if (mixed) s += (size_t)natoms * sizeof(float4);
+  if (comcut) s += (size_t)nrec * sizeof(double) + (size_t)natoms * sizeof(int);
   return s;
 }
 }  // namespace cassgpu
@@ -2524,7 +2532,7 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
     gc_host_box(c, ib, pools[k], h, g);
     g.mu = mu[k] / 0.01;  // kJ/mol to internal units (atomic_to_kJmol)
     g.log_lambda3 = 3.0 * std::log(39.9031268605 * std::sqrt(B.dev.beta / (kTWOPI * mw)));  // de Broglie
-    smem = std::max(smem, gc_smem_bytes(g.natoms, g.nrec, mixed));
+    smem = std::max(smem, gc_smem_bytes(g.natoms, g.nrec, mixed, g.comcut != 0));
     tot_atoms += (size_t)g.natoms;
     tot_rec += h.slots.size();
   }
@@ -2716,7 +2724,7 @@ extern "C" int cass_build_molecule(cass_ctx* c, int32_t im, int32_t is1, int32_t
   GcBox g;
   gc_host_box(c, ib, del_flag ? std::vector<int>() : std::vector<int>{slot}, h, g);
   const int rec = (int)(std::lower_bound(h.slots.begin(), h.slots.end(), slot) - h.slots.begin());
-  const size_t smem = gc_smem_bytes(g.natoms, g.nrec, mixed);
+  const size_t smem = gc_smem_bytes(g.natoms, g.nrec, mixed, g.comcut != 0);
   if (smem > kGcSmemLimit)
     return set_error(CASS_ECAPACITY, "build_molecule holds the box in shared memory: too many atoms");
   const size_t nout = 2 + 3 * (size_t)s.natoms, niout = 2 + kMaxFrags;
