@@ -284,6 +284,16 @@ def gcmc_system(nboxes: int = 16, length: float = 40.0, temperature: float = 300
     return System([sp], boxes, MoleculeSet(), ff, [max_per_box * nboxes])
 
 
+def water_gcmc_system(nboxes: int = 2, nmol: int = 27, length: float = 16.0, temperature: float = 298.0,
+                      rcut: float = 7.0, tol: float = 1e-5, max_per_box: int = 120, seed: int = 11) -> System:
+    """Rigid 3-site waters (LJ + Ewald) on a lattice with random orientations in
+    boxes with free slots, for grand-canonical runs of a charged species."""
+    s = water_nvt_system(nboxes=nboxes, nmol=nmol, length=length, temperature=temperature, rcut=rcut, tol=tol,
+                         seed=seed)
+    s.max_molecules = [max_per_box * nboxes]
+    return s
+
+
 def ideal_gas_system(nboxes: int = 2, length: float = 30.0, temperature: float = 300.0,
                      max_per_box: int = 400) -> System:
     """Non-interacting spheres (epsilon 0) for checks of the grand-canonical acceptance rules."""

@@ -2080,6 +2080,30 @@ struct GcmcChain {
     const double eb = bond_energy(s, m.r.data()), ea = angle_energy(s, m.r.data(), m.exist.data());
     const double ed = dihedral_energy(s, m.r.data(), m.exist.data()), ei = improper_energy(s, m.r.data());
     dE_intra = dE_intra + eb + ea + ed + ei;
+    // Ewald energies (move_insert.f90:274-291): the molecule's structure factor
+    // added to the box's (Update_System_Ewald_Reciprocal_Energy, int_insertion)
+    // and its self energy (Compute_Molecule_Self_Energy)
+    Box& bw = cc->box[ibox()];
+    const bool ew = box_has_ewald(b) && s.has_charge;
+    std::vector<double> cn, sn;
+    double E_recip = mc.E.reciprocal, E_self = 0.0;
+    if (b.charge_style == CASS_CHARGE_COUL) {
+      if (ew) {
+        const size_t nv = b.hx.size();
+        cn.assign(nv, 0.0);
+        sn.assign(nv, 0.0);
+        mol_structure_factor(cc, b, is, m.r.data(), cn.data(), sn.data());
+        double Er = 0.0;
+        for (size_t i = 0; i < nv; ++i) {
+          const double cs = b.cos_sum[i] + cn[i], ss = b.sin_sum[i] + sn[i];
+          Er = Er + b.Cn[i] * (cs * cs + ss * ss);
+        }
+        E_recip = Er * CHARGE_FACTOR;
+        dE_inter = dE_inter + (E_recip - mc.E.reciprocal);
+      }
+      E_self = molecule_self(cc, b, is);
+      dE_inter = dE_inter + E_self;
+    }
     double e_lrc = mc.E.lrc;
     if (b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) {
       e_lrc = lr_correction(cc, b, beads_with(s, 1.0));
@@ -2107,6 +2131,16 @@ struct GcmcChain {
     E.inter_vdw += ev;
     E.inter_q += eq;
     if (b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) E.lrc = e_lrc;
+    if (ew) {
+      for (size_t i = 0; i < cn.size(); ++i) {
+        bw.cos_sum[i] = bw.cos_sum[i] + cn[i];
+        bw.sin_sum[i] = bw.sin_sum[i] + sn[i];
+      }
+      m.cos_mol = cn;
+      m.sin_mol = sn;
+      E.reciprocal = E_recip;
+    }
+    E.self += E_self;
     ++res.n_insert_accepted;
     pool.pop_back();
     m.live = true;
@@ -2148,6 +2182,24 @@ struct GcmcChain {
     eq = eq + eoq;
     dE_intra = dE_intra - eiv - eiq;
     dE_inter = dE_inter - eoq;
+    // Ewald energies (move_delete.f90:261-277): the molecule's structure factor
+    // taken out of the box's (int_deletion) and its self energy
+    Box& bw = cc->box[ibox()];
+    const bool ew = box_has_ewald(b) && s.has_charge;
+    double E_recip = mc.E.reciprocal, E_self = 0.0;
+    if (b.charge_style == CASS_CHARGE_COUL) {
+      if (ew) {
+        double Er = 0.0;
+        for (size_t i = 0; i < b.hx.size(); ++i) {
+          const double cs = b.cos_sum[i] - m.cos_mol[i], ss = b.sin_sum[i] - m.sin_mol[i];
+          Er = Er + b.Cn[i] * (cs * cs + ss * ss);
+        }
+        E_recip = Er * CHARGE_FACTOR;
+        dE_inter = dE_inter + (E_recip - mc.E.reciprocal);
+      }
+      E_self = molecule_self(cc, b, is);
+      dE_inter = dE_inter - E_self;
+    }
     double e_lrc = mc.E.lrc;
     if (b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) {
       e_lrc = lr_correction(cc, b, beads_with(s, -1.0));
@@ -2174,6 +2226,14 @@ struct GcmcChain {
     E.inter_vdw -= ev;
     E.inter_q -= eq;
     if (b.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL) E.lrc = e_lrc;
+    if (ew) {
+      for (size_t i = 0; i < b.hx.size(); ++i) {
+        bw.cos_sum[i] = bw.cos_sum[i] - m.cos_mol[i];
+        bw.sin_sum[i] = bw.sin_sum[i] - m.sin_mol[i];
+      }
+      E.reciprocal = E_recip;
+    }
+    E.self -= E_self;
     ++res.n_delete_accepted;
     m.live = false;
     std::vector<int>& mem = cc->members[ibox()];
@@ -2274,12 +2334,22 @@ struct GcmcChain {
     }
     double dE_intra = eb_n + ea_n + ed_n + ei_n + eiq_n + eiv_n;
     double dE_inter = eq_n + ev_n;
+    // the reciprocal energy of the new conformation (move_regrow.f90:338-354,
+    // Update_System_Ewald_Reciprocal_Energy with int_intra), kept for acceptance
+    Box& bw = cc->box[ibox()];
+    const bool ew = box_has_ewald(b) && s.has_charge;
+    double E_recip = mc.E.reciprocal;
+    if (ew) {
+      E_recip = ewald_move(cc, bw, m);
+      dE_inter = dE_inter + (E_recip - mc.E.reciprocal);
+    }
     const std::vector<double> r_new(m.r);
     const double com_new[3] = {m.com[0], m.com[1], m.com[2]}, dcom_new = m.max_dcom;
     revert();
     ov = cut_regrow(m, slot, true, order, f_live, f_dead, e_prev, ln_prev);
     std::fill(m.exist.begin(), m.exist.end(), 1);
     if (ov) {
+      if (ew) ewald_revert(bw, m);
       mc.err = fail(CASS_ESTATE, "molecule energy too high for a regrowth");
       return;
     }
@@ -2291,7 +2361,11 @@ struct GcmcChain {
     const double dE = dE_intra + dE_inter;
     const double dE_frag = ea_n - ea_o;
     const double ln_pacc = b.beta * (dE - dE_frag) + ln_pfor - ln_prev;
-    if (!accept_or_reject(ln_pacc, rng)) return;
+    if (!accept_or_reject(ln_pacc, rng)) {
+      if (ew) ewald_revert(bw, m);
+      return;
+    }
+    if (ew) mc.E.reciprocal = E_recip;
     m.r = r_new;
     std::copy(com_new, com_new + 3, m.com);
     m.max_dcom = dcom_new;
@@ -3105,7 +3179,8 @@ int orc_gcmc(orc_ctx* c, int32_t nboxes, const int32_t* iboxes, const CassGCMCPa
     for (int j = 0; j < k; ++j)
       if (iboxes[j] == iboxes[k]) return fail(CASS_EINVAL, "box listed twice");
     if (!c->box[ib].energy_valid) return fail(CASS_ESTATE, "system energy of box not computed");
-    if (c->box[ib].charge_style != CASS_CHARGE_NONE) return fail(CASS_EUNSUPPORTED, "gcmc boxes hold no charges");
+    if (c->box[ib].charge_style != CASS_CHARGE_NONE && c->box[ib].charge_sum_style != CASS_QQ_EWALD)
+      return fail(CASS_EUNSUPPORTED, "gcmc: charges need the Ewald sum");
   }
   // free slots of the exchanged species, in ascending order, each to the box
   // holding the fewest atoms so far (live molecules of every species plus the

@@ -32,6 +32,26 @@ def test_gcmc_bookkeeping_all_moves():
                 assert abs(x["energy"][comp] - e[comp]) <= 1e-9 * (abs(e["inter_vdw"]) + 1.0), comp
 
 
+def test_gcmc_ewald_bookkeeping():
+    """Water in Ewald boxes: insertions and deletions change the reciprocal sum
+    by the molecule's structure factor and the self energy by the molecule's
+    (move_insert.f90:274-291, move_delete.f90:261-277); the chain's running
+    energy equals a recomputation of its final state in every component."""
+    s = workloads.water_gcmc_system(nboxes=2)
+    with oracle.open_system(s) as o:
+        for b in (1, 2):
+            o.system_total_energy(b)
+        r = o.gcmc([1, 2], 4000, 1, [-30.0, -34.0], [[0.5], [0.5]], [[0.4], [0.4]], seed=7, kappa_ins=8,
+                   kappa_dih=0, cuts=(0.2, 0.4, 0.7, 1.0, 1.0))
+        for k, x in enumerate(r):
+            assert x["n_insert_accepted"] > 0 and x["n_delete_accepted"] > 0, x
+            e, ov = o.system_total_energy(k + 1)
+            assert not ov
+            scale = abs(e["inter_vdw"]) + abs(e["inter_q"]) + abs(e["reciprocal"]) + abs(e["self"])
+            for comp in ("total", "inter_vdw", "inter_q", "intra_q", "reciprocal", "self"):
+                assert abs(x["energy"][comp] - e[comp]) <= 1e-9 * scale, (comp, x["energy"][comp], e[comp])
+
+
 def test_gcmc_ideal_chain_matches_widom():
     s = workloads.gcmc_system(nboxes=2, length=30.0, max_per_box=400, eps_scale=0.0, rcut_low=1e-3)
     T = s.boxes[0].temperature
