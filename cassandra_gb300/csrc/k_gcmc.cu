@@ -21,6 +21,12 @@
 // memory and added in rank order after one cluster barrier per batch (two
 // partial buffers alternate, so a buffer is rewritten only after every CTA
 // has read it).
+//
+// Charged boxes (Coulomb with the Ewald sum) run the FP64 kernel on one CTA
+// per box: the pair batches add the real-space terms, and each move that
+// changes a charged molecule computes the box's new reciprocal energy from
+// the running structure factors (thread k mod blockDim.x owns k-vector k),
+// which are committed, with the molecule's row, only on acceptance.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -41,8 +47,10 @@ constexpr int kGcMaxSpecies = 8;
 constexpr size_t kGcSmemLimit = 190 * 1024;  // dynamic; the static part is about 35 KB of the 227 KB
 
 struct GcSpecies {
-  int natoms, linear;
+  int natoms, linear, has_charge;
+  int l_coul_cbmc;  // species_list%L_Coul_CBMC: CBMC trial energies include the intermolecular charges
   double mass[kMaxAtoms];
+  double q[kMaxAtoms];
   int type[kMaxAtoms];  // nonbond type per atom, -1: none
 };
 
@@ -86,6 +94,13 @@ struct GcBox {
   int* status;  // 0 ok, 1 overlapping molecule before a move, 2 no free slot
   int comcut;    // LJ CHARMM: molecule pairs selected by Check_MoleculePair_Cutoff (FP64 kernel)
   double rmax;   // rcut_max of that test
+  // charged boxes (Coulomb with the Ewald sum; FP64 kernel, one CTA per box):
+  // the k-vectors (hx, hy, hz, Cn), the box's running structure factors, the
+  // per-molecule rows (slot-major, row stride `stride`) and a scratch row for
+  // the moved molecule's new factors
+  int qon, nvecs, stride;
+  const double4_32a* kvec;
+  double *cos_sum, *sin_sum, *cos_mol, *sin_mol, *new_cos, *new_sin;
 };
 
 // the molecule being built / moved and one stage of trials (shared memory)
@@ -159,6 +174,7 @@ struct GcView {
   double* com;
   double* rdcom;  // per record max_dcom (molecule-pair cutoff boxes)
   int* arec;      // record of each atom
+  const double* sq;  // charge of each atom (charged boxes), else nullptr
   int comcut;
   double rmax;
   int natoms, nrec;
@@ -205,13 +221,22 @@ __device__ __forceinline__ R warp_multi_sum(R (&v)[TG], int lane, int& which) {
 // only when its molecule passes Check_MoleculePair_Cutoff (energy_routines.f90:
 // 3027-3088) against the trial's atoms gs.tids (their COM and max_dcom, masses
 // tmass), overlap test included, as in the reference's molecule loops.
-template <bool MIXED, int TG>
+// In a charged box (FP64 kernel; V.sq and the trial atoms' charges tq set)
+// the real-space Ewald term of each pair within the charge cutoff (rcut_cbmc
+// in CBMC batches) is added as well (Compute_AtomPair_Energy, energy_routines.
+// f90:2014-2049): to the trial's sum, or with SPLITQ (ntr <= TG / 2) to entry
+// t + TG / 2, so that gs.e[t] holds the vdW and gs.e[t + TG / 2] the Coulomb
+// sum of trial t.
+template <bool MIXED, int TG, bool SPLITQ = false>
 __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip_rec, bool cbmc,
-                               const int* ttype, bool convert = true, const double* tmass = nullptr) {
+                               const int* ttype, bool convert = true, const double* tmass = nullptr,
+                               const double* tq = nullptr) {
   const BoxDev& b = *V.b;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntid = gs.ntid;
   const bool mp = !MIXED && V.comcut && tmass != nullptr;
+  const bool qon = !MIXED && V.sq != nullptr && tq != nullptr;
+  const int nout = SPLITQ ? TG : ntr;  // sums written per trial group
   if (mp) {
     for (int t = threadIdx.x; t < ntr; t += blockDim.x) {  // Get_COM, Compute_Max_COM_Distance
       double tm = 0.0, x = 0.0, y = 0.0, z = 0.0;
@@ -300,6 +325,7 @@ __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip
         }
       } else {
         const double xj = V.sx[j], yj = V.sy[j], zj = V.sz[j];
+        const double qj = qon ? V.sq[j] : 0.0;
         const int tj = V.lvt[i];
         unsigned inm = 0xffffffffu;  // trials whose molecule pair with j's molecule interacts
         if (mp) {
@@ -318,6 +344,7 @@ __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip
         }
         for (int k = 0; k < ntid; ++k) {
           const int a = gs.tids[k], ta = ttype[a];
+          const double qa = qon ? tq[a] : 0.0;
 #pragma unroll
           for (int u = 0; u < TG; ++u) {
             if (t0 + u < ntr && ((inm >> u) & 1u)) {
@@ -326,12 +353,14 @@ __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip
               const double dy = fold(tr[1] - yj, b.hL[1], b.L[1]);
               const double dz = fold(tr[2] - zj, b.hL[2], b.L[2]);
               const double r2 = dx * dx + dy * dy + dz * dz;
-              if (tab) {  // Estimate_MoleculePair_Energy (the boxes hold no charges)
-                if (table_pair(b, ntypes, r2, ta, tj, 0.0, 0.0, accd[u]) == 2) ovm |= 1u << u;
+              if (tab) {  // Estimate_MoleculePair_Energy
+                if (table_pair(b, ntypes, r2, ta, tj, qa, qj, accd[u]) == 2) ovm |= 1u << u;
               } else if (r2 < b.rcut_lowsq) {
                 ovm |= 1u << u;
-              } else if (cutoff_mask(b, r2, cbmc) & 1) {
-                accd[u] += vdw_pair(*V.T, b, ta, tj, r2, 1.0);
+              } else {
+                const int m = cutoff_mask(b, r2, cbmc);
+                if (m & 1) accd[u] += vdw_pair(*V.T, b, ta, tj, r2, 1.0);
+                if (qon && (m & 2)) accd[SPLITQ ? (u + TG / 2) % TG : u] += qq_pair_inter(b, qa * qj, r2);
               }
             }
           }
@@ -347,7 +376,7 @@ __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip
       }
     } else {
       const double tot = warp_multi_sum<TG>(accd, lane, which);
-      if ((lane & (32 / TG - 1)) == 0 && t0 + which < ntr) gs.part[w * kMaxKappa + t0 + which] = tot;
+      if ((lane & (32 / TG - 1)) == 0 && t0 + which < nout) gs.part[w * kMaxKappa + t0 + which] = tot;
     }
     ovall |= __reduce_or_sync(0xffffffffu, ovm) << t0;
   }
@@ -356,7 +385,7 @@ __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip
   constexpr bool kF = MIXED && TG > 2;  // FP32 to the end
   const int t = threadIdx.x;
   if (V.csize == 1) {
-    if (t < ntr) {
+    if (t < nout) {
       int o = 0;
       for (int ww = 0; ww < kGcWarps; ++ww) o |= (gs.povl[ww] >> t) & 1;
       if (kF) {
@@ -376,7 +405,7 @@ __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip
     namespace cgr = cooperative_groups;
     cgr::cluster_group cl = cgr::this_cluster();
     const int buf = gs.cbuf;
-    if (t < ntr) {
+    if (t < nout) {
       int o = 0;
       for (int ww = 0; ww < kGcWarps; ++ww) o |= (gs.povl[ww] >> t) & 1;
       if (kF) {
@@ -391,7 +420,7 @@ __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip
       gs.covl[buf][t] = o;
     }
     cl.sync();
-    if (t < ntr) {
+    if (t < nout) {
       int o = 0;
       for (int r = 0; r < V.csize; ++r) o |= *cl.map_shared_rank(&gs.covl[buf][t], r);
       if (kF) {
@@ -409,6 +438,12 @@ __device__ void batch_energies(const GcView& V, GrowState& gs, int ntr, int skip
   }
   __syncthreads();
   if (t == 0) gs.cbuf ^= 1;
+}
+
+// charges of the intermolecular CBMC trial terms of species is: only with
+// L_Coul_CBMC (Compute_MoleculePair_Energy, energy_routines.f90:1684-1686)
+__device__ __forceinline__ const double* gc_cbmc_q(const GcArgs& A, int is) {
+  return A.sp[is].l_coul_cbmc ? A.sp[is].q : nullptr;
 }
 
 // the live-atom list and the sorted live records (thread 0)
@@ -663,7 +698,7 @@ __device__ bool gc_place_fragments(const GcArgs& A, const GcView& V, GrowState& 
         if ((gs.newex >> a) & 1u) gs.tids[gs.ntid++] = a;
     }
     __syncthreads();
-    batch_energies<MIXED, 16>(V, gs, kd, gs.rec, true, S.type, true, S.mass);
+    batch_energies<MIXED, 16>(V, gs, kd, gs.rec, true, S.type, true, S.mass, gc_cbmc_q(A, gs.is));
     if (threadIdx.x == 0) {
       const double beta = b.beta;
       double w[kMaxKappa];
@@ -785,7 +820,7 @@ __device__ bool gc_build(const GcArgs& A, const GcView& V, GrowState& gs, bool d
       for (int d = 0; d < 3; ++d) gs.trial[it][3 * a + d] = gs.r[3 * a + d] - gs.com[d] + gs.draws[3 * it + d];
     }
   __syncthreads();
-  batch_energies<MIXED, 16>(V, gs, ki, gs.rec, true, S.type, true, S.mass);
+  batch_energies<MIXED, 16>(V, gs, ki, gs.rec, true, S.type, true, S.mass, gc_cbmc_q(A, gs.is));
   if (threadIdx.x == 0) {
     const double beta = b.beta;
     double w[kMaxKappa];
@@ -830,8 +865,10 @@ __device__ bool gc_build(const GcArgs& A, const GcView& V, GrowState& gs, bool d
 }
 
 // energies of the whole molecule gs.r (record gs.rec): inter (full cutoffs,
-// block-wide) plus intra and bonded (thread 0); results in out[0..8]:
-// ev, eq, eb, ea, ed, ei, eiv, eiq, overlap flags (inter, intra)
+// block-wide) plus intra and bonded (thread 0); results in out[0..9]: ev, eq,
+// eb, ea, ed, ei, eiv, eiq, then the two parts of eq (the intermolecular
+// real-space sum and the periodic part of the intramolecular one); overlap
+// flags (inter, intra) in ovs
 template <bool MIXED>
 __device__ void gc_mol_energies(const GcArgs& A, const GcView& V, GrowState& gs, const int* ttype, double* out,
                                 int* ovs, bool with_intra = true) {
@@ -843,12 +880,21 @@ __device__ void gc_mol_energies(const GcArgs& A, const GcView& V, GrowState& gs,
     }
   }
   __syncthreads();
-  batch_energies<MIXED, 2>(V, gs, 1, gs.rec, false, ttype, true, A.sp[gs.is].mass);
+  const bool qon = !MIXED && V.sq != nullptr;
+  if constexpr (!MIXED) {
+    if (qon) batch_energies<false, 2, true>(V, gs, 1, gs.rec, false, ttype, true, A.sp[gs.is].mass, A.sp[gs.is].q);
+    else batch_energies<false, 2>(V, gs, 1, gs.rec, false, ttype, true, A.sp[gs.is].mass);
+  } else {
+    batch_energies<true, 2>(V, gs, 1, gs.rec, false, ttype, true, A.sp[gs.is].mass);
+  }
   if (threadIdx.x == 0) {
     IntraOut io{0, 0, 0, 0, 0, 0, 0, false};
     if (with_intra) io = molecule_intra(A.P, gs.is, *V.b, *V.T, gs.r);
+    const double eqx = qon ? gs.e[1] : 0.0;
     out[0] = gs.e[0];
-    out[1] = io.pqq;  // the periodic part of the intramolecular Coulomb sum
+    out[1] = qon ? eqx + io.pqq : io.pqq;  // with the periodic part of the intramolecular Coulomb sum
+    out[8] = eqx;
+    out[9] = io.pqq;
     out[2] = io.bond;
     out[3] = io.angle;
     out[4] = io.dih;
@@ -859,6 +905,84 @@ __device__ void gc_mol_energies(const GcArgs& A, const GcView& V, GrowState& gs,
     ovs[1] = io.overlap ? 1 : 0;
   }
   __syncthreads();
+}
+
+// Reciprocal-space energy of a charged box after a move of the molecule in
+// slot `slot` (Update_System_Ewald_Reciprocal_Energy, energy_routines.f90:
+// 2384-2431): mode 0 adds the structure factors of the new molecule r
+// (int_insertion), 1 takes the molecule's stored factors out (int_deletion),
+// 2 replaces them by those of r (int_translation, int_rotation, int_intra).
+// All threads; k-vector k stays with thread k mod blockDim.x, which writes the
+// molecule's new factors to G.new_cos / G.new_sin.  Returns CHARGE_FACTOR
+// sum_k Cn (S_c^2 + S_s^2) on every thread (red: one double per warp).
+__device__ double gc_recip(const GcBox& G, const GcSpecies& s, const double* r, int slot, int mode, double* red) {
+  const double* cm = G.cos_mol + (size_t)slot * G.stride;
+  const double* smv = G.sin_mol + (size_t)slot * G.stride;
+  double part = 0.0;
+  for (int k = threadIdx.x; k < G.nvecs; k += blockDim.x) {
+    const double4_32a h = G.kvec[k];
+    double cn = 0.0, sn = 0.0;
+    if (mode != 1)
+      for (int a = 0; a < s.natoms; ++a) {
+        const double hdotr = h.x * r[3 * a] + h.y * r[3 * a + 1] + h.z * r[3 * a + 2];
+        double sv, cv;
+        sincos(hdotr, &sv, &cv);
+        cn = cn + s.q[a] * cv;
+        sn = sn + s.q[a] * sv;
+      }
+    double c, sm;
+    if (mode == 0) {
+      c = G.cos_sum[k] + cn;
+      sm = G.sin_sum[k] + sn;
+    } else if (mode == 1) {
+      c = G.cos_sum[k] - cm[k];
+      sm = G.sin_sum[k] - smv[k];
+    } else {
+      c = G.cos_sum[k] + (cn - cm[k]);
+      sm = G.sin_sum[k] + (sn - smv[k]);
+    }
+    part += h.w * (c * c + sm * sm);
+    if (mode != 1) {
+      G.new_cos[k] = cn;
+      G.new_sin[k] = sn;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
+  __syncthreads();
+  double e = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) e += red[w];
+  __syncthreads();  // red is free again
+  return e * kCHARGE_FACTOR;
+}
+
+// the accepted move of gc_recip: the box's sums and the molecule's row
+__device__ void gc_recip_commit(const GcBox& G, int slot, int mode) {
+  double* cm = G.cos_mol + (size_t)slot * G.stride;
+  double* smv = G.sin_mol + (size_t)slot * G.stride;
+  for (int k = threadIdx.x; k < G.nvecs; k += blockDim.x) {
+    if (mode == 0) {
+      G.cos_sum[k] = G.cos_sum[k] + G.new_cos[k];
+      G.sin_sum[k] = G.sin_sum[k] + G.new_sin[k];
+    } else if (mode == 1) {
+      G.cos_sum[k] = G.cos_sum[k] - cm[k];
+      G.sin_sum[k] = G.sin_sum[k] - smv[k];
+    } else {
+      G.cos_sum[k] = G.cos_sum[k] + (G.new_cos[k] - cm[k]);
+      G.sin_sum[k] = G.sin_sum[k] + (G.new_sin[k] - smv[k]);
+    }
+    if (mode != 1) {
+      cm[k] = G.new_cos[k];
+      smv[k] = G.new_sin[k];
+    }
+  }
+}
+
+// Compute_Molecule_Self_Energy (energy_routines.f90:2606-2645), Ewald sum
+__device__ __forceinline__ double gc_self(const GcSpecies& s, const BoxDev& b) {
+  double qq = 0.0;
+  for (int a = 0; a < s.natoms; ++a) qq += s.q[a] * s.q[a];
+  return -qq * kCHARGE_FACTOR * b.alpha / kROOTPI;
 }
 
 // Compute_LR_Correction (energy_routines.f90:2956-3023) for type counts nb,
@@ -1355,11 +1479,19 @@ __device__ void gc_setup(const GcArgs& A, const GcBox& G, const PairTable& T, in
     rdcom = reinterpret_cast<double*>(lv32 + (MIXED ? N : 0));
     arec = reinterpret_cast<int*>(rdcom + R);
   }
+  // charged boxes only: the charge of each atom (after the optional arrays)
+  double* sq = nullptr;
+  if (!MIXED && G.qon) {
+    const size_t o = (size_t)(G.comcut ? reinterpret_cast<unsigned char*>(arec + N)
+                                       : reinterpret_cast<unsigned char*>(lv32)) - (size_t)smem;
+    sq = reinterpret_cast<double*>(smem + ((o + 15) & ~(size_t)15));
+  }
   for (int j = threadIdx.x; j < N; j += blockDim.x) {
     const double4_32a p = G.xyzq[j];
     sx[j] = p.x;
     sy[j] = p.y;
     sz[j] = p.z;
+    if (sq) sq[j] = p.w;
     apos[j] = -1;
   }
   for (int r = threadIdx.x; r < R; r += blockDim.x) {
@@ -1446,6 +1578,7 @@ __device__ void gc_setup(const GcArgs& A, const GcBox& G, const PairTable& T, in
   V.com = scom;
   V.rdcom = rdcom;
   V.arec = arec;
+  V.sq = sq;
   V.comcut = G.comcut;
   V.rmax = G.rmax;
   V.natoms = N;
@@ -1463,6 +1596,8 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
   __shared__ double em[10];
   __shared__ int eov[2];
   __shared__ int mv_kind, mv_rec, mv_is, mv_skip, mv_acc, mv_stop, s_nlv;
+  __shared__ int mv_slot, mv_ew;  // the molecule's slot; the accepted structure-factor update (-1: none)
+  __shared__ double s_red[kGcWarps];
   __shared__ int rs0[kGcMaxSpecies];
   __shared__ double old_r[3 * kMaxAtoms], old_com[3];
   __shared__ int ttype[kMaxAtoms];
@@ -1524,6 +1659,7 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
       }
       mv_skip = 0;
       mv_stop = 0;
+      mv_ew = -1;
       int is = -1, im = 0;
       if (mv_kind == 0 || mv_kind == 1) {  // species choice of Translate / Rotate
         const double* step_sz = mv_kind == 0 ? G.max_disp : G.max_rot;
@@ -1595,6 +1731,7 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
         const int rec = mv_kind == 2 ? pool[npool - 1] : lrec[rs0[is] + im - 1];
         mv_rec = rec;
         mv_is = is;
+        mv_slot = G.rec[rec].x;
         gs.rec = rec;
         gs.is = is;
         gs.na = A.sp[is].natoms;
@@ -1684,7 +1821,18 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
           }
         }
         __syncthreads();
-        batch_energies<MIXED, 2>(V, gs, 2, gs.rec, false, A.sp[is].type, true, A.sp[is].mass);
+        // charged boxes: vdW in gs.e[0..1], Coulomb in gs.e[2..3], and the
+        // reciprocal energy after the move (move_translate.f90:250-290)
+        const bool qon = !MIXED && G.qon;
+        const bool ew = qon && A.sp[is].has_charge;
+        if constexpr (!MIXED) {
+          if (qon) batch_energies<false, 4, true>(V, gs, 2, gs.rec, false, A.sp[is].type, true, A.sp[is].mass, A.sp[is].q);
+          else batch_energies<false, 2>(V, gs, 2, gs.rec, false, A.sp[is].type, true, A.sp[is].mass);
+        } else {
+          batch_energies<true, 2>(V, gs, 2, gs.rec, false, A.sp[is].type, true, A.sp[is].mass);
+        }
+        double e_recip = 0.0;
+        if (ew && !gs.ov[0] && !gs.ov[1]) e_recip = gc_recip(G, A.sp[is], gs.r, mv_slot, 2, s_red);
         if (threadIdx.x == 0) {
           mv_acc = 0;
           if (gs.ov[0]) {  // the molecule overlapped before the move
@@ -1692,11 +1840,22 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
             status = 1;
           } else if (!gs.ov[1]) {
             const double dv = gs.e[1] - gs.e[0];
-            if (gc_accept(b.beta * dv, rng)) {
+            const double dq = qon ? gs.e[3] - gs.e[2] : 0.0;
+            double dE = dv;
+            if (qon) {
+              dE = ew ? e_recip - E.reciprocal : 0.0;
+              dE = dE + dv + dq;
+            }
+            if (gc_accept(b.beta * dE, rng)) {
               mv_acc = 1;
-              E.total = E.total + dv;
-              E.inter = E.inter + dv;
+              E.total = E.total + dE;
+              E.inter = E.inter + dE;
               E.inter_vdw = E.inter_vdw + dv;
+              if (qon) E.inter_q = E.inter_q + dq;
+              if (ew) {
+                E.reciprocal = e_recip;
+                mv_ew = 2;
+              }
               if (mv_kind == 0) {
                 ++RS.n_translate_accepted;
               } else {
@@ -1816,10 +1975,22 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
           __syncthreads();
           if (!gs.flag) {
             gc_mol_energies<MIXED>(A, V, gs, ttype, em, eov);
+            // charged boxes (move_insert.f90:274-291): the reciprocal energy with
+            // the molecule's structure factors added, and its self energy
+            const bool qon = G.qon != 0;
+            const bool ew = qon && A.sp[ise].has_charge;
+            double e_recip = 0.0;
+            if (ew && !eov[0] && !eov[1]) e_recip = gc_recip(G, A.sp[ise], gs.r, mv_slot, 0, s_red);
             if (threadIdx.x == 0 && !eov[0] && !eov[1]) {
               const double ev = em[0], eq = em[1];
               const double eb = em[2], ea = em[3], ed = em[4], ei = em[5], eiv = em[6], eiq = em[7];
               double dE_inter = ev + eq, dE_intra = eiv + eiq + eb + ea + ed + ei;
+              double e_self = 0.0;
+              if (qon) {
+                if (ew) dE_inter = dE_inter + (e_recip - E.reciprocal);
+                e_self = gc_self(A.sp[ise], b);
+                dE_inter = dE_inter + e_self;
+              }
               double nbn[kMaxTypes];
               for (int t = 0; t < kMaxTypes; ++t) nbn[t] = nb[t];
               for (int a = 0; a < gs.na; ++a)
@@ -1850,6 +2021,11 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
                 E.inter_vdw += ev;
                 E.inter_q += eq;
                 if (tail) E.lrc = e_lrc;
+                if (ew) {
+                  E.reciprocal = e_recip;
+                  mv_ew = 0;
+                }
+                E.self += e_self;
                 for (int t = 0; t < kMaxTypes; ++t) nb[t] = nbn[t];
                 ++RS.n_insert_accepted;
                 ++nmol[ise];
@@ -1942,14 +2118,26 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
           __syncthreads();
           if (mv_stop) break;
           gc_mol_energies<MIXED>(A, V, gs, ttype, em, eov);
+          // charged boxes (move_delete.f90:261-277): the reciprocal energy with
+          // the molecule's structure factors taken out, and its self energy
+          const bool qon = G.qon != 0;
+          const bool ew = qon && A.sp[ise].has_charge;
+          double e_recip = 0.0;
+          if (ew) e_recip = gc_recip(G, A.sp[ise], nullptr, mv_slot, 1, s_red);
           if (threadIdx.x == 0) {
             mv_acc = 0;
             const double ev = em[0], eq = em[1];
             const double eb = em[2], ea = em[3], ed = em[4], ei = em[5], eiv = em[6], eiq = em[7];
-            double dE_inter = -ev;
+            double dE_inter = -ev - em[8];
             double dE_intra = -eb - ea - ed - ei;
             dE_intra = dE_intra - eiv - eiq;
-            dE_inter = dE_inter - eq;
+            dE_inter = dE_inter - em[9];
+            double e_self = 0.0;
+            if (qon) {
+              if (ew) dE_inter = dE_inter + (e_recip - E.reciprocal);
+              e_self = gc_self(A.sp[ise], b);
+              dE_inter = dE_inter - e_self;
+            }
             double nbn[kMaxTypes];
             for (int t = 0; t < kMaxTypes; ++t) nbn[t] = nb[t];
             for (int a = 0; a < gs.na; ++a)
@@ -1980,6 +2168,11 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
               E.inter_vdw -= ev;
               E.inter_q -= eq;
               if (tail) E.lrc = e_lrc;
+              if (ew) {
+                E.reciprocal = e_recip;
+                mv_ew = 1;
+              }
+              E.self -= e_self;
               for (int t = 0; t < kMaxTypes; ++t) nb[t] = nbn[t];
               ++RS.n_delete_accepted;
               --nmol[ise];
@@ -2173,10 +2366,16 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
               __syncthreads();
               if (mv_stop) break;
               gc_mol_energies<MIXED>(A, V, gs, ttype, em, eov);
+              // charged boxes: the reciprocal energy of the new configuration
+              // (move_regrow.f90:338-354, int_intra)
+              const bool ew = G.qon && A.sp[ise].has_charge;
+              double e_recip = 0.0;
+              if (ew) e_recip = gc_recip(G, A.sp[ise], rg_new, mv_slot, 2, s_red);
               if (threadIdx.x == 0) {
                 const double* en = rg_en;  // ev, eq, eb, ea, ed, ei, eiv, eiq of the new configuration
                 double dE_intra = en[2] + en[3] + en[4] + en[5] + en[7] + en[6];
                 double dE_inter = en[1] + en[0];
+                if (ew) dE_inter = dE_inter + (e_recip - E.reciprocal);
                 dE_intra = dE_intra - em[2] - em[3] - em[4] - em[5] - em[7] - em[6];
                 dE_inter = dE_inter - em[1] - em[0];
                 const double dE = dE_intra + dE_inter;
@@ -2197,6 +2396,10 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
                   E.intra_q += en[7] - em[7];
                   E.inter_vdw += en[0] - em[0];
                   E.inter_q += en[1] - em[1];
+                  if (ew) {
+                    E.reciprocal = e_recip;
+                    mv_ew = 2;
+                  }
                   ++RS.n_regrow_accepted;
                 }
               }
@@ -2205,6 +2408,7 @@ __global__ void __launch_bounds__(kGcThreads, 1) k_gcmc(GcArgs A, GcBox* boxes, 
         }
       }
       __syncthreads();
+      if (!MIXED && mv_ew >= 0) gc_recip_commit(G, mv_slot, mv_ew);  // accepted moves of charged molecules
       // commit the molecule's coordinates (rejected deletions and regrowths keep
       // the coordinates of their Rosenbluth pass, as the reference does)
       if (threadIdx.x == 0) {
@@ -2333,12 +2537,13 @@ __global__ void __launch_bounds__(kGcThreads, 1)
   }
 }
 
-size_t gc_smem_bytes(int natoms, int nrec, bool mixed, bool comcut) {
+size_t gc_smem_bytes(int natoms, int nrec, bool mixed, bool comcut, bool charged) {
   size_t s = (size_t)natoms * (3 * sizeof(double) + (mixed ? 2 : 3) * sizeof(int)) +
              (size_t)nrec * (3 * sizeof(double) + 5 * sizeof(int));
   s = (s + 15) & ~(size_t)15;
   if (mixed) s += (size_t)natoms * sizeof(float4);
   if (comcut) s += (size_t)nrec * sizeof(double) + (size_t)natoms * sizeof(int);
+  if (charged && !mixed) s = ((s + 15) & ~(size_t)15) + (size_t)natoms * sizeof(double);
   return s;
 }
 }  // namespace cassgpu
@@ -2388,6 +2593,18 @@ static void gc_host_box(cass_ctx* c, int ib, const std::vector<int>& free_slots,
   g.rcut9 = B.rcut9;
   g.comcut = B.comcut ? 1 : 0;
   g.rmax = B.rcut_max;
+  // charged boxes: the Ewald state of the box and the per-molecule structure
+  // factors (scratch rows new_cos / new_sin are the caller's)
+  g.qon = B.desc.charge_style == CASS_CHARGE_COUL ? 1 : 0;
+  if (g.qon && B.nvecs > 0) {
+    g.nvecs = B.nvecs;
+    g.kvec = B.d_kvec.as<double4_32a>();
+    g.cos_sum = B.d_cos_sum.as<double>();
+    g.sin_sum = B.d_sin_sum.as<double>();
+    g.cos_mol = c->d_cos_mol.as<double>();
+    g.sin_mol = c->d_sin_mol.as<double>();
+    g.stride = c->cos_mol_stride;
+  }
   const int nt = c->pt.ntypes;
   for (int ia = 0; ia < nt; ++ia)
     for (int ja = 0; ja < nt; ++ja) {
@@ -2412,6 +2629,8 @@ static void gc_fill_args(cass_ctx* c, int is, int kappa_ins, int kappa_dih, bool
   for (int k = 0; k < c->nspecies; ++k) {
     const SpeciesH& t = c->sp[k];
     A.sp[k].natoms = t.natoms;
+    A.sp[k].has_charge = t.has_charge ? 1 : 0;
+    A.sp[k].l_coul_cbmc = t.l_coul_cbmc ? 1 : 0;
     bool lin = true;
     for (size_t q = 0; q < t.angle_kind.size(); ++q)
       if (t.angle_kind[q] != CASS_BONDED_FIXED || t.angle_param[2 * q] != 180.0) lin = false;
@@ -2419,6 +2638,7 @@ static void gc_fill_args(cass_ctx* c, int is, int kappa_ins, int kappa_dih, bool
     for (int a = 0; a < kMaxAtoms; ++a) A.sp[k].type[a] = -1;
     for (int a = 0; a < t.natoms && a < kMaxAtoms; ++a) {
       A.sp[k].mass[a] = t.mass[a];
+      A.sp[k].q[a] = t.q[a];
       A.sp[k].type[a] = t.type[a];
     }
   }
@@ -2472,6 +2692,8 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
   for (int f = 0; f < s.nfrag; ++f)
     if (s.frag_nconfig[f] < 1) return set_error(CASS_EINVAL, "fragment library is empty");
   bool mixed = c->precision == CASS_PREC_MIXED;
+  bool any_q = false;
+  int max_nv = 0;
   for (int k = 0; k < nboxes; ++k) {
     const int ib = iboxes[k] - 1;
     if (ib < 0 || ib >= c->nboxes) return set_error(CASS_EINVAL, "box index out of range");
@@ -2479,10 +2701,18 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
       if (iboxes[j] == iboxes[k]) return set_error(CASS_EINVAL, "box listed twice");
     const BoxH& B = c->box[ib];
     if (!B.energy_valid) return set_error(CASS_ESTATE, "system energy of box not computed");
-    if (B.desc.charge_style != CASS_CHARGE_NONE) return set_error(CASS_EUNSUPPORTED, "gcmc boxes hold no charges");
+    if (B.desc.charge_style != CASS_CHARGE_NONE && B.desc.charge_sum_style != CASS_QQ_EWALD)
+      return set_error(CASS_EUNSUPPORTED, "gcmc: charges need the Ewald sum");
     if (B.desc.vdw_style != CASS_VDW_LJ) return set_error(CASS_EUNSUPPORTED, "gcmc needs LJ boxes");
+    if (B.desc.charge_style != CASS_CHARGE_NONE) {
+      if (B.nvecs > 0 && !c->d_cos_mol.p) return set_error(CASS_ESTATE, "structure factors not computed");
+      any_q = true;
+      max_nv = std::max(max_nv, B.nvecs);
+    }
     mixed = mixed && (B.desc.vdw_sum_style == CASS_VDW_SUM_CUT || B.desc.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL);
   }
+  // charged boxes run the FP64 kernel, one CTA per box
+  if (any_q) mixed = false;
   int rc;
   CASS_CUDA(cudaSetDevice(c->device));
   if ((rc = ensure_pools(c))) return rc;
@@ -2532,7 +2762,7 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
     gc_host_box(c, ib, pools[k], h, g);
     g.mu = mu[k] / 0.01;  // kJ/mol to internal units (atomic_to_kJmol)
     g.log_lambda3 = 3.0 * std::log(39.9031268605 * std::sqrt(B.dev.beta / (kTWOPI * mw)));  // de Broglie
-    smem = std::max(smem, gc_smem_bytes(g.natoms, g.nrec, mixed, g.comcut != 0));
+    smem = std::max(smem, gc_smem_bytes(g.natoms, g.nrec, mixed, g.comcut != 0, g.qon != 0));
     tot_atoms += (size_t)g.natoms;
     tot_rec += h.slots.size();
   }
@@ -2544,7 +2774,8 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
   const size_t nlog = max_rec + 2;
   const size_t bytes = nboxes * sizeof(GcBox) + nlog * sizeof(double) + tot_atoms * (sizeof(double4_32a) + sizeof(int)) +
                        tot_rec * (sizeof(int4) + sizeof(int)) + 2 * nboxes * nsp * sizeof(double) +
-                       nboxes * (sizeof(CassEnergy) + sizeof(CassGCMCResult) + sizeof(int)) + 1024;
+                       nboxes * (sizeof(CassEnergy) + sizeof(CassGCMCResult) + sizeof(int)) +
+                       2 * (size_t)nboxes * max_nv * sizeof(double) + 1024;
   if ((rc = c->d_gc.reserve(bytes))) return rc;
   char* base = static_cast<char*>(c->d_gc.p);
   auto carve = [&](size_t n, size_t align) {
@@ -2592,6 +2823,10 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
     g.energy = d_E + k;
     g.res = d_res + k;
     g.status = d_status + k;
+    if (g.nvecs > 0) {
+      g.new_cos = reinterpret_cast<double*>(carve(2 * (size_t)g.nvecs * sizeof(double), 16));
+      g.new_sin = g.new_cos + g.nvecs;
+    }
     hE[k] = c->box[iboxes[k] - 1].energy;
   }
   CASS_CUDA(h2d(c, d_box, gb.data(), nboxes * sizeof(GcBox)));
@@ -2601,9 +2836,10 @@ extern "C" int cass_gcmc(cass_ctx* c, int32_t nboxes, const int32_t* iboxes, con
   auto kern = mixed ? k_gcmc<true> : k_gcmc<false>;
   CASS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   // cluster size: the largest of 8, 4, 2 for which every box's cluster can be
-  // resident at once; else one CTA per box
+  // resident at once; else one CTA per box (always for charged boxes, whose
+  // reciprocal-space pass runs on one CTA)
   int csize = 1;
-  for (int cs = 8; cs >= 2; cs >>= 1) {
+  for (int cs = any_q ? 1 : 8; cs >= 2; cs >>= 1) {
     cudaLaunchConfig_t q = {};
     cudaLaunchAttribute qa[1];
     qa[0].id = cudaLaunchAttributeClusterDimension;
@@ -2707,12 +2943,13 @@ extern "C" int cass_build_molecule(cass_ctx* c, int32_t im, int32_t is1, int32_t
     if (s.frag_nconfig[f] < 1) return set_error(CASS_EINVAL, "fragment library is empty");
   const BoxH& B = c->box[ib];
   if (!B.defined) return set_error(CASS_ESTATE, "box not defined");
-  if (B.desc.charge_style != CASS_CHARGE_NONE) return set_error(CASS_EUNSUPPORTED, "build_molecule boxes hold no charges");
+  if (B.desc.charge_style != CASS_CHARGE_NONE && B.desc.charge_sum_style != CASS_QQ_EWALD)
+    return set_error(CASS_EUNSUPPORTED, "build_molecule: charges need the Ewald sum");
   if (B.desc.vdw_style != CASS_VDW_LJ) return set_error(CASS_EUNSUPPORTED, "build_molecule needs LJ boxes");
   const int slot = c->mol_base[is] + im - 1;
   if (del_flag && c->mol_box[slot] != ib) return set_error(CASS_ESTATE, "del_flag: the molecule is not live in the box");
   if (!del_flag && c->mol_box[slot] >= 0) return set_error(CASS_ESTATE, "the molecule to grow is live");
-  bool mixed = c->precision == CASS_PREC_MIXED &&
+  bool mixed = c->precision == CASS_PREC_MIXED && B.desc.charge_style == CASS_CHARGE_NONE &&
                (B.desc.vdw_sum_style == CASS_VDW_SUM_CUT || B.desc.vdw_sum_style == CASS_VDW_SUM_CUT_TAIL);
   int rc;
   CASS_CUDA(cudaSetDevice(c->device));
@@ -2724,7 +2961,7 @@ extern "C" int cass_build_molecule(cass_ctx* c, int32_t im, int32_t is1, int32_t
   GcBox g;
   gc_host_box(c, ib, del_flag ? std::vector<int>() : std::vector<int>{slot}, h, g);
   const int rec = (int)(std::lower_bound(h.slots.begin(), h.slots.end(), slot) - h.slots.begin());
-  const size_t smem = gc_smem_bytes(g.natoms, g.nrec, mixed, g.comcut != 0);
+  const size_t smem = gc_smem_bytes(g.natoms, g.nrec, mixed, g.comcut != 0, g.qon != 0);
   if (smem > kGcSmemLimit)
     return set_error(CASS_ECAPACITY, "build_molecule holds the box in shared memory: too many atoms");
   const size_t nout = 2 + 3 * (size_t)s.natoms, niout = 2 + kMaxFrags;

@@ -346,8 +346,12 @@ int cass_mc_sweeps(cass_ctx* ctx, int32_t nboxes, const int32_t* ibox, const Cas
  * boxes advancing in lockstep in one launch: Translate, Rotate, CBMC Insertion
  * (move_insert.f90), CBMC Deletion (move_delete.f90) and CBMC regrowth
  * (Cut_N_Grow, move_regrow.f90 with Cut_Regrow, fragment_growth.f90:1118-1312),
- * chosen by the cumulative thresholds below.  Boxes must hold no charges (no
- * Ewald sum).  The molecule a move picks is the im-th live molecule of its
+ * chosen by the cumulative thresholds below.  Charged boxes need the Ewald
+ * sum (CASS_EUNSUPPORTED otherwise): every move then carries the real-space
+ * Coulomb terms, the reciprocal energy from the box's running structure
+ * factors (left updated for the calls that follow) and, for insertions and
+ * deletions, the molecule's self energy; they run in FP64 on one CTA per box
+ * whatever the context's precision.  The molecule a move picks is the im-th live molecule of its
  * species in slot order; new molecules take the highest free slot of the
  * box's share of free slots (free slots of the exchanged species are dealt to
  * the listed boxes in turn, in ascending slot order).  Box b draws from the
@@ -398,8 +402,11 @@ int cass_gcmc(cass_ctx* ctx, int32_t nboxes, const int32_t* ibox, const CassGCMC
  *     terms that the calling move adds.
  *   cbmc_overlap out: 1 when every trial of a stage overlapped (ln_pbias and xyz
  *     are then undefined).
- * Boxes as cass_gcmc takes them (LJ, no charges).  FP64 contexts grow in FP64
- * and reproduce the reference's arithmetic; mixed contexts grow in FP32. */
+ * Boxes as cass_gcmc takes them (LJ; charges only with the Ewald sum, where
+ * the trial energies carry the intramolecular charges and, for species with
+ * L_Coul_CBMC, the intermolecular real-space ones within rcut_cbmc).  FP64
+ * contexts, and every context for charged boxes, grow in FP64 and reproduce
+ * the reference's arithmetic; mixed contexts grow uncharged boxes in FP32. */
 int cass_build_molecule(cass_ctx* ctx, int32_t im, int32_t is, int32_t ibox, int32_t del_flag, int32_t kappa_ins,
                         int32_t kappa_dih, uint64_t* rng_state, int32_t* frag_order, double* ln_pseq,
                         double* ln_pbias, double* xyz, int32_t* cbmc_overlap);

@@ -3131,7 +3131,8 @@ int orc_build_molecule(orc_ctx* c, int32_t im, int32_t is1, int32_t ibox1, int32
   if (!s.defined || s.nfrag < 1) return fail(CASS_ESTATE, "species not defined or without fragments");
   if (im < 1 || im > c->max_mol[is]) return fail(CASS_EINVAL, "molecule index out of range");
   if (s.nfrag > 1 && kappa_dih < 1) return fail(CASS_EINVAL, "kappa_dih must be >= 1");
-  if (c->box[ib].charge_style != CASS_CHARGE_NONE) return fail(CASS_EUNSUPPORTED, "build_molecule boxes hold no charges");
+  if (c->box[ib].charge_style != CASS_CHARGE_NONE && c->box[ib].charge_sum_style != CASS_QQ_EWALD)
+    return fail(CASS_EUNSUPPORTED, "build_molecule: charges need the Ewald sum");
   if (int rc = cbmc_ready(c)) return rc;
   const int slot = c->mol_base[is] + im - 1;
   const Mol& live = c->mol[slot];

@@ -6,7 +6,7 @@ import math
 
 import numpy as np
 
-from cassandra_gb300 import workloads
+from cassandra_gb300 import abi, workloads
 from oracle import oracle
 
 KBOLTZ = 0.8314472
@@ -80,3 +80,28 @@ def test_gcmc_deterministic():
             o.system_total_energy(1)
             out.append(o.gcmc([1], 500, 1, [-24.0], [[1.0]], [[0.5]], seed=9))
     assert out[0] == out[1]
+
+
+def test_gcmc_charged_butane_bookkeeping():
+    """Partially charged butane in Ewald boxes, with and without L_Coul_CBMC:
+    insertions, deletions and regrowths (the reciprocal sum of a regrown
+    molecule, move_regrow.f90:338-354) keep the running energy equal to a
+    recomputation in every component."""
+    s = workloads.gcmc_system(nboxes=2, length=25.0, max_per_box=300, rcut=12.0)
+    for a, q in zip(s.species[0].atoms, (0.25, -0.25, -0.25, 0.25)):
+        a.charge = q
+    for bx in s.boxes:
+        bx.charge_style, bx.charge_sum_style, bx.ewald_tol, bx.rcut_coul = abi.CHARGE_COUL, abi.QQ_EWALD, 1e-5, 12.0
+    for l_coul_cbmc in (False, True):
+        s.species[0].l_coul_cbmc = l_coul_cbmc
+        with oracle.open_system(s) as o:
+            for b in (1, 2):
+                o.system_total_energy(b)
+            r = o.gcmc([1, 2], 600, 1, [-22.0, -26.0], [[1.0], [1.0]], [[0.5], [0.5]], seed=5)
+            for k, x in enumerate(r):
+                assert x["n_insert_accepted"] > 0 and x["n_regrow_accepted"] > 0, x
+                e, ov = o.system_total_energy(k + 1)
+                assert not ov
+                scale = abs(e["inter_vdw"]) + abs(e["inter_q"]) + abs(e["reciprocal"]) + abs(e["self"])
+                for comp in ("total", "inter_vdw", "inter_q", "intra_q", "reciprocal", "self", "dihedral"):
+                    assert abs(x["energy"][comp] - e[comp]) <= 1e-9 * scale, (comp, x["energy"][comp], e[comp])

@@ -119,3 +119,35 @@ def test_build_molecule_errors(liquid):
         assert e.value.code == abi.CASS_ESTATE
         with pytest.raises(abi.CassError):
             g.build_molecule(0, 1, 1, False, 8, 8, st)
+
+
+@pytest.mark.parametrize("l_coul_cbmc", [False, True])
+def test_build_molecule_charged_fp64_matches_oracle(liquid, l_coul_cbmc):
+    """The same liquid with partial charges in an Ewald box: the CBMC trial
+    energies carry the intramolecular charges, and with L_Coul_CBMC the
+    intermolecular real-space charges within rcut_cbmc as well."""
+    import copy
+    s, live, xyz, free = liquid
+    s = copy.deepcopy(s)
+    for a, q in zip(s.species[0].atoms, (0.25, -0.25, -0.25, 0.25)):
+        a.charge = q
+    s.species[0].l_coul_cbmc = l_coul_cbmc
+    bx = s.boxes[0]
+    bx.charge_style, bx.charge_sum_style, bx.ewald_tol, bx.rcut_coul = abi.CHARGE_COUL, abi.QQ_EWALD, 1e-5, 12.0
+    rng = np.random.default_rng(9)
+    with oracle.open_system(s) as o, cg.open_system(s, precision=abi.PREC_MIXED) as g:
+        _load(o, (s, live, xyz, free))
+        _load(g, (s, live, xyz, free))
+        for k in range(16):
+            del_flag = k % 2 == 1
+            im = live[k % len(live)] if del_flag else free[k]
+            st = _state(rng)
+            a = o.build_molecule(im, 1, 1, del_flag, 8, 8, st)
+            b = g.build_molecule(im, 1, 1, del_flag, 8, 8, st)  # charged boxes grow in FP64
+            assert a["cbmc_overlap"] == b["cbmc_overlap"], k
+            assert np.array_equal(a["rng_state"], b["rng_state"]), k
+            assert np.array_equal(a["frag_order"], b["frag_order"]), k
+            if a["cbmc_overlap"]:
+                continue
+            assert abs(a["ln_pbias"] - b["ln_pbias"]) <= 1e-9 * max(1.0, abs(a["ln_pbias"])), (k, a, b)
+            assert np.allclose(a["xyz"], b["xyz"], rtol=0, atol=1e-9), k
