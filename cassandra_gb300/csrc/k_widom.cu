@@ -141,10 +141,18 @@ __global__ void k_cell_scatter(const BoxSrc* src, const BoxDev* boxes, const int
   int c = cell_of[b.atom_off + i];
   int pos = cstart[b.cell_off + k + c] + atomicAdd(&fill[b.cell_off + c], 1);
   int g = b.atom_off + pos;
-  c64[g] = src[k].p64[i];
-  c32[g] = src[k].p32[i];
+  // the copies hold the positions their cells were chosen from, wrapped into
+  // [-L/2, L/2) (an atom of a molecule folded by its COM may stick out of the
+  // box), so that a query's per-row image shift is the whole periodic shift
+  double4_32a p = src[k].p64[i];
+  p.x = p.x - b.L[0] * floor((p.x + b.hL[0]) / b.L[0]);
+  p.y = p.y - b.L[1] * floor((p.y + b.hL[1]) / b.L[1]);
+  p.z = p.z - b.L[2] * floor((p.z + b.hL[2]) / b.L[2]);
+  c64[g] = p;
+  const float4 q = src[k].p32[i];
+  c32[g] = make_float4((float)p.x, (float)p.y, (float)p.z, q.w);
   ctype[g] = src[k].meta[i].y;
-  cq32[g] = (float)src[k].p64[i].w;
+  cq32[g] = (float)p.w;
   corig[g] = i;
 }
 

@@ -17,6 +17,7 @@ import pytest
 import cassandra_gb300 as cg
 import helpers
 from cassandra_gb300 import abi, workloads
+from cassandra_gb300.system import MoleculeSet
 from oracle import oracle
 
 pytestmark = pytest.mark.gpu
@@ -284,6 +285,37 @@ def test_widom_mixed_charged_spce_matches_oracle():
     real-space Ewald and LJ pairs in FP32, cutoff decisions as in FP64."""
     s = helpers.pregen_system("water_spce", 0)
     s.species[0].libraries = [workloads.water_species().libraries[0] * 1.0]
+    with oracle.open_system(s) as o, cg.open_system(s, precision=abi.PREC_MIXED) as m:
+        o.system_total_energy(1)
+        m.system_total_energy(1)
+        ro, to = o.widom_insert(1, [1], 1000, 12, 0, seed=11, trace=True)
+        rm, tm = m.widom_insert(1, [1], 1000, 12, 0, seed=11, trace=True)
+    _check_mixed_records(ro, to, rm, tm)
+
+
+def _water_sticking_out(nmol=600, length=26.2, shift=1.3):
+    """Waters shifted by `shift` A and folded back by their COM, so that some
+    hydrogens lie outside the box; 26.2 A gives four cells of rcut_cbmc per
+    side, so the CBMC queries reach periodic images through per-row shifts."""
+    s = workloads.water_box(nmol, length)
+    masses = np.array([15.999, 1.008, 1.008])
+    ms = MoleculeSet()
+    for im, is_, ib, x in zip(s.molecules.im, s.molecules.is_, s.molecules.ibox, s.molecules.xyz):
+        x = np.asarray(x, dtype=np.float64).reshape(-1, 3) + shift
+        com = (x * masses[:, None]).sum(0) / masses.sum()
+        ms.add(im, is_, ib, x - length * np.floor((com + length / 2) / length))
+    s.molecules = ms
+    xyz = np.concatenate([np.asarray(v).reshape(-1, 3) for v in ms.xyz])
+    assert (np.abs(xyz) > length / 2).sum() > 10
+    return s
+
+
+def test_widom_mixed_water_atoms_outside_box():
+    """Atoms outside the box (a molecule is folded by its COM) in a box of four
+    cells per side: the cell-sorted copies are wrapped, so the FP32 queries,
+    which shift whole rows by a box length instead of folding each pair, see
+    every neighbour at its minimum image."""
+    s = _water_sticking_out()
     with oracle.open_system(s) as o, cg.open_system(s, precision=abi.PREC_MIXED) as m:
         o.system_total_energy(1)
         m.system_total_energy(1)
