@@ -30,6 +30,7 @@
 #include <cstring>
 #include <vector>
 
+#include "cass_cbmc_f.cuh"
 #include "cass_ctx.h"
 
 namespace cassgpu {
@@ -140,6 +141,41 @@ __device__ __forceinline__ int mc_pick_species(int nspecies, const double* x, in
   return last;
 }
 
+// the mixed kernel's serial draws: the top 23 bits of the same lfsr258 numbers
+// (draw_f), without the FP64 unit, which on this GPU holds a warp's FP64
+// instruction for many cycles even when one lane issues it
+__device__ __forceinline__ int mc_pick_species_f(int nspecies, const float* x, int last, Lfsr& rng) {
+  const float u = draw_f(rng);
+  for (int is = 0; is < nspecies; ++is)
+    if (u <= x[is]) return is;
+  return last;
+}
+
+template <bool MIXED>
+__device__ __forceinline__ double mc_u(Lfsr& rng) {
+  if constexpr (MIXED) return (double)draw_f(rng);
+  else return rng.next();
+}
+
+// (s, c) += (s', c') for compensated FP32 sums: the rounding error of s + s'
+// (TwoSum, exact in FP32) joins the correction terms
+__device__ __forceinline__ void two_sum_add(float2& a, const float2 b) {
+  const float t = a.x + b.x;
+  const float bp = t - a.x;
+  const float e = (a.x - (t - bp)) + (b.x - bp);
+  a.x = t;
+  a.y = (a.y + b.y) + e;
+}
+
+// warp sum of compensated FP32 pairs, butterfly order (lane 0's is fixed)
+__device__ __forceinline__ float2 warp_sum2(float2 v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const float2 u = make_float2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o));
+    two_sum_add(v, u);
+  }
+  return v;
+}
+
 template <class V>
 __device__ __forceinline__ V block_sum_mc(V v, V* red, int slot) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -188,6 +224,7 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
   __shared__ BoxDev b;
   __shared__ McMove mv;
   __shared__ double red[NW * 8];
+  __shared__ float redf[NW * 4];  // mixed kernel: compensated FP32 pair sums per warp
   __shared__ int redi[NW * 2];
   __shared__ float2 ljp[kMaxTypes * kMaxTypes];
   __shared__ double cd[2][4];  // this CTA's partial sums for the cluster (alternating buffers)
@@ -269,10 +306,17 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
   CassEnergy E;
   CassMCResult R;
   double md[kMaxSpeciesMC], mr[kMaxSpeciesMC], xd[kMaxSpeciesMC], xr[kMaxSpeciesMC];
+  float mdf[kMaxSpeciesMC], xdf[kMaxSpeciesMC], xrf[kMaxSpeciesMC];  // mixed kernel: FP32 copies
   int nt_d[kMaxSpeciesMC], ns_d[kMaxSpeciesMC], nt_r[kMaxSpeciesMC], ns_r[kMaxSpeciesMC];
   int last_d = 0, last_r = 0;
   bool any_d = false, any_r = false;
   double dv = 0, dq = 0;
+  // mixed kernel, one CTA and no k-space work: the move's energy change as
+  // compensated FP32 pairs and its acceptance decided in FP32 (FP64 only for
+  // the bookkeeping of an accepted move)
+  float2 dv2 = make_float2(0.f, 0.f), dq2 = make_float2(0.f, 0.f);
+  bool fast = false;
+  float ptf = 1.0f, betaf = 0.0f;
   if (threadIdx.x == 0) {
     rng = seed_stream(A.seed, G.ibox1, 0);
     E = *G.energy;
@@ -284,6 +328,15 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
     }
     any_d = mc_species_cdf(G, A.nspecies, md, xd, &last_d);
     any_r = mc_species_cdf(G, A.nspecies, mr, xr, &last_r);
+    if (MIXED) {
+      for (int is = 0; is < A.nspecies; ++is) {
+        mdf[is] = (float)md[is];
+        xdf[is] = (float)xd[is];
+        xrf[is] = (float)xr[is];
+      }
+      ptf = (float)A.prob_translate;
+      betaf = (float)b.beta;
+    }
   }
   const long long steps = A.nsweeps * (long long)(A.steps_per_sweep > 0 ? A.steps_per_sweep : M);
   int status = 0;
@@ -294,14 +347,18 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
       mv.skip = 0;
       mv.stop = 0;
       mv.accept = 0;
-      const bool tr = rng.next() <= A.prob_translate;
+      const bool tr = MIXED ? draw_f(rng) <= ptf : rng.next() <= A.prob_translate;
       mv.kind = tr ? 0 : 1;
-      const int is = (tr ? any_d : any_r) ? mc_pick_species(A.nspecies, tr ? xd : xr, tr ? last_d : last_r, rng) : -1;
+      int is = -1;
+      if (tr ? any_d : any_r)
+        is = MIXED ? mc_pick_species_f(A.nspecies, tr ? xdf : xrf, tr ? last_d : last_r, rng)
+                   : mc_pick_species(A.nspecies, tr ? xd : xr, tr ? last_d : last_r, rng);
       if (is < 0) {
         mv.skip = 1;
       } else {
         // INT(rranf() * nmols) + 1, kept in range when rranf() rounds to 1.0
-        const int im = min((int)(rng.next() * G.nmol_sp[is]) + 1, G.nmol_sp[is]);
+        const int im = MIXED ? min((int)(draw_f(rng) * (float)G.nmol_sp[is]) + 1, G.nmol_sp[is])
+                             : min((int)(rng.next() * G.nmol_sp[is]) + 1, G.nmol_sp[is]);
         const int pm = G.first_sp[is] + im - 1;
         const McSpecies& s = A.sp[is];
         mv.is = is;
@@ -323,7 +380,10 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
           ++R.n_translate;
           if (A.nupdate > 0) ++nt_d[is];
           double d[3];
-          for (int k = 0; k < 3; ++k) d[k] = (2.0 * rng.next() - 1.0) * md[is];
+          if (MIXED)
+            for (int k = 0; k < 3; ++k) d[k] = (double)((2.0f * draw_f(rng) - 1.0f) * mdf[is]);
+          else
+            for (int k = 0; k < 3; ++k) d[k] = (2.0 * rng.next() - 1.0) * md[is];
           double cn[3] = {c0 + d[0], c1 + d[1], c2 + d[2]};
           double sh[3];
           for (int k = 0; k < 3; ++k) {  // Fold_Molecule
@@ -342,9 +402,9 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
           if (A.nupdate > 0) ++nt_r[is];
           double Rm[9];
           if (s.linear) {
-            const double theta = acos(1.0 - 2.0 * rng.next());
-            const double phi = (1.0 - 2.0 * rng.next()) * kPI;
-            const double psi = (1.0 - 2.0 * rng.next()) * kPI;
+            const double theta = acos(1.0 - 2.0 * mc_u<MIXED>(rng));
+            const double phi = (1.0 - 2.0 * mc_u<MIXED>(rng)) * kPI;
+            const double psi = (1.0 - 2.0 * mc_u<MIXED>(rng)) * kPI;
             Rm[0] = cos(psi) * cos(phi) - cos(theta) * sin(phi) * sin(psi);
             Rm[1] = cos(psi) * sin(phi) + cos(theta) * cos(phi) * sin(psi);
             Rm[2] = sin(psi) * sin(theta);
@@ -356,8 +416,8 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
             Rm[8] = cos(theta);
           } else {
             double p1 = 0.0, p2 = 0.0, p3 = 0.0;
-            const int axis = (int)(3.0 * rng.next()) + 1;
-            const double ang = (2.0 * rng.next() - 1.0) * mr[is];
+            const int axis = (int)(3.0 * mc_u<MIXED>(rng)) + 1;
+            const double ang = (2.0 * mc_u<MIXED>(rng) - 1.0) * mr[is];
             if (axis == 1) p1 = ang;
             else if (axis == 2) p2 = ang;
             else p3 = ang;
@@ -401,6 +461,7 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
     // ---- B: old and trial energies of the molecule against the other atoms
     const int pm = mv.pm, na = mv.na;
     double pdv = 0, pdq = 0;  // this thread's share of E_new - E_old
+    float2 pv2 = make_float2(0.f, 0.f), pq2 = make_float2(0.f, 0.f);  // the same, mixed kernel
     int po = 0, pn = 0;
     const int j0 = threadIdx.x + crank * blockDim.x, jstep = blockDim.x * csize;
     if (MIXED) {
@@ -437,8 +498,8 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
           kq.add(eq[1] - eq[0]);
         }
       }
-      pdv = kv.value();
-      pdq = kq.value();
+      pv2 = make_float2(kv.s, kv.c);
+      pq2 = make_float2(kq.s, kq.c);
     } else {
       for (int j = j0; j < N; j += jstep) {
         const int mj = smol[j];
@@ -477,8 +538,20 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
         }
       }
     }
-    block_sum_mc(pdv, red, 0);
-    block_sum_mc(pdq, red, 1);
+    if (MIXED) {  // compensated FP32 warp sums (no FP64 instructions in any warp)
+      pv2 = warp_sum2(pv2);
+      pq2 = warp_sum2(pq2);
+      if ((threadIdx.x & 31) == 0) {
+        const int w = threadIdx.x >> 5;
+        redf[4 * w] = pv2.x;
+        redf[4 * w + 1] = pv2.y;
+        redf[4 * w + 2] = pq2.x;
+        redf[4 * w + 3] = pq2.y;
+      }
+    } else {
+      block_sum_mc(pdv, red, 0);
+      block_sum_mc(pdq, red, 1);
+    }
     {
       const int o = __any_sync(0xffffffffu, po), n = __any_sync(0xffffffffu, pn);
       if ((threadIdx.x & 31) == 0) {
@@ -489,12 +562,27 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
     __syncthreads();
     int o = 0, n = 0;
     if (threadIdx.x == 0) {
-      dv = dq = 0.0;
-      for (int w = 0; w < nwarps; ++w) {
-        dv += red[w * 8];
-        dq += red[w * 8 + 1];
-        o |= redi[2 * w];
-        n |= redi[2 * w + 1];
+      if (MIXED) {
+        dv2 = dq2 = make_float2(0.f, 0.f);
+        for (int w = 0; w < nwarps; ++w) {
+          two_sum_add(dv2, make_float2(redf[4 * w], redf[4 * w + 1]));
+          two_sum_add(dq2, make_float2(redf[4 * w + 2], redf[4 * w + 3]));
+          o |= redi[2 * w];
+          n |= redi[2 * w + 1];
+        }
+        fast = csize == 1 && !mv.ewald;
+        if (!fast) {
+          dv = (double)dv2.x + (double)dv2.y;
+          dq = (double)dq2.x + (double)dq2.y;
+        }
+      } else {
+        dv = dq = 0.0;
+        for (int w = 0; w < nwarps; ++w) {
+          dv += red[w * 8];
+          dq += red[w * 8 + 1];
+          o |= redi[2 * w];
+          n |= redi[2 * w + 1];
+        }
       }
       if (csize > 1) {
         cd[cbuf][0] = dv;
@@ -587,7 +675,21 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
     // ---- D: acceptance
     if (threadIdx.x == 0) {
       bool acc = false;
-      if (mv.accept) {
+      if (mv.accept && MIXED && fast) {
+        // accept_or_reject in FP32 (the rule of accept_or_reject.f90:22-65 with
+        // a 23-bit draw); the bookkeeping of an accepted move in FP64
+        const float lnf = betaf * ((dv2.x + dq2.x) + (dv2.y + dq2.y));
+        acc = lnf <= 0.0f || (lnf < (float)kMAX_KBT && draw_f(rng) <= expf(-lnf));
+        if (acc) {
+          dv = (double)dv2.x + (double)dv2.y;
+          dq = (double)dq2.x + (double)dq2.y;
+          const double dE = dv + dq;
+          E.total = E.total + dE;
+          E.inter = E.inter + dE;
+          E.inter_vdw = E.inter_vdw + dv;
+          E.inter_q = E.inter_q + dq;
+        }
+      } else if (mv.accept) {
         double dE = 0.0;
         if (mv.ewald) dE = e_recip - E.reciprocal;
         dE = dE + dv + dq;
@@ -616,6 +718,7 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
                                     ? fmin(b.rcut_vdw, b.rcut_coul) : b.rcut_vdw;
           if (ratio < 0.00005) md[is] = 0.1 * md[is];
           else md[is] = fmin(rsmall, ratio / A.target_accept * md[is]);
+          if (MIXED) mdf[is] = (float)md[is];
         }
       } else {
         if (acc) {
