@@ -315,7 +315,11 @@ int cass_widom_insert(cass_ctx* ctx, int32_t is, int32_t nboxes, const int32_t* 
  * trial position, Update_System_Ewald_Reciprocal_Energy for charged species in
  * Ewald boxes, and accept_or_reject (accept_or_reject.f90:22-65); the
  * energy(ibox) bookkeeping and the structure factors stay FP64.  Box b draws
- * its random numbers from the lfsr258 stream seeded by (seed, b, 0).  Requires
+ * its random numbers from the lfsr258 stream seeded by (seed, b, 0); FP64
+ * contexts use the reference's full uniforms and decisions, mixed contexts the
+ * top 23 bits of the same numbers for the move choices and steps, FP32 pair
+ * energies summed as compensated FP32 pairs, and (on one CTA, without k-space
+ * work) an FP32 acceptance test, so their chains are their own.  Requires
  * a prior cass_system_total_energy of each listed box; afterwards the
  * molecules, the structure factors and the energy of each box are those after
  * its last move.  Replaces one translate/rotate host call sequence per move. */
