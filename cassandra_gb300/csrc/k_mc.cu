@@ -372,6 +372,12 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
           mv.old_r[3 * a] = sx[j];
           mv.old_r[3 * a + 1] = sy[j];
           mv.old_r[3 * a + 2] = sz[j];
+          if (MIXED) {  // (float) of the FP64 position, kept so at every commit
+            const float4 f = s32[j];
+            mv.old_f[3 * a] = f.x;
+            mv.old_f[3 * a + 1] = f.y;
+            mv.old_f[3 * a + 2] = f.z;
+          }
           mv.q[a] = sq[j];
           mv.type[a] = stype[j];
         }
@@ -447,10 +453,7 @@ __global__ void __launch_bounds__(GMEM ? kMcThreadsG : kMcThreads) k_mc_sweeps(M
           mv.com_new[2] = c2;
         }
         if (MIXED)
-          for (int i = 0; i < 3 * mv.na; ++i) {
-            mv.old_f[i] = (float)mv.old_r[i];
-            mv.trial_f[i] = (float)mv.trial[i];
-          }
+          for (int i = 0; i < 3 * mv.na; ++i) mv.trial_f[i] = (float)mv.trial[i];
       }
     }
     __syncthreads();
