@@ -5,6 +5,7 @@ insertions of the same oracle."""
 import math
 
 import numpy as np
+import pytest
 
 from cassandra_gb300 import abi, workloads
 from oracle import oracle
@@ -105,3 +106,21 @@ def test_gcmc_charged_butane_bookkeeping():
                 scale = abs(e["inter_vdw"]) + abs(e["inter_q"]) + abs(e["reciprocal"]) + abs(e["self"])
                 for comp in ("total", "inter_vdw", "inter_q", "intra_q", "reciprocal", "self", "dihedral"):
                     assert abs(x["energy"][comp] - e[comp]) <= 1e-9 * scale, (comp, x["energy"][comp], e[comp])
+
+
+def test_gcmc_charges_need_ewald():
+    """Grand-canonical moves and per-call growth in a charged box whose charges
+    use another sum than Ewald are refused (CASS_EUNSUPPORTED), as the device
+    path refuses them."""
+    s = workloads.water_gcmc_system(nboxes=1)
+    s.boxes[0].charge_sum_style = abi.QQ_DSF
+    with oracle.open_system(s) as o:
+        o.system_total_energy(1)
+        with pytest.raises(abi.CassError) as e:
+            o.gcmc([1], 10, 1, [-30.0], [[0.5]], [[0.4]], seed=1, kappa_ins=8, kappa_dih=0,
+                   cuts=(0.2, 0.4, 0.7, 1.0, 1.0))
+        assert e.value.code == abi.CASS_EUNSUPPORTED
+        st = np.array([5, 600, 5000, 200000, 9000000], dtype=np.uint64)
+        with pytest.raises(abi.CassError) as e:
+            o.build_molecule(100, 1, 1, False, 8, 0, st)
+        assert e.value.code == abi.CASS_EUNSUPPORTED
